@@ -1,0 +1,396 @@
+#!/usr/bin/env python3
+"""Benchmark: RK-stage DOF-updates/s of the 2D Euler DFR right-hand side +
+SSP(5,4) step on GB300, against the CPU restatement timed on the host cores.
+
+One "step" is one 5-stage SSP-RK step over the whole mesh.  DOF-updates per
+step = K * Np * 4 * 5.  Default workload: isentropic vortex on [-5,5]^2,
+256 x 256 quads split into 131,072 triangles with +-10% h interior jitter
+(seed 0), N = 4 (Np = 15), Roe flux, CFL 1, far-field exact-state BCs.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) each rank runs an independent replica on its own GPU
+(the path has no exchange step on one-GPU deployments), the timed region is
+bracketed by barriers and the max over ranks is reported; value is the
+whole-job aggregate.  Prints ONE JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RK-stage DOF-updates/s: FP64 plain vs mixed form at equal L2 err; adjoint/fwd"
+UNIT = "DOF-updates/s"
+
+WORKLOADS = {
+    "vortex256": dict(n=256, N=4, jitter=0.1, seed=0,
+                      desc="isentropic vortex [-5,5]^2, 256x256 quads -> 131072 tris, jitter 0.1h seed 0, N=4"),
+    "vortex1024": dict(n=1024, N=4, jitter=0.1, seed=0,
+                       desc="isentropic vortex [-5,5]^2, 1024x1024 quads -> 2097152 tris, jitter 0.1h seed 0, N=4"),
+    "vortex20": dict(n=20, N=2, jitter=0.0, seed=0,
+                     desc="isentropic vortex [-5,5]^2, 20x20 quads -> 800 tris, N=2"),
+}
+
+
+def args_parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=1000)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
+    p.add_argument("--workload", choices=sorted(WORKLOADS), default="vortex256")
+    p.add_argument("--fp64-steps", type=int, default=100)
+    p.add_argument("--e2e-steps", type=int, default=50)
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_mesh(wl):
+    from gocfd_gb300 import meshes
+    return meshes.vortex_box(wl["n"], jitter=wl["jitter"], seed=wl["seed"])
+
+
+def input_params(N, final_time=1e9):
+    from gocfd_gb300.euler2d import InputParameters2D
+    return InputParameters2D(CFL=1.0, FluxType="roe", InitType="ivortex", PolynomialOrder=N,
+                             FinalTime=final_time, MaxIterations=10 ** 9)
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+        self.marks = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append((time.monotonic(), line.strip()))
+
+    def mark(self):
+        self.marks.append(time.monotonic())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        rows = [s for (t, s) in self.samples if t0 - 0.15 <= t <= t1 + 0.15]
+        if not rows:
+            rows = [s for (_, s) in self.samples]
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            f = [x.strip() for x in r.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names[1:], f[4:8]):
+                if val.lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- roofline
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def algorithmic_bytes(family, K, nInt, nBC, Np, NE, tsz):
+    """Algorithmic DRAM bytes per launch of each kernel family (each array
+    touched once).  S = state bytes per element (FP64), faces/edge DOFs in T."""
+    S = 4 * Np * 8
+    F = 4 * 3 * NE * tsz
+    if family == 0:   # face interpolation: read state, write faces
+        return K * (S + F)
+    if family == 1:   # edge flux: read both sides' faces, write both sides' DOFs, edge data
+        per_int = 2 * (4 * NE * tsz) * 2 + 6 * 8 + 3 * 4
+        per_bc = 2 * (4 * NE * tsz) + 6 * 8 + 3 * 4 + 2 * NE * 8
+        return nInt * per_int + nBC * per_bc
+    if family == 2:   # div + RK update, averaged over the 5 stages: 19 state passes in total
+        return K * (19 * S + 5 * (F + 40)) / 5.0
+    return 0.0
+
+
+def ncu_traffic_per_element(kernel, precision, N):
+    """Per-element DRAM bytes of one launch, measured by ncu and recorded in
+    profiles/*.md as 'traffic_bytes_per_element <kernel> <precision> N=<N>: <v>'."""
+    pat = re.compile(rf"traffic_bytes_per_element\s+{kernel}\s+{precision}\s+N={N}:\s*([0-9.eE+]+)")
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for name in sorted(os.listdir(d)):
+        if not name.endswith((".md", ".txt")):
+            continue
+        with open(os.path.join(d, name)) as f:
+            m = pat.search(f.read())
+        if m:
+            return float(m.group(1))
+    return None
+
+
+# --------------------------------------------------------------------------- CPU oracle
+def cpu_baseline(wl, mesh, seconds, steps=None, warmup=0):
+    """The oracle (C++ FP64, OpenMP on all host cores) on the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    ora = oracle.OracleSolver(wl["N"], mesh.VX, mesh.VY, mesh.EToV, mesh.bc_edges, flux="roe",
+                              init="ivortex", cfl=1.0, vortex_center=(0.0, 0.0))
+    threads = ora.lib.oracle_num_threads()
+    if warmup:
+        ora.step(warmup)
+    t0 = time.perf_counter()
+    ora.step(1)
+    t1 = time.perf_counter()
+    done, el = 1, t1 - t0
+    target = steps if steps is not None else max(1, min(200, int(seconds / max(el, 1e-6))))
+    while done < target:
+        ora.step(1)
+        done += 1
+    el = time.perf_counter() - t0
+    dof = ora.K * ora.el.Np * 4 * 5
+    return dict(value=dof * done / el, unit=UNIT, cores=threads, kind="port", steps=done, seconds=el,
+                sample=f"{done} full SSP-RK steps of the same {ora.K}-element N={wl['N']} workload")
+
+
+# --------------------------------------------------------------------------- GPU arm
+def run_ours(a, world, rank, local):
+    import torch
+    import torch.distributed as dist
+    from gocfd_gb300.euler2d import Euler
+    from gocfd_gb300 import _lib
+
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    wl = WORKLOADS[a.workload]
+    mesh = make_mesh(wl)
+    ip = input_params(wl["N"])
+    solver = Euler(ip, mesh, 1, precision=a.precision, device=local, vortex_center=(0.0, 0.0))
+    K, Np, NE = solver.K, solver.Np, solver.NpEdge
+    dof_per_step = K * Np * 4 * 5
+    stream = torch.cuda.ExternalStream(solver.stream_handle(), device=torch.device("cuda", local))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    solver.enqueue_steps(a.warmup)
+    torch.cuda.synchronize()
+    solver.step(0)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    t_wall0 = time.monotonic()
+    with torch.cuda.stream(stream):
+        for i, (s, e) in enumerate(evs):
+            flush.fill_(float(i & 7))       # L2 flushed between timed steps (not timed)
+            s.record(stream)
+            solver.enqueue_steps(1)
+            e.record(stream)
+    torch.cuda.synchronize()
+    t_wall1 = time.monotonic()
+    barrier()
+    ms = float(sum(s.elapsed_time(e) for s, e in evs))
+    info = solver.step(0)  # raises on a non-finite state
+    clk = clocks.summary(t_wall0, t_wall1)
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * dof_per_step * a.steps / (ms / 1e3)
+
+    # Per-kernel attribution for the roofline (eager launches with events).
+    fam_ms, fam_n = [0.0] * 4, [0] * 4
+    for _ in range(5):
+        m, n = solver.profile_step()
+        fam_ms = [x + y for x, y in zip(fam_ms, m)]
+        fam_n = [x + y for x, y in zip(fam_n, n)]
+    tsz = 4 if a.precision == "fp32" else 8
+    names = ["k_interp", "k_edge_flux", "k_div_update", "k_step"]
+    dom = max(range(3), key=lambda i: fam_ms[i])
+    per_launch_ms = fam_ms[dom] / max(fam_n[dom], 1)
+    nE = solver.nEdges
+    nBC = 4 * WORKLOADS[a.workload]["n"]
+    nInt = nE - nBC
+    alg = algorithmic_bytes(dom, K, nInt, nBC, Np, NE, tsz)
+    peak, peak_kind = measured_peaks()
+    achieved = alg / (per_launch_ms / 1e3) / 1e9
+    tpe = ncu_traffic_per_element(names[dom], a.precision, wl["N"])
+    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": (tpe * K if tpe is not None else None),
+                "algorithmic_bytes": alg, "peak_source": peak_kind,
+                "avg_launch_us": per_launch_ms * 1e3,
+                "kernel_share": {names[i]: fam_ms[i] / max(sum(fam_ms), 1e-12) for i in range(4)}}
+
+    # FP64 drop-in path on the same workload (device-timed, no flush).
+    fp64 = None
+    if a.precision != "fp64" and a.fp64_steps > 0:
+        s64 = Euler(ip, mesh, 1, precision="fp64", device=local, vortex_center=(0.0, 0.0))
+        st64 = torch.cuda.ExternalStream(s64.stream_handle(), device=torch.device("cuda", local))
+        s64.enqueue_steps(2)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(st64):
+            e0.record(st64)
+            s64.enqueue_steps(a.fp64_steps)
+            e1.record(st64)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1)
+        s64.step(0)
+        fp64 = {"value": world * dof_per_step * a.fp64_steps / (ms64 / 1e3),
+                "ms_per_step": ms64 / a.fp64_steps, "steps": a.fp64_steps}
+        s64.close()
+
+    # End to end through the public API: pinned host state in, step, state out.
+    import torch as _t
+    host = [_t.empty((Np, K), dtype=_t.float64, pin_memory=True) for _ in range(4)]
+    hostn = [h.numpy() for h in host]
+    km = np.array([K], np.int32)
+    ptrs = (_lib.PD * 4)(*[h.ctypes.data_as(_lib.PD) for h in hostn])
+    lib = solver.lib
+    _lib.check(lib, solver.ctx, lib.gcfd_get_state(solver.ctx, 1, km.ctypes.data_as(_lib.PI), ptrs))
+    for _ in range(3):
+        _lib.check(lib, solver.ctx, lib.gcfd_set_state(solver.ctx, 1, km.ctypes.data_as(_lib.PI), ptrs))
+        _lib.check(lib, solver.ctx, lib.gcfd_step(solver.ctx, 1, None, None, None, None, None))
+        _lib.check(lib, solver.ctx, lib.gcfd_get_state(solver.ctx, 1, km.ctypes.data_as(_lib.PI), ptrs))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(a.e2e_steps):
+        _lib.check(lib, solver.ctx, lib.gcfd_set_state(solver.ctx, 1, km.ctypes.data_as(_lib.PI), ptrs))
+        _lib.check(lib, solver.ctx, lib.gcfd_step(solver.ctx, 1, None, None, None, None, None))
+        _lib.check(lib, solver.ctx, lib.gcfd_get_state(solver.ctx, 1, km.ctypes.data_as(_lib.PI), ptrs))
+    e2e_s = time.perf_counter() - t0
+    barrier()
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    state_bytes = 4 * Np * K * 8
+    e2e = {"value": world * dof_per_step * a.e2e_steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes,
+           "steps": a.e2e_steps, "api": "gcfd_set_state + gcfd_step + gcfd_get_state, pinned host shards"}
+    clocks.stop()
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu:
+        cpu = cpu_baseline(wl, mesh, a.cpu_seconds)
+    solver.close()
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": a.precision if a.precision == "fp64" else "fp32 (fp64 state/RK)",
+            "data": "synthetic (analytic isentropic-vortex initial condition on a generated mesh)",
+            "config": {"workload": a.workload, "description": wl["desc"], "K": K, "N": wl["N"], "Np": Np,
+                       "dof_updates_per_step": dof_per_step, "flux": "roe", "cfl": 1.0,
+                       "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (256 MB write)",
+                       "timing": "CUDA events per graph-launched step on the solver stream"},
+            "e2e": e2e,
+            "gpu_launches": 22 * a.steps,
+            "clocks": clk,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "fp64_path": fp64,
+            "final_time": info["time"],
+        }
+        if cpu:
+            out["us_per_element_step_cpu"] = 1e6 / (cpu["value"] / (Np * 4 * 5))
+        out["us_per_element_step"] = 1e6 * (ms / a.steps / 1e3) / K * world
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_reference(a, world, rank):
+    """The reference's CPU path, restated in C++ (the Go reference cannot be
+    built here), timed on all host cores with the same workload and metric."""
+    if rank != 0:
+        return
+    wl = WORKLOADS[a.workload]
+    mesh = make_mesh(wl)
+    r = cpu_baseline(wl, mesh, 0.0, steps=a.steps, warmup=a.warmup)
+    out = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world,
+           "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * r["seconds"] / r["steps"],
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+           "data": "synthetic (analytic isentropic-vortex initial condition on a generated mesh)",
+           "config": {"workload": a.workload, "description": wl["desc"], "N": wl["N"], "flux": "roe",
+                      "cfl": 1.0, "parallelism": "OpenMP over host cores"},
+           "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": "port",
+                            "sample": r["sample"]},
+           "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "note": "Go toolchain unavailable: the reference arm is the C++ FP64 restatement of its CPU path"}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    a = args_parse()
+    world, rank, local = dist_env()
+    if a.impl == "reference":
+        run_reference(a, world, rank)
+    else:
+        run_ours(a, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

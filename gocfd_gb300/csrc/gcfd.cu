@@ -1,0 +1,722 @@
+// libgcfd: device context, kernel launchers, per-step CUDA graph and the C ABI
+// declared in include/gcfd.h.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/gcfd.h"
+#include "dfr_element.hpp"
+#include "gcfd_kernels.cuh"
+#include "mesh.hpp"
+
+using namespace gcfd;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct HostFreeStream {
+  double qinf[4];
+  double pinf, cinf, gamma, minf;
+};
+
+// NewFreeStream (fluids.go:378-395).
+HostFreeStream freestream_from_mach(double minf, double gamma, double alpha) {
+  const double pi = 3.14159265358979323846;
+  HostFreeStream f;
+  const double ooggm1 = 1.0 / (gamma * (gamma - 1.0));
+  f.qinf[0] = 1.0;
+  f.qinf[1] = minf * std::cos(alpha * pi / 180.0);
+  f.qinf[2] = minf * std::sin(alpha * pi / 180.0);
+  f.qinf[3] = ooggm1 + 0.5 * minf * minf;
+  f.gamma = gamma;
+  f.minf = minf;
+  const double oorho = 1.0 / f.qinf[0];
+  const double u = f.qinf[1] * oorho, v = f.qinf[2] * oorho;
+  const double p = (gamma - 1.0) * (f.qinf[3] - 0.5 * f.qinf[0] * (u * u + v * v));
+  f.pinf = p;
+  f.cinf = std::sqrt(std::fabs(gamma * p * oorho));
+  return f;
+}
+
+// NewFreestreamFromQinf (fluids.go:397-406): Minf stays 0.
+HostFreeStream freestream_from_q(double gamma, const double q[4]) {
+  HostFreeStream f;
+  for (int n = 0; n < 4; ++n) f.qinf[n] = q[n];
+  f.gamma = gamma;
+  f.minf = 0.0;
+  const double oorho = 1.0 / q[0];
+  const double u = q[1] * oorho, v = q[2] * oorho;
+  const double p = (gamma - 1.0) * (q[3] - 0.5 * q[0] * (u * u + v * v));
+  f.pinf = p;
+  f.cinf = std::sqrt(std::fabs(gamma * p * oorho));
+  return f;
+}
+
+template <typename T>
+FreeStreamT<T> to_device_fs(const HostFreeStream& h) {
+  FreeStreamT<T> f;
+  for (int n = 0; n < 4; ++n) f.qinf[n] = static_cast<T>(h.qinf[n]);
+  f.pinf = static_cast<T>(h.pinf);
+  f.cinf = static_cast<T>(h.cinf);
+  f.gamma = static_cast<T>(h.gamma);
+  f.minf = static_cast<T>(h.minf);
+  return f;
+}
+
+}  // namespace
+
+struct gcfd_ctx {
+  std::string err;
+  gcfd_params prm{};
+  int N = 0, K = 0, Np = 0, NE = 0, NF = 0, nEdges = 0, nInt = 0, nBC = 0;
+  bool fp32 = false;
+  DFRElement el;
+  Topology topo;
+  Geometry geo;
+  HostFreeStream fsFar{}, fsIn{}, fsOut{};
+  double vbeta = 5.0, vx0 = 5.0, vy0 = 0.0, vgamma = 1.4;
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocs;
+  double* Q[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  double* R = nullptr;
+  double* Qtmp = nullptr;
+  double* rhsOut = nullptr;
+  void* QF = nullptr;
+  void* FE = nullptr;
+  double *Iop = nullptr, *Div = nullptr, *Jdet = nullptr, *Jinv = nullptr;
+  int *ekL = nullptr, *ekR = nullptr, *eLR = nullptr, *bcFlag = nullptr, *elemEdge = nullptr;
+  double *enx = nullptr, *eny = nullptr, *eIIL = nullptr, *eIIR = nullptr, *eoohK = nullptr;
+  double *bx = nullptr, *by = nullptr, *edgeSpeed = nullptr, *DT = nullptr;
+  Scalars* sc = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graphExec = nullptr;
+  cudaEvent_t ev[10] = {};
+  bool evReady = false;
+
+  ~gcfd_ctx() {
+    if (graphExec) cudaGraphExecDestroy(graphExec);
+    if (graph) cudaGraphDestroy(graph);
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    for (void* p : allocs) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+int fail(gcfd_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  else g_create_error = msg;
+  return code;
+}
+
+#define GCFD_CUDA(ctx, call)                                                               \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) {                                                               \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? GCFD_ERR_OOM : GCFD_ERR_CUDA,     \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                     \
+    }                                                                                      \
+  } while (0)
+
+template <typename P>
+int dalloc(gcfd_ctx* c, P** p, size_t count) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, count * sizeof(P) > 0 ? count * sizeof(P) : 16);
+  if (e != cudaSuccess)
+    return fail(c, e == cudaErrorMemoryAllocation ? GCFD_ERR_OOM : GCFD_ERR_CUDA,
+                std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  c->allocs.push_back(q);
+  *p = static_cast<P*>(q);
+  return GCFD_OK;
+}
+
+template <typename P>
+int upload(gcfd_ctx* c, P** p, const std::vector<P>& h) {
+  int rc = dalloc(c, p, h.size());
+  if (rc) return rc;
+  if (!h.empty()) GCFD_CUDA(c, cudaMemcpy(*p, h.data(), h.size() * sizeof(P), cudaMemcpyHostToDevice));
+  return GCFD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Launchers, one instantiation per (order, arithmetic type).
+template <int N, typename T>
+struct Launch {
+  static EdgeArgs<T> edge_args(gcfd_ctx* c, const double* time) {
+    EdgeArgs<T> a;
+    a.QF = static_cast<const T*>(c->QF);
+    a.FE = static_cast<T*>(c->FE);
+    a.K = c->K;
+    a.nInt = c->nInt;
+    a.nBC = c->nBC;
+    a.kL = c->ekL;
+    a.kR = c->ekR;
+    a.eLR = c->eLR;
+    a.nx = c->enx;
+    a.ny = c->eny;
+    a.IIL = c->eIIL;
+    a.IIR = c->eIIR;
+    a.oohK = c->eoohK;
+    a.bcFlag = c->bcFlag;
+    a.bx = c->bx;
+    a.by = c->by;
+    a.edgeSpeed = c->edgeSpeed;
+    a.gmax = nullptr;
+    a.time = time;
+    a.flux = c->prm.flux_type;
+    const double g = c->fsFar.gamma;
+    a.gas = Gas<T>{static_cast<T>(g), static_cast<T>(g - 1.0), static_cast<T>(1.0 / (g - 1.0))};
+    a.fsFar = to_device_fs<T>(c->fsFar);
+    a.fsIn = to_device_fs<T>(c->fsIn);
+    a.fsOut = to_device_fs<T>(c->fsOut);
+    a.vbeta = static_cast<T>(c->vbeta);
+    a.vx0 = static_cast<T>(c->vx0);
+    a.vy0 = static_cast<T>(c->vy0);
+    a.vgamma = static_cast<T>(c->vgamma);
+    return a;
+  }
+  static UpdateArgs<T> update_args(gcfd_ctx* c, int stage, const double* Qs) {
+    UpdateArgs<T> a;
+    a.K = c->K;
+    a.stage = stage;
+    a.Qs = Qs;
+    a.Q0 = c->Q[0];
+    a.Q1 = c->Q[1];
+    a.Q2 = c->Q[2];
+    a.Q3 = c->Q[3];
+    a.Q4 = c->Q[4];
+    a.R = c->R;
+    a.FE = static_cast<const T*>(c->FE);
+    a.Div = c->Div;
+    a.Jdet = c->Jdet;
+    a.Jinv = c->Jinv;
+    a.sc = c->sc;
+    a.cfl = c->prm.cfl;
+    a.finalTime = c->prm.final_time;
+    a.localDT = c->prm.local_time_stepping;
+    a.edgeSpeed = c->edgeSpeed;
+    a.elemEdge = c->elemEdge;
+    a.DT = c->DT;
+    a.rhsOut = c->rhsOut;
+    const double g = c->fsFar.gamma;
+    a.gas = Gas<T>{static_cast<T>(g), static_cast<T>(g - 1.0), static_cast<T>(1.0 / (g - 1.0))};
+    return a;
+  }
+  static int grid(int n) { return (n + 127) / 128; }
+
+  static void interp(gcfd_ctx* c, const double* Qs) {
+    k_interp<N, T><<<grid(c->K), 128, 0, c->stream>>>(Qs, static_cast<T*>(c->QF), c->Iop, c->K);
+  }
+  static void edge(gcfd_ctx* c, const double* time, unsigned long long* gmax) {
+    EdgeArgs<T> a = edge_args(c, time);
+    a.gmax = gmax;
+    k_edge_flux<N, T><<<grid(c->nInt + c->nBC), 128, 0, c->stream>>>(a);
+  }
+  static void update(gcfd_ctx* c, int stage, const double* Qs) {
+    k_div_update<N, T><<<grid(c->K), 128, 0, c->stream>>>(update_args(c, stage, Qs));
+  }
+  // One RK step: RungeKutta5SSP.Step (euler.go:408-418).
+  static void step(gcfd_ctx* c, cudaEvent_t* ev, double* ms, int* launches) {
+    auto mark = [&](int i) {
+      if (ev) cudaEventRecord(ev[i], c->stream);
+    };
+    auto acc = [&](int fam, int a, int b) {
+      if (!ev) return;
+      cudaEventSynchronize(ev[b]);
+      float t = 0.f;
+      cudaEventElapsedTime(&t, ev[a], ev[b]);
+      ms[fam] += t;
+      launches[fam] += 1;
+    };
+    mark(0);
+    k_step_begin<<<1, 32, 0, c->stream>>>(c->sc);
+    mark(1);
+    acc(3, 0, 1);
+    for (int s = 0; s < 5; ++s) {
+      mark(2);
+      interp(c, c->Q[s]);
+      mark(3);
+      edge(c, &c->sc->time, &c->sc->gmax[s]);
+      mark(4);
+      update(c, s, c->Q[s]);
+      mark(5);
+      acc(0, 2, 3);
+      acc(1, 3, 4);
+      acc(2, 4, 5);
+    }
+    mark(6);
+    k_step_end<<<1, 32, 0, c->stream>>>(c->sc, c->prm.local_time_stepping);
+    mark(7);
+    acc(3, 6, 7);
+  }
+  static void rhs(gcfd_ctx* c) {
+    interp(c, c->Qtmp);
+    edge(c, &c->sc->rhs_time, &c->sc->gmax[0]);
+    update(c, -1, c->Qtmp);
+  }
+};
+
+struct Ops {
+  void (*step)(gcfd_ctx*, cudaEvent_t*, double*, int*);
+  void (*rhs)(gcfd_ctx*);
+};
+
+template <int N>
+Ops ops_for(bool fp32) {
+  if (fp32) return Ops{&Launch<N, float>::step, &Launch<N, float>::rhs};
+  return Ops{&Launch<N, double>::step, &Launch<N, double>::rhs};
+}
+
+bool select_ops(int N, bool fp32, Ops* o) {
+  switch (N) {
+    case 0: *o = ops_for<0>(fp32); return true;
+    case 1: *o = ops_for<1>(fp32); return true;
+    case 2: *o = ops_for<2>(fp32); return true;
+    case 3: *o = ops_for<3>(fp32); return true;
+    case 4: *o = ops_for<4>(fp32); return true;
+    default: return false;
+  }
+}
+
+int capture_graph(gcfd_ctx* c) {
+  Ops o;
+  select_ops(c->N, c->fp32, &o);
+  GCFD_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  o.step(c, nullptr, nullptr, nullptr);
+  cudaGraph_t g = nullptr;
+  GCFD_CUDA(c, cudaStreamEndCapture(c->stream, &g));
+  c->graph = g;
+  GCFD_CUDA(c, cudaGraphInstantiate(&c->graphExec, g, 0));
+  return GCFD_OK;
+}
+
+int check_shards(gcfd_ctx* c, int nshards, const int32_t* Kmax) {
+  if (nshards <= 0 || !Kmax) return fail(c, GCFD_ERR_ARG, "nshards must be > 0 with Kmax given");
+  long long tot = 0;
+  for (int i = 0; i < nshards; ++i) {
+    if (Kmax[i] < 0) return fail(c, GCFD_ERR_SHAPE, "negative shard size");
+    tot += Kmax[i];
+  }
+  if (tot != c->K)
+    return fail(c, GCFD_ERR_SHAPE, "shard sizes sum to " + std::to_string(tot) + ", mesh has K=" +
+                                       std::to_string(c->K));
+  return GCFD_OK;
+}
+
+int copy_shards(gcfd_ctx* c, double* dst, int nshards, const int32_t* Kmax, const double* const* Q,
+                bool toDevice, double* const* Qout) {
+  const size_t pitch = static_cast<size_t>(c->K) * sizeof(double);
+  long long k0 = 0;
+  for (int np = 0; np < nshards; ++np) {
+    const size_t w = static_cast<size_t>(Kmax[np]) * sizeof(double);
+    if (w == 0) continue;
+    for (int n = 0; n < 4; ++n) {
+      double* d = dst + static_cast<size_t>(n) * c->Np * c->K + k0;
+      if (toDevice) {
+        if (!Q[np * 4 + n]) return fail(c, GCFD_ERR_ARG, "null state pointer");
+        GCFD_CUDA(c, cudaMemcpy2DAsync(d, pitch, Q[np * 4 + n], w, w, c->Np, cudaMemcpyHostToDevice,
+                                       c->stream));
+      } else {
+        if (!Qout[np * 4 + n]) return fail(c, GCFD_ERR_ARG, "null state pointer");
+        GCFD_CUDA(c, cudaMemcpy2DAsync(Qout[np * 4 + n], w, d, pitch, w, c->Np,
+                                       cudaMemcpyDeviceToHost, c->stream));
+      }
+    }
+    k0 += Kmax[np];
+  }
+  return GCFD_OK;
+}
+
+// Initial condition, InitializeSolution (euler.go:728-794).
+std::vector<double> initial_state(gcfd_ctx* c) {
+  const int K = c->K, Np = c->Np;
+  std::vector<double> q(static_cast<size_t>(4) * Np * K);
+  for (int i = 0; i < Np; ++i)
+    for (int k = 0; k < K; ++k) {
+      double s[4];
+      const size_t pt = static_cast<size_t>(i) * K + k;
+      if (c->prm.init_type == GCFD_INIT_IVORTEX) {
+        const double x = c->geo.xSol[pt], y = c->geo.ySol[pt];
+        const double pi = 3.14159265358979323846, g = c->vgamma, GM1 = g - 1.0;
+        double u = 1.0, v = 0.0;
+        const double r2 = (x - c->vx0) * (x - c->vx0) + (y - c->vy0) * (y - c->vy0);
+        const double ex1r = std::exp(1.0 - r2);
+        const double tv1 = 1.0 - (GM1 * c->vbeta * c->vbeta * std::exp(2.0 * (1.0 - r2)) / (16.0 * g * pi * pi));
+        u -= c->vbeta * ex1r * (y - c->vy0) * (0.5 / pi);
+        v += c->vbeta * ex1r * (x - c->vx0) * (0.5 / pi);
+        const double rho = std::pow(tv1, 1.0 / GM1), p = std::pow(rho, g);
+        s[0] = rho; s[1] = rho * u; s[2] = rho * v;
+        s[3] = p * (1.0 / GM1) + 0.5 * rho * (u * u + v * v);
+      } else if (c->prm.init_type == GCFD_INIT_SHOCKTUBE) {
+        const double* src = (c->geo.xSol[pt] < 0.5) ? c->fsIn.qinf : c->fsOut.qinf;
+        for (int n = 0; n < 4; ++n) s[n] = src[n];
+      } else {
+        for (int n = 0; n < 4; ++n) s[n] = c->fsFar.qinf[n];
+      }
+      for (int n = 0; n < 4; ++n) q[(static_cast<size_t>(n) * Np + i) * K + k] = s[n];
+    }
+  return q;
+}
+
+int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
+  const gcfd_params& p = c->prm;
+  c->N = p.N;
+  c->fp32 = (p.precision == GCFD_PREC_FP32);
+  try {
+    c->el = build_dfr_element(p.N);
+  } catch (const std::exception& e) {
+    return fail(c, GCFD_ERR_UNSUPPORTED, e.what());
+  }
+  c->Np = c->el.Np;
+  c->NE = c->el.NpEdge;
+  c->NF = c->el.NpFlux;
+  c->K = m->K;
+  std::string msg = build_topology(m->nverts, m->K, m->etov, m->nbc, m->bc_v1, m->bc_v2, m->bc_flag,
+                                   &c->topo);
+  if (!msg.empty()) return fail(c, GCFD_ERR_ARG, msg);
+  build_geometry(c->el, c->topo, m->vx, m->vy, m->etov, &c->geo);
+  for (int k = 0; k < c->K; ++k)
+    if (!(c->geo.Jdet[k] > 0.0))
+      return fail(c, GCFD_ERR_ARG, "element " + std::to_string(k) +
+                                       " is not counter-clockwise (|J| <= 0)");
+
+  // Free streams and BC relabelling of InitializeSolution (euler.go:728-794).
+  c->fsFar = freestream_from_mach(p.minf, p.gamma, p.alpha);
+  c->fsIn = c->fsFar;
+  c->fsOut = c->fsFar;
+  c->vx0 = p.vortex_x0;
+  c->vy0 = p.vortex_y0;
+  if (p.init_type == GCFD_INIT_IVORTEX) {
+    const double q[4] = {1, 1, 0, 3};
+    c->fsFar = freestream_from_q(1.4, q);
+    for (int& b : c->topo.bc)
+      if (b == BC_Wall) b = BC_IVortex;
+  } else if (p.init_type == GCFD_INIT_SHOCKTUBE) {
+    const double g = 1.4;
+    const double qi[4] = {1, 0, 0, 1 / (g - 1)}, qo[4] = {0.125, 0, 0, 0.1 / (g - 1)};
+    c->fsIn = freestream_from_q(g, qi);
+    c->fsOut = freestream_from_q(g, qo);
+  }
+
+  // Edge tables: interior edges first, then boundary edges, each in mesh order.
+  const Topology& t = c->topo;
+  const Geometry& g = c->geo;
+  std::vector<int> order;
+  for (int en = 0; en < t.nEdges; ++en)
+    if (t.kR[en] >= 0) order.push_back(en);
+  c->nInt = static_cast<int>(order.size());
+  for (int en = 0; en < t.nEdges; ++en)
+    if (t.kR[en] < 0) order.push_back(en);
+  c->nEdges = t.nEdges;
+  c->nBC = c->nEdges - c->nInt;
+  const int K = c->K, NE = c->NE, Np = c->Np;
+  std::vector<int> kL(c->nEdges), kR(c->nEdges), eLR(c->nEdges), flag(std::max(c->nBC, 1));
+  std::vector<double> nx(c->nEdges), ny(c->nEdges), IIL(c->nEdges), IIR(c->nEdges), oohK(c->nEdges);
+  std::vector<double> bx(static_cast<size_t>(std::max(c->nBC, 1)) * NE), by(bx.size());
+  std::vector<int> elemEdge(static_cast<size_t>(3) * K);
+  std::vector<int> pos(t.nEdges);
+  for (int i = 0; i < c->nEdges; ++i) {
+    const int en = order[i];
+    pos[en] = i;
+    kL[i] = t.kL[en];
+    kR[i] = t.kR[en] >= 0 ? t.kR[en] : 0;
+    eLR[i] = t.eL[en] | ((t.eR[en] >= 0 ? t.eR[en] : 0) << 2);
+    const size_t fl = static_cast<size_t>(t.eL[en]) * K + t.kL[en];
+    nx[i] = g.nx[fl];
+    ny[i] = g.ny[fl];
+    IIL[i] = g.IInII[fl];
+    IIR[i] = t.kR[en] >= 0 ? g.IInII[static_cast<size_t>(t.eR[en]) * K + t.kR[en]] : 0.0;
+    oohK[i] = 1.0 / g.hK[t.kL[en]];
+    if (i >= c->nInt) {
+      const int b = i - c->nInt;
+      flag[b] = t.bc[en];
+      for (int q = 0; q < NE; ++q) {
+        const size_t row = static_cast<size_t>(2 * Np + t.eL[en] * NE + q);
+        bx[static_cast<size_t>(b) * NE + q] = g.xFlux[row * K + t.kL[en]];
+        by[static_cast<size_t>(b) * NE + q] = g.yFlux[row * K + t.kL[en]];
+      }
+    }
+  }
+  for (int k = 0; k < K; ++k)
+    for (int ed = 0; ed < 3; ++ed)
+      elemEdge[static_cast<size_t>(ed) * K + k] = pos[t.elemEdge[3 * k + ed]];
+
+  GCFD_CUDA(c, cudaSetDevice(p.device));
+  GCFD_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  const size_t nState = static_cast<size_t>(4) * Np * K;
+  const size_t nFace = static_cast<size_t>(4) * 3 * NE * K;
+  const size_t tsz = c->fp32 ? sizeof(float) : sizeof(double);
+  int rc;
+  for (int s = 0; s < 5; ++s)
+    if ((rc = dalloc(c, &c->Q[s], nState))) return rc;
+  if ((rc = dalloc(c, &c->R, nState))) return rc;
+  if ((rc = dalloc(c, &c->Qtmp, nState))) return rc;
+  if ((rc = dalloc(c, &c->rhsOut, nState))) return rc;
+  {
+    char* qf = nullptr;
+    if ((rc = dalloc(c, &qf, nFace * tsz))) return rc;
+    c->QF = qf;
+    char* fe = nullptr;
+    if ((rc = dalloc(c, &fe, nFace * tsz))) return rc;
+    c->FE = fe;
+  }
+  if ((rc = upload(c, &c->Iop, c->el.FluxEdgeInterp.v))) return rc;
+  if ((rc = upload(c, &c->Div, c->el.DivInt.v))) return rc;
+  if ((rc = upload(c, &c->Jdet, g.Jdet))) return rc;
+  std::vector<double> jinvT(static_cast<size_t>(4) * K);
+  for (int k = 0; k < K; ++k)
+    for (int q = 0; q < 4; ++q) jinvT[static_cast<size_t>(q) * K + k] = g.Jinv[4 * k + q];
+  if ((rc = upload(c, &c->Jinv, jinvT))) return rc;
+  if ((rc = upload(c, &c->ekL, kL))) return rc;
+  if ((rc = upload(c, &c->ekR, kR))) return rc;
+  if ((rc = upload(c, &c->eLR, eLR))) return rc;
+  if ((rc = upload(c, &c->bcFlag, flag))) return rc;
+  if ((rc = upload(c, &c->elemEdge, elemEdge))) return rc;
+  if ((rc = upload(c, &c->enx, nx))) return rc;
+  if ((rc = upload(c, &c->eny, ny))) return rc;
+  if ((rc = upload(c, &c->eIIL, IIL))) return rc;
+  if ((rc = upload(c, &c->eIIR, IIR))) return rc;
+  if ((rc = upload(c, &c->eoohK, oohK))) return rc;
+  if ((rc = upload(c, &c->bx, bx))) return rc;
+  if ((rc = upload(c, &c->by, by))) return rc;
+  if ((rc = dalloc(c, &c->edgeSpeed, static_cast<size_t>(c->nEdges)))) return rc;
+  if ((rc = dalloc(c, &c->DT, static_cast<size_t>(K)))) return rc;
+  if ((rc = dalloc(c, &c->sc, 1))) return rc;
+  GCFD_CUDA(c, cudaMemset(c->sc, 0, sizeof(Scalars)));
+  GCFD_CUDA(c, cudaMemset(c->DT, 0, sizeof(double) * K));
+  GCFD_CUDA(c, cudaMemset(c->R, 0, sizeof(double) * nState));
+  std::vector<double> q0 = initial_state(c);
+  GCFD_CUDA(c, cudaMemcpy(c->Q[0], q0.data(), nState * sizeof(double), cudaMemcpyHostToDevice));
+  for (auto& e : c->ev) GCFD_CUDA(c, cudaEventCreate(&e));
+  if ((rc = capture_graph(c))) return rc;
+  GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GCFD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gcfd_create(const gcfd_mesh* mesh, const gcfd_params* params, gcfd_ctx** out) {
+  g_create_error.clear();
+  if (!mesh || !params || !out) return fail(nullptr, GCFD_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (mesh->K <= 0 || mesh->nverts < 3 || !mesh->vx || !mesh->vy || !mesh->etov)
+    return fail(nullptr, GCFD_ERR_ARG, "mesh needs K > 0, nverts >= 3 and vertex/element arrays");
+  if (mesh->nbc < 0 || (mesh->nbc > 0 && (!mesh->bc_v1 || !mesh->bc_v2 || !mesh->bc_flag)))
+    return fail(nullptr, GCFD_ERR_ARG, "boundary edge arrays missing");
+  if (params->N < 0 || params->N > 4)
+    return fail(nullptr, GCFD_ERR_UNSUPPORTED, "PolynomialOrder must be 0..4");
+  if (params->precision != GCFD_PREC_FP64 && params->precision != GCFD_PREC_FP32)
+    return fail(nullptr, GCFD_ERR_UNSUPPORTED, "unknown precision mode");
+  if (params->flux_type < 0 || params->flux_type > 3)
+    return fail(nullptr, GCFD_ERR_ARG, "unknown flux type");
+  if (params->init_type < 0 || params->init_type > 2)
+    return fail(nullptr, GCFD_ERR_ARG, "unknown init type");
+  if (params->limiter != GCFD_LIMITER_NONE)
+    return fail(nullptr, GCFD_ERR_UNSUPPORTED, "limiter not available in this build");
+  if (!(params->cfl > 0.0)) return fail(nullptr, GCFD_ERR_ARG, "CFL must be > 0");
+  std::unique_ptr<gcfd_ctx> c(new gcfd_ctx());
+  c->prm = *params;
+  int rc = build_context(c.get(), mesh);
+  if (rc != GCFD_OK) {
+    g_create_error = c->err;
+    return rc;
+  }
+  *out = c.release();
+  return GCFD_OK;
+}
+
+int gcfd_destroy(gcfd_ctx* ctx) {
+  if (!ctx) return GCFD_ERR_ARG;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  delete ctx;
+  return GCFD_OK;
+}
+
+const char* gcfd_last_error(const gcfd_ctx* ctx) {
+  return ctx ? ctx->err.c_str() : g_create_error.c_str();
+}
+
+int gcfd_dims(const gcfd_ctx* c, int32_t* K, int32_t* Np, int32_t* NpEdge, int32_t* NpFlux,
+              int32_t* nEdges) {
+  if (!c) return GCFD_ERR_ARG;
+  if (K) *K = c->K;
+  if (Np) *Np = c->Np;
+  if (NpEdge) *NpEdge = c->NE;
+  if (NpFlux) *NpFlux = c->NF;
+  if (nEdges) *nEdges = c->nEdges;
+  return GCFD_OK;
+}
+
+int gcfd_set_state(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const double* const* Q) {
+  if (!c || !Q) return c ? fail(c, GCFD_ERR_ARG, "null state") : GCFD_ERR_ARG;
+  int rc = check_shards(c, nshards, Kmax);
+  if (rc) return rc;
+  if ((rc = copy_shards(c, c->Q[0], nshards, Kmax, Q, true, nullptr))) return rc;
+  GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GCFD_OK;
+}
+
+int gcfd_get_state(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, double* const* Q) {
+  if (!c || !Q) return c ? fail(c, GCFD_ERR_ARG, "null state") : GCFD_ERR_ARG;
+  int rc = check_shards(c, nshards, Kmax);
+  if (rc) return rc;
+  if ((rc = copy_shards(c, c->Q[0], nshards, Kmax, nullptr, false, Q))) return rc;
+  GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GCFD_OK;
+}
+
+int gcfd_set_state_device(gcfd_ctx* c, const double* dQ) {
+  if (!c || !dQ) return c ? fail(c, GCFD_ERR_ARG, "null state") : GCFD_ERR_ARG;
+  GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], dQ, sizeof(double) * 4 * c->Np * static_cast<size_t>(c->K),
+                               cudaMemcpyDeviceToDevice, c->stream));
+  return GCFD_OK;
+}
+
+int gcfd_get_state_device(gcfd_ctx* c, double* dQ) {
+  if (!c || !dQ) return c ? fail(c, GCFD_ERR_ARG, "null state") : GCFD_ERR_ARG;
+  GCFD_CUDA(c, cudaMemcpyAsync(dQ, c->Q[0], sizeof(double) * 4 * c->Np * static_cast<size_t>(c->K),
+                               cudaMemcpyDeviceToDevice, c->stream));
+  return GCFD_OK;
+}
+
+int gcfd_set_time(gcfd_ctx* c, double time) {
+  if (!c) return GCFD_ERR_ARG;
+  GCFD_CUDA(c, cudaMemcpyAsync(&c->sc->time, &time, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GCFD_OK;
+}
+
+int gcfd_get_time(gcfd_ctx* c, double* time, int32_t* steps) {
+  if (!c) return GCFD_ERR_ARG;
+  Scalars h;
+  GCFD_CUDA(c, cudaMemcpyAsync(&h, c->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
+  GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (time) *time = h.time;
+  if (steps) *steps = h.steps;
+  return GCFD_OK;
+}
+
+int gcfd_rhs(gcfd_ctx* c, double time, int32_t nshards, const int32_t* Kmax, const double* const* Q,
+             double* const* RHS) {
+  if (!c || !Q || !RHS) return c ? fail(c, GCFD_ERR_ARG, "null state") : GCFD_ERR_ARG;
+  int rc = check_shards(c, nshards, Kmax);
+  if (rc) return rc;
+  if ((rc = copy_shards(c, c->Qtmp, nshards, Kmax, Q, true, nullptr))) return rc;
+  GCFD_CUDA(c, cudaMemcpyAsync(&c->sc->rhs_time, &time, sizeof(double), cudaMemcpyHostToDevice,
+                               c->stream));
+  Ops o;
+  select_ops(c->N, c->fp32, &o);
+  o.rhs(c);
+  GCFD_CUDA(c, cudaGetLastError());
+  if ((rc = copy_shards(c, c->rhsOut, nshards, Kmax, nullptr, false, RHS))) return rc;
+  GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GCFD_OK;
+}
+
+static double decode_order_key(unsigned long long k) {
+  const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
+  double d;
+  std::memcpy(&d, &b, sizeof(d));
+  return d;
+}
+
+int gcfd_step(gcfd_ctx* c, int32_t nsteps, double* time, double* dt_last, double* resid_max4,
+              double* resid_absmax4, double* resid_rms4) {
+  if (!c) return GCFD_ERR_ARG;
+  if (nsteps < 0) return fail(c, GCFD_ERR_ARG, "nsteps must be >= 0");
+  for (int i = 0; i < nsteps; ++i) GCFD_CUDA(c, cudaGraphLaunch(c->graphExec, c->stream));
+  Scalars h;
+  GCFD_CUDA(c, cudaMemcpyAsync(&h, c->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
+  GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (time) *time = h.time;
+  if (dt_last) *dt_last = h.dt[4];
+  bool finite = true;
+  const double cnt = static_cast<double>(c->Np) * c->K;
+  for (int n = 0; n < 4; ++n) {
+    double am;
+    std::memcpy(&am, &h.rabs[n], sizeof(am));
+    const double mx = decode_order_key(h.rmax[n]);
+    const double rms = std::sqrt(h.rsum2[n] / cnt);
+    if (resid_max4) resid_max4[n] = mx;
+    if (resid_absmax4) resid_absmax4[n] = am;
+    if (resid_rms4) resid_rms4[n] = rms;
+    if (nsteps > 0 && !(std::isfinite(am) && std::isfinite(rms))) finite = false;
+  }
+  if (!finite) return fail(c, GCFD_ERR_NAN, "non-finite RK increment (solution diverged)");
+  return GCFD_OK;
+}
+
+int gcfd_enqueue_steps(gcfd_ctx* c, int32_t nsteps) {
+  if (!c) return GCFD_ERR_ARG;
+  if (nsteps < 0) return fail(c, GCFD_ERR_ARG, "nsteps must be >= 0");
+  for (int i = 0; i < nsteps; ++i) GCFD_CUDA(c, cudaGraphLaunch(c->graphExec, c->stream));
+  return GCFD_OK;
+}
+
+int gcfd_get_stream(gcfd_ctx* c, void** stream) {
+  if (!c || !stream) return GCFD_ERR_ARG;
+  *stream = static_cast<void*>(c->stream);
+  return GCFD_OK;
+}
+
+int gcfd_profile_step(gcfd_ctx* c, double* kernel_ms4, int32_t* launches4) {
+  if (!c || !kernel_ms4 || !launches4) return GCFD_ERR_ARG;
+  double ms[4] = {0, 0, 0, 0};
+  int l[4] = {0, 0, 0, 0};
+  Ops o;
+  select_ops(c->N, c->fp32, &o);
+  o.step(c, c->ev, ms, l);
+  GCFD_CUDA(c, cudaGetLastError());
+  GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < 4; ++i) {
+    kernel_ms4[i] = ms[i];
+    launches4[i] = l[i];
+  }
+  return GCFD_OK;
+}
+
+int gcfd_host_operator(int32_t N, int32_t which, double* out, int32_t* rows, int32_t* cols) {
+  DFRElement e;
+  try {
+    e = build_dfr_element(N);
+  } catch (const std::exception& ex) {
+    g_create_error = ex.what();
+    return GCFD_ERR_UNSUPPORTED;
+  }
+  const DMat* m = nullptr;
+  DMat tmp;
+  switch (which) {
+    case 0: m = &e.FluxEdgeInterp; break;
+    case 1: m = &e.DivInt; break;
+    case 2: m = &e.Div; break;
+    case 3: m = &e.V; break;
+    case 4:
+      tmp = DMat(e.Np, 2);
+      for (int i = 0; i < e.Np; ++i) { tmp(i, 0) = e.r[i]; tmp(i, 1) = e.s[i]; }
+      m = &tmp;
+      break;
+    case 5:
+      tmp = DMat(e.NpFlux, 2);
+      for (int i = 0; i < e.NpFlux; ++i) { tmp(i, 0) = e.rFlux[i]; tmp(i, 1) = e.sFlux[i]; }
+      m = &tmp;
+      break;
+    default: return GCFD_ERR_ARG;
+  }
+  if (rows) *rows = m->rows;
+  if (cols) *cols = m->cols;
+  if (out) std::memcpy(out, m->v.data(), m->v.size() * sizeof(double));
+  return GCFD_OK;
+}
+
+}  // extern "C"

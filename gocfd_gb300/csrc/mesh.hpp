@@ -1,0 +1,60 @@
+// Host-side mesh topology and FP64 geometry for the DFR solver (set-up time).
+//
+// Reference behaviour followed (gocfd):
+//   DG2D/triangulation.go:19-171   edge creation per element (edges v0v1, v1v2, v2v0),
+//                                  first connected triangle = "left", orientation flag,
+//                                  ||n|| scale factor IInII per connection
+//   types/elemental.go:12-46       EdgeKey = min | max<<32, GetVertices(rev)
+//   DG2D/triangulation.go:230-235  GetEdgeCoordinates, oriented for outward normals
+//   DG2D/dfr_startup.go:89-98,125-147,256-314  hK, EdgeLenMax, Jacobian, face normals
+//   DG2D/element_utils.go:163-175  CalculateElementLocalGeometry (x,y of points)
+//   types/cfd.go:11-26             BCFLAG numbering
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "dfr_element.hpp"
+
+namespace gcfd {
+
+enum BCFlag : int {
+  BC_None = 0,
+  BC_In = 1,
+  BC_Dirichlet = 2,
+  BC_Slip = 3,
+  BC_Far = 4,
+  BC_Wall = 5,
+  BC_Cyl = 6,
+  BC_Neuman = 7,
+  BC_Out = 8,
+  BC_IVortex = 9,
+  BC_Periodic = 10,
+  BC_PeriodicReversed = 11,
+};
+
+struct Topology {
+  int K = 0, Nv = 0, nEdges = 0;
+  std::vector<uint64_t> key;            // packed vertex pair
+  std::vector<int> kL, eL, kR, eR;      // kR = eR = -1 on boundary edges
+  std::vector<uint8_t> revL, revR;      // traversal direction flag per connection
+  std::vector<int> bc;                  // BCFlag per edge
+  std::vector<int> elemEdge;            // K*3: edge index of (k, local edge)
+};
+
+struct Geometry {
+  std::vector<double> J, Jinv, Jdet;    // K*4 [xr xs yr ys], K*4 [ys -xs -yr xr]/|J|, K
+  std::vector<double> nx, ny, IInII;    // 3*K, index e*K + k (outward unit normal, ||n||)
+  std::vector<double> edgeLenMax, hK;   // K
+  std::vector<double> xFlux, yFlux;     // NpFlux*K, row-major (point, element)
+  std::vector<double> xSol, ySol;       // Np*K
+};
+
+// Builds the edge table.  Returns an empty string on success, else a message.
+std::string build_topology(int Nv, int K, const int32_t* etov, int nbc, const int32_t* bc_v1,
+                           const int32_t* bc_v2, const int32_t* bc_flag, Topology* topo);
+
+void build_geometry(const DFRElement& el, const Topology& topo, const double* vx,
+                    const double* vy, const int32_t* etov, Geometry* geo);
+
+}  // namespace gcfd

@@ -1,0 +1,156 @@
+/*
+ * libgcfd - GB300 (sm_103a) implementation of gocfd's 2D Euler Direct Flux
+ * Reconstruction right-hand side and 5-stage SSP Runge-Kutta step.
+ *
+ * Plain C ABI: pointers, sizes and int status codes only, so the Go driver
+ * binds it with cgo and Python with ctypes.  Every entry point returns
+ * GCFD_OK (0) or a negative GCFD_ERR_* code; gcfd_last_error() gives the
+ * message for the context (or for a failed gcfd_create, with ctx == NULL).
+ *
+ * State layout (the drop-in contract of model_problems/Euler2D/euler.go:47):
+ * the solution is sharded by contiguous element ranges; shard np holds four
+ * row-major Np x Kmax[np] matrices (rho, rhoU, rhoV, E), element index
+ * fastest (ind = k + i*Kmax, euler.go:513-516).  Shards cover the global
+ * elements in order, as utils.PartitionMap.Split1D lays them out
+ * (utils/parallel_utils.go:172-192).  Host arrays are only read or written
+ * during a call; the library never keeps a caller pointer.
+ *
+ * Threading: one context is used by one host thread at a time.  Separate
+ * contexts own separate CUDA streams and may be used concurrently.
+ */
+#ifndef GCFD_H_
+#define GCFD_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GCFD_OK 0
+#define GCFD_ERR_ARG (-1)
+#define GCFD_ERR_SHAPE (-2)
+#define GCFD_ERR_CUDA (-3)
+#define GCFD_ERR_NAN (-4)
+#define GCFD_ERR_TIMEOUT (-5)
+#define GCFD_ERR_OOM (-6)
+#define GCFD_ERR_UNSUPPORTED (-7)
+
+/* Flux names of model_problems/Euler2D/fluxes.go:18-33. */
+enum { GCFD_FLUX_AVERAGE = 0, GCFD_FLUX_LAX = 1, GCFD_FLUX_ROE = 2, GCFD_FLUX_ROE_ER = 3 };
+/* Init names of model_problems/Euler2D/initialization.go:22-31. */
+enum { GCFD_INIT_FREESTREAM = 0, GCFD_INIT_IVORTEX = 1, GCFD_INIT_SHOCKTUBE = 2 };
+/* Limiter names of model_problems/Euler2D/filter.go:10-23. */
+enum { GCFD_LIMITER_NONE = 0, GCFD_LIMITER_PERSSON_C0 = 1 };
+/* Arithmetic of the RHS.  FP64 is the drop-in; the others keep the conserved
+ * state, the RK accumulation and the residual norms in FP64. */
+enum { GCFD_PREC_FP64 = 0, GCFD_PREC_FP32 = 1 };
+/* BC flags, numbered as types.BCFLAG (types/cfd.go:11-26). */
+enum {
+  GCFD_BC_NONE = 0, GCFD_BC_IN = 1, GCFD_BC_FAR = 4, GCFD_BC_WALL = 5, GCFD_BC_CYL = 6,
+  GCFD_BC_OUT = 8, GCFD_BC_IVORTEX = 9
+};
+
+/* Triangle mesh as readfiles.ReadGambit2d / ReadSU2 return it
+ * (readfiles/readGambitGrid.go:21, readfiles/readSU2Grid.go:156): vertex
+ * coordinates, 0-based element-to-vertex table, and the tagged boundary edges
+ * flattened to (v1, v2, flag) triples. */
+typedef struct {
+  int32_t nverts;
+  const double* vx;
+  const double* vy;
+  int32_t K;
+  const int32_t* etov; /* K x 3 */
+  int32_t nbc;
+  const int32_t* bc_v1;
+  const int32_t* bc_v2;
+  const int32_t* bc_flag;
+} gcfd_mesh;
+
+/* The solver inputs of InputParameters.InputParameters2D
+ * (InputParameters/InputParameters.go:11-28) plus the arithmetic mode. */
+typedef struct {
+  int32_t N;          /* PolynomialOrder, 0..4 */
+  double cfl;         /* CFL */
+  double final_time;  /* FinalTime */
+  double minf;        /* Minf */
+  double gamma;       /* Gamma */
+  double alpha;       /* Alpha, degrees */
+  double kappa;       /* Kappa (shock finder) */
+  int32_t max_iterations;
+  int32_t flux_type;  /* GCFD_FLUX_* */
+  int32_t init_type;  /* GCFD_INIT_* */
+  int32_t limiter;    /* GCFD_LIMITER_* */
+  int32_t local_time_stepping;
+  int32_t precision;  /* GCFD_PREC_* */
+  double vortex_x0, vortex_y0; /* IVORTEX centre; the reference hard-codes (5,0) */
+  int32_t device;     /* CUDA device ordinal */
+} gcfd_params;
+
+typedef struct gcfd_ctx gcfd_ctx;
+
+/* Replaces Euler2D.NewEuler (model_problems/Euler2D/euler.go:61-136): builds
+ * the DFR operators and FP64 geometry on the host, uploads them, sets the
+ * initial condition (InitializeSolution, euler.go:728-794) on the device and
+ * records the per-step CUDA graph. */
+int gcfd_create(const gcfd_mesh* mesh, const gcfd_params* params, gcfd_ctx** out);
+int gcfd_destroy(gcfd_ctx* ctx);
+const char* gcfd_last_error(const gcfd_ctx* ctx);
+
+/* Sizes: elements, solution points, edge points, RT flux points, mesh edges. */
+int gcfd_dims(const gcfd_ctx* ctx, int32_t* K, int32_t* Np, int32_t* NpEdge, int32_t* NpFlux,
+              int32_t* nEdges);
+
+/* Copy the sharded state in / out (c.Q of euler.go:47).  Q[np*4 + n] points at
+ * shard np's Np x Kmax[np] matrix of variable n. */
+int gcfd_set_state(gcfd_ctx* ctx, int32_t nshards, const int32_t* Kmax, const double* const* Q);
+int gcfd_get_state(gcfd_ctx* ctx, int32_t nshards, const int32_t* Kmax, double* const* Q);
+/* The same for a device-resident contiguous 4 x Np x K FP64 array. */
+int gcfd_set_state_device(gcfd_ctx* ctx, const double* dQ);
+int gcfd_get_state_device(gcfd_ctx* ctx, double* dQ);
+
+/* Solver time (RungeKutta5SSP.Time, euler.go:332) and step counter. */
+int gcfd_set_time(gcfd_ctx* ctx, double time);
+int gcfd_get_time(gcfd_ctx* ctx, double* time, int32_t* steps);
+
+/* One right-hand-side evaluation at `time` (BC time), replacing the chain
+ * SetRTFluxInternal -> InterpolateSolutionToEdges -> CalculateEdgeEulerFlux ->
+ * SetRTFluxOnEdges -> RHSInternalPoints (euler.go:665-726, edges.go:325-488)
+ * as the reference tests compose it (euler_test.go:202-222).  Does not change
+ * the solver state. */
+int gcfd_rhs(gcfd_ctx* ctx, double time, int32_t nshards, const int32_t* Kmax,
+             const double* const* Q, double* const* RHS);
+
+/* Advance nsteps RK steps, replacing RungeKutta5SSP.Step (euler.go:408-418)
+ * together with the Time += GlobalDT update of Solve (euler.go:180).  Returns
+ * the time, the last global dt, and per variable the signed max of the final
+ * stage increment R (the reference's printed residual, euler.go:814-849), its
+ * max |R| and its RMS.  Any output pointer may be NULL.  GCFD_ERR_NAN when the
+ * increment is not finite. */
+int gcfd_step(gcfd_ctx* ctx, int32_t nsteps, double* time, double* dt_last, double* resid_max4,
+              double* resid_absmax4, double* resid_rms4);
+
+/* Enqueue nsteps RK steps on the context's stream and return without waiting
+ * (the asynchronous form of gcfd_step; read results with gcfd_step(ctx, 0, ...)
+ * or gcfd_get_state, which synchronise). */
+int gcfd_enqueue_steps(gcfd_ctx* ctx, int32_t nsteps);
+
+/* The CUDA stream (cudaStream_t) all work of the context is ordered on. */
+int gcfd_get_stream(gcfd_ctx* ctx, void** stream);
+
+/* Run one step launch by launch with CUDA events around each kernel and
+ * return the summed device time per kernel family (ms): [0] face
+ * interpolation, [1] edge flux + BCs, [2] divergence + RK update, [3] step
+ * bookkeeping.  Used to attribute time for the roofline. */
+int gcfd_profile_step(gcfd_ctx* ctx, double* kernel_ms4, int32_t* launches4);
+
+/* Host-only (no GPU needed): the FP64 operator matrices built for order N.
+ * which: 0 FluxEdgeInterp (3NpEdge x Np), 1 DivInt (Np x NpFlux),
+ * 2 Div (NpFlux x NpFlux), 3 V (Np x Np), 4 solution r,s (Np x 2),
+ * 5 flux-point r,s (NpFlux x 2).  With out == NULL only rows/cols are set. */
+int gcfd_host_operator(int32_t N, int32_t which, double* out, int32_t* rows, int32_t* cols);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GCFD_H_ */

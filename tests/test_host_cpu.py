@@ -1,0 +1,139 @@
+"""CPU tests of the product's host side: the C-ABI library loads and exports
+every symbol of include/gcfd.h, its FP64 operators match the oracle's
+independent construction and the reference's exactness tests, and the host
+mirror of the Euler2D interface (inputs, partitions, meshes) behaves as the
+reference's.  No GPU compute."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, fixture
+import dfr_ops
+from gocfd_gb300 import _lib, meshes
+from gocfd_gb300.euler2d import InputParameters2D, PartitionMap, set_parallel_degree
+from test_oracle_known_answers import equilateral_triangle, rt_divergence_check
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "gcfd.h")).read()
+    return sorted(set(re.findall(r"\b(gcfd_[a-z_0-9]+)\s*\(", txt)))
+
+
+def test_library_exports_every_header_symbol():
+    lib = _lib.load()
+    syms = header_symbols()
+    assert len(syms) >= 14
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert sorted(_lib.EXPORTS) == syms
+
+
+@pytest.mark.parametrize("N", range(5))
+def test_product_operators_match_oracle(N):
+    el = dfr_ops.build_element(N)
+    I = _lib.host_operator(N, 0)
+    D = _lib.host_operator(N, 1)
+    Div = _lib.host_operator(N, 2)
+    V = _lib.host_operator(N, 3)
+    rs = _lib.host_operator(N, 4)
+    RS = _lib.host_operator(N, 5)
+    assert I.shape == el.FluxEdgeInterp.shape and D.shape == el.DivInt.shape
+    assert np.allclose(rs[:, 0], el.r, atol=1e-15) and np.allclose(rs[:, 1], el.s, atol=1e-15)
+    assert np.allclose(RS[:, 0], el.R, atol=1e-15) and np.allclose(RS[:, 1], el.S, atol=1e-15)
+    assert np.abs(V - el.V).max() < 1e-12
+    assert np.abs(I - el.FluxEdgeInterp).max() < 1e-12
+    scale = np.abs(el.Div).max()
+    # Two constructions of the same RT divergence (different bases): agree to
+    # round-off amplified by the conditioning of the point set.
+    assert np.abs(D - el.DivInt).max() <= 1e-12 * scale * 10 ** (N == 1) * 10 ** (N == 4)
+    assert np.abs(Div - el.Div).max() <= 1e-12 * scale * 10 ** (N == 1) * 10 ** (N == 4)
+
+
+@pytest.mark.parametrize("angle", [0, 25, 90, 210, 310])
+def test_product_rt_divergence_exact(angle):
+    el = dfr_ops.build_element(4)
+    Div = _lib.host_operator(4, 2)
+    VX, VY, EToV = equilateral_triangle(angle)
+    geo = dfr_ops.build_geometry(el, VX, VY, EToV, [])
+    rt_divergence_check(Div, el, geo)
+
+
+def test_unsupported_order_is_an_error():
+    with pytest.raises(_lib.GcfdError):
+        _lib.host_operator(9, 0)
+
+
+def test_input_parameters_parse():
+    txt = """Title: "Test Case"
+CFL: 4.00
+FluxType: Roe
+InitType: IVortex # Can be "Freestream" or "IVortex"
+PolynomialOrder: 2
+FinalTime: 200
+MaxIterations: 10000
+Limiter: persson c0
+Kappa: 5
+LocalTimeStepping: true
+PlotFields: [ "mach", "density" ]
+"""
+    ip = InputParameters2D.parse(txt)
+    assert ip.CFL == 4.0 and ip.FluxType == "Roe" and ip.InitType == "IVortex"
+    assert ip.PolynomialOrder == 2 and ip.FinalTime == 200 and ip.MaxIterations == 10000
+    assert ip.Limiter == "persson c0" and ip.Kappa == 5 and ip.LocalTimeStepping is True
+    assert ip.PlotFields == ["mach", "density"]
+    assert ip.Gamma == 1.4 and ip.Minf == 0.1  # CLI defaults
+
+
+@pytest.mark.parametrize("nb,K", [(1, 10), (3, 10), (7, 100), (16, 131072), (5, 3)])
+def test_partition_map_split1d(nb, K):
+    pm = PartitionMap(nb, K)
+    sizes = [pm.bucket_dimension(i) for i in range(nb)]
+    assert sum(sizes) == K and max(sizes) - min(sizes) <= 1
+    assert pm.Partitions[0][0] == 0 and pm.Partitions[-1][1] == K
+    for a, b in zip(pm.Partitions[:-1], pm.Partitions[1:]):
+        assert a[1] == b[0]
+    rem = K % nb
+    assert all(s == K // nb + 1 for s in sizes[:rem])
+
+
+def test_set_parallel_degree():
+    assert set_parallel_degree(4, 100).ParallelDegree == 4
+    assert set_parallel_degree(10, 5).ParallelDegree == 1
+    assert set_parallel_degree(0, 185 * 1000).ParallelDegree == max(os.cpu_count(), 1000)
+
+
+def test_mesh_readers_on_reference_fixtures():
+    m = meshes.read_mesh(fixture("test_tris_6_nowall.neu"))
+    assert m.K == 2 and len(m.VX) == 4 and list(m.EToV[1]) == [0, 2, 3]
+    m = meshes.read_mesh(fixture("fstepA001.neu"))
+    assert m.K == 381 and {k: len(v) for k, v in m.bc_tags.items()} == {"wall": 55, "inflow": 8, "outflow": 8}
+    m = meshes.read_mesh(fixture("vortex-new.su2"))
+    assert m.K == 2402 and len(m.VX) == 1267
+    with pytest.raises(ValueError):
+        meshes.read_mesh("mesh.msh")
+
+
+def test_structured_mesh_is_ccw_and_roundtrips(tmp_path):
+    m = meshes.vortex_box(6, jitter=0.1, seed=3)
+    v = m.EToV
+    x, y = m.VX, m.VY
+    area = (x[v[:, 1]] - x[v[:, 0]]) * (y[v[:, 2]] - y[v[:, 0]]) - (x[v[:, 2]] - x[v[:, 0]]) * (y[v[:, 1]] - y[v[:, 0]])
+    assert (area > 0).all() and m.K == 72 and len(m.bc_edges) == 24
+    p = tmp_path / "box.neu"
+    meshes.write_gambit(m, str(p))
+    m2 = meshes.read_gambit(str(p))
+    assert np.allclose(m.VX, m2.VX, atol=1e-10) and (m.EToV == m2.EToV).all()
+    assert sorted(m.bc_edges) == sorted(m2.bc_edges)
+    w = meshes.wedge_channel(16, 8)
+    v = w.EToV
+    area = (w.VX[v[:, 1]] - w.VX[v[:, 0]]) * (w.VY[v[:, 2]] - w.VY[v[:, 0]]) - (w.VX[v[:, 2]] - w.VX[v[:, 0]]) * (w.VY[v[:, 1]] - w.VY[v[:, 0]])
+    assert (area > 0).all()
+
+
+def test_bc_tag_parsing():
+    assert meshes.bc_flag("Wall-top") == 5 and meshes.bc_flag("far") == 4
+    assert meshes.bc_flag("inflow") == 1 and meshes.bc_flag("Outflow") == 8
+    with pytest.raises(ValueError):
+        meshes.bc_flag("bogus")
