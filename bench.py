@@ -57,6 +57,9 @@ def args_parse():
     p.add_argument("--e2e-steps", type=int, default=50)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--accuracy", type=int, default=0,
+                   help="instead of timing: run this many steps in FP64 and FP32 and report the "
+                        "relative L2 differences and the errors against the exact vortex")
     return p.parse_args()
 
 
@@ -152,19 +155,32 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def algorithmic_bytes(family, K, nInt, nBC, Np, NE, tsz):
-    """Algorithmic DRAM bytes per launch of each kernel family (each array
-    touched once).  S = state bytes per element (FP64), faces/edge DOFs in T."""
-    S = 4 * Np * 8
-    F = 4 * 3 * NE * tsz
-    if family == 0:   # face interpolation: read state, write faces
-        return K * (S + F)
-    if family == 1:   # edge flux: read both sides' faces, write both sides' DOFs, edge data
-        per_int = 2 * (4 * NE * tsz) * 2 + 6 * 8 + 3 * 4
-        per_bc = 2 * (4 * NE * tsz) + 6 * 8 + 3 * 4 + 2 * NE * 8
+def algorithmic_bytes(family, K, nInt, nBC, Np, NE, precision):
+    """Algorithmic DRAM bytes per launch of each kernel family, every array
+    touched once.  FP64 path: state S8 = 4*Np*8 B per element, faces and edge
+    DOFs per element F8 = 4*3*NpEdge*8 B.  Mixed path: FP32 stage increments
+    S4 = 4*Np*4, edge-major faces/fluxes in FP32; the 5 stage launches are
+    averaged (their traffic differs by stage)."""
+    S8, S4 = 4 * Np * 8, 4 * Np * 4
+    if precision == "fp64":
+        F = 4 * 3 * NE * 8
+        if family == 0:   # k_interp: read state, write faces
+            return K * (S8 + F)
+        if family == 1:   # k_edge_flux: both sides' faces in, both sides' DOFs out, edge data
+            return nInt * (4 * (4 * NE * 8) + 60) + nBC * (2 * (4 * NE * 8) + 60 + 2 * NE * 8)
+        if family == 2:   # k_div_update: 19 state passes over the 5 stages + FE + geometry
+            return K * (19 * S8 + 5 * (F + 40)) / 5.0
+        return 0.0
+    F = 3 * 4 * NE * 4      # one element's faces (or fluxes) over its 3 edges
+    G = 112                 # slots, IInII, Jacobian, reference state in/out
+    if family == 0:         # k_mixed_prepare: Q0 in, dQ0 + faces + reference state out
+        return K * (S8 + S4 + F + 32)
+    if family == 1:         # interior edges: 2 sides' faces + 2 reference states in, fhat + corr + speed out
+        per_int = 2 * 4 * NE * 4 + 64 + 20 + 4 * NE * 4 + 16 + 8
+        per_bc = 4 * NE * 4 + 32 + 20 + 2 * NE * 8 + 4 * NE * 4 + 8
         return nInt * per_int + nBC * per_bc
-    if family == 2:   # div + RK update, averaged over the 5 stages: 19 state passes in total
-        return K * (19 * S + 5 * (F + 40)) / 5.0
+    if family == 2:         # k_mixed_stage over the 5 stages: 18 S4 + 2 S8 + 10 F + 5 (G + corr)
+        return K * (18 * S4 + 2 * S8 + 10 * F + 5 * (G + 48)) / 5.0
     return 0.0
 
 
@@ -259,6 +275,8 @@ def run_ours(a, world, rank, local):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = world * dof_per_step * a.steps / (ms / 1e3)
+    nBC_mesh = 4 * wl["n"]
+    launches_per_step = 2 + 5 * (3 if a.precision == "fp64" else (2 + (nBC_mesh > 0)))
 
     # Per-kernel attribution for the roofline (eager launches with events).
     fam_ms, fam_n = [0.0] * 4, [0] * 4
@@ -266,14 +284,18 @@ def run_ours(a, world, rank, local):
         m, n = solver.profile_step()
         fam_ms = [x + y for x, y in zip(fam_ms, m)]
         fam_n = [x + y for x, y in zip(fam_n, n)]
-    tsz = 4 if a.precision == "fp32" else 8
-    names = ["k_interp", "k_edge_flux", "k_div_update", "k_step"]
+    if a.precision == "fp32":  # the preparation is not part of a graph step
+        fam_ms[0], fam_n[0] = 0.0, 0
+    if a.precision == "fp32":
+        names = ["k_mixed_prepare", "k_mixed_edge", "k_mixed_stage", "k_step"]
+    else:
+        names = ["k_interp", "k_edge_flux", "k_div_update", "k_step"]
     dom = max(range(3), key=lambda i: fam_ms[i])
     per_launch_ms = fam_ms[dom] / max(fam_n[dom], 1)
     nE = solver.nEdges
     nBC = 4 * WORKLOADS[a.workload]["n"]
     nInt = nE - nBC
-    alg = algorithmic_bytes(dom, K, nInt, nBC, Np, NE, tsz)
+    alg = algorithmic_bytes(dom, K, nInt, nBC, Np, NE, a.precision)
     peak, peak_kind = measured_peaks()
     achieved = alg / (per_launch_ms / 1e3) / 1e9
     tpe = ncu_traffic_per_element(names[dom], a.precision, wl["N"])
@@ -347,7 +369,7 @@ def run_ours(a, world, rank, local):
                        "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (256 MB write)",
                        "timing": "CUDA events per graph-launched step on the solver stream"},
             "e2e": e2e,
-            "gpu_launches": 22 * a.steps,
+            "gpu_launches": launches_per_step * a.steps,
             "clocks": clk,
             "roofline": roofline,
             "cpu_baseline": cpu,
@@ -360,6 +382,61 @@ def run_ours(a, world, rank, local):
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def exact_vortex_error(solver, t, vortex=(5.0, 0.0, 0.0, 1.4)):
+    """Relative L2 (over all points and variables) of the state against the
+    exact isentropic vortex translated to time t, at the solution points."""
+    import math
+    g = solver
+    beta, x0, y0, gamma = vortex
+    Q = g.get_global_state()
+    xs, ys = solution_points_xy(g)
+    GM1 = gamma - 1.0
+    xm, ym = xs - t, ys
+    r2 = (xm - x0) ** 2 + (ym - y0) ** 2
+    ex1r = np.exp(1 - r2)
+    u = 1.0 - beta * ex1r * (ym - y0) / (2 * math.pi)
+    v = beta * ex1r * (xm - x0) / (2 * math.pi)
+    rho = (1.0 - GM1 * beta * beta * np.exp(2 * (1 - r2)) / (16 * gamma * math.pi ** 2)) ** (1 / GM1)
+    p = rho ** gamma
+    ex = np.stack([rho, rho * u, rho * v, p / GM1 + 0.5 * rho * (u * u + v * v)])
+    return float(np.linalg.norm(Q - ex) / np.linalg.norm(ex))
+
+
+def solution_points_xy(g):
+    from gocfd_gb300 import _lib
+    rs = _lib.host_operator(g.ip.PolynomialOrder, 4)
+    v = g.mesh.EToV
+    VX, VY = g.mesh.VX, g.mesh.VY
+    r, s = rs[:, 0:1], rs[:, 1:2]
+    X = 0.5 * (-(r + s) * VX[v[:, 0]][None] + (r + 1) * VX[v[:, 1]][None] + (s + 1) * VX[v[:, 2]][None])
+    Y = 0.5 * (-(r + s) * VY[v[:, 0]][None] + (r + 1) * VY[v[:, 1]][None] + (s + 1) * VY[v[:, 2]][None])
+    return X, Y
+
+
+def run_accuracy(a, local):
+    import torch
+    from gocfd_gb300.euler2d import Euler
+    torch.cuda.set_device(local)
+    wl = WORKLOADS[a.workload]
+    mesh = make_mesh(wl)
+    ip = input_params(wl["N"])
+    res = {"workload": a.workload, "steps": a.accuracy}
+    states = {}
+    for prec in ("fp64", "fp32"):
+        s = Euler(ip, mesh, 1, precision=prec, device=local, vortex_center=(0.0, 0.0))
+        info = s.step(a.accuracy)
+        states[prec] = s.get_global_state()
+        res[prec] = {"time": info["time"], "rel_l2_vs_exact": exact_vortex_error(s, info["time"]),
+                     "resid_rms": info["resid_rms"]}
+        s.close()
+    d = states["fp32"] - states["fp64"]
+    res["fp32_vs_fp64_rel_l2"] = float(np.linalg.norm(d) / np.linalg.norm(states["fp64"]))
+    res["fp32_vs_fp64_rel_linf"] = float(np.abs(d).max() / np.abs(states["fp64"]).max())
+    res["fp32_vs_fp64_rel_l2_per_var"] = [float(np.linalg.norm(d[n]) / np.linalg.norm(states["fp64"][n]))
+                                         for n in range(4)]
+    print(json.dumps(res), flush=True)
 
 
 def run_reference(a, world, rank):
@@ -386,7 +463,9 @@ def run_reference(a, world, rank):
 def main():
     a = args_parse()
     world, rank, local = dist_env()
-    if a.impl == "reference":
+    if a.accuracy:
+        run_accuracy(a, local)
+    elif a.impl == "reference":
         run_reference(a, world, rank)
     else:
         run_ours(a, world, rank, local)

@@ -13,6 +13,7 @@
 #include "../../include/gcfd.h"
 #include "dfr_element.hpp"
 #include "gcfd_kernels.cuh"
+#include "gcfd_mixed.cuh"
 #include "mesh.hpp"
 
 using namespace gcfd;
@@ -95,6 +96,19 @@ struct gcfd_ctx {
   double *enx = nullptr, *eny = nullptr, *eIIL = nullptr, *eIIR = nullptr, *eoohK = nullptr;
   double *bx = nullptr, *by = nullptr, *edgeSpeed = nullptr, *DT = nullptr;
   Scalars* sc = nullptr;
+  // mixed (delta form) path
+  float* dQ0 = nullptr;
+  float* Dk[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  float* R3 = nullptr;
+  float *mfaces = nullptr, *mfhat = nullptr, *mcorr = nullptr;
+  double* mbase = nullptr;
+  double* mexBC = nullptr;
+  float *mDivT = nullptr, *mIop = nullptr, *mgeo = nullptr, *mII = nullptr;
+  int* meslot = nullptr;
+  float *mnx = nullptr, *mny = nullptr, *moohK = nullptr;
+  bool dirty = true;  // Q0 changed outside a step: the stage-0 data must be rebuilt
+  std::vector<int> edgeOrder;             // device edge i -> topology edge
+  std::vector<double> hnx, hny, hoohK;    // per device edge
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graphExec = nullptr;
   cudaEvent_t ev[10] = {};
@@ -265,15 +279,128 @@ struct Launch {
   }
 };
 
+// Mixed (delta form) path: edge + stage kernels per RK stage.
+template <int N>
+struct MixedLaunch {
+  static MixedArgs args(gcfd_ctx* c, int stage, double* Q0, const double* time,
+                        unsigned long long* gmax) {
+    MixedArgs a;
+    a.K = c->K;
+    a.nInt = c->nInt;
+    a.nBC = c->nBC;
+    a.stage = stage;
+    a.Q0 = Q0;
+    a.dQ0 = c->dQ0;
+    for (int i = 0; i < 5; ++i) a.D[i] = c->Dk[i];
+    a.R3 = c->R3;
+    a.faces = c->mfaces;
+    a.fhat = c->mfhat;
+    a.corr = c->mcorr;
+    a.base = c->mbase;
+    a.Div = c->mDivT;
+    a.Iop = c->mIop;
+    a.geo = c->mgeo;
+    a.II = c->mII;
+    a.eslot = c->meslot;
+    a.ekL = c->ekL;
+    a.ekR = c->ekR;
+    a.enx = c->mnx;
+    a.eny = c->mny;
+    a.eoohK = c->moohK;
+    a.bcFlag = c->bcFlag;
+    a.bx = c->bx;
+    a.by = c->by;
+    a.exBC = c->mexBC;
+    a.edgeSpeed = c->edgeSpeed;
+    a.gmax = gmax;
+    a.time = time;
+    a.sc = c->sc;
+    a.cfl = c->prm.cfl;
+    a.finalTime = c->prm.final_time;
+    a.localDT = c->prm.local_time_stepping;
+    a.DT = c->DT;
+    a.flux = c->prm.flux_type;
+    a.gamma = static_cast<float>(c->fsFar.gamma);
+    a.gammaD = c->fsFar.gamma;
+    a.fsFar = to_device_fs<double>(c->fsFar);
+    a.fsIn = to_device_fs<double>(c->fsIn);
+    a.fsOut = to_device_fs<double>(c->fsOut);
+    a.vbeta = c->vbeta;
+    a.vx0 = c->vx0;
+    a.vy0 = c->vy0;
+    a.vgamma = c->vgamma;
+    a.rhsOut = c->rhsOut;
+    return a;
+  }
+  static int gridE(gcfd_ctx* c) { return (c->K + 31) / 32; }
+  static void edges(gcfd_ctx* c, int s, double* Q0, const double* time, unsigned long long* gmax) {
+    const MixedArgs a = args(c, s, Q0, time, gmax);
+    if (c->nInt > 0) {
+      if (c->prm.flux_type == GCFD_FLUX_ROE_ER)
+        k_mixed_edge<N, true><<<(c->nInt + 127) / 128, 128, 0, c->stream>>>(a);
+      else
+        k_mixed_edge<N, false><<<(c->nInt + 127) / 128, 128, 0, c->stream>>>(a);
+    }
+    if (c->nBC > 0)
+      k_mixed_edge_bc<N><<<(c->nBC + 7) / 8, dim3(8, MixedDims<N>::NE), 0, c->stream>>>(a);
+  }
+  static void prepare(gcfd_ctx* c, double* Q0) {
+    k_mixed_prepare<N><<<gridE(c), 128, 0, c->stream>>>(args(c, 0, Q0, nullptr, nullptr));
+  }
+  static void step(gcfd_ctx* c, cudaEvent_t* ev, double* ms, int* launches) {
+    auto mark = [&](int i) {
+      if (ev) cudaEventRecord(ev[i], c->stream);
+    };
+    auto acc = [&](int fam, int x, int y) {
+      if (!ev) return;
+      cudaEventSynchronize(ev[y]);
+      float t = 0.f;
+      cudaEventElapsedTime(&t, ev[x], ev[y]);
+      ms[fam] += t;
+      launches[fam] += 1;
+    };
+    if (ev) {  // profiling also times the stage-0 preparation once
+      mark(8);
+      prepare(c, c->Q[0]);
+      mark(9);
+      acc(0, 8, 9);
+    }
+    mark(0);
+    k_step_begin<<<1, 32, 0, c->stream>>>(c->sc);
+    mark(1);
+    acc(3, 0, 1);
+    for (int s = 0; s < 5; ++s) {
+      mark(2);
+      edges(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]);
+      mark(3);
+      k_mixed_stage<N><<<gridE(c), 128, 0, c->stream>>>(args(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]));
+      mark(4);
+      acc(1, 2, 3);
+      acc(2, 3, 4);
+    }
+    mark(6);
+    k_step_end<<<1, 32, 0, c->stream>>>(c->sc, c->prm.local_time_stepping);
+    mark(7);
+    acc(3, 6, 7);
+  }
+  static void rhs(gcfd_ctx* c) {
+    prepare(c, c->Qtmp);
+    edges(c, 0, c->Qtmp, &c->sc->rhs_time, &c->sc->gmax[0]);
+    k_mixed_stage<N><<<gridE(c), 128, 0, c->stream>>>(args(c, -1, c->Qtmp, &c->sc->rhs_time, &c->sc->gmax[0]));
+  }
+  static void prep_state(gcfd_ctx* c) { prepare(c, c->Q[0]); }
+};
+
 struct Ops {
   void (*step)(gcfd_ctx*, cudaEvent_t*, double*, int*);
   void (*rhs)(gcfd_ctx*);
+  void (*prep)(gcfd_ctx*);  // rebuild stage-0 data from Q0 (mixed path), or nullptr
 };
 
 template <int N>
 Ops ops_for(bool fp32) {
-  if (fp32) return Ops{&Launch<N, float>::step, &Launch<N, float>::rhs};
-  return Ops{&Launch<N, double>::step, &Launch<N, double>::rhs};
+  if (fp32) return Ops{&MixedLaunch<N>::step, &MixedLaunch<N>::rhs, &MixedLaunch<N>::prep_state};
+  return Ops{&Launch<N, double>::step, &Launch<N, double>::rhs, nullptr};
 }
 
 bool select_ops(int N, bool fp32, Ops* o) {
@@ -296,6 +423,16 @@ int capture_graph(gcfd_ctx* c) {
   GCFD_CUDA(c, cudaStreamEndCapture(c->stream, &g));
   c->graph = g;
   GCFD_CUDA(c, cudaGraphInstantiate(&c->graphExec, g, 0));
+  return GCFD_OK;
+}
+
+int prepare_if_dirty(gcfd_ctx* c) {
+  if (!c->dirty) return GCFD_OK;
+  Ops o;
+  select_ops(c->N, c->fp32, &o);
+  if (o.prep) o.prep(c);
+  GCFD_CUDA(c, cudaGetLastError());
+  c->dirty = false;
   return GCFD_OK;
 }
 
@@ -365,6 +502,63 @@ std::vector<double> initial_state(gcfd_ctx* c) {
       for (int n = 0; n < 4; ++n) q[(static_cast<size_t>(n) * Np + i) * K + k] = s[n];
     }
   return q;
+}
+
+// Buffers and FP32 operator / geometry copies of the mixed path.
+int build_mixed(gcfd_ctx* c) {
+  const int K = c->K, Np = c->Np, NE = c->NE, NF = c->NF;
+  const int NPP = (Np + 3) & ~3;
+  const size_t nS = static_cast<size_t>(4) * Np * K;
+  int rc;
+  if ((rc = dalloc(c, &c->dQ0, nS))) return rc;
+  for (int i = 1; i <= 4; ++i)
+    if ((rc = dalloc(c, &c->Dk[i], nS))) return rc;
+  if ((rc = dalloc(c, &c->R3, nS))) return rc;
+  if ((rc = dalloc(c, &c->mfaces, static_cast<size_t>(c->nEdges) * 2 * 4 * NE))) return rc;
+  if ((rc = dalloc(c, &c->mfhat, static_cast<size_t>(c->nEdges) * 4 * NE))) return rc;
+  if ((rc = dalloc(c, &c->mcorr, static_cast<size_t>(c->nEdges) * 4))) return rc;
+  if ((rc = dalloc(c, &c->mbase, static_cast<size_t>(K) * 4))) return rc;
+  if ((rc = dalloc(c, &c->mexBC, static_cast<size_t>(std::max(c->nBC, 1)) * NE * 4))) return rc;
+  GCFD_CUDA(c, cudaMemset(c->mfaces, 0, sizeof(float) * c->nEdges * 2 * 4 * NE));
+  GCFD_CUDA(c, cudaMemset(c->mcorr, 0, sizeof(float) * c->nEdges * 4));
+  // DivInt^T, rows = flux DOF j, cols = output point r padded to NPP.
+  std::vector<float> divT(static_cast<size_t>(NF) * NPP, 0.f), iop(static_cast<size_t>(3 * NE) * NPP, 0.f);
+  for (int j = 0; j < NF; ++j)
+    for (int r = 0; r < Np; ++r) divT[static_cast<size_t>(j) * NPP + r] = static_cast<float>(c->el.DivInt(r, j));
+  for (int j = 0; j < 3 * NE; ++j)
+    for (int i = 0; i < Np; ++i) iop[static_cast<size_t>(j) * NPP + i] = static_cast<float>(c->el.FluxEdgeInterp(j, i));
+  if ((rc = upload(c, &c->mDivT, divT))) return rc;
+  if ((rc = upload(c, &c->mIop, iop))) return rc;
+  const Geometry& g = c->geo;
+  std::vector<float> geo(static_cast<size_t>(6) * K), ii(static_cast<size_t>(3) * K);
+  for (int k = 0; k < K; ++k) {
+    geo[k] = static_cast<float>(g.Jdet[k]);
+    for (int q = 0; q < 4; ++q) geo[static_cast<size_t>(q + 1) * K + k] = static_cast<float>(g.Jinv[4 * k + q]);
+    geo[static_cast<size_t>(5) * K + k] = static_cast<float>(1.0 / g.Jdet[k]);
+    for (int e = 0; e < 3; ++e) ii[static_cast<size_t>(e) * K + k] = static_cast<float>(g.IInII[static_cast<size_t>(e) * K + k]);
+  }
+  if ((rc = upload(c, &c->mgeo, geo))) return rc;
+  if ((rc = upload(c, &c->mII, ii))) return rc;
+  std::vector<int> slot(static_cast<size_t>(3) * K);
+  std::vector<int> pos(c->topo.nEdges);
+  for (int i = 0; i < c->nEdges; ++i) pos[c->edgeOrder[i]] = i;
+  for (int k = 0; k < K; ++k)
+    for (int e = 0; e < 3; ++e) {
+      const int en = c->topo.elemEdge[3 * k + e];
+      const int side = (c->topo.kL[en] == k && c->topo.eL[en] == e) ? 0 : 1;
+      slot[static_cast<size_t>(e) * K + k] = pos[en] * 2 + side;
+    }
+  if ((rc = upload(c, &c->meslot, slot))) return rc;
+  std::vector<float> nx(c->nEdges), ny(c->nEdges), oh(c->nEdges);
+  for (int i = 0; i < c->nEdges; ++i) {
+    nx[i] = static_cast<float>(c->hnx[i]);
+    ny[i] = static_cast<float>(c->hny[i]);
+    oh[i] = static_cast<float>(c->hoohK[i]);
+  }
+  if ((rc = upload(c, &c->mnx, nx))) return rc;
+  if ((rc = upload(c, &c->mny, ny))) return rc;
+  if ((rc = upload(c, &c->moohK, oh))) return rc;
+  return GCFD_OK;
 }
 
 int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
@@ -449,6 +643,10 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
   for (int k = 0; k < K; ++k)
     for (int ed = 0; ed < 3; ++ed)
       elemEdge[static_cast<size_t>(ed) * K + k] = pos[t.elemEdge[3 * k + ed]];
+  c->edgeOrder = order;
+  c->hnx = nx;
+  c->hny = ny;
+  c->hoohK = oohK;
 
   GCFD_CUDA(c, cudaSetDevice(p.device));
   GCFD_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
@@ -461,13 +659,15 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
   if ((rc = dalloc(c, &c->R, nState))) return rc;
   if ((rc = dalloc(c, &c->Qtmp, nState))) return rc;
   if ((rc = dalloc(c, &c->rhsOut, nState))) return rc;
-  {
+  if (!c->fp32) {
     char* qf = nullptr;
     if ((rc = dalloc(c, &qf, nFace * tsz))) return rc;
     c->QF = qf;
     char* fe = nullptr;
     if ((rc = dalloc(c, &fe, nFace * tsz))) return rc;
     c->FE = fe;
+  } else if ((rc = build_mixed(c))) {
+    return rc;
   }
   if ((rc = upload(c, &c->Iop, c->el.FluxEdgeInterp.v))) return rc;
   if ((rc = upload(c, &c->Div, c->el.DivInt.v))) return rc;
@@ -563,6 +763,7 @@ int gcfd_set_state(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doub
   int rc = check_shards(c, nshards, Kmax);
   if (rc) return rc;
   if ((rc = copy_shards(c, c->Q[0], nshards, Kmax, Q, true, nullptr))) return rc;
+  c->dirty = true;
   GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
   return GCFD_OK;
 }
@@ -580,6 +781,7 @@ int gcfd_set_state_device(gcfd_ctx* c, const double* dQ) {
   if (!c || !dQ) return c ? fail(c, GCFD_ERR_ARG, "null state") : GCFD_ERR_ARG;
   GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], dQ, sizeof(double) * 4 * c->Np * static_cast<size_t>(c->K),
                                cudaMemcpyDeviceToDevice, c->stream));
+  c->dirty = true;
   return GCFD_OK;
 }
 
@@ -618,6 +820,7 @@ int gcfd_rhs(gcfd_ctx* c, double time, int32_t nshards, const int32_t* Kmax, con
   Ops o;
   select_ops(c->N, c->fp32, &o);
   o.rhs(c);
+  c->dirty = true;  // the mixed path's stage-0 buffers now hold the RHS input
   GCFD_CUDA(c, cudaGetLastError());
   if ((rc = copy_shards(c, c->rhsOut, nshards, Kmax, nullptr, false, RHS))) return rc;
   GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -635,6 +838,8 @@ int gcfd_step(gcfd_ctx* c, int32_t nsteps, double* time, double* dt_last, double
               double* resid_absmax4, double* resid_rms4) {
   if (!c) return GCFD_ERR_ARG;
   if (nsteps < 0) return fail(c, GCFD_ERR_ARG, "nsteps must be >= 0");
+  int rc = prepare_if_dirty(c);
+  if (rc) return rc;
   for (int i = 0; i < nsteps; ++i) GCFD_CUDA(c, cudaGraphLaunch(c->graphExec, c->stream));
   Scalars h;
   GCFD_CUDA(c, cudaMemcpyAsync(&h, c->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
@@ -660,6 +865,8 @@ int gcfd_step(gcfd_ctx* c, int32_t nsteps, double* time, double* dt_last, double
 int gcfd_enqueue_steps(gcfd_ctx* c, int32_t nsteps) {
   if (!c) return GCFD_ERR_ARG;
   if (nsteps < 0) return fail(c, GCFD_ERR_ARG, "nsteps must be >= 0");
+  int rc = prepare_if_dirty(c);
+  if (rc) return rc;
   for (int i = 0; i < nsteps; ++i) GCFD_CUDA(c, cudaGraphLaunch(c->graphExec, c->stream));
   return GCFD_OK;
 }
@@ -677,6 +884,7 @@ int gcfd_profile_step(gcfd_ctx* c, double* kernel_ms4, int32_t* launches4) {
   Ops o;
   select_ops(c->N, c->fp32, &o);
   o.step(c, c->ev, ms, l);
+  c->dirty = false;
   GCFD_CUDA(c, cudaGetLastError());
   GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
   for (int i = 0; i < 4; ++i) {

@@ -84,12 +84,12 @@ __global__ void __launch_bounds__(128) k_interp(const double* __restrict__ Q, T*
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= K) return;
   const size_t sK = static_cast<size_t>(K);
-#pragma unroll
+#pragma unroll 1
   for (int n = 0; n < 4; ++n) {
     T q[NP];
 #pragma unroll
     for (int i = 0; i < NP; ++i) q[i] = static_cast<T>(Q[(n * NP + i) * sK + k]);
-#pragma unroll
+#pragma unroll 2
     for (int j = 0; j < NE3; ++j) {
       T acc = T(0);
 #pragma unroll

@@ -1,0 +1,651 @@
+// Mixed-precision ("delta form") DFR right-hand side and SSP(5,4) step.
+//
+// Arithmetic: every element carries a reference state Qb = the stage state at
+// its solution point 0 (FP64).  The RT divergence of a constant flux is zero
+// (DivInt * dofs(const) = 0), so the RHS is computed from
+//     dF = F(Q) - F(Qb)          at the interior points, and
+//     fhat - n.F(Qb)             at the edge points,
+// with exact delta-flux algebra in FP32 on dQ = Q - Qb.  Rounding errors then
+// scale with |dQ| ~ h |grad Q| instead of |Q|, which is what keeps FP32 GEMMs
+// against the reference's ill-conditioned DivInt within the FP64 result.
+//
+// State: Q0 (the conserved state) stays FP64.  SSP(5,4) stage k is stored as
+// the FP32 increment D_k = Q_k - Q0: the stage weights on (Q0, Q_k) sum to one
+// (euler.go:511-564), so Q_{k+1} = Q0 + b D_k + c dt RHS exactly, and the final
+// increment R = a2 D2 + a3 D3 + a4 D4 + ... is added to Q0 once per step in FP64.
+//
+// Layouts (HBM):
+//   Q0[n][i][k] FP64, dQ0[n][i][k] = Q0 - Q0(point 0) FP32, D1..D4, R3 FP32
+//   faces[g][side][n][p]  FP32 dQ at edge points, side 0 = left element's CCW
+//                         order, side 1 = right element's CCW order
+//   fhat[g][n][p]         FP32 fhat - n_L.F(Qb_L), left order
+//   corr[g][n]            FP32 n_L.(F(Qb_R) - F(Qb_L))
+//   base[k][n]            FP64 Qb of the current stage (gathered by the edge kernel)
+// Element kernels run one thread per (element, variable): a block is 32
+// elements x 4 variables, warp w owns variable w, so every row access is a
+// 128-byte coalesced transaction.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gcfd_kernels.cuh"
+
+namespace gcfd {
+
+// Base-state primitives in FP32.  They only ever multiply deltas, so their own
+// FP32 rounding enters the result at second order; no FP64 division needed.
+struct BasePrim {
+  float rho, m, n, E, u, v, p, H;
+};
+
+__device__ __forceinline__ BasePrim base_prim(const double b[4], float gm1) {
+  BasePrim s;
+  s.rho = static_cast<float>(b[0]);
+  s.m = static_cast<float>(b[1]);
+  s.n = static_cast<float>(b[2]);
+  s.E = static_cast<float>(b[3]);
+  const float ir = 1.0f / s.rho;
+  s.u = s.m * ir;
+  s.v = s.n * ir;
+  s.p = gm1 * (s.E - 0.5f * (s.m * s.u + s.n * s.v));
+  s.H = s.E + s.p;
+  return s;
+}
+
+// Velocity and pressure deltas of state Qb + d relative to Qb.
+struct DeltaPrim {
+  float du, dv, dp;
+};
+__device__ __forceinline__ DeltaPrim delta_prim(const BasePrim& b, const float d[4], float gm1) {
+  DeltaPrim r;
+  const float ir = 1.0f / (b.rho + d[0]);
+  r.du = (d[1] - b.u * d[0]) * ir;
+  r.dv = (d[2] - b.v * d[0]) * ir;
+  r.dp = gm1 * (d[3] - 0.5f * (b.m * r.du + d[1] * b.u + d[1] * r.du + b.n * r.dv + d[2] * b.v +
+                               d[2] * r.dv));
+  return r;
+}
+
+// Component c of F_x(Qb + d) - F_x(Qb) and F_y(...) - F_y(Qb) (exact algebra).
+__device__ __forceinline__ void delta_flux_c(int c, const BasePrim& b, const float d[4],
+                                             const DeltaPrim& q, float* dFx, float* dFy) {
+  switch (c) {
+    case 0:
+      *dFx = d[1];
+      *dFy = d[2];
+      break;
+    case 1:
+      *dFx = b.m * q.du + d[1] * b.u + d[1] * q.du + q.dp;
+      *dFy = b.n * q.du + d[2] * b.u + d[2] * q.du;
+      break;
+    case 2:
+      *dFx = b.m * q.dv + d[1] * b.v + d[1] * q.dv;
+      *dFy = b.n * q.dv + d[2] * b.v + d[2] * q.dv + q.dp;
+      break;
+    default: {
+      const float dH = d[3] + q.dp;
+      *dFx = b.u * dH + q.du * (b.H + dH);
+      *dFy = b.v * dH + q.dv * (b.H + dH);
+    }
+  }
+}
+
+// n . (F(Qb + d) - F(Qb)) for all four components.
+__device__ __forceinline__ void delta_normal_flux(const BasePrim& b, const float d[4], float nx,
+                                                  float ny, float gm1, float out[4]) {
+  const DeltaPrim q = delta_prim(b, d, gm1);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    float fx, fy;
+    delta_flux_c(c, b, d, q, &fx, &fy);
+    out[c] = nx * fx + ny * fy;
+  }
+}
+
+// Riemann flux minus n.F(Qb), from the two sides' deltas relative to Qb
+// (AvgFlux / LaxFlux / RoeFlux of fluxes.go:135-190,284-413 in delta form).
+__device__ __forceinline__ void riemann_delta(int kind, const BasePrim& b, const float dL[4],
+                                              const float dR[4], float nx, float ny, float gamma,
+                                              float f[4]) {
+  const float gm1 = gamma - 1.0f;
+  float cL[4], cR[4];
+  delta_normal_flux(b, dL, nx, ny, gm1, cL);
+  delta_normal_flux(b, dR, nx, ny, gm1, cR);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) f[c] = 0.5f * (cL[c] + cR[c]);
+  if (kind == kFluxAverage) return;
+  float QL[4], QR[4];
+  const float bq[4] = {b.rho, b.m, b.n, b.E};
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    QL[c] = bq[c] + dL[c];
+    QR[c] = bq[c] + dR[c];
+  }
+  const Gas<float> g{gamma, gm1, 1.0f / gm1};
+  if (kind == kFluxLax) {
+    const float uL = QL[1] / QL[0], vL = QL[2] / QL[0], uR = QR[1] / QR[0], vR = QR[2] / QR[0];
+    const float CL = sound_speed(g, QL[0], QL[1], QL[2], QL[3]);
+    const float CR = sound_speed(g, QR[0], QR[1], QR[2], QR[3]);
+    const float maxV = fmaxf(sqrtf(uL * uL + vL * vL) + CL, sqrtf(uR * uR + vR * vR) + CR);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) f[c] += 0.5f * maxV * (dL[c] - dR[c]);
+    return;
+  }
+  // Roe: averages from the full states, jumps from the deltas.
+  const DeltaPrim qL = delta_prim(b, dL, gm1), qR = delta_prim(b, dR, gm1);
+  const float rhoL = QL[0], rhoR = QR[0];
+  const float uxL = b.u + qL.du, uyL = b.v + qL.dv, uxR = b.u + qR.du, uyR = b.v + qR.dv;
+  const float uL = uxL * nx + uyL * ny, vL = -uxL * ny + uyL * nx;
+  const float uR = uxR * nx + uyR * ny, vR = -uxR * ny + uyR * nx;
+  const float pL = b.p + qL.dp, pR = b.p + qR.dp;
+  const float hL = (QL[3] + pL) / rhoL, hR = (QR[3] + pR) / rhoR;
+  const float rLs = sqrtf(rhoL), rRs = sqrtf(rhoR), rs = rLs + rRs;
+  const float rho = rLs * rRs;
+  const float u = (rLs * uL + rRs * uR) / rs;
+  const float v = (rLs * vL + rRs * vR) / rs;
+  const float h = (rLs * hL + rRs * hR) / rs;
+  const float c2 = gm1 * (h - 0.5f * (u * u + v * v));
+  const float C = sqrtf(c2);
+  const float dun = (qR.du - qL.du) * nx + (qR.dv - qL.dv) * ny;     // uR - uL
+  const float dvt = -(qR.du - qL.du) * ny + (qR.dv - qL.dv) * nx;    // vR - vL
+  const float dpj = qR.dp - qL.dp;                                    // pR - pL
+  const float drj = dR[0] - dL[0];                                    // rhoR - rhoL
+  float dW1 = -0.5f * (rho * dun) / C + 0.5f * dpj / c2;
+  float dW2 = drj - dpj / c2;
+  float dW3 = rho * dvt;
+  float dW4 = 0.5f * (rho * dun) / C + 0.5f * dpj / c2;
+  dW1 = fabsf(u - C) * dW1;
+  dW2 = fabsf(u) * dW2;
+  dW3 = fabsf(u) * dW3;
+  dW4 = fabsf(u + C) * dW4;
+  const float d0 = -0.5f * (dW1 + dW2 + dW4);
+  const float d1 = -0.5f * (dW1 * (u - C) + dW2 * u + dW4 * (u + C));
+  const float d2 = -0.5f * (dW1 * v + dW2 * v + dW3 + dW4 * v);
+  const float d3 = -0.5f * (dW1 * (h - u * C) + 0.5f * dW2 * (u * u + v * v) + dW3 * v + dW4 * (h + u * C));
+  f[0] += d0;
+  f[1] += nx * d1 - ny * d2;
+  f[2] += ny * d1 + nx * d2;
+  f[3] += d3;
+}
+
+// ---------------------------------------------------------------------------
+struct MixedArgs {
+  int K, nInt, nBC;
+  int stage;
+  double* Q0;                 // FP64 state
+  float* dQ0;                 // Q0 - Q0(point 0)
+  float* D[5];                // D[1..4] stage increments (D[0] unused), D[4] slot 0 = R3 store
+  float* R3;                  // stage-3 RHS
+  float* faces;               // [g][2][4][NE]
+  float* fhat;                // [g][4][NE]
+  float* corr;                // [g][4]
+  double* base;               // [k][4] reference state; updated in place to the next stage's
+  const float* Div;           // DivInt^T padded: [NF][NPP]
+  const float* Iop;           // FluxEdgeInterp padded: [NE3][NPP]
+  const float* geo;           // [6][K]: Jdet, Jinv0..3, 1/Jdet
+  const float* II;            // [3][K] IInII
+  const int* eslot;           // [3][K] edge id * 2 + side
+  // edge kernel
+  const int* ekL;
+  const int* ekR;
+  const float* enx;
+  const float* eny;
+  const float* eoohK;
+  const int* bcFlag;
+  const double* bx;
+  const double* by;
+  double* exBC;               // [nBC][NE][4] exact boundary states of the current step
+  double* edgeSpeed;
+  unsigned long long* gmax;
+  const double* time;
+  Scalars* sc;
+  double cfl, finalTime;
+  int localDT;
+  double* DT;
+  int flux;
+  float gamma;
+  double gammaD;
+  FreeStreamT<double> fsFar, fsIn, fsOut;
+  double vbeta, vx0, vy0, vgamma;
+  double* rhsOut;             // stage -1: RHS in FP64 [n][i][k]
+};
+
+// SSP(5,4) weights of rkAdvance (euler.go:511-564) in increment form:
+// D1 = C0 dtR, D_{k+1} = B_k D_k + C_k dtR, R = A2 D2 + A3 D3 + A4 D4 + R3W dtR3 + C4 dtR.
+constexpr float kSspC0 = 0.391752226571890f;
+constexpr float kSspB1 = 0.555629506348765f, kSspC1 = 0.368410593050371f;
+constexpr float kSspB2 = 0.379898148511597f, kSspC2 = 0.251891774271694f;
+constexpr float kSspB3 = 0.821920045606868f, kSspC3 = 0.544974750228521f;
+constexpr float kSspA2 = 0.517231671970585f, kSspA3 = 0.096059710526146f;
+constexpr float kSspA4 = 0.386708617503269f, kSspR3 = 0.063692468666290f;
+constexpr float kSspC4 = 0.226007483236906f;
+
+template <int N>
+struct MixedDims {
+  static constexpr int NP = Dims<N>::NP, NE = Dims<N>::NE, NE3 = Dims<N>::NE3, NF = Dims<N>::NF;
+  static constexpr int NPP = (NP + 3) & ~3;  // padded to float4
+};
+
+// Writes the element's 3 edges of face deltas for variable n (rows e*NE + p).
+template <int N>
+__device__ __forceinline__ void write_faces(const MixedArgs& a, const float* sI, int k, int n,
+                                            const float dq[]) {
+  constexpr int NE = MixedDims<N>::NE, NPP = MixedDims<N>::NPP;
+  const size_t sK = static_cast<size_t>(a.K);
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    const int slot = a.eslot[e * sK + k];
+    float* dst = a.faces + (static_cast<size_t>(slot) * 4 + n) * NE;
+#pragma unroll
+    for (int p = 0; p < NE; ++p) {
+      const float4* row = reinterpret_cast<const float4*>(sI + (e * NE + p) * NPP);
+      float acc = 0.0f;
+#pragma unroll
+      for (int i4 = 0; i4 < NPP / 4; ++i4) {
+        const float4 w = row[i4];
+        acc = fmaf(w.x, dq[4 * i4 + 0], acc);
+        acc = fmaf(w.y, dq[4 * i4 + 1], acc);
+        acc = fmaf(w.z, dq[4 * i4 + 2], acc);
+        acc = fmaf(w.w, dq[4 * i4 + 3], acc);
+      }
+      dst[p] = acc;
+    }
+  }
+}
+
+// Stage-0 preparation from the FP64 state: dQ0, faces, reference states.
+template <int N>
+__global__ void __launch_bounds__(128) k_mixed_prepare(MixedArgs a) {
+  constexpr int NP = MixedDims<N>::NP, NE3 = MixedDims<N>::NE3, NPP = MixedDims<N>::NPP;
+  __shared__ __align__(16) float sI[NE3 * NPP];
+  for (int i = threadIdx.x; i < NE3 * NPP; i += blockDim.x) sI[i] = a.Iop[i];
+  __syncthreads();
+  const int n = threadIdx.x >> 5;
+  const int k = blockIdx.x * 32 + (threadIdx.x & 31);
+  if (k >= a.K) return;
+  const size_t sK = static_cast<size_t>(a.K);
+  const double* q = a.Q0 + static_cast<size_t>(n) * NP * sK + k;
+  const double q0 = q[0];
+  float dq[NPP];
+#pragma unroll
+  for (int i = 0; i < NPP; ++i) dq[i] = 0.0f;
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    dq[i] = static_cast<float>(q[i * sK] - q0);
+    a.dQ0[(static_cast<size_t>(n) * NP + i) * sK + k] = dq[i];
+  }
+  a.base[static_cast<size_t>(k) * 4 + n] = q0;
+  write_faces<N>(a, sI, k, n, dq);
+}
+
+// (c) interior-edge fluxes in delta form, one thread per mesh edge.  RoeER
+// instantiates the Roe-ER flux in FP64 (fluxes.go:415-503 has no delta form).
+template <int N, bool RoeER>
+__global__ void __launch_bounds__(128) k_mixed_edge(MixedArgs a) {
+  constexpr int NE = MixedDims<N>::NE;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  double smax = 0.0;
+  if (g < a.nInt) {
+    const int kL = a.ekL[g], kR = a.ekR[g];
+    const float nx = a.enx[g], ny = a.eny[g];
+    const float oohK = a.eoohK[g];
+    double bL[4];
+    float dB[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) bL[c] = a.base[static_cast<size_t>(kL) * 4 + c];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) dB[c] = static_cast<float>(a.base[static_cast<size_t>(kR) * 4 + c] - bL[c]);
+    const double gm1d = a.gammaD - 1.0;
+    const float gm1 = a.gamma - 1.0f;
+    const BasePrim b = base_prim(bL, gm1);
+    const Gas<float> gf{a.gamma, gm1, 1.0f / gm1};
+    const float* fL = a.faces + static_cast<size_t>(g) * 2 * 4 * NE;
+    const float* fR = fL + 4 * NE;
+    float* fo = a.fhat + static_cast<size_t>(g) * 4 * NE;
+    float sm = 0.0f;
+#pragma unroll
+    for (int p = 0; p < NE; ++p) {
+      float dl[4], dr[4], f[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        dl[c] = fL[c * NE + p];
+        dr[c] = fR[c * NE + (NE - 1 - p)] + dB[c];
+      }
+      if (RoeER) {
+        double QLd[4], QRd[4], fd[4], Fx[4], Fy[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          QLd[c] = bL[c] + dl[c];
+          QRd[c] = bL[c] + dr[c];
+        }
+        const Gas<double> gd{a.gammaD, gm1d, 1.0 / gm1d};
+        flux_roe_er(gd, QLd, QRd, static_cast<double>(nx), static_cast<double>(ny), fd);
+        euler_flux(gd, bL, Fx, Fy);
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+          f[c] = static_cast<float>(fd[c] - (static_cast<double>(nx) * Fx[c] + static_cast<double>(ny) * Fy[c]));
+      } else {
+        riemann_delta(a.flux, b, dl, dr, nx, ny, a.gamma, f);
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) fo[c * NE + p] = f[c];
+      const float QL[4] = {b.rho + dl[0], b.m + dl[1], b.n + dl[2], b.E + dl[3]};
+      sm = fmaxf(sm, oohK * (speed(QL[0], QL[1], QL[2]) + sound_speed(gf, QL[0], QL[1], QL[2], QL[3])));
+    }
+    float cr[4];
+    delta_normal_flux(b, dB, nx, ny, gm1, cr);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) a.corr[static_cast<size_t>(g) * 4 + c] = cr[c];
+    smax = static_cast<double>(sm);
+    a.edgeSpeed[g] = smax;
+  }
+  smax = warp_max(smax);
+  if ((threadIdx.x & 31) == 0)
+    atomicMax(a.gmax, static_cast<unsigned long long>(__double_as_longlong(smax)));
+}
+
+// (c) boundary edges: face state, characteristic / wall / exact-state BC and
+// the physical normal flux in FP64 (bcs.go:11-133, edges.go:413-452), then the
+// delta to FP32.  GB300's FP64 pipe is narrow and these points carry the
+// transcendental work (exp/pow), so one thread owns one (edge, point): a block
+// is 8 edges (threadIdx.x) x NpEdge points (threadIdx.y), spread over many SMs.
+template <int N>
+__global__ void __launch_bounds__(8 * MixedDims<N>::NE) k_mixed_edge_bc(MixedArgs a) {
+  constexpr int NE = MixedDims<N>::NE;
+  __shared__ double sspeed[NE][8];
+  const int tx = threadIdx.x, p = threadIdx.y;
+  const int bb = blockIdx.x * 8 + tx;
+  double ws = 0.0;
+  int g = -1;
+  if (bb < a.nBC) {
+    g = a.nInt + bb;
+    const int kL = a.ekL[g];
+    const double nxd = a.enx[g], nyd = a.eny[g];
+    double bL[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) bL[c] = a.base[static_cast<size_t>(kL) * 4 + c];
+    const double gm1d = a.gammaD - 1.0;
+    const Gas<double> gd{a.gammaD, gm1d, 1.0 / gm1d};
+    double Fx[4], Fy[4];
+    euler_flux(gd, bL, Fx, Fy);
+    const float* fL = a.faces + static_cast<size_t>(g) * 2 * 4 * NE;
+    double qi[4], qb[4], f[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) qi[c] = bL[c] + static_cast<double>(fL[c * NE + p]);
+    bool wall = false;
+    switch (a.bcFlag[bb]) {
+      case 4: riemann_bc(a.fsFar, qi, a.fsFar.qinf, nxd, nyd, qb); break;
+      case 1: riemann_bc(a.fsIn, qi, a.fsIn.qinf, nxd, nyd, qb); break;
+      case 8: riemann_bc(a.fsOut, qi, a.fsOut.qinf, nxd, nyd, qb); break;
+      case 9: {
+        // The BC time is frozen for the 5 stages (euler.go:621): evaluate the
+        // exact state once per step and reuse it.
+        double ex[4];
+        double* cache = a.exBC + (static_cast<size_t>(bb) * NE + p) * 4;
+        if (a.stage <= 0) {
+          ivortex_state(a.vbeta, a.vx0, a.vy0, a.vgamma, *a.time, a.bx[bb * NE + p], a.by[bb * NE + p], ex);
+          if (a.stage == 0)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) cache[c] = ex[c];
+        } else {
+#pragma unroll
+          for (int c = 0; c < 4; ++c) ex[c] = cache[c];
+        }
+        riemann_bc(a.fsFar, qi, ex, nxd, nyd, qb);
+        break;
+      }
+      case 5: case 6:
+        wall = true;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) qb[c] = qi[c];
+        break;
+      default:
+#pragma unroll
+        for (int c = 0; c < 4; ++c) qb[c] = qi[c];
+    }
+    if (wall) {
+      const double pw = pressure(gd, qi[0], qi[1], qi[2], qi[3]);
+      f[0] = 0.0; f[1] = nxd * pw; f[2] = nyd * pw; f[3] = 0.0;
+    } else {
+      double Gx[4], Gy[4];
+      euler_flux(gd, qb, Gx, Gy);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) f[c] = nxd * Gx[c] + nyd * Gy[c];
+    }
+    float* fo = a.fhat + static_cast<size_t>(g) * 4 * NE;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) fo[c * NE + p] = static_cast<float>(f[c] - (nxd * Fx[c] + nyd * Fy[c]));
+    ws = static_cast<double>(a.eoohK[g]) * (speed(qb[0], qb[1], qb[2]) + sound_speed(gd, qb[0], qb[1], qb[2], qb[3]));
+  }
+  sspeed[p][tx] = ws;
+  __syncthreads();
+  if (p == 0) {
+    double m = 0.0;
+#pragma unroll
+    for (int q = 0; q < NE; ++q) m = fmax(m, sspeed[q][tx]);
+    if (g >= 0) a.edgeSpeed[g] = m;
+    // lanes 0..7 of the p == 0 row hold all 8 edges of the block
+    for (int o = 4; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0x000000ffu, m, o, 8));
+    if (tx == 0) atomicMax(a.gmax, static_cast<unsigned long long>(__double_as_longlong(m)));
+  }
+}
+
+// (b)+(e): delta-form divergence, SSP stage update on the FP32 increments, and
+// the next stage's faces / reference states.  stage -1 writes the RHS only.
+template <int N>
+__global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
+  constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NE3 = MixedDims<N>::NE3;
+  constexpr int NF = MixedDims<N>::NF, NPP = MixedDims<N>::NPP;
+  __shared__ __align__(16) float sD[NF * NPP];
+  __shared__ __align__(16) float sI[NE3 * NPP];
+  __shared__ float sdq[4][NP][33];
+  __shared__ double sbase[4][32];
+  __shared__ float sfh[4][NE3][32];   // this element's edge fluxes, prefetched
+  __shared__ float scorr[4][3][32];
+  for (int i = threadIdx.x; i < NF * NPP; i += blockDim.x) sD[i] = a.Div[i];
+  for (int i = threadIdx.x; i < NE3 * NPP; i += blockDim.x) sI[i] = a.Iop[i];
+  const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = blockIdx.x * 32 + lane;
+  const bool active = k < a.K;
+  const size_t sK = static_cast<size_t>(a.K);
+  const int s = a.stage;
+  // Stage input deltas relative to point 0 of the stage state.
+  float dq0[NP], ds[NP];
+  if (active) {
+    const float* q0 = a.dQ0 + static_cast<size_t>(n) * NP * sK + k;
+#pragma unroll
+    for (int i = 0; i < NP; ++i) dq0[i] = q0[i * sK];
+    if (s >= 1) {
+      const float* d = a.D[s] + static_cast<size_t>(n) * NP * sK + k;
+#pragma unroll
+      for (int i = 0; i < NP; ++i) ds[i] = d[i * sK];
+    } else {
+#pragma unroll
+      for (int i = 0; i < NP; ++i) ds[i] = 0.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < NP; ++i) sdq[n][i][lane] = dq0[i] + (ds[i] - ds[0]);
+    sbase[n][lane] = a.base[static_cast<size_t>(k) * 4 + n];
+  }
+  // Prefetch the element's edge fluxes (a gather: 3 edges x NpEdge per
+  // variable) into shared memory asynchronously; the interior work below hides
+  // the latency.  Each thread later reads only what it copied itself.
+  int eslot[3];
+  float eII[3];
+  if (active) {
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      eslot[e] = a.eslot[e * sK + k];
+      eII[e] = a.II[e * sK + k];
+      const float* fh = a.fhat + (static_cast<size_t>(eslot[e] >> 1) * 4 + n) * NE;
+#pragma unroll
+      for (int p = 0; p < NE; ++p) {
+        const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(&sfh[n][e * NE + p][lane]));
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(fh + p));
+      }
+      if (eslot[e] & 1) {
+        const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(&scorr[n][e][lane]));
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst),
+                     "l"(a.corr + static_cast<size_t>(eslot[e] >> 1) * 4 + n));
+      }
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+  }
+  // Local time step of this stage: DT persists across stages, so every thread
+  // of the element reads it before the barrier and one writes it after.
+  double dtLocal = 0.0;
+  if (active && a.localDT && s >= 0) {
+    double v = (s == 0) ? -100.0 : a.DT[k];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) v = fmax(v, a.edgeSpeed[eslot[e] >> 1]);
+    dtLocal = a.cfl / v;
+  }
+  __syncthreads();
+  double rmax = -1.7976931348623157e308, rabs = 0.0, rs2 = 0.0;
+  if (active) {
+    const float Jd = a.geo[k], J0 = a.geo[sK + k], J1 = a.geo[2 * sK + k];
+    const float J2 = a.geo[3 * sK + k], J3 = a.geo[4 * sK + k], ooJ = a.geo[5 * sK + k];
+    double bq[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) bq[c] = sbase[c][lane];
+    const float gm1 = a.gamma - 1.0f;
+    const BasePrim b = base_prim(bq, gm1);
+    float acc[NPP];
+#pragma unroll
+    for (int r = 0; r < NPP; ++r) acc[r] = 0.0f;
+    // Interior transformed delta fluxes, DivInt columns 0..2NP-1.
+#pragma unroll 3
+    for (int i = 0; i < NP; ++i) {
+      const float d[4] = {sdq[0][i][lane], sdq[1][i][lane], sdq[2][i][lane], sdq[3][i][lane]};
+      const DeltaPrim q = delta_prim(b, d, gm1);
+      float fx, fy;
+      delta_flux_c(n, b, d, q, &fx, &fy);
+      const float Fr = Jd * (J0 * fx + J1 * fy);
+      const float Fs = Jd * (J2 * fx + J3 * fy);
+      const float4* cr = reinterpret_cast<const float4*>(sD + i * NPP);
+      const float4* cs = reinterpret_cast<const float4*>(sD + (NP + i) * NPP);
+#pragma unroll
+      for (int r4 = 0; r4 < NPP / 4; ++r4) {
+        const float4 x = cr[r4], y = cs[r4];
+        acc[4 * r4 + 0] = fmaf(x.x, Fr, fmaf(y.x, Fs, acc[4 * r4 + 0]));
+        acc[4 * r4 + 1] = fmaf(x.y, Fr, fmaf(y.y, Fs, acc[4 * r4 + 1]));
+        acc[4 * r4 + 2] = fmaf(x.z, Fr, fmaf(y.z, Fs, acc[4 * r4 + 2]));
+        acc[4 * r4 + 3] = fmaf(x.w, Fr, fmaf(y.w, Fs, acc[4 * r4 + 3]));
+      }
+    }
+    // Edge DOFs: IInII * (s fhat - n_e.F(Qb)), owner order / reversed for the right side.
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      const bool right = eslot[e] & 1;
+      const float ii = eII[e];
+      const float cc = right ? scorr[n][e][lane] : 0.0f;
+#pragma unroll
+      for (int p = 0; p < NE; ++p) {
+        const float dof = right ? -(sfh[n][e * NE + NE - 1 - p][lane] - cc) * ii : sfh[n][e * NE + p][lane] * ii;
+        const float4* col = reinterpret_cast<const float4*>(sD + (2 * NP + e * NE + p) * NPP);
+#pragma unroll
+        for (int r4 = 0; r4 < NPP / 4; ++r4) {
+          const float4 x = col[r4];
+          acc[4 * r4 + 0] = fmaf(x.x, dof, acc[4 * r4 + 0]);
+          acc[4 * r4 + 1] = fmaf(x.y, dof, acc[4 * r4 + 1]);
+          acc[4 * r4 + 2] = fmaf(x.z, dof, acc[4 * r4 + 2]);
+          acc[4 * r4 + 3] = fmaf(x.w, dof, acc[4 * r4 + 3]);
+        }
+      }
+    }
+    float rhs[NP];
+#pragma unroll
+    for (int r = 0; r < NP; ++r) rhs[r] = -acc[r] * ooJ;
+    if (s < 0) {
+#pragma unroll
+      for (int r = 0; r < NP; ++r) a.rhsOut[(static_cast<size_t>(n) * NP + r) * sK + k] = rhs[r];
+    } else {
+      double dtk;
+      if (a.localDT) {
+        dtk = dtLocal;
+        if (n == 0) a.DT[k] = dtk;
+      } else {
+        const double gm = __longlong_as_double(static_cast<long long>(a.sc->gmax[s]));
+        dtk = a.cfl / gm;
+        const double t = a.sc->time;
+        if (t + dtk > a.finalTime) dtk = a.finalTime - t;
+        if (k == 0 && n == 0) a.sc->dt[s] = dtk;
+      }
+      const float dt = static_cast<float>(dtk);
+      float dn[NP];
+      const size_t off = static_cast<size_t>(n) * NP * sK + k;
+      if (s == 0) {
+#pragma unroll
+        for (int r = 0; r < NP; ++r) dn[r] = kSspC0 * (dt * rhs[r]);
+      } else if (s == 1) {
+#pragma unroll
+        for (int r = 0; r < NP; ++r) dn[r] = kSspB1 * ds[r] + kSspC1 * (dt * rhs[r]);
+      } else if (s == 2) {
+#pragma unroll
+        for (int r = 0; r < NP; ++r) dn[r] = kSspB2 * ds[r] + kSspC2 * (dt * rhs[r]);
+      } else if (s == 3) {
+#pragma unroll
+        for (int r = 0; r < NP; ++r) {
+          a.R3[off + r * sK] = rhs[r];
+          dn[r] = kSspB3 * ds[r] + kSspC3 * (dt * rhs[r]);
+        }
+      }
+      if (s < 4) {
+        float* dst = a.D[s + 1] + off;
+#pragma unroll
+        for (int r = 0; r < NP; ++r) dst[r * sK] = dn[r];
+        float dqn[NPP];
+#pragma unroll
+        for (int r = 0; r < NPP; ++r) dqn[r] = (r < NP) ? dq0[r] + (dn[r] - dn[0]) : 0.0f;
+        write_faces<N>(a, sI, k, n, dqn);
+        a.base[static_cast<size_t>(k) * 4 + n] = a.Q0[off] + static_cast<double>(dn[0]);
+      } else {
+        // Final increment and the FP64 accumulation (rkAdvance stage 4).
+        const float* D2 = a.D[2] + off;
+        const float* D3 = a.D[3] + off;
+        const float* R3 = a.R3 + off;
+        double* q0 = a.Q0 + off;
+        double qn[NP];
+        float fmx = -3.4028235e38f, fab = 0.0f, fs2 = 0.0f;  // per-thread partials (15 values)
+#pragma unroll
+        for (int r = 0; r < NP; ++r) {
+          const float inc = kSspA2 * D2[r * sK] + kSspA3 * D3[r * sK] + kSspA4 * ds[r] +
+                            kSspR3 * (dt * R3[r * sK]) + kSspC4 * (dt * rhs[r]);
+          qn[r] = q0[r * sK] + static_cast<double>(inc);
+          q0[r * sK] = qn[r];
+          fmx = fmaxf(fmx, inc);
+          fab = fmaxf(fab, fabsf(inc));
+          fs2 = fmaf(inc, inc, fs2);
+          if (inc != inc) fab = inc;
+        }
+        rmax = fmx;
+        rabs = fab;
+        rs2 = fs2;
+        // Prepare the next step's stage 0 from the new state.
+        float dqn[NPP];
+#pragma unroll
+        for (int r = 0; r < NPP; ++r) dqn[r] = 0.0f;
+#pragma unroll
+        for (int r = 0; r < NP; ++r) {
+          dqn[r] = static_cast<float>(qn[r] - qn[0]);
+          a.dQ0[off + r * sK] = dqn[r];
+        }
+        write_faces<N>(a, sI, k, n, dqn);
+        a.base[static_cast<size_t>(k) * 4 + n] = qn[0];
+      }
+    }
+  }
+  if (s == 4) {
+    const unsigned long long km = warp_max_u64(order_key(rmax));
+    const double am = warp_max(rabs);
+    const double s2 = warp_sum(rs2);
+    if (lane == 0) {
+      atomicMax(&a.sc->rmax[n], km);
+      atomicMax(&a.sc->rabs[n], static_cast<unsigned long long>(__double_as_longlong(am)));
+      atomicAdd(&a.sc->rsum2[n], s2);
+    }
+  }
+}
+
+}  // namespace gcfd

