@@ -212,7 +212,9 @@ struct FreeStreamT {
 
 // Characteristic boundary state, RiemannBC (bcs.go:70-133).  QInf may differ
 // from fs.qinf (IVortex passes the exact state) while pinf/cinf stay fs's.
-template <typename T>
+// FewerPow uses p = rho C^2 / gamma, equal to Beta rho^gamma by construction
+// (rho^(gamma-1) = C^2 / (gamma Beta)), which saves one pow per point.
+template <typename T, bool FewerPow = false>
 __device__ __forceinline__ void riemann_bc(const FreeStreamT<T>& fs, const T qi[4],
                                            const T QInf[4], T nx, T ny, T out[4]) {
   const T Gamma = fs.gamma, GM1 = Gamma - T(1), OOGM1 = T(1) / GM1;
@@ -240,7 +242,7 @@ __device__ __forceinline__ void riemann_bc(const FreeStreamT<T>& fs, const T qi[
     const T u = Vnorm * nx + Vtang * tx;
     const T v = Vnorm * ny + Vtang * ty;
     const T rho = dpow(C * C / (Gamma * Beta), OOGM1);
-    const T p = Beta * dpow(rho, Gamma);
+    const T p = FewerPow ? rho * C * C / Gamma : Beta * dpow(rho, Gamma);
     out[0] = rho;
     out[1] = rho * u;
     out[2] = rho * v;

@@ -101,8 +101,12 @@ struct gcfd_ctx {
   float* Dk[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   float* R3 = nullptr;
   float *mfaces = nullptr, *mfhat = nullptr, *mcorr = nullptr;
-  double* mbase = nullptr;
+  float2* mbase = nullptr;
   double* mexBC = nullptr;
+  float *Qhi = nullptr, *Qlo = nullptr;
+  bool fp64Stale = false;  // mixed path: Q[0] lags the compensated state
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t evFork = nullptr, evJoin = nullptr;
   float *mDivT = nullptr, *mIop = nullptr, *mgeo = nullptr, *mII = nullptr;
   int* meslot = nullptr;
   float *mnx = nullptr, *mny = nullptr, *moohK = nullptr;
@@ -120,6 +124,9 @@ struct gcfd_ctx {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
+    if (evFork) cudaEventDestroy(evFork);
+    if (evJoin) cudaEventDestroy(evJoin);
+    if (stream2) cudaStreamDestroy(stream2);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -290,6 +297,8 @@ struct MixedLaunch {
     a.nBC = c->nBC;
     a.stage = stage;
     a.Q0 = Q0;
+    a.Qhi = c->Qhi;
+    a.Qlo = c->Qlo;
     a.dQ0 = c->dQ0;
     for (int i = 0; i < 5; ++i) a.D[i] = c->Dk[i];
     a.R3 = c->R3;
@@ -333,16 +342,29 @@ struct MixedLaunch {
     return a;
   }
   static int gridE(gcfd_ctx* c) { return (c->K + 31) / 32; }
-  static void edges(gcfd_ctx* c, int s, double* Q0, const double* time, unsigned long long* gmax) {
+  // Interior edges on the main stream; boundary edges (FP64, transcendental
+  // work, few threads) concurrently on a forked stream, joined before the stage.
+  static void edges(gcfd_ctx* c, int s, double* Q0, const double* time, unsigned long long* gmax,
+                    bool fork) {
     const MixedArgs a = args(c, s, Q0, time, gmax);
+    cudaStream_t sb = c->stream;
+    if (fork && c->nBC > 0) {
+      cudaEventRecord(c->evFork, c->stream);
+      cudaStreamWaitEvent(c->stream2, c->evFork, 0);
+      sb = c->stream2;
+    }
+    if (c->nBC > 0)
+      k_mixed_edge_bc<N><<<(c->nBC + 7) / 8, dim3(8, MixedDims<N>::NE), 0, sb>>>(a);
     if (c->nInt > 0) {
       if (c->prm.flux_type == GCFD_FLUX_ROE_ER)
         k_mixed_edge<N, true><<<(c->nInt + 127) / 128, 128, 0, c->stream>>>(a);
       else
         k_mixed_edge<N, false><<<(c->nInt + 127) / 128, 128, 0, c->stream>>>(a);
     }
-    if (c->nBC > 0)
-      k_mixed_edge_bc<N><<<(c->nBC + 7) / 8, dim3(8, MixedDims<N>::NE), 0, c->stream>>>(a);
+    if (fork && c->nBC > 0) {
+      cudaEventRecord(c->evJoin, c->stream2);
+      cudaStreamWaitEvent(c->stream, c->evJoin, 0);
+    }
   }
   static void prepare(gcfd_ctx* c, double* Q0) {
     k_mixed_prepare<N><<<gridE(c), 128, 0, c->stream>>>(args(c, 0, Q0, nullptr, nullptr));
@@ -371,7 +393,7 @@ struct MixedLaunch {
     acc(3, 0, 1);
     for (int s = 0; s < 5; ++s) {
       mark(2);
-      edges(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]);
+      edges(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s], ev == nullptr);
       mark(3);
       k_mixed_stage<N><<<gridE(c), 128, 0, c->stream>>>(args(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]));
       mark(4);
@@ -385,11 +407,22 @@ struct MixedLaunch {
   }
   static void rhs(gcfd_ctx* c) {
     prepare(c, c->Qtmp);
-    edges(c, 0, c->Qtmp, &c->sc->rhs_time, &c->sc->gmax[0]);
+    edges(c, -1, c->Qtmp, &c->sc->rhs_time, &c->sc->gmax[0], false);
     k_mixed_stage<N><<<gridE(c), 128, 0, c->stream>>>(args(c, -1, c->Qtmp, &c->sc->rhs_time, &c->sc->gmax[0]));
   }
   static void prep_state(gcfd_ctx* c) { prepare(c, c->Q[0]); }
 };
+
+// Mixed path: rebuild the FP64 state Q[0] from the compensated pair.
+int sync_fp64_state(gcfd_ctx* c) {
+  if (!c->fp32 || !c->fp64Stale) return GCFD_OK;
+  const size_t n = static_cast<size_t>(4) * c->Np * c->K;
+  k_mixed_to_fp64<<<static_cast<int>(std::min<size_t>((n + 255) / 256, 152 * 16)), 256, 0, c->stream>>>(
+      c->Qhi, c->Qlo, c->Q[0], n);
+  GCFD_CUDA(c, cudaGetLastError());
+  c->fp64Stale = false;
+  return GCFD_OK;
+}
 
 struct Ops {
   void (*step)(gcfd_ctx*, cudaEvent_t*, double*, int*);
@@ -514,12 +547,19 @@ int build_mixed(gcfd_ctx* c) {
   for (int i = 1; i <= 4; ++i)
     if ((rc = dalloc(c, &c->Dk[i], nS))) return rc;
   if ((rc = dalloc(c, &c->R3, nS))) return rc;
-  if ((rc = dalloc(c, &c->mfaces, static_cast<size_t>(c->nEdges) * 2 * 4 * NE))) return rc;
-  if ((rc = dalloc(c, &c->mfhat, static_cast<size_t>(c->nEdges) * 4 * NE))) return rc;
+  const int NEP = (NE + 1) & ~1;  // edge-major stride, see MixedDims::NEP
+  if ((rc = dalloc(c, &c->mfaces, static_cast<size_t>(c->nEdges) * 2 * 4 * NEP))) return rc;
+  if ((rc = dalloc(c, &c->mfhat, static_cast<size_t>(c->nEdges) * 4 * NEP))) return rc;
   if ((rc = dalloc(c, &c->mcorr, static_cast<size_t>(c->nEdges) * 4))) return rc;
   if ((rc = dalloc(c, &c->mbase, static_cast<size_t>(K) * 4))) return rc;
+  if ((rc = dalloc(c, &c->Qhi, nS))) return rc;
+  if ((rc = dalloc(c, &c->Qlo, nS))) return rc;
+  GCFD_CUDA(c, cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+  GCFD_CUDA(c, cudaEventCreateWithFlags(&c->evFork, cudaEventDisableTiming));
+  GCFD_CUDA(c, cudaEventCreateWithFlags(&c->evJoin, cudaEventDisableTiming));
   if ((rc = dalloc(c, &c->mexBC, static_cast<size_t>(std::max(c->nBC, 1)) * NE * 4))) return rc;
-  GCFD_CUDA(c, cudaMemset(c->mfaces, 0, sizeof(float) * c->nEdges * 2 * 4 * NE));
+  GCFD_CUDA(c, cudaMemset(c->mfaces, 0, sizeof(float) * c->nEdges * 2 * 4 * NEP));
+  GCFD_CUDA(c, cudaMemset(c->mfhat, 0, sizeof(float) * c->nEdges * 4 * NEP));
   GCFD_CUDA(c, cudaMemset(c->mcorr, 0, sizeof(float) * c->nEdges * 4));
   // DivInt^T, rows = flux DOF j, cols = output point r padded to NPP.
   std::vector<float> divT(static_cast<size_t>(NF) * NPP, 0.f), iop(static_cast<size_t>(3 * NE) * NPP, 0.f);
@@ -764,6 +804,7 @@ int gcfd_set_state(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doub
   if (rc) return rc;
   if ((rc = copy_shards(c, c->Q[0], nshards, Kmax, Q, true, nullptr))) return rc;
   c->dirty = true;
+  c->fp64Stale = false;
   GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
   return GCFD_OK;
 }
@@ -772,6 +813,7 @@ int gcfd_get_state(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, double* co
   if (!c || !Q) return c ? fail(c, GCFD_ERR_ARG, "null state") : GCFD_ERR_ARG;
   int rc = check_shards(c, nshards, Kmax);
   if (rc) return rc;
+  if ((rc = sync_fp64_state(c))) return rc;
   if ((rc = copy_shards(c, c->Q[0], nshards, Kmax, nullptr, false, Q))) return rc;
   GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
   return GCFD_OK;
@@ -782,11 +824,14 @@ int gcfd_set_state_device(gcfd_ctx* c, const double* dQ) {
   GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], dQ, sizeof(double) * 4 * c->Np * static_cast<size_t>(c->K),
                                cudaMemcpyDeviceToDevice, c->stream));
   c->dirty = true;
+  c->fp64Stale = false;
   return GCFD_OK;
 }
 
 int gcfd_get_state_device(gcfd_ctx* c, double* dQ) {
   if (!c || !dQ) return c ? fail(c, GCFD_ERR_ARG, "null state") : GCFD_ERR_ARG;
+  int rc = sync_fp64_state(c);
+  if (rc) return rc;
   GCFD_CUDA(c, cudaMemcpyAsync(dQ, c->Q[0], sizeof(double) * 4 * c->Np * static_cast<size_t>(c->K),
                                cudaMemcpyDeviceToDevice, c->stream));
   return GCFD_OK;
@@ -814,6 +859,7 @@ int gcfd_rhs(gcfd_ctx* c, double time, int32_t nshards, const int32_t* Kmax, con
   if (!c || !Q || !RHS) return c ? fail(c, GCFD_ERR_ARG, "null state") : GCFD_ERR_ARG;
   int rc = check_shards(c, nshards, Kmax);
   if (rc) return rc;
+  if ((rc = sync_fp64_state(c))) return rc;  // the RHS reuses the stage-0 buffers
   if ((rc = copy_shards(c, c->Qtmp, nshards, Kmax, Q, true, nullptr))) return rc;
   GCFD_CUDA(c, cudaMemcpyAsync(&c->sc->rhs_time, &time, sizeof(double), cudaMemcpyHostToDevice,
                                c->stream));
@@ -841,6 +887,7 @@ int gcfd_step(gcfd_ctx* c, int32_t nsteps, double* time, double* dt_last, double
   int rc = prepare_if_dirty(c);
   if (rc) return rc;
   for (int i = 0; i < nsteps; ++i) GCFD_CUDA(c, cudaGraphLaunch(c->graphExec, c->stream));
+  if (nsteps > 0 && c->fp32) c->fp64Stale = true;
   Scalars h;
   GCFD_CUDA(c, cudaMemcpyAsync(&h, c->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
   GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -868,6 +915,7 @@ int gcfd_enqueue_steps(gcfd_ctx* c, int32_t nsteps) {
   int rc = prepare_if_dirty(c);
   if (rc) return rc;
   for (int i = 0; i < nsteps; ++i) GCFD_CUDA(c, cudaGraphLaunch(c->graphExec, c->stream));
+  if (nsteps > 0 && c->fp32) c->fp64Stale = true;
   return GCFD_OK;
 }
 
@@ -881,10 +929,13 @@ int gcfd_profile_step(gcfd_ctx* c, double* kernel_ms4, int32_t* launches4) {
   if (!c || !kernel_ms4 || !launches4) return GCFD_ERR_ARG;
   double ms[4] = {0, 0, 0, 0};
   int l[4] = {0, 0, 0, 0};
+  int rc = sync_fp64_state(c);
+  if (rc) return rc;
   Ops o;
   select_ops(c->N, c->fp32, &o);
   o.step(c, c->ev, ms, l);
   c->dirty = false;
+  if (c->fp32) c->fp64Stale = true;
   GCFD_CUDA(c, cudaGetLastError());
   GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
   for (int i = 0; i < 4; ++i) {

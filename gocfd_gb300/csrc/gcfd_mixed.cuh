@@ -9,18 +9,25 @@
 // scale with |dQ| ~ h |grad Q| instead of |Q|, which is what keeps FP32 GEMMs
 // against the reference's ill-conditioned DivInt within the FP64 result.
 //
-// State: Q0 (the conserved state) stays FP64.  SSP(5,4) stage k is stored as
-// the FP32 increment D_k = Q_k - Q0: the stage weights on (Q0, Q_k) sum to one
-// (euler.go:511-564), so Q_{k+1} = Q0 + b D_k + c dt RHS exactly, and the final
-// increment R = a2 D2 + a3 D3 + a4 D4 + ... is added to Q0 once per step in FP64.
+// State: the conserved state Q0 is accumulated in compensated FP32 (a hi/lo
+// float pair per value, ~48 significant bits), which keeps the step free of
+// FP64 instructions - GB300's FP64 pipe runs at 1/64 of the FP32 rate.  The
+// FP64 copy of Q0 is rebuilt from hi + lo whenever the caller reads it.
+// SSP(5,4) stage k is stored as the FP32 increment D_k = Q_k - Q0: the stage
+// weights on (Q0, Q_k) sum to one (euler.go:511-564), so Q_{k+1} = Q0 + b D_k +
+// c dt RHS exactly, and the final increment R = a2 D2 + a3 D3 + a4 D4 + ... is
+// added to Q0 once per step.
 //
 // Layouts (HBM):
-//   Q0[n][i][k] FP64, dQ0[n][i][k] = Q0 - Q0(point 0) FP32, D1..D4, R3 FP32
+//   Qhi/Qlo[n][i][k] FP32 pair (state), dQ0[n][i][k] = Q0 - Q0(point 0) FP32,
+//   D1..D4, R3 FP32 stage increments / stage-3 RHS
 //   faces[g][side][n][p]  FP32 dQ at edge points, side 0 = left element's CCW
-//                         order, side 1 = right element's CCW order
-//   fhat[g][n][p]         FP32 fhat - n_L.F(Qb_L), left order
+//                         order, side 1 = right element's CCW order; p padded
+//                         to NEP = NpEdge rounded up to even
+//   fhat[g][n][p]         FP32 fhat - n_L.F(Qb_L), left order, p padded to NEP
 //   corr[g][n]            FP32 n_L.(F(Qb_R) - F(Qb_L))
-//   base[k][n]            FP64 Qb of the current stage (gathered by the edge kernel)
+//   base[k][n]            float2 (hi, lo) Qb of the current stage, gathered by the
+//                         edge kernels
 // Element kernels run one thread per (element, variable): a block is 32
 // elements x 4 variables, warp w owns variable w, so every row access is a
 // 128-byte coalesced transaction.
@@ -38,12 +45,12 @@ struct BasePrim {
   float rho, m, n, E, u, v, p, H;
 };
 
-__device__ __forceinline__ BasePrim base_prim(const double b[4], float gm1) {
+__device__ __forceinline__ BasePrim base_prim(const float b[4], float gm1) {
   BasePrim s;
-  s.rho = static_cast<float>(b[0]);
-  s.m = static_cast<float>(b[1]);
-  s.n = static_cast<float>(b[2]);
-  s.E = static_cast<float>(b[3]);
+  s.rho = b[0];
+  s.m = b[1];
+  s.n = b[2];
+  s.E = b[3];
   const float ir = 1.0f / s.rho;
   s.u = s.m * ir;
   s.v = s.n * ir;
@@ -169,23 +176,48 @@ __device__ __forceinline__ void riemann_delta(int kind, const BasePrim& b, const
 }
 
 // ---------------------------------------------------------------------------
+// Compensated FP32 arithmetic (Knuth two-sum, Dekker fast-two-sum).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  e = b - (s - a);
+}
+// (hi, lo) += x
+__device__ __forceinline__ void df_add(float& hi, float& lo, float x) {
+  float s, e;
+  two_sum(hi, x, s, e);
+  e += lo;
+  fast_two_sum(s, e, hi, lo);
+}
+// (ah, al) - (bh, bl) rounded to FP32; exact in the leading part whenever the
+// two values are within a factor of two (Sterbenz).
+__device__ __forceinline__ float df_diff(float ah, float al, float bh, float bl) {
+  return (ah - bh) + (al - bl);
+}
+
 struct MixedArgs {
   int K, nInt, nBC;
   int stage;
-  double* Q0;                 // FP64 state
+  double* Q0;                 // FP64 state (source after set_state, target of to_fp64)
+  float* Qhi;                 // compensated FP32 state
+  float* Qlo;
   float* dQ0;                 // Q0 - Q0(point 0)
-  float* D[5];                // D[1..4] stage increments (D[0] unused), D[4] slot 0 = R3 store
+  float* D[5];                // D[1..4] stage increments (D[0] unused)
   float* R3;                  // stage-3 RHS
   float* faces;               // [g][2][4][NE]
   float* fhat;                // [g][4][NE]
   float* corr;                // [g][4]
-  double* base;               // [k][4] reference state; updated in place to the next stage's
+  float2* base;               // [k][4] (hi, lo) reference state; updated in place per stage
   const float* Div;           // DivInt^T padded: [NF][NPP]
   const float* Iop;           // FluxEdgeInterp padded: [NE3][NPP]
   const float* geo;           // [6][K]: Jdet, Jinv0..3, 1/Jdet
   const float* II;            // [3][K] IInII
   const int* eslot;           // [3][K] edge id * 2 + side
-  // edge kernel
+  // edge kernels
   const int* ekL;
   const int* ekR;
   const float* enx;
@@ -224,18 +256,20 @@ template <int N>
 struct MixedDims {
   static constexpr int NP = Dims<N>::NP, NE = Dims<N>::NE, NE3 = Dims<N>::NE3, NF = Dims<N>::NF;
   static constexpr int NPP = (NP + 3) & ~3;  // padded to float4
+  // Edge-major stride per (slot, variable): NpEdge rounded up to even, so every
+  // (slot, variable) run starts 8-byte aligned and moves as float2.
+  static constexpr int NEP = (NE + 1) & ~1;
 };
 
 // Writes the element's 3 edges of face deltas for variable n (rows e*NE + p).
 template <int N>
-__device__ __forceinline__ void write_faces(const MixedArgs& a, const float* sI, int k, int n,
-                                            const float dq[]) {
-  constexpr int NE = MixedDims<N>::NE, NPP = MixedDims<N>::NPP;
-  const size_t sK = static_cast<size_t>(a.K);
+__device__ __forceinline__ void write_faces(const MixedArgs& a, const float* sI, const int eslot[3],
+                                            int n, const float dq[]) {
+  constexpr int NE = MixedDims<N>::NE, NPP = MixedDims<N>::NPP, NEP = MixedDims<N>::NEP;
 #pragma unroll
   for (int e = 0; e < 3; ++e) {
-    const int slot = a.eslot[e * sK + k];
-    float* dst = a.faces + (static_cast<size_t>(slot) * 4 + n) * NE;
+    float* dst = a.faces + (static_cast<size_t>(eslot[e]) * 4 + n) * NEP;
+    float out[NE];
 #pragma unroll
     for (int p = 0; p < NE; ++p) {
       const float4* row = reinterpret_cast<const float4*>(sI + (e * NE + p) * NPP);
@@ -248,12 +282,16 @@ __device__ __forceinline__ void write_faces(const MixedArgs& a, const float* sI,
         acc = fmaf(w.z, dq[4 * i4 + 2], acc);
         acc = fmaf(w.w, dq[4 * i4 + 3], acc);
       }
-      dst[p] = acc;
+      out[p] = acc;
     }
+    // (slot*4 + n) * NEP floats with NEP even: 8-byte aligned, pairs go out as float2.
+#pragma unroll
+    for (int p = 0; p + 1 < NE; p += 2) reinterpret_cast<float2*>(dst)[p / 2] = make_float2(out[p], out[p + 1]);
+    if (NE & 1) dst[NE - 1] = out[NE - 1];
   }
 }
 
-// Stage-0 preparation from the FP64 state: dQ0, faces, reference states.
+// Stage-0 preparation from the FP64 state: hi/lo split, dQ0, faces, reference states.
 template <int N>
 __global__ void __launch_bounds__(128) k_mixed_prepare(MixedArgs a) {
   constexpr int NP = MixedDims<N>::NP, NE3 = MixedDims<N>::NE3, NPP = MixedDims<N>::NPP;
@@ -264,78 +302,117 @@ __global__ void __launch_bounds__(128) k_mixed_prepare(MixedArgs a) {
   const int k = blockIdx.x * 32 + (threadIdx.x & 31);
   if (k >= a.K) return;
   const size_t sK = static_cast<size_t>(a.K);
-  const double* q = a.Q0 + static_cast<size_t>(n) * NP * sK + k;
-  const double q0 = q[0];
+  const size_t off = static_cast<size_t>(n) * NP * sK + k;
+  const double q0 = a.Q0[off];
   float dq[NPP];
 #pragma unroll
   for (int i = 0; i < NPP; ++i) dq[i] = 0.0f;
 #pragma unroll
   for (int i = 0; i < NP; ++i) {
-    dq[i] = static_cast<float>(q[i * sK] - q0);
-    a.dQ0[(static_cast<size_t>(n) * NP + i) * sK + k] = dq[i];
+    const double q = a.Q0[off + i * sK];
+    const float hi = static_cast<float>(q);
+    a.Qhi[off + i * sK] = hi;
+    a.Qlo[off + i * sK] = static_cast<float>(q - static_cast<double>(hi));
+    dq[i] = static_cast<float>(q - q0);
+    a.dQ0[off + i * sK] = dq[i];
   }
-  a.base[static_cast<size_t>(k) * 4 + n] = q0;
-  write_faces<N>(a, sI, k, n, dq);
+  const float h0 = static_cast<float>(q0);
+  a.base[static_cast<size_t>(k) * 4 + n] = make_float2(h0, static_cast<float>(q0 - static_cast<double>(h0)));
+  int es[3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) es[e] = a.eslot[e * sK + k];
+  write_faces<N>(a, sI, es, n, dq);
+}
+
+// FP64 copy of the compensated state, for gcfd_get_state.
+__global__ void k_mixed_to_fp64(const float* __restrict__ hi, const float* __restrict__ lo,
+                                double* __restrict__ q, size_t n) {
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x)
+    q[i] = static_cast<double>(hi[i]) + static_cast<double>(lo[i]);
 }
 
 // (c) interior-edge fluxes in delta form, one thread per mesh edge.  RoeER
 // instantiates the Roe-ER flux in FP64 (fluxes.go:415-503 has no delta form).
 template <int N, bool RoeER>
 __global__ void __launch_bounds__(128) k_mixed_edge(MixedArgs a) {
-  constexpr int NE = MixedDims<N>::NE;
+  constexpr int NE = MixedDims<N>::NE, NEP = MixedDims<N>::NEP;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   double smax = 0.0;
   if (g < a.nInt) {
     const int kL = a.ekL[g], kR = a.ekR[g];
     const float nx = a.enx[g], ny = a.eny[g];
     const float oohK = a.eoohK[g];
-    double bL[4];
-    float dB[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) bL[c] = a.base[static_cast<size_t>(kL) * 4 + c];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) dB[c] = static_cast<float>(a.base[static_cast<size_t>(kR) * 4 + c] - bL[c]);
-    const double gm1d = a.gammaD - 1.0;
+    float bh[4], bl[4], dB[4];
+    const float4* pL = reinterpret_cast<const float4*>(a.base + static_cast<size_t>(kL) * 4);
+    const float4* pR = reinterpret_cast<const float4*>(a.base + static_cast<size_t>(kR) * 4);
+    const float4 L01 = pL[0], L23 = pL[1], R01 = pR[0], R23 = pR[1];
+    bh[0] = L01.x; bl[0] = L01.y; bh[1] = L01.z; bl[1] = L01.w;
+    bh[2] = L23.x; bl[2] = L23.y; bh[3] = L23.z; bl[3] = L23.w;
+    dB[0] = df_diff(R01.x, R01.y, bh[0], bl[0]);
+    dB[1] = df_diff(R01.z, R01.w, bh[1], bl[1]);
+    dB[2] = df_diff(R23.x, R23.y, bh[2], bl[2]);
+    dB[3] = df_diff(R23.z, R23.w, bh[3], bl[3]);
     const float gm1 = a.gamma - 1.0f;
-    const BasePrim b = base_prim(bL, gm1);
+    const BasePrim b = base_prim(bh, gm1);
     const Gas<float> gf{a.gamma, gm1, 1.0f / gm1};
-    const float* fL = a.faces + static_cast<size_t>(g) * 2 * 4 * NE;
-    const float* fR = fL + 4 * NE;
-    float* fo = a.fhat + static_cast<size_t>(g) * 4 * NE;
+    const float* fL = a.faces + static_cast<size_t>(g) * 2 * 4 * NEP;
+    const float* fR = fL + 4 * NEP;
+    float dl[4][NEP], dr[4][NEP];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+#pragma unroll
+      for (int p = 0; p < NEP; p += 2) {
+        const float2 l = reinterpret_cast<const float2*>(fL + c * NEP)[p / 2];
+        const float2 r = reinterpret_cast<const float2*>(fR + c * NEP)[p / 2];
+        dl[c][p] = l.x; dl[c][p + 1] = l.y;
+        dr[c][p] = r.x; dr[c][p + 1] = r.y;
+      }
+    }
+    float fo[4][NE];
     float sm = 0.0f;
 #pragma unroll
     for (int p = 0; p < NE; ++p) {
-      float dl[4], dr[4], f[4];
+      float ql[4], qr[4], f[4];
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        dl[c] = fL[c * NE + p];
-        dr[c] = fR[c * NE + (NE - 1 - p)] + dB[c];
+        ql[c] = dl[c][p];
+        qr[c] = dr[c][NE - 1 - p] + dB[c];
       }
       if (RoeER) {
-        double QLd[4], QRd[4], fd[4], Fx[4], Fy[4];
+        double QLd[4], QRd[4], fd[4], Fx[4], Fy[4], bd[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-          QLd[c] = bL[c] + dl[c];
-          QRd[c] = bL[c] + dr[c];
+          bd[c] = static_cast<double>(bh[c]) + static_cast<double>(bl[c]);
+          QLd[c] = bd[c] + ql[c];
+          QRd[c] = bd[c] + qr[c];
         }
+        const double gm1d = a.gammaD - 1.0;
         const Gas<double> gd{a.gammaD, gm1d, 1.0 / gm1d};
         flux_roe_er(gd, QLd, QRd, static_cast<double>(nx), static_cast<double>(ny), fd);
-        euler_flux(gd, bL, Fx, Fy);
+        euler_flux(gd, bd, Fx, Fy);
 #pragma unroll
         for (int c = 0; c < 4; ++c)
           f[c] = static_cast<float>(fd[c] - (static_cast<double>(nx) * Fx[c] + static_cast<double>(ny) * Fy[c]));
       } else {
-        riemann_delta(a.flux, b, dl, dr, nx, ny, a.gamma, f);
+        riemann_delta(a.flux, b, ql, qr, nx, ny, a.gamma, f);
       }
 #pragma unroll
-      for (int c = 0; c < 4; ++c) fo[c * NE + p] = f[c];
-      const float QL[4] = {b.rho + dl[0], b.m + dl[1], b.n + dl[2], b.E + dl[3]};
+      for (int c = 0; c < 4; ++c) fo[c][p] = f[c];
+      const float QL[4] = {b.rho + ql[0], b.m + ql[1], b.n + ql[2], b.E + ql[3]};
       sm = fmaxf(sm, oohK * (speed(QL[0], QL[1], QL[2]) + sound_speed(gf, QL[0], QL[1], QL[2], QL[3])));
+    }
+    float* out = a.fhat + static_cast<size_t>(g) * 4 * NEP;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+#pragma unroll
+      for (int p = 0; p + 1 < NE; p += 2)
+        reinterpret_cast<float2*>(out + c * NEP)[p / 2] = make_float2(fo[c][p], fo[c][p + 1]);
+      if (NE & 1) out[c * NEP + NE - 1] = fo[c][NE - 1];
     }
     float cr[4];
     delta_normal_flux(b, dB, nx, ny, gm1, cr);
-#pragma unroll
-    for (int c = 0; c < 4; ++c) a.corr[static_cast<size_t>(g) * 4 + c] = cr[c];
+    reinterpret_cast<float4*>(a.corr)[g] = make_float4(cr[0], cr[1], cr[2], cr[3]);
     smax = static_cast<double>(sm);
     a.edgeSpeed[g] = smax;
   }
@@ -348,10 +425,11 @@ __global__ void __launch_bounds__(128) k_mixed_edge(MixedArgs a) {
 // the physical normal flux in FP64 (bcs.go:11-133, edges.go:413-452), then the
 // delta to FP32.  GB300's FP64 pipe is narrow and these points carry the
 // transcendental work (exp/pow), so one thread owns one (edge, point): a block
-// is 8 edges (threadIdx.x) x NpEdge points (threadIdx.y), spread over many SMs.
+// is 8 edges (threadIdx.x) x NpEdge points (threadIdx.y), spread over many SMs,
+// and the kernel runs on a forked stream beside the interior-edge kernel.
 template <int N>
 __global__ void __launch_bounds__(8 * MixedDims<N>::NE) k_mixed_edge_bc(MixedArgs a) {
-  constexpr int NE = MixedDims<N>::NE;
+  constexpr int NE = MixedDims<N>::NE, NEP = MixedDims<N>::NEP;
   __shared__ double sspeed[NE][8];
   const int tx = threadIdx.x, p = threadIdx.y;
   const int bb = blockIdx.x * 8 + tx;
@@ -363,20 +441,23 @@ __global__ void __launch_bounds__(8 * MixedDims<N>::NE) k_mixed_edge_bc(MixedArg
     const double nxd = a.enx[g], nyd = a.eny[g];
     double bL[4];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) bL[c] = a.base[static_cast<size_t>(kL) * 4 + c];
+    for (int c = 0; c < 4; ++c) {
+      const float2 v = a.base[static_cast<size_t>(kL) * 4 + c];
+      bL[c] = static_cast<double>(v.x) + static_cast<double>(v.y);
+    }
     const double gm1d = a.gammaD - 1.0;
     const Gas<double> gd{a.gammaD, gm1d, 1.0 / gm1d};
     double Fx[4], Fy[4];
     euler_flux(gd, bL, Fx, Fy);
-    const float* fL = a.faces + static_cast<size_t>(g) * 2 * 4 * NE;
+    const float* fL = a.faces + static_cast<size_t>(g) * 2 * 4 * NEP;
     double qi[4], qb[4], f[4];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) qi[c] = bL[c] + static_cast<double>(fL[c * NE + p]);
+    for (int c = 0; c < 4; ++c) qi[c] = bL[c] + static_cast<double>(fL[c * NEP + p]);
     bool wall = false;
     switch (a.bcFlag[bb]) {
-      case 4: riemann_bc(a.fsFar, qi, a.fsFar.qinf, nxd, nyd, qb); break;
-      case 1: riemann_bc(a.fsIn, qi, a.fsIn.qinf, nxd, nyd, qb); break;
-      case 8: riemann_bc(a.fsOut, qi, a.fsOut.qinf, nxd, nyd, qb); break;
+      case 4: riemann_bc<double, true>(a.fsFar, qi, a.fsFar.qinf, nxd, nyd, qb); break;
+      case 1: riemann_bc<double, true>(a.fsIn, qi, a.fsIn.qinf, nxd, nyd, qb); break;
+      case 8: riemann_bc<double, true>(a.fsOut, qi, a.fsOut.qinf, nxd, nyd, qb); break;
       case 9: {
         // The BC time is frozen for the 5 stages (euler.go:621): evaluate the
         // exact state once per step and reuse it.
@@ -391,7 +472,7 @@ __global__ void __launch_bounds__(8 * MixedDims<N>::NE) k_mixed_edge_bc(MixedArg
 #pragma unroll
           for (int c = 0; c < 4; ++c) ex[c] = cache[c];
         }
-        riemann_bc(a.fsFar, qi, ex, nxd, nyd, qb);
+        riemann_bc<double, true>(a.fsFar, qi, ex, nxd, nyd, qb);
         break;
       }
       case 5: case 6:
@@ -412,9 +493,9 @@ __global__ void __launch_bounds__(8 * MixedDims<N>::NE) k_mixed_edge_bc(MixedArg
 #pragma unroll
       for (int c = 0; c < 4; ++c) f[c] = nxd * Gx[c] + nyd * Gy[c];
     }
-    float* fo = a.fhat + static_cast<size_t>(g) * 4 * NE;
+    float* fo = a.fhat + static_cast<size_t>(g) * 4 * NEP;
 #pragma unroll
-    for (int c = 0; c < 4; ++c) fo[c * NE + p] = static_cast<float>(f[c] - (nxd * Fx[c] + nyd * Fy[c]));
+    for (int c = 0; c < 4; ++c) fo[c * NEP + p] = static_cast<float>(f[c] - (nxd * Fx[c] + nyd * Fy[c]));
     ws = static_cast<double>(a.eoohK[g]) * (speed(qb[0], qb[1], qb[2]) + sound_speed(gd, qb[0], qb[1], qb[2], qb[3]));
   }
   sspeed[p][tx] = ws;
@@ -435,11 +516,11 @@ __global__ void __launch_bounds__(8 * MixedDims<N>::NE) k_mixed_edge_bc(MixedArg
 template <int N>
 __global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
   constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NE3 = MixedDims<N>::NE3;
-  constexpr int NF = MixedDims<N>::NF, NPP = MixedDims<N>::NPP;
+  constexpr int NF = MixedDims<N>::NF, NPP = MixedDims<N>::NPP, NEP = MixedDims<N>::NEP;
   __shared__ __align__(16) float sD[NF * NPP];
   __shared__ __align__(16) float sI[NE3 * NPP];
   __shared__ float sdq[4][NP][33];
-  __shared__ double sbase[4][32];
+  __shared__ float sbase[4][32];
   __shared__ float sfh[4][NE3][32];   // this element's edge fluxes, prefetched
   __shared__ float scorr[4][3][32];
   for (int i = threadIdx.x; i < NF * NPP; i += blockDim.x) sD[i] = a.Div[i];
@@ -448,36 +529,19 @@ __global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
   const int k = blockIdx.x * 32 + lane;
   const bool active = k < a.K;
   const size_t sK = static_cast<size_t>(a.K);
+  const size_t off = static_cast<size_t>(n) * NP * sK + k;
   const int s = a.stage;
-  // Stage input deltas relative to point 0 of the stage state.
-  float dq0[NP], ds[NP];
-  if (active) {
-    const float* q0 = a.dQ0 + static_cast<size_t>(n) * NP * sK + k;
-#pragma unroll
-    for (int i = 0; i < NP; ++i) dq0[i] = q0[i * sK];
-    if (s >= 1) {
-      const float* d = a.D[s] + static_cast<size_t>(n) * NP * sK + k;
-#pragma unroll
-      for (int i = 0; i < NP; ++i) ds[i] = d[i * sK];
-    } else {
-#pragma unroll
-      for (int i = 0; i < NP; ++i) ds[i] = 0.0f;
-    }
-#pragma unroll
-    for (int i = 0; i < NP; ++i) sdq[n][i][lane] = dq0[i] + (ds[i] - ds[0]);
-    sbase[n][lane] = a.base[static_cast<size_t>(k) * 4 + n];
-  }
   // Prefetch the element's edge fluxes (a gather: 3 edges x NpEdge per
   // variable) into shared memory asynchronously; the interior work below hides
   // the latency.  Each thread later reads only what it copied itself.
-  int eslot[3];
-  float eII[3];
+  int eslot[3] = {0, 0, 0};
+  float eII[3] = {0.f, 0.f, 0.f};
   if (active) {
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
       eslot[e] = a.eslot[e * sK + k];
       eII[e] = a.II[e * sK + k];
-      const float* fh = a.fhat + (static_cast<size_t>(eslot[e] >> 1) * 4 + n) * NE;
+      const float* fh = a.fhat + (static_cast<size_t>(eslot[e] >> 1) * 4 + n) * NEP;
 #pragma unroll
       for (int p = 0; p < NE; ++p) {
         const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(&sfh[n][e * NE + p][lane]));
@@ -491,6 +555,22 @@ __global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
     }
     asm volatile("cp.async.commit_group;\n" ::);
   }
+  // Stage input deltas relative to point 0 of the stage state.
+  float dq0[NP], ds[NP];
+  if (active) {
+#pragma unroll
+    for (int i = 0; i < NP; ++i) dq0[i] = a.dQ0[off + i * sK];
+    if (s >= 1) {
+#pragma unroll
+      for (int i = 0; i < NP; ++i) ds[i] = a.D[s][off + i * sK];
+    } else {
+#pragma unroll
+      for (int i = 0; i < NP; ++i) ds[i] = 0.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < NP; ++i) sdq[n][i][lane] = dq0[i] + (ds[i] - ds[0]);
+    sbase[n][lane] = a.base[static_cast<size_t>(k) * 4 + n].x;
+  }
   // Local time step of this stage: DT persists across stages, so every thread
   // of the element reads it before the barrier and one writes it after.
   double dtLocal = 0.0;
@@ -501,13 +581,11 @@ __global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
     dtLocal = a.cfl / v;
   }
   __syncthreads();
-  double rmax = -1.7976931348623157e308, rabs = 0.0, rs2 = 0.0;
+  float rmax = -3.4028235e38f, rabs = 0.0f, rs2 = 0.0f;
   if (active) {
     const float Jd = a.geo[k], J0 = a.geo[sK + k], J1 = a.geo[2 * sK + k];
     const float J2 = a.geo[3 * sK + k], J3 = a.geo[4 * sK + k], ooJ = a.geo[5 * sK + k];
-    double bq[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) bq[c] = sbase[c][lane];
+    const float bq[4] = {sbase[0][lane], sbase[1][lane], sbase[2][lane], sbase[3][lane]};
     const float gm1 = a.gamma - 1.0f;
     const BasePrim b = base_prim(bq, gm1);
     float acc[NPP];
@@ -559,7 +637,7 @@ __global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
     for (int r = 0; r < NP; ++r) rhs[r] = -acc[r] * ooJ;
     if (s < 0) {
 #pragma unroll
-      for (int r = 0; r < NP; ++r) a.rhsOut[(static_cast<size_t>(n) * NP + r) * sK + k] = rhs[r];
+      for (int r = 0; r < NP; ++r) a.rhsOut[off + r * sK] = rhs[r];
     } else {
       double dtk;
       if (a.localDT) {
@@ -574,7 +652,6 @@ __global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
       }
       const float dt = static_cast<float>(dtk);
       float dn[NP];
-      const size_t off = static_cast<size_t>(n) * NP * sK + k;
       if (s == 0) {
 #pragma unroll
         for (int r = 0; r < NP; ++r) dn[r] = kSspC0 * (dt * rhs[r]);
@@ -598,48 +675,45 @@ __global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
         float dqn[NPP];
 #pragma unroll
         for (int r = 0; r < NPP; ++r) dqn[r] = (r < NP) ? dq0[r] + (dn[r] - dn[0]) : 0.0f;
-        write_faces<N>(a, sI, k, n, dqn);
-        a.base[static_cast<size_t>(k) * 4 + n] = a.Q0[off] + static_cast<double>(dn[0]);
+        write_faces<N>(a, sI, eslot, n, dqn);
+        float h = a.Qhi[off], l = a.Qlo[off];
+        df_add(h, l, dn[0]);
+        a.base[static_cast<size_t>(k) * 4 + n] = make_float2(h, l);
       } else {
-        // Final increment and the FP64 accumulation (rkAdvance stage 4).
-        const float* D2 = a.D[2] + off;
-        const float* D3 = a.D[3] + off;
-        const float* R3 = a.R3 + off;
-        double* q0 = a.Q0 + off;
-        double qn[NP];
-        float fmx = -3.4028235e38f, fab = 0.0f, fs2 = 0.0f;  // per-thread partials (15 values)
+        // Final increment and the compensated accumulation (rkAdvance stage 4).
+        float qh[NP], ql[NP];
 #pragma unroll
         for (int r = 0; r < NP; ++r) {
-          const float inc = kSspA2 * D2[r * sK] + kSspA3 * D3[r * sK] + kSspA4 * ds[r] +
-                            kSspR3 * (dt * R3[r * sK]) + kSspC4 * (dt * rhs[r]);
-          qn[r] = q0[r * sK] + static_cast<double>(inc);
-          q0[r * sK] = qn[r];
-          fmx = fmaxf(fmx, inc);
-          fab = fmaxf(fab, fabsf(inc));
-          fs2 = fmaf(inc, inc, fs2);
-          if (inc != inc) fab = inc;
+          const float inc = kSspA2 * a.D[2][off + r * sK] + kSspA3 * a.D[3][off + r * sK] + kSspA4 * ds[r] +
+                            kSspR3 * (dt * a.R3[off + r * sK]) + kSspC4 * (dt * rhs[r]);
+          qh[r] = a.Qhi[off + r * sK];
+          ql[r] = a.Qlo[off + r * sK];
+          df_add(qh[r], ql[r], inc);
+          a.Qhi[off + r * sK] = qh[r];
+          a.Qlo[off + r * sK] = ql[r];
+          rmax = fmaxf(rmax, inc);
+          rabs = fmaxf(rabs, fabsf(inc));
+          rs2 = fmaf(inc, inc, rs2);
+          if (inc != inc) rabs = inc;
         }
-        rmax = fmx;
-        rabs = fab;
-        rs2 = fs2;
         // Prepare the next step's stage 0 from the new state.
         float dqn[NPP];
 #pragma unroll
         for (int r = 0; r < NPP; ++r) dqn[r] = 0.0f;
 #pragma unroll
         for (int r = 0; r < NP; ++r) {
-          dqn[r] = static_cast<float>(qn[r] - qn[0]);
+          dqn[r] = df_diff(qh[r], ql[r], qh[0], ql[0]);
           a.dQ0[off + r * sK] = dqn[r];
         }
-        write_faces<N>(a, sI, k, n, dqn);
-        a.base[static_cast<size_t>(k) * 4 + n] = qn[0];
+        write_faces<N>(a, sI, eslot, n, dqn);
+        a.base[static_cast<size_t>(k) * 4 + n] = make_float2(qh[0], ql[0]);
       }
     }
   }
   if (s == 4) {
-    const unsigned long long km = warp_max_u64(order_key(rmax));
-    const double am = warp_max(rabs);
-    const double s2 = warp_sum(rs2);
+    const unsigned long long km = warp_max_u64(order_key(static_cast<double>(rmax)));
+    const double am = warp_max(static_cast<double>(rabs));
+    const double s2 = warp_sum(static_cast<double>(rs2));
     if (lane == 0) {
       atomicMax(&a.sc->rmax[n], km);
       atomicMax(&a.sc->rabs[n], static_cast<unsigned long long>(__double_as_longlong(am)));
