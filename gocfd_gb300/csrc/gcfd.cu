@@ -7,6 +7,7 @@
 #include <cstring>
 #include <memory>
 #include <stdexcept>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -14,6 +15,7 @@
 #include "dfr_element.hpp"
 #include "gcfd_kernels.cuh"
 #include "gcfd_mixed.cuh"
+#include "gcfd_diss.cuh"
 #include "mesh.hpp"
 
 using namespace gcfd;
@@ -111,6 +113,16 @@ struct gcfd_ctx {
   int* meslot = nullptr;
   float *mnx = nullptr, *mny = nullptr, *moohK = nullptr;
   bool dirty = true;  // Q0 changed outside a step: the stage-0 data must be rebuilt
+  // artificial dissipation (PerssonC0, FP64 path)
+  bool diss = false;
+  unsigned long long *sigV = nullptr, *epsV = nullptr;
+  double *DissX = nullptr, *DissY = nullptr, *VF = nullptr, *viscSpeed = nullptr;
+  double *DTVisc = nullptr, *dDiv = nullptr, *dBary = nullptr, *dV = nullptr, *dVinv = nullptr;
+  double *dmf = nullptr, *dSensP = nullptr, *dMass = nullptr, *dSensD = nullptr, *dhK = nullptr;
+  double *dnxE = nullptr, *dnyE = nullptr, *dIIE = nullptr;
+  int* detov = nullptr;
+  int nverts = 0;
+  double dissKappa = 5.0;
   std::vector<int> edgeOrder;             // device edge i -> topology edge
   std::vector<double> hnx, hny, hoohK;    // per device edge
   cudaGraph_t graph = nullptr;
@@ -230,9 +242,85 @@ struct Launch {
     a.rhsOut = c->rhsOut;
     const double g = c->fsFar.gamma;
     a.gas = Gas<T>{static_cast<T>(g), static_cast<T>(g - 1.0), static_cast<T>(1.0 / (g - 1.0))};
+    a.DissX = c->DissX;
+    a.DissY = c->DissY;
+    a.VF = c->VF;
+    a.viscSpeed = c->viscSpeed;
+    a.sigV = c->sigV;
+    a.etov = c->detov;
+    a.V = c->dV;
+    a.Vinv = c->dVinv;
+    a.mf = c->dmf;
+    a.IIE = c->dIIE;
+    a.ekL = c->ekL;
+    a.eLR = c->eLR;
+    a.gvisc = c->sc->gvisc;
+    a.DTVisc = c->DTVisc;
+    a.cdiff = 1.0 / (double(c->N + 1) * double(c->N + 1));
+    return a;
+  }
+  static DissArgs diss_args(gcfd_ctx* c, int stage, double* Qs) {
+    DissArgs a;
+    a.K = c->K;
+    a.nInt = c->nInt;
+    a.nBC = c->nBC;
+    a.stage = stage;
+    a.Qs = Qs;
+    a.Qlim = Qs;
+    a.QF = static_cast<double*>(c->QF);
+    a.Iop = c->Iop;
+    a.etov = c->detov;
+    a.hK = c->dhK;
+    a.SensP = c->dSensP;
+    a.Mass = c->dMass;
+    a.SensD = c->dSensD;
+    a.V = c->dV;
+    a.Vinv = c->dVinv;
+    a.mf = c->dmf;
+    a.Div = c->dDiv;
+    a.Bary = c->dBary;
+    a.Jinv = c->Jinv;
+    a.Jdet = c->Jdet;
+    a.nxE = c->dnxE;
+    a.nyE = c->dnyE;
+    a.IIE = c->dIIE;
+    a.elemEdge = c->elemEdge;
+    a.ekL = c->ekL;
+    a.ekR = c->ekR;
+    a.eLR = c->eLR;
+    a.enx = c->enx;
+    a.eny = c->eny;
+    a.eIIL = c->eIIL;
+    a.eoohK = c->eoohK;
+    a.sigV = c->sigV;
+    a.epsV = c->epsV;
+    a.DissX = c->DissX;
+    a.DissY = c->DissY;
+    a.VF = c->VF;
+    a.viscSpeed = c->viscSpeed;
+    a.gvisc = (stage >= 0) ? &c->sc->gvisc[stage] : &c->sc->gvisc[0];
+    a.kappa = c->dissKappa;
+    a.eps0 = 5.0 / 1.5;
+    a.S0 = 4.0 / std::pow(double(c->N + 1), 4.0);
+    a.omega = double(c->N * c->N);
     return a;
   }
   static int grid(int n) { return (n + 127) / 128; }
+  // Sensor, vertex smoothing, rkStep-2 limiter and faces (replaces interp).
+  static void diss_front(gcfd_ctx* c, int stage, double* Qs) {
+    cudaMemsetAsync(c->sigV, 0, sizeof(unsigned long long) * c->nverts, c->stream);
+    cudaMemsetAsync(c->epsV, 0, sizeof(unsigned long long) * c->nverts, c->stream);
+    const DissArgs d = diss_args(c, stage, Qs);
+    k_diss_sensor<N><<<grid(c->K), 128, 0, c->stream>>>(d);
+    if (stage == 2) k_diss_limit<N><<<grid(4 * c->K), 128, 0, c->stream>>>(d);
+    interp(c, Qs);
+  }
+  static void diss_middle(gcfd_ctx* c, int stage, double* Qs) {
+    const DissArgs d = diss_args(c, stage, Qs);
+    constexpr int NF = Dims<N>::NF;
+    k_diss_grad<N><<<grid(c->K), 128, sizeof(double) * (NF * NF + NF * 3), c->stream>>>(d);
+    k_diss_edge<N><<<grid(c->nInt + c->nBC), 128, 0, c->stream>>>(d);
+  }
 
   static void interp(gcfd_ctx* c, const double* Qs) {
     k_interp<N, T><<<grid(c->K), 128, 0, c->stream>>>(Qs, static_cast<T*>(c->QF), c->Iop, c->K);
@@ -243,7 +331,15 @@ struct Launch {
     k_edge_flux<N, T><<<grid(c->nInt + c->nBC), 128, 0, c->stream>>>(a);
   }
   static void update(gcfd_ctx* c, int stage, const double* Qs) {
-    k_div_update<N, T><<<grid(c->K), 128, 0, c->stream>>>(update_args(c, stage, Qs));
+    if (c->diss) {
+      // Euler RHS into rhsOut, then dissipation + filter + stage update.
+      if constexpr (std::is_same<T, double>::value) {
+        k_div_update<N, T><<<grid(c->K), 128, 0, c->stream>>>(update_args(c, -1, Qs));
+        k_diss_update<N><<<grid(c->K), 128, 0, c->stream>>>(update_args(c, stage, Qs));
+      }
+    } else {
+      k_div_update<N, T><<<grid(c->K), 128, 0, c->stream>>>(update_args(c, stage, Qs));
+    }
   }
   // One RK step: RungeKutta5SSP.Step (euler.go:408-418).
   static void step(gcfd_ctx* c, cudaEvent_t* ev, double* ms, int* launches) {
@@ -264,9 +360,11 @@ struct Launch {
     acc(3, 0, 1);
     for (int s = 0; s < 5; ++s) {
       mark(2);
-      interp(c, c->Q[s]);
+      if (c->diss) diss_front(c, s, c->Q[s]);
+      else interp(c, c->Q[s]);
       mark(3);
       edge(c, &c->sc->time, &c->sc->gmax[s]);
+      if (c->diss) diss_middle(c, s, c->Q[s]);
       mark(4);
       update(c, s, c->Q[s]);
       mark(5);
@@ -280,8 +378,10 @@ struct Launch {
     acc(3, 6, 7);
   }
   static void rhs(gcfd_ctx* c) {
-    interp(c, c->Qtmp);
+    if (c->diss) diss_front(c, -1, c->Qtmp);
+    else interp(c, c->Qtmp);
     edge(c, &c->sc->rhs_time, &c->sc->gmax[0]);
+    if (c->diss) diss_middle(c, -1, c->Qtmp);
     update(c, -1, c->Qtmp);
   }
 };
@@ -537,6 +637,39 @@ std::vector<double> initial_state(gcfd_ctx* c) {
   return q;
 }
 
+// Buffers and operators of the artificial dissipation (FP64 path).
+int build_diss(gcfd_ctx* c, const gcfd_mesh* m) {
+  const int K = c->K, Np = c->Np, NE = c->NE;
+  const int NR = Np + 3 * NE;
+  int rc;
+  c->nverts = m->nverts;
+  if ((rc = dalloc(c, &c->sigV, static_cast<size_t>(c->nverts)))) return rc;
+  if ((rc = dalloc(c, &c->epsV, static_cast<size_t>(c->nverts)))) return rc;
+  if ((rc = dalloc(c, &c->DissX, static_cast<size_t>(4) * NR * K))) return rc;
+  if ((rc = dalloc(c, &c->DissY, static_cast<size_t>(4) * NR * K))) return rc;
+  if ((rc = dalloc(c, &c->VF, static_cast<size_t>(c->nEdges) * 4 * NE))) return rc;
+  if ((rc = dalloc(c, &c->viscSpeed, static_cast<size_t>(c->nEdges)))) return rc;
+  if ((rc = dalloc(c, &c->DTVisc, static_cast<size_t>(K)))) return rc;
+  GCFD_CUDA(c, cudaMemset(c->DTVisc, 0, sizeof(double) * K));
+  if ((rc = upload(c, &c->dDiv, c->el.Div.v))) return rc;
+  if ((rc = upload(c, &c->dBary, c->el.Bary.v))) return rc;
+  if ((rc = upload(c, &c->dV, c->el.V.v))) return rc;
+  if ((rc = upload(c, &c->dVinv, c->el.Vinv.v))) return rc;
+  if ((rc = upload(c, &c->dmf, c->el.ModeFilter))) return rc;
+  if ((rc = upload(c, &c->dSensP, c->el.SensP.v))) return rc;
+  if ((rc = upload(c, &c->dMass, c->el.MassMatrix.v))) return rc;
+  if ((rc = upload(c, &c->dSensD, c->el.SensD.v))) return rc;
+  if ((rc = upload(c, &c->dhK, c->geo.hK))) return rc;
+  if ((rc = upload(c, &c->dnxE, c->geo.nx))) return rc;
+  if ((rc = upload(c, &c->dnyE, c->geo.ny))) return rc;
+  if ((rc = upload(c, &c->dIIE, c->geo.IInII))) return rc;
+  std::vector<int> ev(static_cast<size_t>(3) * K);
+  for (int k = 0; k < K; ++k)
+    for (int v = 0; v < 3; ++v) ev[static_cast<size_t>(v) * K + k] = m->etov[3 * k + v];
+  if ((rc = upload(c, &c->detov, ev))) return rc;
+  return GCFD_OK;
+}
+
 // Buffers and FP32 operator / geometry copies of the mixed path.
 int build_mixed(gcfd_ctx* c) {
   const int K = c->K, Np = c->Np, NE = c->NE, NF = c->NF;
@@ -605,6 +738,12 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
   const gcfd_params& p = c->prm;
   c->N = p.N;
   c->fp32 = (p.precision == GCFD_PREC_FP32);
+  // NewEuler creates the dissipation only for PerssonC0 with N > 0 (euler.go:107-112);
+  // the sensor ramp takes Kappa when given, else 5 (dissipation.go:140-147).
+  c->diss = (p.limiter == GCFD_LIMITER_PERSSON_C0) && p.N > 0;
+  c->dissKappa = (p.kappa != 0.0) ? p.kappa : 5.0;
+  if (c->diss && c->fp32)
+    return fail(c, GCFD_ERR_UNSUPPORTED, "PerssonC0 dissipation runs on the FP64 path only in this build");
   try {
     c->el = build_dfr_element(p.N);
   } catch (const std::exception& e) {
@@ -709,6 +848,7 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
   } else if ((rc = build_mixed(c))) {
     return rc;
   }
+  if (c->diss && (rc = build_diss(c, m))) return rc;
   if ((rc = upload(c, &c->Iop, c->el.FluxEdgeInterp.v))) return rc;
   if ((rc = upload(c, &c->Div, c->el.DivInt.v))) return rc;
   if ((rc = upload(c, &c->Jdet, g.Jdet))) return rc;
@@ -762,8 +902,8 @@ int gcfd_create(const gcfd_mesh* mesh, const gcfd_params* params, gcfd_ctx** out
     return fail(nullptr, GCFD_ERR_ARG, "unknown flux type");
   if (params->init_type < 0 || params->init_type > 2)
     return fail(nullptr, GCFD_ERR_ARG, "unknown init type");
-  if (params->limiter != GCFD_LIMITER_NONE)
-    return fail(nullptr, GCFD_ERR_UNSUPPORTED, "limiter not available in this build");
+  if (params->limiter != GCFD_LIMITER_NONE && params->limiter != GCFD_LIMITER_PERSSON_C0)
+    return fail(nullptr, GCFD_ERR_ARG, "unknown limiter");
   if (!(params->cfl > 0.0)) return fail(nullptr, GCFD_ERR_ARG, "CFL must be > 0");
   std::unique_ptr<gcfd_ctx> c(new gcfd_ctx());
   c->prm = *params;

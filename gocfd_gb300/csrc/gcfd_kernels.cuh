@@ -33,6 +33,7 @@ struct Scalars {
   unsigned long long rmax[4];   // signed max of the final increment, order-preserving key
   unsigned long long rabs[4];   // max |R| (double bits)
   double rsum2[4];              // sum R^2
+  unsigned long long gvisc[5];  // per stage max viscous wave speed (artificial dissipation)
   int steps;
   int pad;
 };
@@ -258,6 +259,22 @@ struct UpdateArgs {
   double* DT;                // K, persistent across stages (local time stepping)
   double* rhsOut;            // stage == -1
   Gas<T> gas;
+  // artificial dissipation (read by k_diss_update)
+  const double* DissX;       // [4][Np + 3NpEdge][K]
+  const double* DissY;
+  const double* VF;          // [edge][4][NpEdge] viscous normal flux
+  const double* viscSpeed;   // per edge
+  const unsigned long long* sigV;  // per vertex sigma (double bits)
+  const int* etov;           // [3][K]
+  const double* V;           // Np x Np
+  const double* Vinv;
+  const double* mf;          // Np
+  const double* IIE;         // [3][K]
+  const int* ekL;
+  const int* eLR;
+  const unsigned long long* gvisc;  // per stage
+  double* DTVisc;            // K, persistent (CalcElementMaxWaveSpeed never resets it)
+  double cdiff;              // 1/(N+1)^2
 };
 
 __constant__ double kSSP[5][6] = {
@@ -268,6 +285,55 @@ __constant__ double kSSP[5][6] = {
     {0.517231671970585, 0.096059710526146, 0.386708617503269, 0.063692468666290,
      0.226007483236906, 0}};
 
+// One point of the SSP(5,4) stage update (rkAdvance, euler.go:460-566); the
+// final stage folds the increment into the residual partials.
+template <typename T>
+__device__ __forceinline__ void ssp_stage_update(const UpdateArgs<T>& a, size_t ind, double rhs, double dtk,
+                                                 double& rmax, double& rabs, double& rs2) {
+  const int s = a.stage;
+  const double dtRHS = dtk * rhs;
+  if (s == 0) {
+    a.Q1[ind] = a.Q0[ind] + kSSP[0][0] * dtRHS;
+  } else if (s == 1) {
+    a.Q2[ind] = kSSP[1][0] * a.Q0[ind] + kSSP[1][1] * a.Q1[ind] + kSSP[1][2] * dtRHS;
+  } else if (s == 2) {
+    a.Q3[ind] = kSSP[2][0] * a.Q0[ind] + kSSP[2][1] * a.Q2[ind] + kSSP[2][2] * dtRHS;
+  } else if (s == 3) {
+    a.R[ind] = rhs;
+    a.Q4[ind] = kSSP[3][0] * a.Q0[ind] + kSSP[3][1] * a.Q3[ind] + kSSP[3][2] * dtRHS;
+  } else {
+    const double dtR3 = dtk * a.R[ind];
+    const double q0 = a.Q0[ind];
+    const double inc = -q0 + kSSP[4][0] * a.Q2[ind] + kSSP[4][1] * a.Q3[ind] + kSSP[4][2] * a.Q4[ind] +
+                       kSSP[4][3] * dtR3 + kSSP[4][4] * dtRHS;
+    a.R[ind] = inc;
+    a.Q0[ind] = q0 + inc;
+    rmax = fmax(rmax, inc);
+    rabs = fmax(rabs, fabs(inc));
+    rs2 += inc * inc;
+    if (inc != inc) rabs = inc;  // keep NaN visible
+  }
+}
+
+// Block-wide residual partials of the final stage -> Scalars (per warp atomics).
+__device__ __forceinline__ void residual_reduce(Scalars* sc, const double rmax[4], const double rabs[4],
+                                                const double rs2[4]) {
+#pragma unroll
+  for (int n = 0; n < 4; ++n) {
+    const unsigned long long km = warp_max_u64(order_key(rmax[n]));
+    const double am = warp_max(rabs[n]);
+    const double s2 = warp_sum(rs2[n]);
+    if ((threadIdx.x & 31) == 0) {
+      atomicMax(&sc->rmax[n], km);
+      atomicMax(&sc->rabs[n], static_cast<unsigned long long>(__double_as_longlong(am)));
+      atomicAdd(&sc->rsum2[n], s2);
+    }
+  }
+}
+
+// stage -1: write -Div(F)/J to rhsOut. Steps with artificial dissipation use
+// that form too, into a scratch array; k_diss_update then adds the viscous
+// terms, filters and applies the stage update.
 template <int N, typename T>
 __global__ void __launch_bounds__(128) k_div_update(UpdateArgs<T> a) {
   constexpr int NP = Dims<N>::NP, NE3 = Dims<N>::NE3, NF = Dims<N>::NF;
@@ -314,12 +380,16 @@ __global__ void __launch_bounds__(128) k_div_update(UpdateArgs<T> a) {
       }
     }
     const T mooj = -(T(1) / Jd);
+#pragma unroll
+    for (int n = 0; n < 4; ++n)
+#pragma unroll
+      for (int r = 0; r < NP; ++r) acc[n][r] = acc[n][r] * mooj;
     if (a.stage < 0) {
 #pragma unroll
       for (int n = 0; n < 4; ++n)
 #pragma unroll
         for (int r = 0; r < NP; ++r)
-          a.rhsOut[(n * NP + r) * sK + k] = static_cast<double>(acc[n][r] * mooj);
+          a.rhsOut[(n * NP + r) * sK + k] = static_cast<double>(acc[n][r]);
     } else {
       // Time step of this stage (CalcElementMaxWaveSpeed, calculateGlobalDT,
       // CalculateLocalDT: edges.go:291-323, euler.go:945-1002).
@@ -337,59 +407,25 @@ __global__ void __launch_bounds__(128) k_div_update(UpdateArgs<T> a) {
         if (t + dtk > a.finalTime) dtk = a.finalTime - t;
         if (k == 0) a.sc->dt[a.stage] = dtk;
       }
-      const int s = a.stage;
 #pragma unroll
-      for (int n = 0; n < 4; ++n) {
+      for (int n = 0; n < 4; ++n)
 #pragma unroll
-        for (int r = 0; r < NP; ++r) {
-          const size_t ind = (n * NP + r) * sK + k;
-          const double rhs = static_cast<double>(acc[n][r] * mooj);
-          const double dtRHS = dtk * rhs;
-          if (s == 0) {
-            a.Q1[ind] = a.Q0[ind] + kSSP[0][0] * dtRHS;
-          } else if (s == 1) {
-            a.Q2[ind] = kSSP[1][0] * a.Q0[ind] + kSSP[1][1] * a.Q1[ind] + kSSP[1][2] * dtRHS;
-          } else if (s == 2) {
-            a.Q3[ind] = kSSP[2][0] * a.Q0[ind] + kSSP[2][1] * a.Q2[ind] + kSSP[2][2] * dtRHS;
-          } else if (s == 3) {
-            a.R[ind] = rhs;
-            a.Q4[ind] = kSSP[3][0] * a.Q0[ind] + kSSP[3][1] * a.Q3[ind] + kSSP[3][2] * dtRHS;
-          } else {
-            const double dtR3 = dtk * a.R[ind];
-            const double q0 = a.Q0[ind];
-            const double inc = -q0 + kSSP[4][0] * a.Q2[ind] + kSSP[4][1] * a.Q3[ind] +
-                               kSSP[4][2] * a.Q4[ind] + kSSP[4][3] * dtR3 + kSSP[4][4] * dtRHS;
-            a.R[ind] = inc;
-            a.Q0[ind] = q0 + inc;
-            rloc_max[n] = fmax(rloc_max[n], inc);
-            rloc_abs[n] = fmax(rloc_abs[n], fabs(inc));
-            rloc_s2[n] += inc * inc;
-            if (inc != inc) rloc_abs[n] = inc;  // keep NaN visible
-          }
-        }
-      }
+        for (int r = 0; r < NP; ++r)
+          ssp_stage_update(a, (n * NP + r) * sK + k, static_cast<double>(acc[n][r]), dtk, rloc_max[n],
+                           rloc_abs[n], rloc_s2[n]);
     }
   }
-  if (a.stage == 4) {
-#pragma unroll
-    for (int n = 0; n < 4; ++n) {
-      const unsigned long long km = warp_max_u64(order_key(rloc_max[n]));
-      const double am = warp_max(rloc_abs[n]);
-      const double s2 = warp_sum(rloc_s2[n]);
-      if ((threadIdx.x & 31) == 0) {
-        atomicMax(&a.sc->rmax[n], km);
-        atomicMax(&a.sc->rabs[n], static_cast<unsigned long long>(__double_as_longlong(am)));
-        atomicAdd(&a.sc->rsum2[n], s2);
-      }
-    }
-  }
+  if (a.stage == 4) residual_reduce(a.sc, rloc_max, rloc_abs, rloc_s2);
 }
 
 // Step bookkeeping: reset the per-stage reductions before a step, advance the
 // time by the last stage's dt after it (Solve, euler.go:176-181).
 __global__ void k_step_begin(Scalars* sc) {
   const int t = threadIdx.x;
-  if (t < 5) sc->gmax[t] = 0ULL;
+  if (t < 5) {
+    sc->gmax[t] = 0ULL;
+    sc->gvisc[t] = 0ULL;
+  }
   if (t < 4) {
     sc->rmax[t] = 0ULL;
     sc->rabs[t] = 0ULL;

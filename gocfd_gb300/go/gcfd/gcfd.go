@@ -1,0 +1,181 @@
+// Package gcfd binds libgcfd (include/gcfd.h) for the gocfd Euler2D solver.
+//
+// It is the thin cgo layer between model_problems/Euler2D (NewEuler,
+// RungeKutta5SSP.Step, the RHS chain) and the GB300 kernels.  Every non-zero
+// status becomes an error; Euler2D turns it into a panic, as the reference
+// does for its own failures.
+//
+// Host arrays stay owned by Go: the library copies them during the call and
+// keeps no pointer.  The per-shard pointer table lives in C memory and holds
+// Go pointers only while they are pinned (runtime.Pinner, Go 1.21+).
+package gcfd
+
+/*
+#cgo CFLAGS: -I${SRCDIR}/../../../include
+#cgo LDFLAGS: -L${SRCDIR}/../.. -lgcfd -Wl,-rpath,${SRCDIR}/../..
+#include <stdlib.h>
+#include "gcfd.h"
+*/
+import "C"
+
+import (
+	"fmt"
+	"runtime"
+	"unsafe"
+)
+
+// Precision modes of gcfd_params.precision.
+const (
+	PrecFP64 = int(C.GCFD_PREC_FP64) // the drop-in
+	PrecFP32 = int(C.GCFD_PREC_FP32) // delta-form FP32 arithmetic, compensated state
+)
+
+// Params mirrors InputParameters.InputParameters2D plus the arithmetic mode.
+type Params struct {
+	N                             int
+	CFL, FinalTime, Minf, Gamma   float64
+	Alpha, Kappa                  float64
+	MaxIterations                 int
+	FluxType, InitType, Limiter   int // GCFD_FLUX_*, GCFD_INIT_*, GCFD_LIMITER_*
+	LocalTimeStepping             bool
+	Precision                     int
+	VortexX0, VortexY0            float64
+	Device                        int
+}
+
+// Context is one device-resident solver.
+type Context struct {
+	ctx *C.gcfd_ctx
+}
+
+func status(ctx *C.gcfd_ctx, rc C.int) error {
+	if rc == C.GCFD_OK {
+		return nil
+	}
+	return fmt.Errorf("gcfd: status %d: %s", int(rc), C.GoString(C.gcfd_last_error(ctx)))
+}
+
+// New replaces Euler2D.NewEuler's set-up: vertices, 0-based element table
+// (K x 3, row-major) and the boundary edges as (v1, v2, BCFLAG) triples.
+func New(vx, vy []float64, etov []int32, bcV1, bcV2, bcFlag []int32, p Params) (*Context, error) {
+	var pin runtime.Pinner
+	defer pin.Unpin()
+	m := C.gcfd_mesh{
+		nverts: C.int32_t(len(vx)), vx: (*C.double)(unsafe.Pointer(&vx[0])),
+		vy: (*C.double)(unsafe.Pointer(&vy[0])),
+		K:  C.int32_t(len(etov) / 3), etov: (*C.int32_t)(unsafe.Pointer(&etov[0])),
+		nbc: C.int32_t(len(bcFlag)),
+	}
+	if len(bcFlag) > 0 {
+		m.bc_v1 = (*C.int32_t)(unsafe.Pointer(&bcV1[0]))
+		m.bc_v2 = (*C.int32_t)(unsafe.Pointer(&bcV2[0]))
+		m.bc_flag = (*C.int32_t)(unsafe.Pointer(&bcFlag[0]))
+	}
+	pin.Pin(&vx[0])
+	pin.Pin(&vy[0])
+	pin.Pin(&etov[0])
+	if len(bcFlag) > 0 {
+		pin.Pin(&bcV1[0])
+		pin.Pin(&bcV2[0])
+		pin.Pin(&bcFlag[0])
+	}
+	lts := 0
+	if p.LocalTimeStepping {
+		lts = 1
+	}
+	cp := C.gcfd_params{
+		N: C.int32_t(p.N), cfl: C.double(p.CFL), final_time: C.double(p.FinalTime),
+		minf: C.double(p.Minf), gamma: C.double(p.Gamma), alpha: C.double(p.Alpha),
+		kappa: C.double(p.Kappa), max_iterations: C.int32_t(p.MaxIterations),
+		flux_type: C.int32_t(p.FluxType), init_type: C.int32_t(p.InitType),
+		limiter: C.int32_t(p.Limiter), local_time_stepping: C.int32_t(lts),
+		precision: C.int32_t(p.Precision), vortex_x0: C.double(p.VortexX0),
+		vortex_y0: C.double(p.VortexY0), device: C.int32_t(p.Device),
+	}
+	c := &Context{}
+	if err := status(nil, C.gcfd_create(&m, &cp, &c.ctx)); err != nil {
+		return nil, err
+	}
+	runtime.SetFinalizer(c, (*Context).Close)
+	return c, nil
+}
+
+// Close releases the device context.
+func (c *Context) Close() {
+	if c.ctx != nil {
+		C.gcfd_destroy(c.ctx)
+		c.ctx = nil
+	}
+}
+
+// shardTable pins the shards' Np x Kmax data and builds the C pointer table
+// Q[np*4 + n] the ABI expects; free() must be called after the C call.
+func shardTable(pin *runtime.Pinner, Q [][4][]float64) (**C.double, *C.int32_t, func()) {
+	ns := len(Q)
+	tab := (*[1 << 28]*C.double)(C.malloc(C.size_t(ns*4) * C.size_t(unsafe.Sizeof(uintptr(0)))))[: ns*4 : ns*4]
+	km := (*[1 << 28]C.int32_t)(C.malloc(C.size_t(ns) * 4))[:ns:ns]
+	for np := range Q {
+		for n := 0; n < 4; n++ {
+			pin.Pin(&Q[np][n][0])
+			tab[np*4+n] = (*C.double)(unsafe.Pointer(&Q[np][n][0]))
+		}
+	}
+	return &tab[0], &km[0], func() {
+		C.free(unsafe.Pointer(&tab[0]))
+		C.free(unsafe.Pointer(&km[0]))
+	}
+}
+
+// SetState copies the reference's sharded c.Q (Np x Kmax[np] per variable).
+func (c *Context) SetState(Q [][4][]float64, Kmax []int) error {
+	var pin runtime.Pinner
+	defer pin.Unpin()
+	tab, km, free := shardTable(&pin, Q)
+	defer free()
+	kmS := unsafe.Slice(km, len(Kmax))
+	for i, k := range Kmax {
+		kmS[i] = C.int32_t(k)
+	}
+	return status(c.ctx, C.gcfd_set_state(c.ctx, C.int32_t(len(Q)), km, tab))
+}
+
+// GetState copies the device state back into the sharded c.Q.
+func (c *Context) GetState(Q [][4][]float64, Kmax []int) error {
+	var pin runtime.Pinner
+	defer pin.Unpin()
+	tab, km, free := shardTable(&pin, Q)
+	defer free()
+	kmS := unsafe.Slice(km, len(Kmax))
+	for i, k := range Kmax {
+		kmS[i] = C.int32_t(k)
+	}
+	return status(c.ctx, C.gcfd_get_state(c.ctx, C.int32_t(len(Q)), km, tab))
+}
+
+// Step replaces RungeKutta5SSP.Step plus Solve's Time += GlobalDT; it returns
+// the time, the last global dt and the signed max of the final increment per
+// variable (PrintUpdate's residuals).
+func (c *Context) Step(nsteps int) (time, dt float64, resid [4]float64, err error) {
+	var t, d C.double
+	var r [4]C.double
+	err = status(c.ctx, C.gcfd_step(c.ctx, C.int32_t(nsteps), &t, &d, &r[0], nil, nil))
+	for i := range r {
+		resid[i] = float64(r[i])
+	}
+	return float64(t), float64(d), resid, err
+}
+
+// RHS evaluates the right-hand side of Q at BC time t into RHS (same shards).
+func (c *Context) RHS(t float64, Q, RHS [][4][]float64, Kmax []int) error {
+	var pin runtime.Pinner
+	defer pin.Unpin()
+	tq, km, freeQ := shardTable(&pin, Q)
+	defer freeQ()
+	tr, _, freeR := shardTable(&pin, RHS)
+	defer freeR()
+	kmS := unsafe.Slice(km, len(Kmax))
+	for i, k := range Kmax {
+		kmS[i] = C.int32_t(k)
+	}
+	return status(c.ctx, C.gcfd_rhs(c.ctx, C.double(t), C.int32_t(len(Q)), km, tq, tr))
+}

@@ -60,6 +60,20 @@ struct oracle_problem {
   double gamma;                  // FSFar.Gamma, used by every flow function
   oracle_fs far, in, out;
   double vbeta, vx0, vy0, vgamma;
+  // Artificial dissipation (PerssonC0, dissipation.go / dfr_shock_capturing.go); diss == 0 disables it.
+  int32_t diss;
+  int32_t nverts;
+  const int64_t* EtoV;          // K x 3
+  const double* V;              // Np x Np modal Vandermonde
+  const double* Vinv;
+  const double* SensD;          // Np x Np, I - Clipper
+  const double* SensP;          // Np x Np, MassMatrix * SensD
+  const double* Mass;           // Np x Np
+  const double* ModeFilter;     // Np
+  const double* Div;            // NpFlux x NpFlux
+  const double* Bary;           // NpFlux x 3
+  double kappa;                 // shock-finder Kappa (sigma ramp half width)
+  double eps0;                  // viscosity scale (5 / 1.5)
 };
 
 }  // extern "C"
@@ -313,7 +327,7 @@ void interpolate_to_edges(const oracle_problem* p, const double* Q, double* QF) 
 
 // CalculateEdgeEulerFlux (edges.go:325-452): BCs overwrite the left face state
 // in place; the normal flux of every edge lands in EdgeFlux in left order.
-void edge_fluxes(const oracle_problem* p, double time, double* QF, double* EF) {
+void edge_fluxes(const oracle_problem* p, double time, double* QF, double* EF, double* EQ = nullptr) {
   const int K = p->K, NE = p->NpEdge, NE3 = 3 * NE, Nint = p->Np;
 #pragma omp parallel for schedule(static)
   for (int en = 0; en < p->nEdges; ++en) {
@@ -323,6 +337,9 @@ void edge_fluxes(const oracle_problem* p, double time, double* QF, double* EF) {
     const int shiftL = eL * NE;
     auto qf = [&](int n, int row, int k) -> double& { return QF[(static_cast<size_t>(n) * NE3 + row) * K + k]; };
     double* out = EF + static_cast<size_t>(en) * NE * 4;
+    if (EQ)  // EdgeQValues: the left face state before any BC (edges.go:343-350)
+      for (int i = 0; i < NE; ++i)
+        for (int n = 0; n < 4; ++n) EQ[(static_cast<size_t>(en) * NE + i) * 4 + n] = qf(n, i + shiftL, kL);
     if (p->kR[en] >= 0) {
       const int kR = static_cast<int>(p->kR[en]), eR = static_cast<int>(p->eR[en]);
       const int shiftR = eR * NE;
@@ -445,6 +462,235 @@ void assemble_rhs(const oracle_problem* p, const double* Q, const double* EF, do
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Artificial dissipation (PerssonC0): model_problems/Euler2D/dissipation.go and
+// DG2D/dfr_shock_capturing.go.
+
+struct DissWork {
+  std::vector<double> Se, sigma, eps, sigV, epsV, Eps;  // Eps: NpFlux x K (C0 epsilon)
+  std::vector<double> DissX, DissY;                      // 4 x NpFlux x K
+  std::vector<double> EQ;                                // nEdges x NpEdge x 4 left face states
+  std::vector<double> VF;                                // nEdges x NpEdge x 4 viscous normal flux
+  std::vector<double> viscSpeed;                         // nEdges
+  DissWork(const oracle_problem* p) {
+    const size_t K = p->K;
+    Se.assign(K, 0.); sigma.assign(K, 0.); eps.assign(K, 0.);
+    sigV.assign(p->nverts, 0.); epsV.assign(p->nverts, 0.);
+    Eps.assign(static_cast<size_t>(p->NpFlux) * K, 0.);
+    DissX.assign(4 * static_cast<size_t>(p->NpFlux) * K, 0.);
+    DissY.assign(DissX.size(), 0.);
+    EQ.assign(static_cast<size_t>(p->nEdges) * p->NpEdge * 4, 0.);
+    VF.assign(EQ.size(), 0.);
+    viscSpeed.assign(p->nEdges, 0.);
+  }
+};
+
+// UpdateSeMoment (dfr_shock_capturing.go:142-166), UpdateShockFinderSigma
+// (dissipation.go:491-518, S0 = 4/(N+1)^4), CalculateElementViscosity
+// (dissipation.go:397-412).  A NaN moment keeps sigma = 0.
+void shock_sensor(const oracle_problem* p, const double* Q, DissWork& w) {
+  const int K = p->K, Np = p->Np;
+  const double S0 = 4. / std::pow(double(p->N + 1), 4.);
+  const double left = S0 - p->kappa, right = S0 + p->kappa, ookappa = 0.5 / p->kappa;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < K; ++k) {
+    double num = 0., den = 0.;
+    for (int i = 0; i < Np; ++i) {
+      double x = 0., y = 0., dq = 0.;
+      for (int j = 0; j < Np; ++j) {
+        const double rj = Q[static_cast<size_t>(j) * K + k];
+        x += p->SensP[i * Np + j] * rj;
+        y += p->Mass[i * Np + j] * rj;
+        dq += p->SensD[i * Np + j] * rj;
+      }
+      num += dq * x;
+      den += Q[static_cast<size_t>(i) * K + k] * y;
+    }
+    const double se = std::log10(num / den);
+    double sigma = 0.;
+    if (se < left) sigma = 0.;
+    else if (se >= left && se <= right) sigma = 0.5 * (1. + std::sin(M_PI * ookappa * (se - S0)));
+    else if (se > right) sigma = 1.;
+    w.Se[k] = se;
+    w.sigma[k] = sigma;
+    w.eps[k] = p->eps0 * p->hK[k] * sigma;
+  }
+}
+
+// MergeElementScalarToVertices (euler.go:1048-1065) with max, then
+// MergeVertexScalarToElement (euler.go:1067-1086) with sum / 3 for sigma and
+// InterpolateEpsilonSigma (dissipation.go:219-242) for epsilon.
+void vertex_smoothing(const oracle_problem* p, DissWork& w) {
+  const int K = p->K, NF = p->NpFlux;
+  std::fill(w.sigV.begin(), w.sigV.end(), -1.);
+  std::fill(w.epsV.begin(), w.epsV.end(), -1.);
+  for (int k = 0; k < K; ++k)
+    for (int v = 0; v < 3; ++v) {
+      const int64_t vert = p->EtoV[3 * static_cast<size_t>(k) + v];
+      w.sigV[vert] = std::max(w.sigV[vert], w.sigma[k]);
+      w.epsV[vert] = std::max(w.epsV[vert], w.eps[k]);
+    }
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < K; ++k) {
+    double acc = 0.;
+    for (int v = 0; v < 3; ++v) acc = acc + w.sigV[p->EtoV[3 * static_cast<size_t>(k) + v]];
+    w.sigma[k] = acc / 3.;
+    for (int i = 0; i < NF; ++i) {
+      double e = 0.;
+      for (int v = 0; v < 3; ++v) e += p->Bary[i * 3 + v] * w.epsV[p->EtoV[3 * static_cast<size_t>(k) + v]];
+      w.Eps[static_cast<size_t>(i) * K + k] = e;
+    }
+  }
+}
+
+// limitAndFilterSolution (dissipation.go:606-622) for the 4 variables.
+void limit_filter(const oracle_problem* p, double* U, const std::vector<double>& sigma) {
+  const int K = p->K, Np = p->Np;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < K; ++k) {
+    const double alpha = std::sin(0.5 * M_PI * sigma[k]);
+    for (int n = 0; n < 4; ++n) {
+      double* u = U + static_cast<size_t>(n) * Np * K + k;
+      std::vector<double> m(Np, 0.);
+      for (int i = 0; i < Np; ++i)
+        for (int j = 0; j < Np; ++j) m[i] += p->Vinv[i * Np + j] * u[static_cast<size_t>(j) * K];
+      for (int i = 1; i < Np; ++i) m[i] *= p->ModeFilter[i] * (1. - alpha);
+      for (int i = 0; i < Np; ++i) {
+        double acc = 0.;
+        for (int j = 0; j < Np; ++j) acc += p->V[i * Np + j] * m[j];
+        u[static_cast<size_t>(i) * K] = acc;
+      }
+    }
+  }
+}
+
+// CalculateEpsilonGradient (dissipation.go:244-272) via
+// GetSolutionGradientUsingRTElement (euler.go:864-918) and the RT metrics of
+// CalculateRTBasedDerivativeMetrics (dfr_startup.go:213-254).
+void epsilon_gradient(const oracle_problem* p, const double* Q, DissWork& w) {
+  const int K = p->K, Np = p->Np, NE = p->NpEdge, NF = p->NpFlux;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < K; ++k) {
+    const double* Ji = p->Jinv + 4 * static_cast<size_t>(k);
+    const double ooJd = 1. / p->Jdet[k];
+    std::vector<double> DX(NF), DY(NF);
+    for (int n = 0; n < 4; ++n) {
+      for (int i = 0; i < Np; ++i) {
+        const double Un = Q[(static_cast<size_t>(n) * Np + i) * K + k];
+        DX[i] = Ji[0] * Un;
+        DY[i] = Ji[1] * Un;
+        DX[i + Np] = Ji[2] * Un;
+        DY[i + Np] = Ji[3] * Un;
+      }
+      for (int e = 0; e < 3; ++e) {
+        const int64_t en = p->EtoEdge[3 * static_cast<size_t>(k) + e];
+        const bool own = p->kL[en] == k;
+        const size_t fi = static_cast<size_t>(e) * K + k;
+        const double mx = ooJd * p->nx[fi] * p->IInII[fi], my = ooJd * p->ny[fi] * p->IInII[fi];
+        for (int i = 0; i < NE; ++i) {
+          const int ii = own ? i : NE - 1 - i;
+          const double Un = w.EQ[(static_cast<size_t>(en) * NE + ii) * 4 + n];
+          DX[2 * Np + e * NE + i] = mx * Un;
+          DY[2 * Np + e * NE + i] = my * Un;
+        }
+      }
+      for (int r = 0; r < NF; ++r) {
+        double gx = 0., gy = 0.;
+        for (int j = 0; j < NF; ++j) {
+          gx += p->Div[r * NF + j] * DX[j];
+          gy += p->Div[r * NF + j] * DY[j];
+        }
+        const double e = w.Eps[static_cast<size_t>(r) * K + k];
+        w.DissX[(static_cast<size_t>(n) * NF + r) * K + k] = gx * e;
+        w.DissY[(static_cast<size_t>(n) * NF + r) * K + k] = gy * e;
+      }
+    }
+  }
+}
+
+// StoreEdgeAggregates' viscous part (edges.go:274-286) and StoreEdgeViscousFlux
+// (edges.go:151-244), including its use of the left normal on both sides and
+// of the stored left face states for both "sides" of the penalty jump.
+void viscous_edges(const oracle_problem* p, DissWork& w) {
+  const int K = p->K, NE = p->NpEdge, NF = p->NpFlux, Nint = p->Np;
+  const double Omega = double(p->N * p->N);
+#pragma omp parallel for schedule(static)
+  for (int en = 0; en < p->nEdges; ++en) {
+    const int kL = static_cast<int>(p->kL[en]), eL = static_cast<int>(p->eL[en]);
+    const size_t fiL = static_cast<size_t>(eL) * K + kL;
+    const double nxL = p->nx[fiL], nyL = p->ny[fiL];
+    const double oohK = 1. / p->hK[kL];
+    double vmax = -DBL_MAX;
+    for (int i = 0; i < NE; ++i)
+      vmax = std::max(oohK * oohK * w.Eps[static_cast<size_t>(2 * Nint + eL * NE + i) * K + kL], vmax);
+    w.viscSpeed[en] = vmax;
+    double* vf = w.VF.data() + static_cast<size_t>(en) * NE * 4;
+    const int shiftL = eL * NE;
+    if (p->kR[en] < 0) {
+      for (int n = 0; n < 4; ++n)
+        for (int i = 0; i < NE; ++i) {
+          const size_t indL = static_cast<size_t>(n) * NF * K + static_cast<size_t>(2 * Nint + shiftL + i) * K + kL;
+          vf[i * 4 + n] = nxL * w.DissX[indL] + nyL * w.DissY[indL];
+        }
+      continue;
+    }
+    const int kR = static_cast<int>(p->kR[en]), shiftR = static_cast<int>(p->eR[en]) * NE;
+    const double len = (eL == 1) ? 2. * std::sqrt(2.) * p->IInII[fiL] : 2. * p->IInII[fiL];
+    const double ooLen = 1. / len;
+    for (int n = 0; n < 4; ++n)
+      for (int i = 0; i < NE; ++i) {
+        const size_t indL = static_cast<size_t>(n) * NF * K + static_cast<size_t>(2 * Nint + shiftL + i) * K + kL;
+        const size_t indR = static_cast<size_t>(n) * NF * K + static_cast<size_t>(2 * Nint + shiftR + NE - 1 - i) * K + kR;
+        const double vFL = nxL * w.DissX[indL] + nyL * w.DissY[indL];
+        const double vFR = nxL * w.DissX[indR] + nyL * w.DissY[indR];
+        vf[i * 4 + n] = 0.5 * (vFL + vFR);
+      }
+    for (int n = 0; n < 4; ++n)
+      for (int i = 0; i < NE; ++i) {
+        const double epsL = w.Eps[static_cast<size_t>(2 * Nint + shiftL + i) * K + kL];
+        const double epsR = w.Eps[static_cast<size_t>(2 * Nint + shiftR + NE - 1 - i) * K + kR];
+        const double lam = 0.5 * (epsL + epsR);
+        const int ii = NE - 1 - i;
+        const double* eq = w.EQ.data() + static_cast<size_t>(en) * NE * 4;
+        vf[i * 4 + n] -= (Omega * lam * ooLen) * (eq[i * 4 + n] - eq[ii * 4 + n]);
+      }
+  }
+}
+
+// AddDissipation (dissipation.go:274-346): RHS += DivInt * DOF(eps grad Q) / |J|.
+void add_dissipation(const oracle_problem* p, DissWork& w, double* RHS) {
+  const int K = p->K, Np = p->Np, NE = p->NpEdge, NF = p->NpFlux;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < K; ++k) {
+    const double Jd = p->Jdet[k];
+    const double* Ji = p->Jinv + 4 * static_cast<size_t>(k);
+    std::vector<double> DOF(NF);
+    for (int n = 0; n < 4; ++n) {
+      for (int i = 0; i < Np; ++i) {
+        const size_t ind = (static_cast<size_t>(n) * NF + i) * K + k;
+        DOF[i] = Jd * (Ji[0] * w.DissX[ind] + Ji[1] * w.DissY[ind]);
+        DOF[i + Np] = Jd * (Ji[2] * w.DissX[ind] + Ji[3] * w.DissY[ind]);
+      }
+      for (int e = 0; e < 3; ++e) {
+        const int64_t en = p->EtoEdge[3 * static_cast<size_t>(k) + e];
+        const int sign = (p->kL[en] == k) ? 1 : -1;
+        const double II = p->IInII[static_cast<size_t>(e) * K + k];
+        for (int i = 0; i < NE; ++i) {
+          const int ii = (sign == -1) ? NE - 1 - i : i;
+          DOF[2 * Np + e * NE + i] = w.VF[(static_cast<size_t>(en) * NE + ii) * 4 + n] * II * double(sign);
+        }
+      }
+      const double oojd = 1. / Jd;
+      for (int r = 0; r < Np; ++r) {
+        double d = 0.;
+        for (int j = 0; j < NF; ++j) d += p->DivInt[r * NF + j] * DOF[j];
+        RHS[(static_cast<size_t>(n) * Np + r) * K + k] += oojd * d;
+      }
+    }
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -467,11 +713,25 @@ void oracle_set_threads(int n) {
 
 // One RHS evaluation, as the reference tests compose it (euler_test.go:202-222).
 // Q, RHS: 4 x Np x K.  QFaceOut (optional): BC-overwritten faces 4 x 3NpEdge x K.
+// With dissipation enabled the RHS is the one a step uses at a stage other
+// than rkStep 2: Euler RHS + AddDissipation, then the modal filter.
 int oracle_rhs(const oracle_problem* p, double time, const double* Q, double* RHS, double* QFaceOut) {
   Work w(p);
+  const bool diss = p->diss != 0;
+  DissWork dw(p);
+  if (diss) {
+    shock_sensor(p, Q, dw);
+    vertex_smoothing(p, dw);
+  }
   interpolate_to_edges(p, Q, w.QFace.data());
-  edge_fluxes(p, time, w.QFace.data(), w.EdgeFlux.data());
+  edge_fluxes(p, time, w.QFace.data(), w.EdgeFlux.data(), diss ? dw.EQ.data() : nullptr);
   assemble_rhs(p, Q, w.EdgeFlux.data(), w.FRT.data(), RHS);
+  if (diss) {
+    epsilon_gradient(p, Q, dw);
+    viscous_edges(p, dw);
+    add_dissipation(p, dw, RHS);
+    limit_filter(p, RHS, dw.sigma);
+  }
   if (QFaceOut) std::memcpy(QFaceOut, w.QFace.data(), w.QFace.size() * sizeof(double));
   return 0;
 }
@@ -491,38 +751,66 @@ int oracle_rhs_faces(const oracle_problem* p, double time, const double* Q, cons
 // updated in place; R (optional, 4 x Np x K) receives the final increment.
 // DT (K) carries the per-element time step across stages and steps.
 int oracle_step(const oracle_problem* p, int nsteps, double* Q, double* time, double* dt_last,
-                double* R, double* DT) {
+                double* R, double* DT, double* DTVisc) {
   const int K = p->K, Np = p->Np;
   const size_t S = static_cast<size_t>(4) * Np * K;
   std::vector<double> Q1(S), Q2(S), Q3(S), Q4(S), RHS(S), Res(S, 0.);
-  std::vector<double> DTloc(K, 0.);
+  std::vector<double> DTloc(K, 0.), DTVloc(K, 0.);
   double* dt = DT ? DT : DTloc.data();
+  double* dtv = DTVisc ? DTVisc : DTVloc.data();
   Work w(p);
+  const bool diss = p->diss != 0;
+  DissWork dw(p);
+  const double C_diff = 1. / (double(p->N + 1) * double(p->N + 1));
   double GlobalDT = 0.;
   for (int st = 0; st < nsteps; ++st) {
     for (int rkStep = 0; rkStep < 5; ++rkStep) {
-      const double* QQQ = rkStep == 0 ? Q : rkStep == 1 ? Q1.data() : rkStep == 2 ? Q2.data()
-                        : rkStep == 3 ? Q3.data() : Q4.data();
+      double* QQQ = rkStep == 0 ? Q : rkStep == 1 ? Q1.data() : rkStep == 2 ? Q2.data()
+                  : rkStep == 3 ? Q3.data() : Q4.data();
+      if (diss) {
+        shock_sensor(p, QQQ, dw);
+        vertex_smoothing(p, dw);
+        if (rkStep == 2) limit_filter(p, QQQ, dw.sigma);
+      }
       interpolate_to_edges(p, QQQ, w.QFace.data());
-      edge_fluxes(p, *time, w.QFace.data(), w.EdgeFlux.data());
+      edge_fluxes(p, *time, w.QFace.data(), w.EdgeFlux.data(), diss ? dw.EQ.data() : nullptr);
+      if (diss) epsilon_gradient(p, QQQ, dw);
       edge_aggregates(p, w.QFace.data(), w.EdgeSpeed.data());
+      if (diss) viscous_edges(p, dw);
       if (rkStep == 0)
         for (int k = 0; k < K; ++k) dt[k] = -100;
-      double gmax = -DBL_MAX;
+      double gmax = -DBL_MAX, gvisc = -DBL_MAX;
       for (int k = 0; k < K; ++k)
         for (int e = 0; e < 3; ++e) {
-          const double s = w.EdgeSpeed[p->EtoEdge[3 * static_cast<size_t>(k) + e]];
+          const int64_t en = p->EtoEdge[3 * static_cast<size_t>(k) + e];
+          const double s = w.EdgeSpeed[en];
           gmax = std::max(gmax, s);
           dt[k] = std::max(dt[k], s);
+          if (diss) {
+            const double v = dw.viscSpeed[en];
+            gvisc = std::max(gvisc, v);
+            dtv[k] = std::max(dtv[k], v);
+          }
         }
       if (!p->local_dt) {
         GlobalDT = p->cfl / gmax;
+        if (diss) GlobalDT = std::min(GlobalDT, C_diff / gvisc);
         if (*time + GlobalDT > p->final_time) GlobalDT = p->final_time - *time;
         for (int k = 0; k < K; ++k) dt[k] = GlobalDT;
       } else {
         for (int k = 0; k < K; ++k) dt[k] = p->cfl / dt[k];
+        if (diss)
+          for (int k = 0; k < K; ++k)
+            if (dtv[k] > 1.e-9) {
+              dtv[k] = C_diff / dtv[k];
+              dt[k] = std::min(dt[k], dtv[k]);
+            }
       }
       assemble_rhs(p, QQQ, w.EdgeFlux.data(), w.FRT.data(), RHS.data());
+      if (diss) {
+        add_dissipation(p, dw, RHS.data());
+        limit_filter(p, RHS.data(), dw.sigma);
+      }
 #pragma omp parallel for schedule(static)
       for (int k = 0; k < K; ++k) {
         for (int n = 0; n < 4; ++n)
@@ -551,6 +839,71 @@ int oracle_step(const oracle_problem* p, int nsteps, double* Q, double* time, do
   }
   if (dt_last) *dt_last = GlobalDT;
   if (R) std::memcpy(R, Res.data(), S * sizeof(double));
+  return 0;
+}
+
+// The standalone indicator of ModeAliasShockFinder.ShockIndicator
+// (dfr_shock_capturing.go:189-235): moment with the mass-matrix diagonal,
+// S0 = 4/N^4; used by the reference's TestShockFinder.
+double oracle_shock_indicator(const oracle_problem* p, const double* q, const double* Clipper, double kappa) {
+  const int Np = p->Np;
+  double mNum = 0., mDen = 0.;
+  for (int i = 0; i < Np; ++i) {
+    double c = 0.;
+    for (int j = 0; j < Np; ++j) c += Clipper[i * Np + j] * q[j];
+    const double mass = p->Mass[i + i * Np];
+    const double t1 = q[i] - c;
+    mNum += mass * (t1 * t1);
+    mDen += mass * (q[i] * q[i]);
+  }
+  const double Se = std::log10(mNum / mDen);
+  const double S0 = 4. / std::pow(double(p->N), 4.);
+  const double left = S0 - kappa, right = S0 + kappa, ookappa = 0.5 / kappa;
+  if (Se < left) return 0.;
+  if (Se >= left && Se <= right) return 0.5 * (1. + std::sin(M_PI * ookappa * (Se - S0)));
+  return 1.;
+}
+
+// EpsilonSigmaMaxToVertices (dissipation.go:163-217) on a given element
+// scalar: the maximum over the elements sharing each vertex (TestDissipation).
+int oracle_vertex_max(const oracle_problem* p, const double* elem, double* vert) {
+  for (int v = 0; v < p->nverts; ++v) vert[v] = -DBL_MAX;
+  for (int k = 0; k < p->K; ++k)
+    for (int v = 0; v < 3; ++v) {
+      const int64_t i = p->EtoV[3 * static_cast<size_t>(k) + v];
+      vert[i] = std::max(vert[i], elem[k]);
+    }
+  return 0;
+}
+
+// Physical gradient at all NpFlux flux points from the RT element, with the
+// edge values taken from each edge's left element (GetSolutionGradient,
+// euler.go:864-918), for the polynomial exactness test of TestDissipation2.
+// GX, GY: 4 x NpFlux x K.
+int oracle_gradient(const oracle_problem* p, const double* Q, double* GX, double* GY) {
+  Work w(p);
+  DissWork dw(p);
+  interpolate_to_edges(p, Q, w.QFace.data());
+  edge_fluxes(p, 0., w.QFace.data(), w.EdgeFlux.data(), dw.EQ.data());
+  std::fill(dw.Eps.begin(), dw.Eps.end(), 1.);
+  epsilon_gradient(p, Q, dw);
+  std::memcpy(GX, dw.DissX.data(), dw.DissX.size() * sizeof(double));
+  std::memcpy(GY, dw.DissY.data(), dw.DissY.size() * sizeof(double));
+  return 0;
+}
+
+// Element scalars of the last sensor evaluation, for tests: Se, sigma, eps per
+// element after one sensor + vertex pass on Q.
+int oracle_sensor(const oracle_problem* p, const double* Q, double* Se, double* sigmaElem, double* epsElem,
+                  double* sigmaAvg, double* epsVertex) {
+  DissWork dw(p);
+  shock_sensor(p, Q, dw);
+  std::memcpy(Se, dw.Se.data(), p->K * sizeof(double));
+  std::memcpy(sigmaElem, dw.sigma.data(), p->K * sizeof(double));
+  std::memcpy(epsElem, dw.eps.data(), p->K * sizeof(double));
+  vertex_smoothing(p, dw);
+  std::memcpy(sigmaAvg, dw.sigma.data(), p->K * sizeof(double));
+  std::memcpy(epsVertex, dw.epsV.data(), p->nverts * sizeof(double));
   return 0;
 }
 

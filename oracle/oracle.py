@@ -62,6 +62,9 @@ class _Problem(C.Structure):
         ("cfl", C.c_double), ("final_time", C.c_double), ("gamma", C.c_double),
         ("far", _FS), ("inn", _FS), ("out", _FS),
         ("vbeta", C.c_double), ("vx0", C.c_double), ("vy0", C.c_double), ("vgamma", C.c_double),
+        ("diss", C.c_int32), ("nverts", C.c_int32), ("EtoV", PL), ("V", PD), ("Vinv", PD), ("SensD", PD),
+        ("SensP", PD), ("Mass", PD), ("ModeFilter", PD), ("Div", PD), ("Bary", PD),
+        ("kappa", C.c_double), ("eps0", C.c_double),
     ]
 
 
@@ -72,7 +75,12 @@ def load():
             lib = C.CDLL(build())
             lib.oracle_rhs.argtypes = [C.POINTER(_Problem), C.c_double, PD, PD, PD]
             lib.oracle_rhs_faces.argtypes = [C.POINTER(_Problem), C.c_double, PD, PD, PD]
-            lib.oracle_step.argtypes = [C.POINTER(_Problem), C.c_int, PD, PD, PD, PD, PD]
+            lib.oracle_step.argtypes = [C.POINTER(_Problem), C.c_int, PD, PD, PD, PD, PD, PD]
+            lib.oracle_shock_indicator.argtypes = [C.POINTER(_Problem), PD, PD, C.c_double]
+            lib.oracle_shock_indicator.restype = C.c_double
+            lib.oracle_sensor.argtypes = [C.POINTER(_Problem), PD, PD, PD, PD, PD, PD]
+            lib.oracle_vertex_max.argtypes = [C.POINTER(_Problem), PD, PD]
+            lib.oracle_gradient.argtypes = [C.POINTER(_Problem), PD, PD, PD]
             lib.oracle_num_threads.restype = C.c_int
             lib.oracle_set_threads.argtypes = [C.c_int]
             _lib = lib
@@ -106,7 +114,7 @@ class OracleSolver:
 
     def __init__(self, N, VX, VY, EToV, bc_edges, *, flux="roe", init="freestream", cfl=1.0,
                  final_time=1e30, minf=0.1, gamma=1.4, alpha=0.0, local_dt=False,
-                 vortex_center=(5.0, 0.0), flux_mock=0):
+                 vortex_center=(5.0, 0.0), flux_mock=0, limiter="", kappa=0.0):
         self.el = dfr_ops.build_element(N)
         bc_edges = list(bc_edges) if bc_edges is not None else []
         if init == "ivortex":  # Wall -> IVortex relabel (euler.go:780-790)
@@ -154,11 +162,29 @@ class OracleSolver:
                 s.qinf[i] = fs["qinf"][i]
             s.pinf, s.cinf, s.gamma, s.minf = fs["pinf"], fs["cinf"], fs["gamma"], fs["minf"]
         p.vbeta, p.vx0, p.vy0, p.vgamma = self.vortex
+        # PerssonC0 dissipation (euler.go:107-112: only for N > 0); Eps0 = 5/1.5
+        # regardless of Kappa, which only sets the sensor ramp (dissipation.go:140-147).
+        self.diss = limiter.strip().lower() in ("perssonc0", "persson c0") and N != 0
+        el = self.el
+        k.update(EtoV=np.ascontiguousarray(np.asarray(EToV, np.int64)), V=np.ascontiguousarray(el.V),
+                 Vinv=np.ascontiguousarray(el.Vinv), SD=np.ascontiguousarray(el.SensD),
+                 SP=np.ascontiguousarray(el.SensP), M=np.ascontiguousarray(el.MassMatrix),
+                 MF=np.ascontiguousarray(el.ModeFilter), Div=np.ascontiguousarray(el.Div),
+                 Bary=np.ascontiguousarray(el.Bary), Clip=np.ascontiguousarray(el.Clipper))
+        p.diss = int(self.diss)
+        p.nverts = len(VX)
+        p.EtoV = k["EtoV"].ctypes.data_as(PL)
+        for name, key in (("V", "V"), ("Vinv", "Vinv"), ("SensD", "SD"), ("SensP", "SP"), ("Mass", "M"),
+                          ("ModeFilter", "MF"), ("Div", "Div"), ("Bary", "Bary")):
+            setattr(p, name, k[key].ctypes.data_as(PD))
+        p.kappa = 5.0 if kappa == 0.0 else kappa
+        p.eps0 = 5.0 / 1.5
         self.p = p
         self.lib = load()
         self.Q = self.initial_state()
         self.time = 0.0
         self.DT = np.zeros(self.K)
+        self.DTVisc = np.zeros(self.K)
 
     def initial_state(self):
         """InitializeSolution (euler.go:728-794); returns 4 x Np x K."""
@@ -197,9 +223,60 @@ class OracleSolver:
         t = C.c_double(self.time)
         dt = C.c_double(0.0)
         self.lib.oracle_step(C.byref(self.p), nsteps, self.Q.ctypes.data_as(PD), C.byref(t), C.byref(dt),
-                             R.ctypes.data_as(PD), self.DT.ctypes.data_as(PD))
+                             R.ctypes.data_as(PD), self.DT.ctypes.data_as(PD), self.DTVisc.ctypes.data_as(PD))
         self.time = t.value
         return t.value, dt.value, R
+
+
+    def shock_indicator(self, q, kappa):
+        """ModeAliasShockFinder.ShockIndicator on one element's density values."""
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        return self.lib.oracle_shock_indicator(C.byref(self.p), q.ctypes.data_as(PD),
+                                               self._keep["Clip"].ctypes.data_as(PD), float(kappa))
+
+    def vertex_max(self, elem):
+        """Maximum of an element scalar over the elements at each vertex."""
+        elem = np.ascontiguousarray(elem, dtype=np.float64)
+        out = np.zeros(self.p.nverts)
+        self.lib.oracle_vertex_max(C.byref(self.p), elem.ctypes.data_as(PD), out.ctypes.data_as(PD))
+        return out
+
+    def gradient(self, Q):
+        """(d/dx, d/dy) of each variable at the NpFlux flux points, 4 x NpFlux x K each."""
+        Q = np.ascontiguousarray(Q, dtype=np.float64)
+        gx = np.zeros((4, self.el.NpFlux, self.K))
+        gy = np.zeros_like(gx)
+        self.lib.oracle_gradient(C.byref(self.p), Q.ctypes.data_as(PD), gx.ctypes.data_as(PD),
+                                 gy.ctypes.data_as(PD))
+        return gx, gy
+
+    def sensor(self, Q):
+        """(Se, sigma, eps, sigma vertex-averaged, eps at vertices) for state Q."""
+        Q = np.ascontiguousarray(Q, dtype=np.float64)
+        out = [np.zeros(self.K) for _ in range(4)] + [np.zeros(self.p.nverts)]
+        self.lib.oracle_sensor(C.byref(self.p), Q.ctypes.data_as(PD), *[o.ctypes.data_as(PD) for o in out])
+        return out
+
+
+def shock_conditions(M1, alpha=0.0, gamma=1.4):
+    """ShockConditions (DG2D/test_functions2.go:184-240): pre/post normal-shock states."""
+    a = alpha * math.pi / 180.0
+    rho1, p1, u1, v1 = 1.0, 1.0, M1, 0.0
+    u1n = u1 * math.cos(a) + v1 * math.sin(a)
+    u1t = -u1 * math.sin(a) + v1 * math.cos(a)
+    M1n = u1n / math.sqrt(gamma * p1 / rho1)
+    En1 = p1 / (gamma - 1) + 0.5 * rho1 * (u1 * u1 + v1 * v1)
+    U1 = [rho1, rho1 * u1, rho1 * v1, En1]
+    if M1n < 1.0:
+        return U1, list(U1)
+    rr = ((gamma + 1) * M1n * M1n) / ((gamma - 1) * M1n * M1n + 2)
+    pr = 1 + (2 * gamma / (gamma + 1)) * (M1n * M1n - 1)
+    u2n = u1n * ((gamma - 1) * M1n * M1n + 2) / ((gamma + 1) * M1n * M1n)
+    rho2, p2, u2t = rho1 * rr, p1 * pr, u1t
+    u2 = u2n * math.cos(a) - u2t * math.sin(a)
+    v2 = u2n * math.sin(a) + u2t * math.cos(a)
+    En2 = p2 / (gamma - 1) + 0.5 * rho2 * (u2 * u2 + v2 * v2)
+    return U1, [rho2, rho2 * u2, rho2 * v2, En2]
 
 
 def ivortex_state(vortex, t, x, y):
