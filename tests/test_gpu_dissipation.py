@@ -57,10 +57,12 @@ def test_rhs_parity_shocktube(N, kappa):
     Q0 = gpu.get_global_state()
     assert np.array_equal(Q0, ora.Q)
     rng = np.random.default_rng(N)
-    Q = smooth_tube(ora)
+    # at N = 1 a narrower jump extrapolates to negative face pressures
+    Q = smooth_tube(ora, 0.02 if N == 1 else 0.005)
     Q = np.ascontiguousarray(Q * (1.0 + 0.01 * rng.uniform(-1, 1, Q.shape)))
     r = gpu.rhs_global(Q)
     ref = ora.rhs(Q)
+    assert np.all(np.isfinite(ref))
     assert_rhs_close(r, ref, N)
     # the shock has switched the sensor on somewhere
     _, sig, _, _, _ = ora.sensor(Q)
@@ -93,8 +95,9 @@ def test_step_parity_shocktube(N, local_dt):
     assert np.all(np.isfinite(Q))
     assert rel_l2(Q, ora.Q) <= 1e-10, rel_l2(Q, ora.Q)
     if not local_dt:
-        assert abs(t - to) <= 1e-12 * max(1.0, abs(to))
-        assert abs(dt - dto) <= 1e-12 * abs(dto)
+        # the viscous limit C/max(eps/h^2) carries the dissipation's round-off
+        assert abs(t - to) <= 1e-10 * max(1.0, abs(to))
+        assert abs(dt - dto) <= 1e-10 * abs(dto)
     gpu.close()
 
 
