@@ -30,7 +30,7 @@ EXPORTS = [
     "gcfd_create", "gcfd_destroy", "gcfd_last_error", "gcfd_dims", "gcfd_set_state",
     "gcfd_get_state", "gcfd_set_state_device", "gcfd_get_state_device", "gcfd_set_time",
     "gcfd_get_time", "gcfd_rhs", "gcfd_step", "gcfd_enqueue_steps", "gcfd_get_stream", "gcfd_profile_step",
-    "gcfd_host_operator",
+    "gcfd_host_operator", "gcfd_residual_norms_static",
 ]
 
 
@@ -96,6 +96,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         lib.gcfd_get_stream.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
         lib.gcfd_profile_step.argtypes = [C.c_void_p, PD, PI]
         lib.gcfd_host_operator.argtypes = [C.c_int32, C.c_int32, PD, PI, PI]
+        lib.gcfd_residual_norms_static.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, PD, PD, PD]
         _lib = lib
         return lib
 

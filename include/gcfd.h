@@ -150,6 +150,38 @@ int gcfd_profile_step(gcfd_ctx* ctx, double* kernel_ms4, int32_t* launches4);
  * 5 flux-point r,s (NpFlux x 2).  With out == NULL only rows/cols are set. */
 int gcfd_host_operator(int32_t N, int32_t which, double* out, int32_t* rows, int32_t* cols);
 
+/* Residual norms of an increment array that the caller owns, computed without
+ * allocating anything.  This entry point has no counterpart in the reference.
+ *
+ * It is for callers that cannot call cudaMalloc when they need the norms: a
+ * host framework whose own allocator owns the GPU's memory and allows no
+ * allocation behind its back, or a steady-state loop that must not allocate
+ * (an allocation can fail mid-run, and cudaFree synchronises the device).
+ * Such a caller keeps the increments of a step (for example the difference of
+ * two gcfd_get_state_device snapshots) in its own memory and asks for the same
+ * numbers gcfd_step reports: per variable the signed max, the max |R| and the
+ * RMS over the Np x K points.
+ *
+ * dR: device pointer, 4 x Np x K FP64 (variable, point, element fastest), on
+ * the device that is current for the calling thread.  stream: a cudaStream_t
+ * (NULL for the default stream); the call enqueues its two kernels and one
+ * 96-byte copy there and waits for that stream.  Any output pointer may be NULL.
+ *
+ * The intermediate per-block partials live in one fixed device array built
+ * into the library (1.5 MiB, no per-call allocation), which caps Np x K at
+ * GCFD_RESID_STATIC_MAX_POINTS; larger inputs return GCFD_ERR_SHAPE with a
+ * message in gcfd_last_error(NULL).  Every part of that array that a call
+ * reads is written earlier in the same call, so nothing carries over from one
+ * call to the next.  All calls on a device share the array: calls that can
+ * overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress, which can load the module);
+ * make that first call before any stream capture.  GCFD_ERR_NAN when an
+ * increment is not finite (the outputs are still written). */
+#define GCFD_RESID_STATIC_MAX_POINTS 33554432 /* 16384 blocks x 2048 points */
+int gcfd_residual_norms_static(const double* dR, int32_t Np, int32_t K, void* stream, double* resid_max4,
+                               double* resid_absmax4, double* resid_rms4);
+
 #ifdef __cplusplus
 }
 #endif
