@@ -54,6 +54,7 @@ def args_parse():
     p.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
     p.add_argument("--workload", choices=sorted(WORKLOADS), default="vortex256")
     p.add_argument("--fp64-steps", type=int, default=100)
+    p.add_argument("--adj-steps", type=int, default=20, help="steps of the FP64 adjoint timing (0: skip)")
     p.add_argument("--e2e-steps", type=int, default=50)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu", action="store_true")
@@ -324,6 +325,35 @@ def run_ours(a, world, rank, local):
                 "ms_per_step": ms64 / a.fp64_steps, "steps": a.fp64_steps}
         s64.close()
 
+    # Adjoint cost: the reverse sweep of a recorded FP64 window (checkpoint every
+    # step: each reverse step recomputes its forward step once with the stage
+    # tape, then runs the stage adjoints) against the FP64 forward step.
+    adjoint = None
+    if a.adj_steps > 0:
+        sa = Euler(ip, mesh, 1, precision="fp64", device=local, vortex_center=(0.0, 0.0))
+        sta = torch.cuda.ExternalStream(sa.stream_handle(), device=torch.device("cuda", local))
+        sa.enqueue_steps(2)
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(sta):
+            f0.record(sta)
+            sa.enqueue_steps(a.adj_steps)
+            f1.record(sta)
+        torch.cuda.synchronize()
+        fwd_ms = f0.elapsed_time(f1) / a.adj_steps
+        sa.record(a.adj_steps, 1)
+        qbar = np.ones((4, Np, K))
+        sa.step_vjp(qbar)  # warm-up (allocations, first launches)
+        sa.record(a.adj_steps, 1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sa.step_vjp(qbar)
+        adj_ms = (time.perf_counter() - t0) * 1e3 / a.adj_steps
+        adjoint = {"ms_per_step": adj_ms, "forward_ms_per_step": fwd_ms, "ratio": adj_ms / fwd_ms,
+                   "steps": a.adj_steps, "checkpoint_every": 1, "path": "fp64",
+                   "timing": "host clock around gcfd_step_vjp (synchronous), forward by CUDA events"}
+        sa.close()
+
     # End to end through the public API: pinned host state in, step, state out.
     import torch as _t
     host = [_t.empty((Np, K), dtype=_t.float64, pin_memory=True) for _ in range(4)]
@@ -374,6 +404,7 @@ def run_ours(a, world, rank, local):
             "roofline": roofline,
             "cpu_baseline": cpu,
             "fp64_path": fp64,
+            "adjoint": adjoint,
             "final_time": info["time"],
         }
         if cpu:

@@ -30,7 +30,8 @@ EXPORTS = [
     "gcfd_create", "gcfd_destroy", "gcfd_last_error", "gcfd_dims", "gcfd_set_state",
     "gcfd_get_state", "gcfd_set_state_device", "gcfd_get_state_device", "gcfd_set_time",
     "gcfd_get_time", "gcfd_rhs", "gcfd_step", "gcfd_enqueue_steps", "gcfd_get_stream", "gcfd_profile_step",
-    "gcfd_host_operator", "gcfd_residual_norms_static",
+    "gcfd_host_operator", "gcfd_residual_norms_static", "gcfd_functional", "gcfd_rhs_vjp",
+    "gcfd_record_steps", "gcfd_step_vjp",
 ]
 
 
@@ -97,6 +98,11 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         lib.gcfd_profile_step.argtypes = [C.c_void_p, PD, PI]
         lib.gcfd_host_operator.argtypes = [C.c_int32, C.c_int32, PD, PI, PI]
         lib.gcfd_residual_norms_static.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, PD, PD, PD]
+        lib.gcfd_functional.argtypes = [C.c_void_p, C.c_int32, PD, C.c_int32, PI, C.POINTER(PD), PD]
+        lib.gcfd_rhs_vjp.argtypes = [C.c_void_p, C.c_double, C.c_int32, PI, C.POINTER(PD), C.POINTER(PD),
+                                     C.POINTER(PD), PD, PD]
+        lib.gcfd_record_steps.argtypes = [C.c_void_p, C.c_int32, C.c_int32, PD, PD]
+        lib.gcfd_step_vjp.argtypes = [C.c_void_p, C.c_int32, PI, C.POINTER(PD), C.c_double, C.POINTER(PD), PD, PD]
         _lib = lib
         return lib
 

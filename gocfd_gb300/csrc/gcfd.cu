@@ -17,6 +17,7 @@
 #include "gcfd_kernels.cuh"
 #include "gcfd_mixed.cuh"
 #include "gcfd_diss.cuh"
+#include "gcfd_adjoint.cuh"
 #include "mesh.hpp"
 
 using namespace gcfd;
@@ -124,6 +125,23 @@ struct gcfd_ctx {
   int* detov = nullptr;
   int nverts = 0;
   double dissKappa = 5.0;
+  // adjoint (FP64 path): per-step tape, adjoint work arrays, recorded window
+  bool adjReady = false;
+  double* tapeRHS[5] = {};
+  double* tapeES[5] = {};
+  double* tapeDT[5] = {};
+  Scalars* tapeSc0 = nullptr;  // scalars before the taped step (BC time)
+  Scalars* tapeSc = nullptr;   // after it (per-stage gmax and dt)
+  double* Qb[5] = {};
+  double *Qbf = nullptr, *Rb3 = nullptr, *QFb = nullptr, *FEb = nullptr;
+  double *carry = nullptr, *dtOwnK = nullptr, *esBar = nullptr;
+  double* adjS = nullptr;      // [0,5) dt adjoints, [5,9) Qinf adjoint, [9] t-bar current, [10] t-bar next, [11] J
+  int* argEdge = nullptr;      // [5]
+  double *dXs = nullptr, *dYs = nullptr, *edgeW = nullptr;
+  int winSteps = 0, winEvery = 1;
+  std::vector<void*> winAllocs;
+  double *ckpt = nullptr, *ckptT = nullptr, *segQ = nullptr, *segT = nullptr, *endQ = nullptr;
+  Scalars* endSc = nullptr;
   std::vector<int> edgeOrder;             // device edge i -> topology edge
   std::vector<double> hnx, hny, hoohK;    // per device edge
   cudaGraph_t graph = nullptr;
@@ -137,6 +155,7 @@ struct gcfd_ctx {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
+    for (void* p : winAllocs) cudaFree(p);
     if (evFork) cudaEventDestroy(evFork);
     if (evJoin) cudaEventDestroy(evJoin);
     if (stream2) cudaStreamDestroy(stream2);
@@ -258,6 +277,7 @@ struct Launch {
     a.gvisc = c->sc->gvisc;
     a.DTVisc = c->DTVisc;
     a.cdiff = 1.0 / (double(c->N + 1) * double(c->N + 1));
+    a.tapeRHS = nullptr;
     return a;
   }
   static DissArgs diss_args(gcfd_ctx* c, int stage, double* Qs) {
@@ -513,6 +533,180 @@ struct MixedLaunch {
   }
   static void prep_state(gcfd_ctx* c) { prepare(c, c->Q[0]); }
 };
+
+// Adjoint launchers (FP64 path).
+template <int N>
+struct AdjLaunch {
+  using L = Launch<N, double>;
+  static int grid(int n) { return (n + 127) / 128; }
+  static EdgeArgs<double> edge_args(gcfd_ctx* c, const double* time) {
+    EdgeArgs<double> e = L::edge_args(c, time);
+    e.QF = static_cast<const double*>(c->QF);
+    return e;
+  }
+  static AdjEdgeArgs adj_edge_args(gcfd_ctx* c) {
+    AdjEdgeArgs x;
+    x.FEb = c->FEb;
+    x.QFb = c->QFb;
+    x.qinfb = c->adjS + 5;
+    x.tb = c->adjS + 9;
+    x.esBar = c->esBar;
+    x.useManualRoe = 1;
+    return x;
+  }
+  static AdjArgs adj_args(gcfd_ctx* c, int s, const double* Qs, const double* Qbn, double* Qbs) {
+    AdjArgs a;
+    a.K = c->K;
+    a.stage = s;
+    a.localDT = c->prm.local_time_stepping;
+    a.Qs = Qs;
+    a.Qbn = Qbn;
+    a.rhs = s >= 0 ? c->tapeRHS[s] : nullptr;
+    a.rhs3 = c->tapeRHS[3];
+    a.Qb0 = c->Qb[0];
+    a.Qbs = Qbs;
+    a.Qb2 = c->Qb[2];
+    a.Qb3 = c->Qb[3];
+    a.Rb3 = c->Rb3;
+    a.dtS = c->tapeSc->dt;
+    a.dtK = s >= 0 ? c->tapeDT[s] : nullptr;
+    a.dtbarG = c->adjS;
+    a.dtOwnK = c->dtOwnK;
+    a.DivInt = c->Div;
+    a.Jdet = c->Jdet;
+    a.Jinv = c->Jinv;
+    a.FEb = c->FEb;
+    const double g = c->fsFar.gamma;
+    a.gas = Gas<double>{g, g - 1.0, 1.0 / (g - 1.0)};
+    return a;
+  }
+  // Forward step with the tape: the same launches as L::step (so the states
+  // are bit-identical to the recorded trajectory), plus per-stage copies of
+  // the edge speeds and local dt, and the stage RHS written by k_div_update.
+  static void tape_step(gcfd_ctx* c) {
+    cudaMemcpyAsync(c->tapeSc0, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream);
+    k_step_begin<<<1, 32, 0, c->stream>>>(c->sc);
+    for (int s = 0; s < 5; ++s) {
+      L::interp(c, c->Q[s]);
+      L::edge(c, &c->sc->time, &c->sc->gmax[s]);
+      cudaMemcpyAsync(c->tapeES[s], c->edgeSpeed, sizeof(double) * c->nEdges, cudaMemcpyDeviceToDevice,
+                      c->stream);
+      UpdateArgs<double> u = L::update_args(c, s, c->Q[s]);
+      u.tapeRHS = c->tapeRHS[s];
+      k_div_update<N, double><<<grid(c->K), 128, 0, c->stream>>>(u);
+      if (c->prm.local_time_stepping)
+        cudaMemcpyAsync(c->tapeDT[s], c->DT, sizeof(double) * c->K, cudaMemcpyDeviceToDevice, c->stream);
+    }
+    k_step_end<<<1, 32, 0, c->stream>>>(c->sc, c->prm.local_time_stepping);
+    cudaMemcpyAsync(c->tapeSc, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream);
+  }
+  // The reverse of stage s.  Q0 is the step's initial state.
+  static void reverse_stage(gcfd_ctx* c, int s, const double* Q0) {
+    const double* Qs = (s == 0) ? Q0 : c->Q[s];
+    L::interp(c, Qs);
+    const double* Qbn = (s == 4) ? c->Qbf : c->Qb[s + 1];
+    k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, s, Qs, Qbn, c->Qb[s]));
+    const EdgeArgs<double> e = edge_args(c, &c->tapeSc0->time);
+    const AdjEdgeArgs x = adj_edge_args(c);
+    const int nE = c->nInt + c->nBC;
+    k_adj_edge<N><<<grid(nE), 128, 0, c->stream>>>(e, x);
+    cudaMemsetAsync(c->esBar, 0, sizeof(double) * nE, c->stream);
+    AdjDtArgs d;
+    d.K = c->K;
+    d.stage = s;
+    d.nEdges = nE;
+    d.cfl = c->prm.cfl;
+    d.finalTime = c->prm.final_time;
+    d.gmaxS = reinterpret_cast<const double*>(c->tapeSc->gmax);
+    d.tn = &c->tapeSc0->time;
+    d.dtbarG = c->adjS;
+    d.tbarNext = c->adjS + 10;
+    d.tbarCur = c->adjS + 9;
+    d.argEdge = c->argEdge + s;
+    d.esBar = c->esBar;
+    d.dtPrev = s > 0 ? c->tapeDT[s - 1] : nullptr;
+    d.edgeSpeed = c->tapeES[s];
+    d.elemEdge = c->elemEdge;
+    d.dtOwnK = c->dtOwnK;
+    d.carry = c->carry;
+    if (c->prm.local_time_stepping) {
+      k_adj_lts<<<grid(c->K), 128, 0, c->stream>>>(d);
+    } else {
+      cudaMemsetAsync(c->argEdge + s, 0x7f, sizeof(int), c->stream);
+      k_adj_argmax<<<grid(nE), 128, 0, c->stream>>>(c->tapeES[s], d.gmaxS, s, nE, c->argEdge + s);
+      k_adj_gsel<<<1, 32, 0, c->stream>>>(d);
+    }
+    k_adj_speed<N><<<grid(nE), 128, 0, c->stream>>>(e, x);
+    k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[s], c->K);
+  }
+  // Adjoint of one step whose initial state is Q0 (already in c->Q[0]) and
+  // time is in c->sc.  In: Qbf, adjS[10] (t-bar of the step's end).  Out:
+  // Qbf <- adjoint of Q0, adjS[10] <- t-bar of the step's start.
+  static void reverse_step(gcfd_ctx* c, const double* Q0) {
+    tape_step(c);
+    const size_t S = sizeof(double) * 4 * c->Np * static_cast<size_t>(c->K);
+    for (int i = 0; i < 4; ++i) cudaMemsetAsync(c->Qb[i], 0, S, c->stream);
+    cudaMemsetAsync(c->adjS, 0, sizeof(double) * 5, c->stream);
+    cudaMemcpyAsync(c->adjS + 9, c->adjS + 10, sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemsetAsync(c->carry, 0, sizeof(double) * c->K, c->stream);
+    for (int s = 4; s >= 0; --s) reverse_stage(c, s, Q0);
+    std::swap(c->Qbf, c->Qb[0]);
+    cudaMemcpyAsync(c->adjS + 10, c->adjS + 9, sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  }
+  // RHS adjoint at c->Qtmp and sc->rhs_time: Qb[0] <- J^T Qbf.
+  static void rhs_vjp(gcfd_ctx* c) {
+    L::interp(c, c->Qtmp);
+    const size_t S = sizeof(double) * 4 * c->Np * static_cast<size_t>(c->K);
+    cudaMemsetAsync(c->Qb[0], 0, S, c->stream);
+    k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, -1, c->Qtmp, c->Qbf, c->Qb[0]));
+    const EdgeArgs<double> e = edge_args(c, &c->sc->rhs_time);
+    k_adj_edge<N><<<grid(c->nInt + c->nBC), 128, 0, c->stream>>>(e, adj_edge_args(c));
+    k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[0], c->K);
+  }
+  // Functionals of the current state Q[0]: J into adjS[11], dJ/dQ into Qb[0],
+  // dJ/dt into adjS[9].
+  static void functional(gcfd_ctx* c, int kind) {
+    const size_t S = sizeof(double) * 4 * c->Np * static_cast<size_t>(c->K);
+    cudaMemsetAsync(c->Qb[0], 0, S, c->stream);
+    if (kind == GCFD_FUNC_VORTEX_ERROR) {
+      k_func_vortex<N><<<grid(c->K), 128, 0, c->stream>>>(c->Q[0], c->dXs, c->dYs, c->K, c->vbeta, c->vx0, c->vy0,
+                                                          c->vgamma, &c->sc->time, c->Qb[0], c->adjS + 11,
+                                                          c->adjS + 9);
+      return;
+    }
+    L::interp(c, c->Q[0]);
+    cudaMemsetAsync(c->QFb, 0, sizeof(double) * 4 * 3 * c->NE * static_cast<size_t>(c->K), c->stream);
+    const EdgeArgs<double> e = edge_args(c, &c->sc->time);
+    if (c->nBC > 0)
+      k_func_wall<N><<<grid(c->nBC), 128, 0, c->stream>>>(e, c->edgeW, kind == GCFD_FUNC_WALL_FORCE_Y, c->QFb,
+                                                          c->adjS + 11);
+    k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[0], c->K);
+  }
+};
+
+struct AdjOps {
+  void (*tape_step)(gcfd_ctx*);
+  void (*reverse_step)(gcfd_ctx*, const double*);
+  void (*rhs_vjp)(gcfd_ctx*);
+  void (*functional)(gcfd_ctx*, int);
+};
+
+template <int N>
+AdjOps adj_ops_for() {
+  return AdjOps{&AdjLaunch<N>::tape_step, &AdjLaunch<N>::reverse_step, &AdjLaunch<N>::rhs_vjp,
+                &AdjLaunch<N>::functional};
+}
+
+bool select_adj_ops(int N, AdjOps* o) {
+  switch (N) {
+    case 0: *o = adj_ops_for<0>(); return true;
+    case 1: *o = adj_ops_for<1>(); return true;
+    case 2: *o = adj_ops_for<2>(); return true;
+    case 3: *o = adj_ops_for<3>(); return true;
+    case 4: *o = adj_ops_for<4>(); return true;
+    default: return false;
+  }
+}
 
 // Mixed path: rebuild the FP64 state Q[0] from the compensated pair.
 int sync_fp64_state(gcfd_ctx* c) {
@@ -1116,6 +1310,233 @@ int gcfd_host_operator(int32_t N, int32_t which, double* out, int32_t* rows, int
   if (rows) *rows = m->rows;
   if (cols) *cols = m->cols;
   if (out) std::memcpy(out, m->v.data(), m->v.size() * sizeof(double));
+  return GCFD_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Adjoint entry points.
+namespace {
+
+int adj_check(gcfd_ctx* c) {
+  if (c->fp32) return fail(c, GCFD_ERR_UNSUPPORTED, "the adjoint runs on the FP64 path only");
+  if (c->diss) return fail(c, GCFD_ERR_UNSUPPORTED, "the adjoint does not cover the PerssonC0 dissipation");
+  return GCFD_OK;
+}
+
+// Interpolatory weights of the NpEdge edge flux points on [-1, 1], normalised
+// to sum to one (exact for polynomials of degree NpEdge - 1 along the edge).
+std::vector<double> edge_weights(const gcfd_ctx* c) {
+  const int NE = c->NE, off = 2 * c->Np;
+  std::vector<double> t(NE), A(static_cast<size_t>(NE) * NE), w(NE);
+  for (int p = 0; p < NE; ++p) t[p] = c->el.rFlux[off + p];
+  for (int m = 0; m < NE; ++m) {
+    for (int p = 0; p < NE; ++p) A[m * NE + p] = std::pow(t[p], m);
+    w[m] = (m % 2 == 0) ? 1.0 / (m + 1) : 0.0;
+  }
+  // Gaussian elimination with partial pivoting
+  for (int col = 0; col < NE; ++col) {
+    int piv = col;
+    for (int r = col + 1; r < NE; ++r)
+      if (std::fabs(A[r * NE + col]) > std::fabs(A[piv * NE + col])) piv = r;
+    if (piv != col) {
+      for (int j = 0; j < NE; ++j) std::swap(A[col * NE + j], A[piv * NE + j]);
+      std::swap(w[col], w[piv]);
+    }
+    for (int r = col + 1; r < NE; ++r) {
+      const double f = A[r * NE + col] / A[col * NE + col];
+      for (int j = col; j < NE; ++j) A[r * NE + j] -= f * A[col * NE + j];
+      w[r] -= f * w[col];
+    }
+  }
+  for (int r = NE - 1; r >= 0; --r) {
+    double s = w[r];
+    for (int j = r + 1; j < NE; ++j) s -= A[r * NE + j] * w[j];
+    w[r] = s / A[r * NE + r];
+  }
+  return w;
+}
+
+int adj_init(gcfd_ctx* c) {
+  if (c->adjReady) return GCFD_OK;
+  int rc = adj_check(c);
+  if (rc) return rc;
+  const size_t S = static_cast<size_t>(4) * c->Np * c->K;
+  const size_t F = static_cast<size_t>(4) * 3 * c->NE * c->K;
+  const int nE = c->nInt + c->nBC;
+  for (int s = 0; s < 5; ++s) {
+    if ((rc = dalloc(c, &c->tapeRHS[s], S))) return rc;
+    if ((rc = dalloc(c, &c->tapeES[s], static_cast<size_t>(nE)))) return rc;
+    if ((rc = dalloc(c, &c->tapeDT[s], static_cast<size_t>(c->K)))) return rc;
+    if ((rc = dalloc(c, &c->Qb[s], S))) return rc;
+  }
+  if ((rc = dalloc(c, &c->tapeSc0, 1))) return rc;
+  if ((rc = dalloc(c, &c->tapeSc, 1))) return rc;
+  if ((rc = dalloc(c, &c->Qbf, S))) return rc;
+  if ((rc = dalloc(c, &c->Rb3, S))) return rc;
+  if ((rc = dalloc(c, &c->QFb, F))) return rc;
+  if ((rc = dalloc(c, &c->FEb, F))) return rc;
+  if ((rc = dalloc(c, &c->carry, static_cast<size_t>(c->K)))) return rc;
+  if ((rc = dalloc(c, &c->dtOwnK, static_cast<size_t>(c->K)))) return rc;
+  if ((rc = dalloc(c, &c->esBar, static_cast<size_t>(nE)))) return rc;
+  if ((rc = dalloc(c, &c->adjS, 16))) return rc;
+  if ((rc = dalloc(c, &c->argEdge, 8))) return rc;
+  if ((rc = upload(c, &c->dXs, c->geo.xSol))) return rc;
+  if ((rc = upload(c, &c->dYs, c->geo.ySol))) return rc;
+  if ((rc = upload(c, &c->edgeW, edge_weights(c)))) return rc;
+  GCFD_CUDA(c, cudaMemsetAsync(c->adjS, 0, sizeof(double) * 16, c->stream));
+  c->adjReady = true;
+  return GCFD_OK;
+}
+
+int win_alloc(gcfd_ctx* c, double** p, size_t count) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, count * sizeof(double) > 0 ? count * sizeof(double) : 16);
+  if (e != cudaSuccess)
+    return fail(c, e == cudaErrorMemoryAllocation ? GCFD_ERR_OOM : GCFD_ERR_CUDA,
+                std::string("cudaMalloc (adjoint window): ") + cudaGetErrorString(e));
+  c->winAllocs.push_back(q);
+  *p = static_cast<double*>(q);
+  return GCFD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gcfd_functional(gcfd_ctx* c, int32_t kind, double* J, int32_t nshards, const int32_t* Kmax,
+                    double* const* Qbar, double* tbar) {
+  if (!c || !J) return c ? fail(c, GCFD_ERR_ARG, "null J") : GCFD_ERR_ARG;
+  if (kind < GCFD_FUNC_WALL_FORCE_X || kind > GCFD_FUNC_VORTEX_ERROR)
+    return fail(c, GCFD_ERR_ARG, "unknown functional kind");
+  int rc = adj_init(c);
+  if (rc) return rc;
+  if (Qbar && (rc = check_shards(c, nshards, Kmax))) return rc;
+  AdjOps o;
+  select_adj_ops(c->N, &o);
+  GCFD_CUDA(c, cudaMemsetAsync(c->adjS + 9, 0, sizeof(double) * 3, c->stream));
+  o.functional(c, kind);
+  GCFD_CUDA(c, cudaGetLastError());
+  double h[3];
+  GCFD_CUDA(c, cudaMemcpyAsync(h, c->adjS + 9, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  if (Qbar && (rc = copy_shards(c, c->Qb[0], nshards, Kmax, nullptr, false, Qbar))) return rc;
+  GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
+  *J = h[2];
+  if (tbar) *tbar = h[0];
+  return GCFD_OK;
+}
+
+int gcfd_rhs_vjp(gcfd_ctx* c, double time, int32_t nshards, const int32_t* Kmax, const double* const* Q,
+                 const double* const* RHSbar, double* const* Qbar, double* qinf_bar4, double* time_bar) {
+  if (!c || !Q || !RHSbar || !Qbar) return c ? fail(c, GCFD_ERR_ARG, "null state") : GCFD_ERR_ARG;
+  int rc = adj_init(c);
+  if (rc) return rc;
+  if ((rc = check_shards(c, nshards, Kmax))) return rc;
+  if ((rc = copy_shards(c, c->Qtmp, nshards, Kmax, Q, true, nullptr))) return rc;
+  if ((rc = copy_shards(c, c->Qbf, nshards, Kmax, RHSbar, true, nullptr))) return rc;
+  GCFD_CUDA(c, cudaMemcpyAsync(&c->sc->rhs_time, &time, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GCFD_CUDA(c, cudaMemsetAsync(c->adjS + 5, 0, sizeof(double) * 5, c->stream));
+  AdjOps o;
+  select_adj_ops(c->N, &o);
+  o.rhs_vjp(c);
+  GCFD_CUDA(c, cudaGetLastError());
+  double h[5];
+  GCFD_CUDA(c, cudaMemcpyAsync(h, c->adjS + 5, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  if ((rc = copy_shards(c, c->Qb[0], nshards, Kmax, nullptr, false, Qbar))) return rc;
+  GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (qinf_bar4)
+    for (int i = 0; i < 4; ++i) qinf_bar4[i] = h[i];
+  if (time_bar) *time_bar = h[4];
+  return GCFD_OK;
+}
+
+int gcfd_record_steps(gcfd_ctx* c, int32_t nsteps, int32_t every, double* time, double* dt_last) {
+  if (!c) return GCFD_ERR_ARG;
+  if (nsteps < 1 || every < 1) return fail(c, GCFD_ERR_ARG, "nsteps and checkpoint_every must be >= 1");
+  int rc = adj_init(c);
+  if (rc) return rc;
+  GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (void* p : c->winAllocs) cudaFree(p);
+  c->winAllocs.clear();
+  c->winSteps = 0;
+  const size_t S = static_cast<size_t>(4) * c->Np * c->K;
+  const int nck = (nsteps + every - 1) / every;
+  if ((rc = win_alloc(c, &c->ckpt, S * nck))) return rc;
+  if ((rc = win_alloc(c, &c->ckptT, static_cast<size_t>(nck)))) return rc;
+  if ((rc = win_alloc(c, &c->segQ, S * std::min(every, nsteps)))) return rc;
+  if ((rc = win_alloc(c, &c->segT, static_cast<size_t>(std::min(every, nsteps))))) return rc;
+  if ((rc = win_alloc(c, &c->endQ, S))) return rc;
+  double* sc = nullptr;
+  if ((rc = win_alloc(c, &sc, (sizeof(Scalars) + 7) / 8))) return rc;
+  c->endSc = reinterpret_cast<Scalars*>(sc);
+  for (int n = 0; n < nsteps; ++n) {
+    if (n % every == 0) {
+      const int j = n / every;
+      GCFD_CUDA(c, cudaMemcpyAsync(c->ckpt + S * j, c->Q[0], S * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   c->stream));
+      GCFD_CUDA(c, cudaMemcpyAsync(c->ckptT + j, &c->sc->time, sizeof(double), cudaMemcpyDeviceToDevice,
+                                   c->stream));
+    }
+    GCFD_CUDA(c, cudaGraphLaunch(c->graphExec, c->stream));
+  }
+  GCFD_CUDA(c, cudaMemcpyAsync(c->endQ, c->Q[0], S * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  GCFD_CUDA(c, cudaMemcpyAsync(c->endSc, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream));
+  Scalars h;
+  GCFD_CUDA(c, cudaMemcpyAsync(&h, c->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
+  GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->winSteps = nsteps;
+  c->winEvery = every;
+  if (time) *time = h.time;
+  if (dt_last) *dt_last = h.dt[4];
+  return GCFD_OK;
+}
+
+int gcfd_step_vjp(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const double* const* Qfinal_bar,
+                  double tfinal_bar, double* const* Q0_bar, double* qinf_bar4, double* t0_bar) {
+  if (!c || !Qfinal_bar || !Q0_bar) return c ? fail(c, GCFD_ERR_ARG, "null adjoint") : GCFD_ERR_ARG;
+  int rc = adj_check(c);
+  if (rc) return rc;
+  if (c->winSteps < 1) return fail(c, GCFD_ERR_ARG, "no recorded window: call gcfd_record_steps first");
+  if ((rc = check_shards(c, nshards, Kmax))) return rc;
+  AdjOps o;
+  select_adj_ops(c->N, &o);
+  const size_t S = static_cast<size_t>(4) * c->Np * c->K;
+  const size_t SB = S * sizeof(double);
+  if ((rc = copy_shards(c, c->Qbf, nshards, Kmax, Qfinal_bar, true, nullptr))) return rc;
+  GCFD_CUDA(c, cudaMemsetAsync(c->adjS, 0, sizeof(double) * 12, c->stream));
+  GCFD_CUDA(c, cudaMemcpyAsync(c->adjS + 10, &tfinal_bar, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  const int every = c->winEvery, nsteps = c->winSteps;
+  const int nseg = (nsteps + every - 1) / every;
+  for (int seg = nseg - 1; seg >= 0; --seg) {
+    const int n0 = seg * every, m = std::min(every, nsteps - n0);
+    GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], c->ckpt + S * seg, SB, cudaMemcpyDeviceToDevice, c->stream));
+    GCFD_CUDA(c, cudaMemcpyAsync(&c->sc->time, c->ckptT + seg, sizeof(double), cudaMemcpyDeviceToDevice,
+                                 c->stream));
+    for (int i = 0; i < m; ++i) {
+      GCFD_CUDA(c, cudaMemcpyAsync(c->segQ + S * i, c->Q[0], SB, cudaMemcpyDeviceToDevice, c->stream));
+      GCFD_CUDA(c, cudaMemcpyAsync(c->segT + i, &c->sc->time, sizeof(double), cudaMemcpyDeviceToDevice,
+                                   c->stream));
+      if (i + 1 < m) GCFD_CUDA(c, cudaGraphLaunch(c->graphExec, c->stream));
+    }
+    for (int i = m - 1; i >= 0; --i) {
+      GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], c->segQ + S * i, SB, cudaMemcpyDeviceToDevice, c->stream));
+      GCFD_CUDA(c, cudaMemcpyAsync(&c->sc->time, c->segT + i, sizeof(double), cudaMemcpyDeviceToDevice,
+                                   c->stream));
+      o.reverse_step(c, c->segQ + S * i);
+      GCFD_CUDA(c, cudaGetLastError());
+    }
+  }
+  double h[6];
+  GCFD_CUDA(c, cudaMemcpyAsync(h, c->adjS + 5, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  if ((rc = copy_shards(c, c->Qbf, nshards, Kmax, nullptr, false, Q0_bar))) return rc;
+  // back to the window's end
+  GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], c->endQ, SB, cudaMemcpyDeviceToDevice, c->stream));
+  GCFD_CUDA(c, cudaMemcpyAsync(c->sc, c->endSc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream));
+  GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (qinf_bar4)
+    for (int i = 0; i < 4; ++i) qinf_bar4[i] = h[i];
+  if (t0_bar) *t0_bar = h[5];
   return GCFD_OK;
 }
 

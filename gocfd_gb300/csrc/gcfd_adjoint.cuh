@@ -1,0 +1,704 @@
+// Adjoint (vector-Jacobian products) of the FP64 right-hand side and of the
+// SSP(5,4) step.  The forward restates RHSInternalPoints / CalculateEdgeEulerFlux
+// / SetRTFluxOnEdges / rkAdvance (euler.go:460-726, edges.go:325-488); the
+// adjoint is the exact transpose of that discrete map, including the
+// dependence of the time step on the state (global: dt = CFL / max wave speed,
+// clipped to FinalTime; local: the running max of CalculateLocalDT) and of the
+// IVortex boundary state on the solver time.
+//
+// Per RK stage s, in reverse:
+//   k_adj_div     R-bar from the stage output's adjoint, the SSP combination
+//                 terms, the dt adjoint partials, DivInt^T, the interior flux
+//                 Jacobian^T (reverse mode written out), edge-DOF adjoints
+//   k_adj_edge    Riemann flux Jacobian^T per edge point (Roe in reverse mode,
+//                 the other fluxes and every boundary condition by dual numbers)
+//   k_adj_gsel /  the dt adjoint onto the wave speed that set it (global:
+//   k_adj_lts     the argmax edge; local: per element, carried to the previous
+//                 stage when the previous DT was the max)
+//   k_adj_speed   wave speed Jacobian^T at each edge's max point
+//   k_adj_interp  FluxEdgeInterp^T of the face adjoints
+#pragma once
+#include "gcfd_dual.cuh"
+#include "gcfd_kernels.cuh"
+
+namespace gcfd {
+
+// Euler flux (FluxCalcBase, fluxes.go:76-87) in reverse: qb += (dFx/dq)^T Fxb + (dFy/dq)^T Fyb.
+__device__ __forceinline__ void euler_flux_vjp(const Gas<double>& g, const double q[4], const double Fxb[4],
+                                               const double Fyb[4], double qb[4]) {
+  const double rho = q[0], m = q[1], n = q[2], E = q[3];
+  const double oorho = 1.0 / rho;
+  const double u = m * oorho, v = n * oorho;
+  const double p = g.gm1 * (E - 0.5 * rho * (u * u + v * v));
+  double mb = Fxb[0] + u * Fxb[1] + v * Fxb[2];
+  double nb = Fyb[0] + u * Fyb[1] + v * Fyb[2];
+  double ub = m * Fxb[1] + (E + p) * Fxb[3] + n * Fyb[1];
+  double vb = m * Fxb[2] + n * Fyb[2] + (E + p) * Fyb[3];
+  double Eb = u * Fxb[3] + v * Fyb[3];
+  const double pb = Fxb[1] + u * Fxb[3] + Fyb[2] + v * Fyb[3];
+  // p = gm1 (E - (m^2 + n^2) / (2 rho))
+  double rhob = g.gm1 * 0.5 * (u * u + v * v) * pb;
+  mb -= g.gm1 * u * pb;
+  nb -= g.gm1 * v * pb;
+  Eb += g.gm1 * pb;
+  // u = m / rho, v = n / rho
+  mb += ub * oorho;
+  nb += vb * oorho;
+  rhob -= (u * ub + v * vb) * oorho;
+  qb[0] += rhob;
+  qb[1] += mb;
+  qb[2] += nb;
+  qb[3] += Eb;
+}
+
+// Static pressure (fluids.go:422-453) in reverse.
+__device__ __forceinline__ void pressure_vjp(const Gas<double>& g, const double q[4], double pb, double qb[4]) {
+  const double oorho = 1.0 / q[0];
+  const double u = q[1] * oorho, v = q[2] * oorho;
+  qb[0] += g.gm1 * 0.5 * (u * u + v * v) * pb;
+  qb[1] -= g.gm1 * u * pb;
+  qb[2] -= g.gm1 * v * pb;
+  qb[3] += g.gm1 * pb;
+}
+
+__device__ __forceinline__ double sgn(double x) { return x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : 0.0); }
+
+// RoeFlux (fluxes.go:284-413) in reverse: QLb, QRb += (df/dQL)^T fb, (df/dQR)^T fb.
+__device__ __forceinline__ void roe_vjp(const Gas<double>& g, const double QL[4], const double QR[4], double nx,
+                                        double ny, const double fbo[4], double QLb[4], double QRb[4]) {
+  // forward
+  const double rhoULr = QL[1] * nx + QL[2] * ny, rhoVLr = -QL[1] * ny + QL[2] * nx;
+  const double rhoURr = QR[1] * nx + QR[2] * ny, rhoVRr = -QR[1] * ny + QR[2] * nx;
+  const double rhoL = QL[0], uL = rhoULr / QL[0], vL = rhoVLr / QL[0];
+  const double rhoR = QR[0], uR = rhoURr / QR[0], vR = rhoVRr / QR[0];
+  const double pL = pressure(g, QL[0], QL[1], QL[2], QL[3]);
+  const double pR = pressure(g, QR[0], QR[1], QR[2], QR[3]);
+  const double hL = (QL[3] + pL) / rhoL, hR = (QR[3] + pR) / rhoR;
+  const double rhoLs = sqrt(rhoL), rhoRs = sqrt(rhoR);
+  const double S = rhoLs + rhoRs;
+  const double rho = rhoLs * rhoRs;
+  const double u = (rhoLs * uL + rhoRs * uR) / S;
+  const double v = (rhoLs * vL + rhoRs * vR) / S;
+  const double h = (rhoLs * hL + rhoRs * hR) / S;
+  const double c2 = g.gm1 * (h - 0.5 * (u * u + v * v));
+  const double C = sqrt(c2);
+  const double du = uR - uL, dp = pR - pL;
+  const double a1 = -0.5 * (rho * du) / C + 0.5 * dp / c2;
+  const double a2 = (rhoR - rhoL) - dp / c2;
+  const double a3 = rho * (vR - vL);
+  const double a4 = 0.5 * (rho * du) / C + 0.5 * dp / c2;
+  const double l1 = fabs(u - C), l2 = fabs(u), l4 = fabs(u + C);
+  const double W1 = l1 * a1, W2 = l2 * a2, W3 = l2 * a3, W4 = l4 * a4;
+  // output rotation: out0 = f0, out1 = nx f1 - ny f2, out2 = ny f1 + nx f2, out3 = f3
+  const double f0b = fbo[0], f1b = nx * fbo[1] + ny * fbo[2], f2b = -ny * fbo[1] + nx * fbo[2], f3b = fbo[3];
+  double rhoULrb = 0.5 * f0b + 0.5 * uL * f1b;
+  double rhoURrb = 0.5 * f0b + 0.5 * uR * f1b;
+  double rhoVLrb = 0.5 * uL * f2b;
+  double rhoVRrb = 0.5 * uR * f2b;
+  double uLb = 0.5 * rhoULr * f1b + 0.5 * rhoVLr * f2b + 0.5 * (pL + QL[3]) * f3b;
+  double uRb = 0.5 * rhoURr * f1b + 0.5 * rhoVRr * f2b + 0.5 * (pR + QR[3]) * f3b;
+  double vLb = 0.0, vRb = 0.0;
+  double pLb = 0.5 * f1b + 0.5 * uL * f3b;
+  double pRb = 0.5 * f1b + 0.5 * uR * f3b;
+  double QL3b = 0.5 * uL * f3b, QR3b = 0.5 * uR * f3b;
+  // dissipation terms: f0 -= T0/2, f1 -= T1/2, f2 -= T2/2, f3 -= T3/2
+  const double T0b = -0.5 * f0b, T1b = -0.5 * f1b, T2b = -0.5 * f2b, T3b = -0.5 * f3b;
+  const double W1b = T0b + (u - C) * T1b + v * T2b + (h - u * C) * T3b;
+  const double W2b = T0b + u * T1b + v * T2b + 0.5 * (u * u + v * v) * T3b;
+  const double W3b = T2b + v * T3b;
+  const double W4b = T0b + (u + C) * T1b + v * T2b + (h + u * C) * T3b;
+  double ub = (W1 + W2 + W4) * T1b + (-W1 * C + W2 * u + W4 * C) * T3b;
+  double vb = (W1 + W2 + W4) * T2b + (W2 * v + W3) * T3b;
+  double hb = (W1 + W4) * T3b;
+  double Cb = (-W1 + W4) * T1b + (-W1 * u + W4 * u) * T3b;
+  // W = l * a
+  const double a1b = l1 * W1b, a2b = l2 * W2b, a3b = l2 * W3b, a4b = l4 * W4b;
+  const double l1b = a1 * W1b, l2b = a2 * W2b + a3 * W3b, l4b = a4 * W4b;
+  const double s1 = sgn(u - C), s2 = sgn(u), s4 = sgn(u + C);
+  ub += s1 * l1b + s2 * l2b + s4 * l4b;
+  Cb += -s1 * l1b + s4 * l4b;
+  // a1..a4
+  double rhob = (-0.5 * du / C) * a1b + (vR - vL) * a3b + (0.5 * du / C) * a4b;
+  double dub = (-0.5 * rho / C) * a1b + (0.5 * rho / C) * a4b;
+  Cb += (0.5 * rho * du / (C * C)) * a1b - (0.5 * rho * du / (C * C)) * a4b;
+  double dpb = (0.5 / c2) * a1b - a2b / c2 + (0.5 / c2) * a4b;
+  double c2b = (-0.5 * dp / (c2 * c2)) * a1b + (dp / (c2 * c2)) * a2b - (0.5 * dp / (c2 * c2)) * a4b;
+  double rhoRb = a2b, rhoLb = -a2b;
+  vRb += rho * a3b;
+  vLb -= rho * a3b;
+  uRb += dub;
+  uLb -= dub;
+  pRb += dpb;
+  pLb -= dpb;
+  // C = sqrt(c2); c2 = gm1 (h - (u^2 + v^2) / 2)
+  c2b += Cb * 0.5 / C;
+  hb += g.gm1 * c2b;
+  ub -= g.gm1 * u * c2b;
+  vb -= g.gm1 * v * c2b;
+  // Roe averages
+  const double oS = 1.0 / S;
+  uLb += rhoLs * oS * ub;
+  uRb += rhoRs * oS * ub;
+  vLb += rhoLs * oS * vb;
+  vRb += rhoRs * oS * vb;
+  const double hLb = rhoLs * oS * hb, hRb = rhoRs * oS * hb;
+  double rhoLsb = ((uL - u) * ub + (vL - v) * vb + (hL - h) * hb) * oS + rhoRs * rhob;
+  double rhoRsb = ((uR - u) * ub + (vR - v) * vb + (hR - h) * hb) * oS + rhoLs * rhob;
+  rhoLb += 0.5 / rhoLs * rhoLsb;
+  rhoRb += 0.5 / rhoRs * rhoRsb;
+  // h = (E + p) / rho
+  QL3b += hLb / rhoL;
+  pLb += hLb / rhoL;
+  rhoLb -= hL / rhoL * hLb;
+  QR3b += hRb / rhoR;
+  pRb += hRb / rhoR;
+  rhoRb -= hR / rhoR * hRb;
+  // rotated velocities
+  rhoULrb += uLb / QL[0];
+  rhoVLrb += vLb / QL[0];
+  rhoLb -= (uL * uLb + vL * vLb) / QL[0];
+  rhoURrb += uRb / QR[0];
+  rhoVRrb += vRb / QR[0];
+  rhoRb -= (uR * uRb + vR * vRb) / QR[0];
+  QLb[0] += rhoLb;
+  QRb[0] += rhoRb;
+  QLb[3] += QL3b;
+  QRb[3] += QR3b;
+  QLb[1] += nx * rhoULrb - ny * rhoVLrb;
+  QLb[2] += ny * rhoULrb + nx * rhoVLrb;
+  QRb[1] += nx * rhoURrb - ny * rhoVRrb;
+  QRb[2] += ny * rhoURrb + nx * rhoVRrb;
+  pressure_vjp(g, QL, pLb, QLb);
+  pressure_vjp(g, QR, pRb, QRb);
+}
+
+// Any interior flux by forward-mode duals (8 tangents: QL then QR).
+__device__ __noinline__ void riemann_vjp_dual(int kind, const Gas<double>& g, const double QL[4], const double QR[4],
+                                              double nx, double ny, const double fb[4], double QLb[4],
+                                              double QRb[4]) {
+  using D = Dual<8>;
+  D qL[4], qR[4], f[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    qL[i] = seed<8>(QL[i], i);
+    qR[i] = seed<8>(QR[i], 4 + i);
+  }
+  riemann_flux<D>(kind, dual_gas<8>(g), qL, qR, D(nx), D(ny), f);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    double sl = 0.0, sr = 0.0;
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      sl += fb[n] * f[n].d[j];
+      sr += fb[n] * f[n].d[4 + j];
+    }
+    QLb[j] += sl;
+    QRb[j] += sr;
+  }
+}
+
+// Edge-point wave speed oohK (|u| + c) (StoreEdgeAggregates, edges.go:274-286) in reverse.
+__device__ __forceinline__ void wave_speed_vjp(const Gas<double>& g, double oohK, const double q[4], double wb,
+                                               double qb[4]) {
+  using D = Dual<4>;
+  D d[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) d[i] = seed<4>(q[i], i);
+  const Gas<D> gd = dual_gas<4>(g);
+  const D ws = D(oohK) * (speed(d[0], d[1], d[2]) + sound_speed(gd, d[0], d[1], d[2], d[3]));
+#pragma unroll
+  for (int i = 0; i < 4; ++i) qb[i] += wb * ws.d[i];
+}
+
+// One boundary edge point by duals (tangents: interior face state 0..3, the
+// far-field Qinf 4..7 with its derived pinf / cinf, solver time 8): the
+// boundary flux n.F(qb) (or the wall pressure flux) and the wave speed of qb.
+// bp indexes the boundary flux-point coordinates (boundary edge * NpEdge + point).
+template <typename T>
+__device__ __forceinline__ void bc_point(const EdgeArgs<double>& a, int flag, int bp, const T qi[4], T nx, T ny,
+                                         const FreeStreamT<T>& far, const FreeStreamT<T>& in,
+                                         const FreeStreamT<T>& out, T t, T oohK, T f[4], T& ws) {
+  const Gas<T> g{T(a.gas.gamma), T(a.gas.gm1), T(a.gas.oogm1)};
+  T qb[4];
+  bool wall = false;
+  switch (flag) {
+    case 4: riemann_bc(far, qi, far.qinf, nx, ny, qb); break;
+    case 1: riemann_bc(in, qi, in.qinf, nx, ny, qb); break;
+    case 8: riemann_bc(out, qi, out.qinf, nx, ny, qb); break;
+    case 9: {
+      T ex[4];
+      ivortex_state(T(a.vbeta), T(a.vx0), T(a.vy0), T(a.vgamma), t, T(a.bx[bp]), T(a.by[bp]), ex);
+      riemann_bc(far, qi, ex, nx, ny, qb);
+      break;
+    }
+    case 5:
+    case 6:
+      wall = true;
+#pragma unroll
+      for (int n = 0; n < 4; ++n) qb[n] = qi[n];
+      break;
+    default:
+#pragma unroll
+      for (int n = 0; n < 4; ++n) qb[n] = qi[n];
+  }
+  if (wall) {
+    const T pw = pressure(g, qi[0], qi[1], qi[2], qi[3]);
+    f[0] = T(0.0); f[1] = nx * pw; f[2] = ny * pw; f[3] = T(0.0);
+  } else {
+    T Fx[4], Fy[4];
+    euler_flux(g, qb, Fx, Fy);
+#pragma unroll
+    for (int n = 0; n < 4; ++n) f[n] = nx * Fx[n] + ny * Fy[n];
+  }
+  ws = oohK * (speed(qb[0], qb[1], qb[2]) + sound_speed(g, qb[0], qb[1], qb[2], qb[3]));
+}
+
+// Reverse of bc_point: qib += J^T (fb, wsb); qinfb (4) and tb get the far-field and time parts.
+__device__ __noinline__ void bc_point_vjp(const EdgeArgs<double>& a, int flag, int bp, const double qi[4],
+                                          double nx, double ny, double t, double oohK, const double fb[4], double wsb,
+                                          double qib[4], double qinfb[4], double* tb) {
+  using D = Dual<9>;
+  D q[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) q[i] = seed<9>(qi[i], i);
+  FreeStreamT<D> far, in, out;
+  const Gas<D> gd = dual_gas<9>(a.gas);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    far.qinf[i] = seed<9>(a.fsFar.qinf[i], 4 + i);
+    in.qinf[i] = D(a.fsIn.qinf[i]);
+    out.qinf[i] = D(a.fsOut.qinf[i]);
+  }
+  // pinf, cinf follow Qinf (FreeStream, fluids.go:370-406); values kept bit-equal to the forward's
+  far.pinf = pressure(gd, far.qinf[0], far.qinf[1], far.qinf[2], far.qinf[3]);
+  far.cinf = sound_speed(gd, far.qinf[0], far.qinf[1], far.qinf[2], far.qinf[3]);
+  far.pinf.v = a.fsFar.pinf;
+  far.cinf.v = a.fsFar.cinf;
+  far.gamma = D(a.fsFar.gamma);
+  far.minf = D(a.fsFar.minf);
+  in.pinf = D(a.fsIn.pinf); in.cinf = D(a.fsIn.cinf); in.gamma = D(a.fsIn.gamma); in.minf = D(a.fsIn.minf);
+  out.pinf = D(a.fsOut.pinf); out.cinf = D(a.fsOut.cinf); out.gamma = D(a.fsOut.gamma); out.minf = D(a.fsOut.minf);
+  D f[4], ws;
+  bc_point<D>(a, flag, bp, q, D(nx), D(ny), far, in, out, seed<9>(t, 8), D(oohK), f, ws);
+#pragma unroll
+  for (int j = 0; j < 9; ++j) {
+    double s = wsb * ws.d[j];
+#pragma unroll
+    for (int n = 0; n < 4; ++n) s += fb[n] * f[n].d[j];
+    if (j < 4) qib[j] += s;
+    else if (j < 8) qinfb[j - 4] += s;
+    else *tb += s;
+  }
+}
+
+struct AdjArgs {
+  int K, stage, localDT;
+  const double* Qs;     // stage state
+  const double* Qbn;    // adjoint of the stage output (stage -1: the RHS adjoint)
+  const double* rhs;    // taped RHS of this stage
+  const double* rhs3;   // taped RHS of stage 3 (stage 4)
+  double* Qb0;          // adjoint of the step's initial state (accumulated)
+  double* Qbs;          // adjoint of this stage's state (accumulated)
+  double* Qb2;          // stage 4 feeds the stage-2 and stage-3 states directly
+  double* Qb3;
+  double* Rb3;          // W3 dt4 Qbar_final, stage 4 -> stage 3
+  const double* dtS;    // taped global dt per stage [5]
+  const double* dtK;    // taped local dt of this stage [K]
+  double* dtbarG;       // [5] global dt adjoints
+  double* dtOwnK;       // [K] local dt adjoint of this stage
+  const double* DivInt;
+  const double* Jdet;
+  const double* Jinv;
+  double* FEb;          // [n][3NE][K]
+  Gas<double> gas;
+};
+
+// Forward stage coefficients (rkAdvance, euler.go:460-566): stage s < 4 forms
+// Q_{s+1} = alpha Q0 + beta Q_s + gamma dt RHS_s; stage 4 forms
+// Q_final = A2 Q2 + A3 Q3 + A4 Q4 + W3 dt4 RHS_3 + C4 dt4 RHS_4.
+__device__ __forceinline__ void stage_coeffs(int s, double& alpha, double& beta, double& gamma) {
+  switch (s) {
+    case 0: alpha = 1.0; beta = 0.0; gamma = kSSP[0][0]; break;
+    case 1: alpha = kSSP[1][0]; beta = kSSP[1][1]; gamma = kSSP[1][2]; break;
+    case 2: alpha = kSSP[2][0]; beta = kSSP[2][1]; gamma = kSSP[2][2]; break;
+    default: alpha = kSSP[3][0]; beta = kSSP[3][1]; gamma = kSSP[3][2]; break;
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(128) k_adj_div(AdjArgs a) {
+  constexpr int NP = Dims<N>::NP, NE3 = Dims<N>::NE3, NF = Dims<N>::NF;
+  __shared__ double sD[NP * NF];
+  stage_operator(sD, a.DivInt, NP * NF);
+  __syncthreads();
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = k < a.K;
+  const size_t sK = static_cast<size_t>(a.K);
+  const int s = a.stage;
+  double dtb = 0.0;
+  if (active) {
+    double Rb[4][NP];
+    if (s < 0) {
+#pragma unroll
+      for (int n = 0; n < 4; ++n)
+#pragma unroll
+        for (int r = 0; r < NP; ++r) Rb[n][r] = a.Qbn[(n * NP + r) * sK + k];
+    } else if (s == 4) {
+      const double dt4 = a.localDT ? a.dtK[k] : a.dtS[4];
+      const double A2 = kSSP[4][0], A3 = kSSP[4][1], A4 = kSSP[4][2], W3 = kSSP[4][3], C4 = kSSP[4][4];
+#pragma unroll
+      for (int n = 0; n < 4; ++n)
+#pragma unroll
+        for (int r = 0; r < NP; ++r) {
+          const size_t ind = (n * NP + r) * sK + k;
+          const double qb = a.Qbn[ind];
+          Rb[n][r] = C4 * dt4 * qb;
+          a.Rb3[ind] = W3 * dt4 * qb;
+          dtb += qb * (W3 * a.rhs3[ind] + C4 * a.rhs[ind]);
+          a.Qb2[ind] += A2 * qb;
+          a.Qb3[ind] += A3 * qb;
+          a.Qbs[ind] = A4 * qb;
+        }
+    } else {
+      double al, be, ga;
+      stage_coeffs(s, al, be, ga);
+      const double dt = a.localDT ? a.dtK[k] : a.dtS[s];
+#pragma unroll
+      for (int n = 0; n < 4; ++n)
+#pragma unroll
+        for (int r = 0; r < NP; ++r) {
+          const size_t ind = (n * NP + r) * sK + k;
+          const double qb = a.Qbn[ind];
+          Rb[n][r] = ga * dt * qb + (s == 3 ? a.Rb3[ind] : 0.0);
+          dtb += ga * qb * a.rhs[ind];
+          a.Qb0[ind] += al * qb;
+          if (be != 0.0) a.Qbs[ind] += be * qb;
+        }
+    }
+    // RHS = -(1/J) DivInt . DOF  =>  DOFb = -(1/J) DivInt^T Rb
+    const double Jd = a.Jdet[k], mooj = -(1.0 / Jd);
+    const double J0 = a.Jinv[k], J1 = a.Jinv[sK + k], J2 = a.Jinv[2 * sK + k], J3 = a.Jinv[3 * sK + k];
+#pragma unroll 1
+    for (int i = 0; i < NP; ++i) {
+      double Fxb[4], Fyb[4], q[4], qb[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+        double fr = 0.0, fs = 0.0;
+#pragma unroll
+        for (int r = 0; r < NP; ++r) {
+          fr += sD[r * NF + i] * Rb[n][r];
+          fs += sD[r * NF + NP + i] * Rb[n][r];
+        }
+        fr *= mooj;
+        fs *= mooj;
+        Fxb[n] = Jd * (J0 * fr + J2 * fs);
+        Fyb[n] = Jd * (J1 * fr + J3 * fs);
+        q[n] = a.Qs[(n * NP + i) * sK + k];
+      }
+      euler_flux_vjp(a.gas, q, Fxb, Fyb, qb);
+#pragma unroll
+      for (int n = 0; n < 4; ++n) a.Qbs[(n * NP + i) * sK + k] += qb[n];
+    }
+#pragma unroll 1
+    for (int j = 0; j < NE3; ++j) {
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+        double d = 0.0;
+#pragma unroll
+        for (int r = 0; r < NP; ++r) d += sD[r * NF + 2 * NP + j] * Rb[n][r];
+        a.FEb[(n * NE3 + j) * sK + k] = mooj * d;
+      }
+    }
+    if (s >= 0 && a.localDT) a.dtOwnK[k] = dtb;
+  }
+  if (s >= 0 && !a.localDT) {
+    const double t = warp_sum(active ? dtb : 0.0);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&a.dtbarG[s], t);
+  }
+}
+
+struct AdjEdgeArgs {
+  double* FEb;     // [n][3NE][K] edge DOF adjoints (from k_adj_div)
+  double* QFb;     // [n][3NE][K] face adjoints (written here)
+  double* qinfb;   // [4] far-field Qinf adjoint
+  double* tb;      // solver-time adjoint
+  double* esBar;   // per edge: adjoint of the edge's max wave speed
+  int useManualRoe;
+};
+
+template <int N>
+__global__ void __launch_bounds__(128) k_adj_edge(EdgeArgs<double> a, AdjEdgeArgs x) {
+  constexpr int NE = Dims<N>::NE, NE3 = Dims<N>::NE3;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.nInt + a.nBC) return;
+  const size_t sK = static_cast<size_t>(a.K);
+  const int kL = a.kL[e];
+  const int eL = a.eLR[e] & 3;
+  const double nx = a.nx[e], ny = a.ny[e];
+  const double IIL = a.IIL[e];
+  if (e < a.nInt) {
+    const int kR = a.kR[e];
+    const int eR = a.eLR[e] >> 2;
+    const double IIR = a.IIR[e];
+#pragma unroll 1
+    for (int p = 0; p < NE; ++p) {
+      const int jL = eL * NE + p, jR = eR * NE + (NE - 1 - p);
+      double qL[4], qR[4], fb[4], qLb[4] = {0.0, 0.0, 0.0, 0.0}, qRb[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+        qL[n] = a.QF[(n * NE3 + jL) * sK + kL];
+        qR[n] = a.QF[(n * NE3 + jR) * sK + kR];
+        fb[n] = IIL * x.FEb[(n * NE3 + jL) * sK + kL] - IIR * x.FEb[(n * NE3 + jR) * sK + kR];
+      }
+      if (a.flux == kFluxRoe && x.useManualRoe)
+        roe_vjp(a.gas, qL, qR, nx, ny, fb, qLb, qRb);
+      else
+        riemann_vjp_dual(a.flux, a.gas, qL, qR, nx, ny, fb, qLb, qRb);
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+        x.QFb[(n * NE3 + jL) * sK + kL] = qLb[n];
+        x.QFb[(n * NE3 + jR) * sK + kR] = qRb[n];
+      }
+    }
+  } else {
+    const int b = e - a.nInt;
+    const int flag = a.bcFlag[b];
+    const double t = *a.time;
+    double qinfb[4] = {0.0, 0.0, 0.0, 0.0}, tb = 0.0;
+#pragma unroll 1
+    for (int p = 0; p < NE; ++p) {
+      const int jL = eL * NE + p;
+      double qi[4], fb[4], qib[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+        qi[n] = a.QF[(n * NE3 + jL) * sK + kL];
+        fb[n] = IIL * x.FEb[(n * NE3 + jL) * sK + kL];
+      }
+      bc_point_vjp(a, flag, b * NE + p, qi, nx, ny, t, a.oohK[e], fb, 0.0, qib, qinfb, &tb);
+#pragma unroll
+      for (int n = 0; n < 4; ++n) x.QFb[(n * NE3 + jL) * sK + kL] = qib[n];
+    }
+#pragma unroll
+    for (int n = 0; n < 4; ++n)
+      if (qinfb[n] != 0.0) atomicAdd(&x.qinfb[n], qinfb[n]);
+    if (tb != 0.0) atomicAdd(x.tb, tb);
+  }
+}
+
+// Global dt: the edge that set this stage's max wave speed.
+__global__ void k_adj_argmax(const double* edgeSpeed, const double* gmaxS, int stage, int nEdges, int* argEdge) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < nEdges && edgeSpeed[g] == gmaxS[stage]) atomicMin(argEdge, g);
+}
+
+struct AdjDtArgs {
+  int K, stage, nEdges;
+  double cfl, finalTime;
+  const double* gmaxS;     // taped per-stage max wave speed [5]
+  const double* tn;        // taped step start time
+  const double* dtbarG;    // [5]
+  const double* tbarNext;  // adjoint of the step's end time (stage 4 only)
+  double* tbarCur;         // adjoint of the step's start time
+  const int* argEdge;
+  double* esBar;           // per edge
+  // local dt
+  const double* dtPrev;    // taped local dt of stage s-1 [K] (stage > 0)
+  const double* edgeSpeed; // taped edge speeds of this stage
+  const int* elemEdge;     // [3][K]
+  const double* dtOwnK;
+  double* carry;           // [K]: adjoint carried to the previous stage's dt
+};
+
+// Global: dt = min-clip(CFL / gmax) (calculateGlobalDT, euler.go:945-971).
+__global__ void k_adj_gsel(AdjDtArgs a) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int s = a.stage;
+  double dtb = a.dtbarG[s];
+  if (s == 4) dtb += *a.tbarNext;  // Time += GlobalDT of the last stage
+  const double gm = a.gmaxS[s];
+  const double dtU = a.cfl / gm;
+  if (*a.tn + dtU > a.finalTime) {
+    *a.tbarCur -= dtb;  // dt = FinalTime - t
+  } else {
+    const int g = *a.argEdge;
+    if (g >= 0 && g < a.nEdges) a.esBar[g] += -a.cfl / (gm * gm) * dtb;
+  }
+}
+
+// Local: DT_k = CFL / max(DT_k(prev stage) or -100 at stage 0, edge speeds)
+// (CalculateLocalDT, euler.go:973-1002).
+__global__ void k_adj_lts(AdjDtArgs a) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.K) return;
+  const size_t sK = static_cast<size_t>(a.K);
+  const int s = a.stage;
+  double v = (s == 0) ? -100.0 : a.dtPrev[k];
+  int arg = -1;
+  int eg[3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    eg[e] = a.elemEdge[e * sK + k];
+    const double w = a.edgeSpeed[eg[e]];
+    if (w > v) { v = w; arg = e; }
+  }
+  const double dtb = a.dtOwnK[k] + a.carry[k];
+  const double vb = -a.cfl / (v * v) * dtb;
+  if (arg < 0) {
+    a.carry[k] = (s == 0) ? 0.0 : vb;
+  } else {
+    a.carry[k] = 0.0;
+    atomicAdd(&a.esBar[eg[arg]], vb);
+  }
+}
+
+// esBar[g] onto the face state at the edge's max wave-speed point.
+template <int N>
+__global__ void __launch_bounds__(128) k_adj_speed(EdgeArgs<double> a, AdjEdgeArgs x) {
+  constexpr int NE = Dims<N>::NE, NE3 = Dims<N>::NE3;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.nInt + a.nBC) return;
+  const double wbar = x.esBar[e];
+  if (wbar == 0.0) return;
+  const size_t sK = static_cast<size_t>(a.K);
+  const int kL = a.kL[e];
+  const int eL = a.eLR[e] & 3;
+  const double nx = a.nx[e], ny = a.ny[e];
+  const double oohK = a.oohK[e];
+  const bool bc = e >= a.nInt;
+  const int b = e - a.nInt;
+  const int flag = bc ? a.bcFlag[b] : 0;
+  const double t = *a.time;
+  // the point the forward max picked: first strict increase (dmax(smax, ws) from -1)
+  double best = -1.0;
+  int pb = 0;
+  for (int p = 0; p < NE; ++p) {
+    const int jL = eL * NE + p;
+    double qi[4];
+#pragma unroll
+    for (int n = 0; n < 4; ++n) qi[n] = a.QF[(n * NE3 + jL) * sK + kL];
+    double ws;
+    if (bc) {
+      double f[4];
+      bc_point<double>(a, flag, b * NE + p, qi, nx, ny, a.fsFar, a.fsIn, a.fsOut, t, oohK, f, ws);
+    } else {
+      ws = oohK * (speed(qi[0], qi[1], qi[2]) + sound_speed(a.gas, qi[0], qi[1], qi[2], qi[3]));
+    }
+    if (ws > best) { best = ws; pb = p; }
+  }
+  const int jL = eL * NE + pb;
+  double qi[4], qib[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+  for (int n = 0; n < 4; ++n) qi[n] = a.QF[(n * NE3 + jL) * sK + kL];
+  if (bc) {
+    double qinfb[4] = {0.0, 0.0, 0.0, 0.0}, tb = 0.0;
+    const double fb[4] = {0.0, 0.0, 0.0, 0.0};
+    bc_point_vjp(a, flag, b * NE + pb, qi, nx, ny, t, oohK, fb, wbar, qib, qinfb, &tb);
+#pragma unroll
+    for (int n = 0; n < 4; ++n)
+      if (qinfb[n] != 0.0) atomicAdd(&x.qinfb[n], qinfb[n]);
+    if (tb != 0.0) atomicAdd(x.tb, tb);
+  } else {
+    wave_speed_vjp(a.gas, oohK, qi, wbar, qib);
+  }
+#pragma unroll
+  for (int n = 0; n < 4; ++n) x.QFb[(n * NE3 + jL) * sK + kL] += qib[n];
+}
+
+// Qbs += FluxEdgeInterp^T QFb, one thread per (variable, element).
+template <int N>
+__global__ void __launch_bounds__(128) k_adj_interp(const double* QFb, const double* Iop, double* Qbs, int K) {
+  constexpr int NP = Dims<N>::NP, NE3 = Dims<N>::NE3;
+  __shared__ double sI[NE3 * NP];
+  stage_operator(sI, Iop, NE3 * NP);
+  __syncthreads();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 4 * K) return;
+  const int n = t / K, k = t - n * K;
+  const size_t sK = static_cast<size_t>(K);
+  double f[NE3];
+#pragma unroll
+  for (int j = 0; j < NE3; ++j) f[j] = QFb[(n * NE3 + j) * sK + k];
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 0; j < NE3; ++j) acc += sI[j * NP + i] * f[j];
+    Qbs[(n * NP + i) * sK + k] += acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Functionals of the state, with their gradients.
+
+// Pressure force on Wall / Cyl boundary edges, sum over edges of
+// |edge| sum_p w_p p(q_p) n_x (or n_y): the integrated wall pressure force of
+// the wall dump in OutputFinal (euler.go:251-316), with the face states at the
+// edge's flux points and the interpolatory weights of those points.
+template <int N>
+__global__ void __launch_bounds__(128) k_func_wall(EdgeArgs<double> a, const double* w, int ycomp, double* QFb,
+                                                   double* J) {
+  constexpr int NE = Dims<N>::NE, NE3 = Dims<N>::NE3;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  double jl = 0.0;
+  if (b < a.nBC) {
+    const int flag = a.bcFlag[b];
+    if (flag == 5 || flag == 6) {
+      const int e = a.nInt + b;
+      const size_t sK = static_cast<size_t>(a.K);
+      const int kL = a.kL[e];
+      const int eL = a.eLR[e] & 3;
+      const double nc = ycomp ? a.ny[e] : a.nx[e];
+      const double len = a.IIL[e] * (eL == 1 ? 2.0 * sqrt(2.0) : 2.0);
+      for (int p = 0; p < NE; ++p) {
+        const int jL = eL * NE + p;
+        double q[4], qb[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int n = 0; n < 4; ++n) q[n] = a.QF[(n * NE3 + jL) * sK + kL];
+        const double c = len * w[p] * nc;
+        jl += c * pressure(a.gas, q[0], q[1], q[2], q[3]);
+        pressure_vjp(a.gas, q, c, qb);
+#pragma unroll
+        for (int n = 0; n < 4; ++n) QFb[(n * NE3 + jL) * sK + kL] += qb[n];
+      }
+    }
+  }
+  jl = warp_sum(jl);
+  if ((threadIdx.x & 31) == 0 && jl != 0.0) atomicAdd(J, jl);
+}
+
+// Squared error against the exact isentropic vortex at the solver time,
+// sum over solution points and variables of (Q - Q_exact(t))^2
+// (IVortex.GetStateC, isentropic_vortex/analytic_vortex.go:31-82).
+template <int N>
+__global__ void __launch_bounds__(128) k_func_vortex(const double* Q, const double* X, const double* Y, int K,
+                                                     double beta, double x0, double y0, double gamma,
+                                                     const double* time, double* Qb, double* J, double* tb) {
+  constexpr int NP = Dims<N>::NP;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  double jl = 0.0, tl = 0.0;
+  if (k < K) {
+    const size_t sK = static_cast<size_t>(K);
+    const Dual<1> t = seed<1>(*time, 0);
+    for (int i = 0; i < NP; ++i) {
+      const size_t pt = static_cast<size_t>(i) * sK + k;
+      Dual<1> ex[4];
+      ivortex_state(Dual<1>(beta), Dual<1>(x0), Dual<1>(y0), Dual<1>(gamma), t, Dual<1>(X[pt]), Dual<1>(Y[pt]), ex);
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+        const size_t ind = (n * NP + i) * sK + k;
+        const double d = Q[ind] - ex[n].v;
+        jl += d * d;
+        Qb[ind] = 2.0 * d;
+        tl -= 2.0 * d * ex[n].d[0];
+      }
+    }
+  }
+  jl = warp_sum(jl);
+  tl = warp_sum(tl);
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(J, jl);
+    atomicAdd(tb, tl);
+  }
+}
+
+}  // namespace gcfd

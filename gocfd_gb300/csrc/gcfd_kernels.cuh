@@ -275,6 +275,7 @@ struct UpdateArgs {
   const unsigned long long* gvisc;  // per stage
   double* DTVisc;            // K, persistent (CalcElementMaxWaveSpeed never resets it)
   double cdiff;              // 1/(N+1)^2
+  double* tapeRHS;           // when set, the stage's RHS is stored there (adjoint tape)
 };
 
 __constant__ double kSSP[5][6] = {
@@ -410,9 +411,11 @@ __global__ void __launch_bounds__(128) k_div_update(UpdateArgs<T> a) {
 #pragma unroll
       for (int n = 0; n < 4; ++n)
 #pragma unroll
-        for (int r = 0; r < NP; ++r)
+        for (int r = 0; r < NP; ++r) {
+          if (a.tapeRHS) a.tapeRHS[(n * NP + r) * sK + k] = static_cast<double>(acc[n][r]);
           ssp_stage_update(a, (n * NP + r) * sK + k, static_cast<double>(acc[n][r]), dtk, rloc_max[n],
                            rloc_abs[n], rloc_s2[n]);
+        }
     }
   }
   if (a.stage == 4) residual_reduce(a.sc, rloc_max, rloc_abs, rloc_s2);

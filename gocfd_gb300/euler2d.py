@@ -267,6 +267,49 @@ class Euler:
     def rhs_global(self, Qg: np.ndarray, time: float = 0.0) -> np.ndarray:
         return self.unshard(self.rhs(self.shard(np.asarray(Qg, dtype=np.float64)), time))
 
+    # -- adjoint (FP64 path) --------------------------------------------------------------
+    FUNCTIONALS = {"wall_force_x": 0, "wall_force_y": 1, "vortex_error": 2}
+
+    def functional(self, kind: str):
+        """(J, dJ/dQ as a global 4 x Np x K array, dJ/dtime) of the current state."""
+        J, tb = C.c_double(), C.c_double()
+        out = self.new_sharded()
+        km = self._kmax()
+        _lib.check(self.lib, self.ctx, self.lib.gcfd_functional(self.ctx, self.FUNCTIONALS[kind], C.byref(J), len(km),
+                                                               km.ctypes.data_as(_lib.PI), self._ptrs(out),
+                                                               C.byref(tb)))
+        return J.value, self.unshard(out), tb.value
+
+    def rhs_vjp_global(self, Qg: np.ndarray, Rbar: np.ndarray, time: float = 0.0):
+        """(dRHS/dQ)^T Rbar at (Qg, time); returns (Qbar, Qinf_bar[4], time_bar)."""
+        out = self.new_sharded()
+        km = self._kmax()
+        qinf, tb = (C.c_double * 4)(), C.c_double()
+        _lib.check(self.lib, self.ctx, self.lib.gcfd_rhs_vjp(
+            self.ctx, float(time), len(km), km.ctypes.data_as(_lib.PI),
+            self._ptrs(self.shard(np.asarray(Qg, dtype=np.float64))),
+            self._ptrs(self.shard(np.asarray(Rbar, dtype=np.float64))), self._ptrs(out), qinf, C.byref(tb)))
+        return self.unshard(out), np.array(qinf[:]), tb.value
+
+    def record(self, nsteps: int, checkpoint_every: int = 1):
+        """Advance nsteps keeping checkpoints for step_vjp; returns (time, dt_last)."""
+        t, dt = C.c_double(), C.c_double()
+        _lib.check(self.lib, self.ctx, self.lib.gcfd_record_steps(self.ctx, int(nsteps), int(checkpoint_every),
+                                                                 C.byref(t), C.byref(dt)))
+        self.steps += nsteps
+        return t.value, dt.value
+
+    def step_vjp(self, Qbar_final: np.ndarray, tbar_final: float = 0.0):
+        """Adjoint of the recorded window: (Q0_bar, Qinf_bar[4], t0_bar)."""
+        out = self.new_sharded()
+        km = self._kmax()
+        qinf, tb = (C.c_double * 4)(), C.c_double()
+        _lib.check(self.lib, self.ctx, self.lib.gcfd_step_vjp(
+            self.ctx, len(km), km.ctypes.data_as(_lib.PI),
+            self._ptrs(self.shard(np.asarray(Qbar_final, dtype=np.float64))), float(tbar_final),
+            self._ptrs(out), qinf, C.byref(tb)))
+        return self.unshard(out), np.array(qinf[:]), tb.value
+
     def step(self, nsteps: int = 1):
         """Advance nsteps; returns dict(time, dt, resid_max, resid_absmax, resid_rms)."""
         t, dt = C.c_double(), C.c_double()

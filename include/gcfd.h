@@ -150,6 +150,50 @@ int gcfd_profile_step(gcfd_ctx* ctx, double* kernel_ms4, int32_t* launches4);
  * 5 flux-point r,s (NpFlux x 2).  With out == NULL only rows/cols are set. */
 int gcfd_host_operator(int32_t N, int32_t which, double* out, int32_t* rows, int32_t* cols);
 
+/* ---- Adjoint (vector-Jacobian products), FP64 path without PerssonC0 ----
+ * The reference has no adjoint; these transpose its discrete RHS and step
+ * exactly, including the time step's dependence on the state (the global max
+ * wave speed of calculateGlobalDT, euler.go:945-971, with the FinalTime clip;
+ * the running max of CalculateLocalDT, euler.go:973-1002) and the IVortex
+ * boundary state's dependence on the solver time.  The mixed path and the
+ * PerssonC0 dissipation return GCFD_ERR_UNSUPPORTED. */
+
+/* Functionals of the current state: the wall pressure force, summed over Wall
+ * and Cyl boundary edges as |edge| sum_p w_p p n_x (or n_y), with the
+ * interpolatory weights of the edge flux points (the integrated form of the
+ * wall data OutputFinal writes, euler.go:251-316); and the squared error
+ * sum (Q - Q_exact(t))^2 against the isentropic vortex at the solver time
+ * (IVortex.GetStateC, isentropic_vortex/analytic_vortex.go:31-82). */
+#define GCFD_FUNC_WALL_FORCE_X 0
+#define GCFD_FUNC_WALL_FORCE_Y 1
+#define GCFD_FUNC_VORTEX_ERROR 2
+/* J and, when Qbar is given, dJ/dQ (sharded like gcfd_get_state) and dJ/dt. */
+int gcfd_functional(gcfd_ctx* ctx, int32_t kind, double* J, int32_t nshards, const int32_t* Kmax,
+                    double* const* Qbar, double* tbar);
+
+/* Adjoint of gcfd_rhs at (Q, time): Qbar = (dRHS/dQ)^T RHSbar, plus the
+ * far-field Qinf adjoint (4, with pinf and cinf following Qinf as FreeStream
+ * derives them, fluids.go:370-406) and d/dtime (IVortex boundaries).  Replaces
+ * nothing in the reference: the transpose of SetRTFluxInternal ->
+ * InterpolateSolutionToEdges -> CalculateEdgeEulerFlux -> SetRTFluxOnEdges ->
+ * RHSInternalPoints (euler.go:665-726, edges.go:325-488). */
+int gcfd_rhs_vjp(gcfd_ctx* ctx, double time, int32_t nshards, const int32_t* Kmax, const double* const* Q,
+                 const double* const* RHSbar, double* const* Qbar, double* qinf_bar4, double* time_bar);
+
+/* Advance nsteps like gcfd_step, keeping a checkpoint of the state every
+ * checkpoint_every steps for a following gcfd_step_vjp (memory: the
+ * checkpoints plus checkpoint_every states). */
+int gcfd_record_steps(gcfd_ctx* ctx, int32_t nsteps, int32_t checkpoint_every, double* time, double* dt_last);
+
+/* Adjoint of the recorded window (RungeKutta5SSP.Step x nsteps, euler.go:408-418):
+ * from the adjoint of the final state (and of the final time) to the adjoint
+ * of the window's initial state, the far-field Qinf (4) and the initial time.
+ * Each segment of checkpoint_every steps is recomputed from its checkpoint and
+ * each step once more with its stage tape.  The solver state and time are the
+ * window's end again on return. */
+int gcfd_step_vjp(gcfd_ctx* ctx, int32_t nshards, const int32_t* Kmax, const double* const* Qfinal_bar,
+                  double tfinal_bar, double* const* Q0_bar, double* qinf_bar4, double* t0_bar);
+
 /* Residual norms of an increment array that the caller owns, computed without
  * allocating anything.  This entry point has no counterpart in the reference.
  *
