@@ -341,17 +341,24 @@ def run_ours(a, world, rank, local):
             f1.record(sta)
         torch.cuda.synchronize()
         fwd_ms = f0.elapsed_time(f1) / a.adj_steps
-        sa.record(a.adj_steps, 1)
         qbar = np.ones((4, Np, K))
+        sa.record(2, 1)
         sa.step_vjp(qbar)  # warm-up (allocations, first launches)
-        sa.record(a.adj_steps, 1)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        sa.step_vjp(qbar)
-        adj_ms = (time.perf_counter() - t0) * 1e3 / a.adj_steps
+
+        def sweep(n):
+            sa.record(n, 1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sa.step_vjp(qbar)
+            return (time.perf_counter() - t0) * 1e3
+        n1, n2 = max(1, a.adj_steps // 2), a.adj_steps + max(1, a.adj_steps // 2)
+        t1, t2 = sweep(n1), sweep(n2)
+        adj_ms = (t2 - t1) / (n2 - n1)  # per reverse step, without the window's fixed costs
         adjoint = {"ms_per_step": adj_ms, "forward_ms_per_step": fwd_ms, "ratio": adj_ms / fwd_ms,
-                   "steps": a.adj_steps, "checkpoint_every": 1, "path": "fp64",
-                   "timing": "host clock around gcfd_step_vjp (synchronous), forward by CUDA events"}
+                   "window_ms": {str(n1): t1, str(n2): t2}, "checkpoint_every": 1, "path": "fp64",
+                   "timing": "host clock around gcfd_step_vjp (synchronous) for two window lengths; per-step "
+                             "cost = difference / difference in steps (the adjoint's host transfer and set-up "
+                             "are per window); forward by CUDA events"}
         sa.close()
 
     # End to end through the public API: pinned host state in, step, state out.

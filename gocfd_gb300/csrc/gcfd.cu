@@ -130,6 +130,7 @@ struct gcfd_ctx {
   double* tapeRHS[5] = {};
   double* tapeES[5] = {};
   double* tapeDT[5] = {};
+  double* tapeQF[5] = {};
   Scalars* tapeSc0 = nullptr;  // scalars before the taped step (BC time)
   Scalars* tapeSc = nullptr;   // after it (per-stage gmax and dt)
   double* Qb[5] = {};
@@ -586,9 +587,12 @@ struct AdjLaunch {
   static void tape_step(gcfd_ctx* c) {
     cudaMemcpyAsync(c->tapeSc0, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream);
     k_step_begin<<<1, 32, 0, c->stream>>>(c->sc);
+    void* faces = c->QF;
     for (int s = 0; s < 5; ++s) {
+      c->QF = c->tapeQF[s];  // the stage's faces stay on the tape
       L::interp(c, c->Q[s]);
       L::edge(c, &c->sc->time, &c->sc->gmax[s]);
+      c->QF = faces;
       cudaMemcpyAsync(c->tapeES[s], c->edgeSpeed, sizeof(double) * c->nEdges, cudaMemcpyDeviceToDevice,
                       c->stream);
       UpdateArgs<double> u = L::update_args(c, s, c->Q[s]);
@@ -601,15 +605,24 @@ struct AdjLaunch {
     cudaMemcpyAsync(c->tapeSc, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream);
   }
   // The reverse of stage s.  Q0 is the step's initial state.
+  static void edges(gcfd_ctx* c, const EdgeArgs<double>& e, const AdjEdgeArgs& x) {
+    if (c->nInt > 0) {
+      if (e.flux == kFluxRoe && x.useManualRoe)
+        k_adj_edge<N, true><<<grid(c->nInt), 128, 0, c->stream>>>(e, x);
+      else
+        k_adj_edge<N, false><<<grid(c->nInt), 128, 0, c->stream>>>(e, x);
+    }
+    if (c->nBC > 0) k_adj_edge_bc<N><<<grid(c->nBC * Dims<N>::NE), 128, 0, c->stream>>>(e, x);
+  }
   static void reverse_stage(gcfd_ctx* c, int s, const double* Q0) {
     const double* Qs = (s == 0) ? Q0 : c->Q[s];
-    L::interp(c, Qs);
     const double* Qbn = (s == 4) ? c->Qbf : c->Qb[s + 1];
     k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, s, Qs, Qbn, c->Qb[s]));
-    const EdgeArgs<double> e = edge_args(c, &c->tapeSc0->time);
+    EdgeArgs<double> e = edge_args(c, &c->tapeSc0->time);
+    e.QF = c->tapeQF[s];
     const AdjEdgeArgs x = adj_edge_args(c);
     const int nE = c->nInt + c->nBC;
-    k_adj_edge<N><<<grid(nE), 128, 0, c->stream>>>(e, x);
+    edges(c, e, x);
     cudaMemsetAsync(c->esBar, 0, sizeof(double) * nE, c->stream);
     AdjDtArgs d;
     d.K = c->K;
@@ -644,8 +657,7 @@ struct AdjLaunch {
   // Qbf <- adjoint of Q0, adjS[10] <- t-bar of the step's start.
   static void reverse_step(gcfd_ctx* c, const double* Q0) {
     tape_step(c);
-    const size_t S = sizeof(double) * 4 * c->Np * static_cast<size_t>(c->K);
-    for (int i = 0; i < 4; ++i) cudaMemsetAsync(c->Qb[i], 0, S, c->stream);
+    // no zeroing of the stage adjoints: k_adj_div's first write to each is a store
     cudaMemsetAsync(c->adjS, 0, sizeof(double) * 5, c->stream);
     cudaMemcpyAsync(c->adjS + 9, c->adjS + 10, sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
     cudaMemsetAsync(c->carry, 0, sizeof(double) * c->K, c->stream);
@@ -660,7 +672,7 @@ struct AdjLaunch {
     cudaMemsetAsync(c->Qb[0], 0, S, c->stream);
     k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, -1, c->Qtmp, c->Qbf, c->Qb[0]));
     const EdgeArgs<double> e = edge_args(c, &c->sc->rhs_time);
-    k_adj_edge<N><<<grid(c->nInt + c->nBC), 128, 0, c->stream>>>(e, adj_edge_args(c));
+    edges(c, e, adj_edge_args(c));
     k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[0], c->K);
   }
   // Functionals of the current state Q[0]: J into adjS[11], dJ/dQ into Qb[0],
@@ -1369,6 +1381,7 @@ int adj_init(gcfd_ctx* c) {
     if ((rc = dalloc(c, &c->tapeRHS[s], S))) return rc;
     if ((rc = dalloc(c, &c->tapeES[s], static_cast<size_t>(nE)))) return rc;
     if ((rc = dalloc(c, &c->tapeDT[s], static_cast<size_t>(c->K)))) return rc;
+    if ((rc = dalloc(c, &c->tapeQF[s], F))) return rc;
     if ((rc = dalloc(c, &c->Qb[s], S))) return rc;
   }
   if ((rc = dalloc(c, &c->tapeSc0, 1))) return rc;

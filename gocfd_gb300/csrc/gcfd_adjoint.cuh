@@ -64,29 +64,33 @@ __device__ __forceinline__ void pressure_vjp(const Gas<double>& g, const double 
 __device__ __forceinline__ double sgn(double x) { return x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : 0.0); }
 
 // RoeFlux (fluxes.go:284-413) in reverse: QLb, QRb += (df/dQL)^T fb, (df/dQR)^T fb.
+// Divisions are taken once as reciprocals (FP64 division is a multi-instruction
+// sequence); the forward intermediates are recomputed from QL, QR.
 __device__ __forceinline__ void roe_vjp(const Gas<double>& g, const double QL[4], const double QR[4], double nx,
                                         double ny, const double fbo[4], double QLb[4], double QRb[4]) {
   // forward
+  const double iL = 1.0 / QL[0], iR = 1.0 / QR[0];
   const double rhoULr = QL[1] * nx + QL[2] * ny, rhoVLr = -QL[1] * ny + QL[2] * nx;
   const double rhoURr = QR[1] * nx + QR[2] * ny, rhoVRr = -QR[1] * ny + QR[2] * nx;
-  const double rhoL = QL[0], uL = rhoULr / QL[0], vL = rhoVLr / QL[0];
-  const double rhoR = QR[0], uR = rhoURr / QR[0], vR = rhoVRr / QR[0];
-  const double pL = pressure(g, QL[0], QL[1], QL[2], QL[3]);
-  const double pR = pressure(g, QR[0], QR[1], QR[2], QR[3]);
-  const double hL = (QL[3] + pL) / rhoL, hR = (QR[3] + pR) / rhoR;
+  const double rhoL = QL[0], uL = rhoULr * iL, vL = rhoVLr * iL;
+  const double rhoR = QR[0], uR = rhoURr * iR, vR = rhoVRr * iR;
+  const double uxL = QL[1] * iL, uyL = QL[2] * iL, uxR = QR[1] * iR, uyR = QR[2] * iR;
+  const double pL = g.gm1 * (QL[3] - 0.5 * rhoL * (uxL * uxL + uyL * uyL));
+  const double pR = g.gm1 * (QR[3] - 0.5 * rhoR * (uxR * uxR + uyR * uyR));
+  const double hL = (QL[3] + pL) * iL, hR = (QR[3] + pR) * iR;
   const double rhoLs = sqrt(rhoL), rhoRs = sqrt(rhoR);
-  const double S = rhoLs + rhoRs;
+  const double S = rhoLs + rhoRs, oS = 1.0 / S;
   const double rho = rhoLs * rhoRs;
-  const double u = (rhoLs * uL + rhoRs * uR) / S;
-  const double v = (rhoLs * vL + rhoRs * vR) / S;
-  const double h = (rhoLs * hL + rhoRs * hR) / S;
+  const double u = (rhoLs * uL + rhoRs * uR) * oS;
+  const double v = (rhoLs * vL + rhoRs * vR) * oS;
+  const double h = (rhoLs * hL + rhoRs * hR) * oS;
   const double c2 = g.gm1 * (h - 0.5 * (u * u + v * v));
-  const double C = sqrt(c2);
+  const double C = sqrt(c2), oC = 1.0 / C, oc2 = oC * oC;
   const double du = uR - uL, dp = pR - pL;
-  const double a1 = -0.5 * (rho * du) / C + 0.5 * dp / c2;
-  const double a2 = (rhoR - rhoL) - dp / c2;
+  const double a1 = -0.5 * (rho * du) * oC + 0.5 * dp * oc2;
+  const double a2 = (rhoR - rhoL) - dp * oc2;
   const double a3 = rho * (vR - vL);
-  const double a4 = 0.5 * (rho * du) / C + 0.5 * dp / c2;
+  const double a4 = 0.5 * (rho * du) * oC + 0.5 * dp * oc2;
   const double l1 = fabs(u - C), l2 = fabs(u), l4 = fabs(u + C);
   const double W1 = l1 * a1, W2 = l2 * a2, W3 = l2 * a3, W4 = l4 * a4;
   // output rotation: out0 = f0, out1 = nx f1 - ny f2, out2 = ny f1 + nx f2, out3 = f3
@@ -118,11 +122,12 @@ __device__ __forceinline__ void roe_vjp(const Gas<double>& g, const double QL[4]
   ub += s1 * l1b + s2 * l2b + s4 * l4b;
   Cb += -s1 * l1b + s4 * l4b;
   // a1..a4
-  double rhob = (-0.5 * du / C) * a1b + (vR - vL) * a3b + (0.5 * du / C) * a4b;
-  double dub = (-0.5 * rho / C) * a1b + (0.5 * rho / C) * a4b;
-  Cb += (0.5 * rho * du / (C * C)) * a1b - (0.5 * rho * du / (C * C)) * a4b;
-  double dpb = (0.5 / c2) * a1b - a2b / c2 + (0.5 / c2) * a4b;
-  double c2b = (-0.5 * dp / (c2 * c2)) * a1b + (dp / (c2 * c2)) * a2b - (0.5 * dp / (c2 * c2)) * a4b;
+  const double a14 = a4b - a1b;
+  double rhob = 0.5 * du * oC * a14 + (vR - vL) * a3b;
+  const double dub = 0.5 * rho * oC * a14;
+  Cb -= 0.5 * rho * du * oc2 * a14;
+  const double dpb = oc2 * (0.5 * (a1b + a4b) - a2b);
+  double c2b = dp * oc2 * oc2 * (a2b - 0.5 * (a1b + a4b));
   double rhoRb = a2b, rhoLb = -a2b;
   vRb += rho * a3b;
   vLb -= rho * a3b;
@@ -131,45 +136,45 @@ __device__ __forceinline__ void roe_vjp(const Gas<double>& g, const double QL[4]
   pRb += dpb;
   pLb -= dpb;
   // C = sqrt(c2); c2 = gm1 (h - (u^2 + v^2) / 2)
-  c2b += Cb * 0.5 / C;
+  c2b += 0.5 * Cb * oC;
   hb += g.gm1 * c2b;
   ub -= g.gm1 * u * c2b;
   vb -= g.gm1 * v * c2b;
   // Roe averages
-  const double oS = 1.0 / S;
   uLb += rhoLs * oS * ub;
   uRb += rhoRs * oS * ub;
   vLb += rhoLs * oS * vb;
   vRb += rhoRs * oS * vb;
   const double hLb = rhoLs * oS * hb, hRb = rhoRs * oS * hb;
-  double rhoLsb = ((uL - u) * ub + (vL - v) * vb + (hL - h) * hb) * oS + rhoRs * rhob;
-  double rhoRsb = ((uR - u) * ub + (vR - v) * vb + (hR - h) * hb) * oS + rhoLs * rhob;
-  rhoLb += 0.5 / rhoLs * rhoLsb;
-  rhoRb += 0.5 / rhoRs * rhoRsb;
+  const double rhoLsb = ((uL - u) * ub + (vL - v) * vb + (hL - h) * hb) * oS + rhoRs * rhob;
+  const double rhoRsb = ((uR - u) * ub + (vR - v) * vb + (hR - h) * hb) * oS + rhoLs * rhob;
+  rhoLb += 0.5 * rhoLsb / rhoLs;
+  rhoRb += 0.5 * rhoRsb / rhoRs;
   // h = (E + p) / rho
-  QL3b += hLb / rhoL;
-  pLb += hLb / rhoL;
-  rhoLb -= hL / rhoL * hLb;
-  QR3b += hRb / rhoR;
-  pRb += hRb / rhoR;
-  rhoRb -= hR / rhoR * hRb;
+  QL3b += hLb * iL;
+  pLb += hLb * iL;
+  rhoLb -= hL * iL * hLb;
+  QR3b += hRb * iR;
+  pRb += hRb * iR;
+  rhoRb -= hR * iR * hRb;
   // rotated velocities
-  rhoULrb += uLb / QL[0];
-  rhoVLrb += vLb / QL[0];
-  rhoLb -= (uL * uLb + vL * vLb) / QL[0];
-  rhoURrb += uRb / QR[0];
-  rhoVRrb += vRb / QR[0];
-  rhoRb -= (uR * uRb + vR * vRb) / QR[0];
+  rhoULrb += uLb * iL;
+  rhoVLrb += vLb * iL;
+  rhoLb -= (uL * uLb + vL * vLb) * iL;
+  rhoURrb += uRb * iR;
+  rhoVRrb += vRb * iR;
+  rhoRb -= (uR * uRb + vR * vRb) * iR;
+  // p = gm1 (E - (m^2 + n^2) / (2 rho))
+  rhoLb += g.gm1 * 0.5 * (uxL * uxL + uyL * uyL) * pLb;
+  rhoRb += g.gm1 * 0.5 * (uxR * uxR + uyR * uyR) * pRb;
   QLb[0] += rhoLb;
   QRb[0] += rhoRb;
-  QLb[3] += QL3b;
-  QRb[3] += QR3b;
-  QLb[1] += nx * rhoULrb - ny * rhoVLrb;
-  QLb[2] += ny * rhoULrb + nx * rhoVLrb;
-  QRb[1] += nx * rhoURrb - ny * rhoVRrb;
-  QRb[2] += ny * rhoURrb + nx * rhoVRrb;
-  pressure_vjp(g, QL, pLb, QLb);
-  pressure_vjp(g, QR, pRb, QRb);
+  QLb[3] += QL3b + g.gm1 * pLb;
+  QRb[3] += QR3b + g.gm1 * pRb;
+  QLb[1] += nx * rhoULrb - ny * rhoVLrb - g.gm1 * uxL * pLb;
+  QLb[2] += ny * rhoULrb + nx * rhoVLrb - g.gm1 * uyL * pLb;
+  QRb[1] += nx * rhoURrb - ny * rhoVRrb - g.gm1 * uxR * pRb;
+  QRb[2] += ny * rhoURrb + nx * rhoVRrb - g.gm1 * uyR * pRb;
 }
 
 // Any interior flux by forward-mode duals (8 tangents: QL then QR).
@@ -355,8 +360,8 @@ __global__ void __launch_bounds__(128) k_adj_div(AdjArgs a) {
           Rb[n][r] = C4 * dt4 * qb;
           a.Rb3[ind] = W3 * dt4 * qb;
           dtb += qb * (W3 * a.rhs3[ind] + C4 * a.rhs[ind]);
-          a.Qb2[ind] += A2 * qb;
-          a.Qb3[ind] += A3 * qb;
+          a.Qb2[ind] = A2 * qb;  // stage 4 is the first writer of the stage-2..4 adjoints
+          a.Qb3[ind] = A3 * qb;
           a.Qbs[ind] = A4 * qb;
         }
     } else {
@@ -371,8 +376,11 @@ __global__ void __launch_bounds__(128) k_adj_div(AdjArgs a) {
           const double qb = a.Qbn[ind];
           Rb[n][r] = ga * dt * qb + (s == 3 ? a.Rb3[ind] : 0.0);
           dtb += ga * qb * a.rhs[ind];
-          a.Qb0[ind] += al * qb;
-          if (be != 0.0) a.Qbs[ind] += be * qb;
+          // first writers: stage 3 of the step's Q0 adjoint, stage 1 of its own
+          if (s == 3) a.Qb0[ind] = al * qb;
+          else a.Qb0[ind] += al * qb;
+          if (s == 1) a.Qbs[ind] = be * qb;
+          else if (be != 0.0) a.Qbs[ind] += be * qb;
         }
     }
     // RHS = -(1/J) DivInt . DOF  =>  DOFb = -(1/J) DivInt^T Rb
@@ -426,58 +434,68 @@ struct AdjEdgeArgs {
   int useManualRoe;
 };
 
-template <int N>
+// Interior edges [0, nInt): Riemann flux Jacobian^T at each edge point
+// (ROE: the reverse-mode Roe adjoint; otherwise the dual-number one).
+template <int N, bool ROE>
 __global__ void __launch_bounds__(128) k_adj_edge(EdgeArgs<double> a, AdjEdgeArgs x) {
   constexpr int NE = Dims<N>::NE, NE3 = Dims<N>::NE3;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= a.nInt + a.nBC) return;
+  if (e >= a.nInt) return;
   const size_t sK = static_cast<size_t>(a.K);
-  const int kL = a.kL[e];
-  const int eL = a.eLR[e] & 3;
+  const int kL = a.kL[e], kR = a.kR[e];
+  const int eL = a.eLR[e] & 3, eR = a.eLR[e] >> 2;
   const double nx = a.nx[e], ny = a.ny[e];
-  const double IIL = a.IIL[e];
-  if (e < a.nInt) {
-    const int kR = a.kR[e];
-    const int eR = a.eLR[e] >> 2;
-    const double IIR = a.IIR[e];
+  const double IIL = a.IIL[e], IIR = a.IIR[e];
 #pragma unroll 1
-    for (int p = 0; p < NE; ++p) {
-      const int jL = eL * NE + p, jR = eR * NE + (NE - 1 - p);
-      double qL[4], qR[4], fb[4], qLb[4] = {0.0, 0.0, 0.0, 0.0}, qRb[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int p = 0; p < NE; ++p) {
+    const int jL = eL * NE + p, jR = eR * NE + (NE - 1 - p);
+    double qL[4], qR[4], fb[4], qLb[4] = {0.0, 0.0, 0.0, 0.0}, qRb[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
-      for (int n = 0; n < 4; ++n) {
-        qL[n] = a.QF[(n * NE3 + jL) * sK + kL];
-        qR[n] = a.QF[(n * NE3 + jR) * sK + kR];
-        fb[n] = IIL * x.FEb[(n * NE3 + jL) * sK + kL] - IIR * x.FEb[(n * NE3 + jR) * sK + kR];
-      }
-      if (a.flux == kFluxRoe && x.useManualRoe)
-        roe_vjp(a.gas, qL, qR, nx, ny, fb, qLb, qRb);
-      else
-        riemann_vjp_dual(a.flux, a.gas, qL, qR, nx, ny, fb, qLb, qRb);
-#pragma unroll
-      for (int n = 0; n < 4; ++n) {
-        x.QFb[(n * NE3 + jL) * sK + kL] = qLb[n];
-        x.QFb[(n * NE3 + jR) * sK + kR] = qRb[n];
-      }
+    for (int n = 0; n < 4; ++n) {
+      qL[n] = a.QF[(n * NE3 + jL) * sK + kL];
+      qR[n] = a.QF[(n * NE3 + jR) * sK + kR];
+      fb[n] = IIL * x.FEb[(n * NE3 + jL) * sK + kL] - IIR * x.FEb[(n * NE3 + jR) * sK + kR];
     }
-  } else {
-    const int b = e - a.nInt;
-    const int flag = a.bcFlag[b];
-    const double t = *a.time;
-    double qinfb[4] = {0.0, 0.0, 0.0, 0.0}, tb = 0.0;
-#pragma unroll 1
-    for (int p = 0; p < NE; ++p) {
-      const int jL = eL * NE + p;
-      double qi[4], fb[4], qib[4] = {0.0, 0.0, 0.0, 0.0};
+    if (ROE)
+      roe_vjp(a.gas, qL, qR, nx, ny, fb, qLb, qRb);
+    else
+      riemann_vjp_dual(a.flux, a.gas, qL, qR, nx, ny, fb, qLb, qRb);
 #pragma unroll
-      for (int n = 0; n < 4; ++n) {
-        qi[n] = a.QF[(n * NE3 + jL) * sK + kL];
-        fb[n] = IIL * x.FEb[(n * NE3 + jL) * sK + kL];
-      }
-      bc_point_vjp(a, flag, b * NE + p, qi, nx, ny, t, a.oohK[e], fb, 0.0, qib, qinfb, &tb);
-#pragma unroll
-      for (int n = 0; n < 4; ++n) x.QFb[(n * NE3 + jL) * sK + kL] = qib[n];
+    for (int n = 0; n < 4; ++n) {
+      x.QFb[(n * NE3 + jL) * sK + kL] = qLb[n];
+      x.QFb[(n * NE3 + jR) * sK + kR] = qRb[n];
     }
+  }
+}
+
+// Boundary edges [nInt, nInt + nBC): boundary state and flux by duals, one
+// thread per (boundary edge, edge point).
+template <int N>
+__global__ void __launch_bounds__(128) k_adj_edge_bc(EdgeArgs<double> a, AdjEdgeArgs x) {
+  constexpr int NE = Dims<N>::NE, NE3 = Dims<N>::NE3;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  double qinfb[4] = {0.0, 0.0, 0.0, 0.0}, tb = 0.0;
+  if (tid < a.nBC * NE) {
+    const int b = tid / NE, p = tid - b * NE;
+    const int e = a.nInt + b;
+    const size_t sK = static_cast<size_t>(a.K);
+    const int kL = a.kL[e];
+    const int jL = (a.eLR[e] & 3) * NE + p;
+    const double IIL = a.IIL[e];
+    double qi[4], fb[4], qib[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      qi[n] = a.QF[(n * NE3 + jL) * sK + kL];
+      fb[n] = IIL * x.FEb[(n * NE3 + jL) * sK + kL];
+    }
+    bc_point_vjp(a, a.bcFlag[b], tid, qi, a.nx[e], a.ny[e], *a.time, a.oohK[e], fb, 0.0, qib, qinfb, &tb);
+#pragma unroll
+    for (int n = 0; n < 4; ++n) x.QFb[(n * NE3 + jL) * sK + kL] = qib[n];
+  }
+#pragma unroll
+  for (int n = 0; n < 4; ++n) qinfb[n] = warp_sum(qinfb[n]);
+  tb = warp_sum(tb);
+  if ((threadIdx.x & 31) == 0) {
 #pragma unroll
     for (int n = 0; n < 4; ++n)
       if (qinfb[n] != 0.0) atomicAdd(&x.qinfb[n], qinfb[n]);
