@@ -51,7 +51,7 @@ def args_parse():
     p.add_argument("--steps", type=int, default=1000)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
+    p.add_argument("--precision", choices=["fp32", "tf32x3", "fp64"], default="fp32")
     p.add_argument("--workload", choices=sorted(WORKLOADS), default="vortex256")
     p.add_argument("--fp64-steps", type=int, default=100)
     p.add_argument("--adj-steps", type=int, default=20, help="steps of the FP64 adjoint timing (0: skip)")
@@ -285,10 +285,12 @@ def run_ours(a, world, rank, local):
         m, n = solver.profile_step()
         fam_ms = [x + y for x, y in zip(fam_ms, m)]
         fam_n = [x + y for x, y in zip(fam_n, n)]
-    if a.precision == "fp32":  # the preparation is not part of a graph step
+    if a.precision != "fp64":  # the preparation is not part of a graph step
         fam_ms[0], fam_n[0] = 0.0, 0
     if a.precision == "fp32":
         names = ["k_mixed_prepare", "k_mixed_edge", "k_mixed_stage", "k_step"]
+    elif a.precision == "tf32x3":
+        names = ["k_mixed_prepare", "k_mixed_edge", "k_mixed_stage_tc", "k_step"]
     else:
         names = ["k_interp", "k_edge_flux", "k_div_update", "k_step"]
     dom = max(range(3), key=lambda i: fam_ms[i])
@@ -305,6 +307,28 @@ def run_ours(a, world, rank, local):
                 "algorithmic_bytes": alg, "peak_source": peak_kind,
                 "avg_launch_us": per_launch_ms * 1e3,
                 "kernel_share": {names[i]: fam_ms[i] / max(sum(fam_ms), 1e-12) for i in range(4)}}
+
+    # The other mixed variant (FMA or tensor-core divergence) on the same workload.
+    other = None
+    if a.precision in ("fp32", "tf32x3") and a.fp64_steps > 0:
+        oprec = "tf32x3" if a.precision == "fp32" else "fp32"
+        so = Euler(ip, mesh, 1, precision=oprec, device=local, vortex_center=(0.0, 0.0))
+        sto = torch.cuda.ExternalStream(so.stream_handle(), device=torch.device("cuda", local))
+        so.enqueue_steps(3)
+        torch.cuda.synchronize()
+        evo = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(20)]
+        with torch.cuda.stream(sto):
+            for i, (s0, s1) in enumerate(evo):
+                flush.fill_(float(i & 7))
+                s0.record(sto)
+                so.enqueue_steps(1)
+                s1.record(sto)
+        torch.cuda.synchronize()
+        mso = float(sum(s0.elapsed_time(s1) for s0, s1 in evo)) / len(evo)
+        so.step(0)
+        other = {"precision": oprec, "value": world * dof_per_step / (mso / 1e3), "ms_per_step": mso,
+                 "steps": len(evo)}
+        so.close()
 
     # FP64 drop-in path on the same workload (device-timed, no flush).
     fp64 = None
@@ -399,7 +423,8 @@ def run_ours(a, world, rank, local):
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": a.precision if a.precision == "fp64" else "fp32 (fp64 state/RK)",
+            "vs_baseline": None, "dtype": {"fp64": "fp64", "fp32": "fp32 (fp64 state/RK)",
+                                                  "tf32x3": "3xtf32 tensor-core GEMM, fp32 elsewhere (fp64 state/RK)"}[a.precision],
             "data": "synthetic (analytic isentropic-vortex initial condition on a generated mesh)",
             "config": {"workload": a.workload, "description": wl["desc"], "K": K, "N": wl["N"], "Np": Np,
                        "dof_updates_per_step": dof_per_step, "flux": "roe", "cfl": 1.0,
@@ -411,6 +436,7 @@ def run_ours(a, world, rank, local):
             "roofline": roofline,
             "cpu_baseline": cpu,
             "fp64_path": fp64,
+            "other_mixed_path": other,
             "adjoint": adjoint,
             "final_time": info["time"],
         }

@@ -16,6 +16,7 @@
 #include "dfr_element.hpp"
 #include "gcfd_kernels.cuh"
 #include "gcfd_mixed.cuh"
+#include "gcfd_mixed_tc.cuh"
 #include "gcfd_diss.cuh"
 #include "gcfd_adjoint.cuh"
 #include "mesh.hpp"
@@ -115,6 +116,9 @@ struct gcfd_ctx {
   int* meslot = nullptr;
   float *mnx = nullptr, *mny = nullptr, *moohK = nullptr;
   bool dirty = true;  // Q0 changed outside a step: the stage-0 data must be rebuilt
+  bool tc = false;     // mixed path with the divergence GEMM on the tensor cores (3xTF32)
+  float* mBtc = nullptr;
+  int tcDynSmem = 0;   // dynamic shared memory that caps the stage kernel's CTAs per SM to its TMEM share
   // artificial dissipation (PerssonC0, FP64 path)
   bool diss = false;
   unsigned long long *sigV = nullptr, *epsV = nullptr;
@@ -461,9 +465,17 @@ struct MixedLaunch {
     a.vy0 = c->vy0;
     a.vgamma = c->vgamma;
     a.rhsOut = c->rhsOut;
+    a.Btc = c->mBtc;
+    a.err = reinterpret_cast<unsigned int*>(&c->sc->errFlags);
     return a;
   }
   static int gridE(gcfd_ctx* c) { return (c->K + 31) / 32; }
+  static void stage_kernel(gcfd_ctx* c, const MixedArgs& a) {
+    if (c->tc)
+      k_mixed_stage_tc<N><<<gridE(c), 128, c->tcDynSmem, c->stream>>>(a);
+    else
+      k_mixed_stage<N><<<gridE(c), 128, 0, c->stream>>>(a);
+  }
   // Interior edges on the main stream; boundary edges (FP64, transcendental
   // work, few threads) concurrently on a forked stream, joined before the stage.
   static void edges(gcfd_ctx* c, int s, double* Q0, const double* time, unsigned long long* gmax,
@@ -517,7 +529,7 @@ struct MixedLaunch {
       mark(2);
       edges(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s], ev == nullptr);
       mark(3);
-      k_mixed_stage<N><<<gridE(c), 128, 0, c->stream>>>(args(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]));
+      stage_kernel(c, args(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]));
       mark(4);
       acc(1, 2, 3);
       acc(2, 3, 4);
@@ -530,7 +542,7 @@ struct MixedLaunch {
   static void rhs(gcfd_ctx* c) {
     prepare(c, c->Qtmp);
     edges(c, -1, c->Qtmp, &c->sc->rhs_time, &c->sc->gmax[0], false);
-    k_mixed_stage<N><<<gridE(c), 128, 0, c->stream>>>(args(c, -1, c->Qtmp, &c->sc->rhs_time, &c->sc->gmax[0]));
+    stage_kernel(c, args(c, -1, c->Qtmp, &c->sc->rhs_time, &c->sc->gmax[0]));
   }
   static void prep_state(gcfd_ctx* c) { prepare(c, c->Q[0]); }
 };
@@ -877,6 +889,65 @@ int build_diss(gcfd_ctx* c, const gcfd_mesh* m) {
   return GCFD_OK;
 }
 
+// Tensor-core operand: DivInt (16 x NFP, zero padded, columns in the stage
+// kernel's K order) split into TF32 hi and lo parts, each laid out as the
+// kernel's shared-memory B operand, and
+// the dynamic shared memory that keeps the stage kernel's CTAs per SM within
+// the Tensor Memory they allocate (512 columns per SM).
+float tf32_round(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, sizeof(u));
+  u = (u + 0x1000u) & 0xFFFFE000u;  // nearest, ties away from zero, like cvt.rna.tf32.f32
+  float r;
+  std::memcpy(&r, &u, sizeof(r));
+  return r;
+}
+
+template <int N>
+int build_tc_n(gcfd_ctx* c) {
+  constexpr int NFP = TcDims<N>::NFP, BSZ = TcDims<N>::BSZ, NCOLS = TcDims<N>::NCOLS;
+  std::vector<float> b(2 * static_cast<size_t>(BSZ), 0.f);
+  // K order of the kernel's rows: Fr_0, Fs_0, Fr_1, Fs_1, ..., then the edge DOFs.
+  const int Np = c->Np;
+  for (int r = 0; r < Np; ++r)
+    for (int j = 0; j < c->NF; ++j) {
+      const int col = j < 2 * Np ? ((j & 1) ? Np + j / 2 : j / 2) : j;
+      const double v = c->el.DivInt(r, col);
+      const float hi = tf32_round(static_cast<float>(v));
+      const float lo = tf32_round(static_cast<float>(v - static_cast<double>(hi)));
+      b[tc_b_index(r, j, NFP)] = hi;
+      b[BSZ + tc_b_index(r, j, NFP)] = lo;
+    }
+  int rc = upload(c, &c->mBtc, b);
+  if (rc) return rc;
+  cudaFuncAttributes attr{};
+  GCFD_CUDA(c, cudaFuncGetAttributes(&attr, k_mixed_stage_tc<N>));
+  const int perSM = 512 / NCOLS;  // CTAs whose TMEM fits at once
+  int smemPerSM = 0;
+  GCFD_CUDA(c, cudaDeviceGetAttribute(&smemPerSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->prm.device));
+  // Smallest per-CTA footprint (with the shared memory the runtime reserves per
+  // CTA) at which perSM + 1 CTAs no longer fit on an SM.
+  int reserved = 0;
+  GCFD_CUDA(c, cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, c->prm.device));
+  const int want = smemPerSM / (perSM + 1) + 1 - reserved;
+  c->tcDynSmem = std::max(0, want - static_cast<int>(attr.sharedSizeBytes));
+  if (c->tcDynSmem > 48 * 1024)
+    GCFD_CUDA(c, cudaFuncSetAttribute(k_mixed_stage_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      c->tcDynSmem));
+  return GCFD_OK;
+}
+
+int build_tc(gcfd_ctx* c) {
+  switch (c->N) {
+    case 0: return build_tc_n<0>(c);
+    case 1: return build_tc_n<1>(c);
+    case 2: return build_tc_n<2>(c);
+    case 3: return build_tc_n<3>(c);
+    case 4: return build_tc_n<4>(c);
+    default: return fail(c, GCFD_ERR_UNSUPPORTED, "tensor-core path: N <= 4");
+  }
+}
+
 // Buffers and FP32 operator / geometry copies of the mixed path.
 int build_mixed(gcfd_ctx* c) {
   const int K = c->K, Np = c->Np, NE = c->NE, NF = c->NF;
@@ -908,6 +979,7 @@ int build_mixed(gcfd_ctx* c) {
   for (int j = 0; j < 3 * NE; ++j)
     for (int i = 0; i < Np; ++i) iop[static_cast<size_t>(j) * NPP + i] = static_cast<float>(c->el.FluxEdgeInterp(j, i));
   if ((rc = upload(c, &c->mDivT, divT))) return rc;
+  if (c->tc && (rc = build_tc(c))) return rc;
   if ((rc = upload(c, &c->mIop, iop))) return rc;
   const Geometry& g = c->geo;
   std::vector<float> geo(static_cast<size_t>(6) * K), ii(static_cast<size_t>(3) * K);
@@ -944,7 +1016,8 @@ int build_mixed(gcfd_ctx* c) {
 int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
   const gcfd_params& p = c->prm;
   c->N = p.N;
-  c->fp32 = (p.precision == GCFD_PREC_FP32);
+  c->fp32 = (p.precision == GCFD_PREC_FP32 || p.precision == GCFD_PREC_TF32X3);
+  c->tc = (p.precision == GCFD_PREC_TF32X3);
   // NewEuler creates the dissipation only for PerssonC0 with N > 0 (euler.go:107-112);
   // the sensor ramp takes Kappa when given, else 5 (dissipation.go:140-147).
   c->diss = (p.limiter == GCFD_LIMITER_PERSSON_C0) && p.N > 0;
@@ -1103,7 +1176,8 @@ int gcfd_create(const gcfd_mesh* mesh, const gcfd_params* params, gcfd_ctx** out
     return fail(nullptr, GCFD_ERR_ARG, "boundary edge arrays missing");
   if (params->N < 0 || params->N > 4)
     return fail(nullptr, GCFD_ERR_UNSUPPORTED, "PolynomialOrder must be 0..4");
-  if (params->precision != GCFD_PREC_FP64 && params->precision != GCFD_PREC_FP32)
+  if (params->precision != GCFD_PREC_FP64 && params->precision != GCFD_PREC_FP32 &&
+      params->precision != GCFD_PREC_TF32X3)
     return fail(nullptr, GCFD_ERR_UNSUPPORTED, "unknown precision mode");
   if (params->flux_type < 0 || params->flux_type > 3)
     return fail(nullptr, GCFD_ERR_ARG, "unknown flux type");
@@ -1252,6 +1326,8 @@ int gcfd_step(gcfd_ctx* c, int32_t nsteps, double* time, double* dt_last, double
     if (resid_rms4) resid_rms4[n] = rms;
     if (nsteps > 0 && !(std::isfinite(am) && std::isfinite(rms))) finite = false;
   }
+  if (h.errFlags)
+    return fail(c, GCFD_ERR_TIMEOUT, "a tensor-core completion wait ran out of its iteration bound");
   if (!finite) return fail(c, GCFD_ERR_NAN, "non-finite RK increment (solution diverged)");
   return GCFD_OK;
 }

@@ -240,6 +240,8 @@ struct MixedArgs {
   FreeStreamT<double> fsFar, fsIn, fsOut;
   double vbeta, vx0, vy0, vgamma;
   double* rhsOut;             // stage -1: RHS in FP64 [n][i][k]
+  const float* Btc;           // tensor-core path: DivInt split hi / lo in the shared-memory operand layout
+  unsigned int* err;          // error flags (bit 0: a tensor-core wait ran out)
 };
 
 // SSP(5,4) weights of rkAdvance (euler.go:511-564) in increment form:
@@ -511,6 +513,92 @@ __global__ void __launch_bounds__(8 * MixedDims<N>::NE) k_mixed_edge_bc(MixedArg
   }
 }
 
+// The stage update after the divergence (shared by the FMA and tensor-core
+// stage kernels): the RHS goes to rhsOut (stage -1) or into the SSP increments,
+// the next stage's faces and reference state, and at stage 4 the compensated
+// state and the residual partials.
+template <int N>
+__device__ __forceinline__ void stage_tail(const MixedArgs& a, const float* sI, const int eslot[3], int n, int k,
+                                           size_t off, size_t sK, int s, const float rhs[], const float dq0[],
+                                           const float ds[], double dtLocal, float& rmax, float& rabs,
+                                           float& rs2) {
+  constexpr int NP = MixedDims<N>::NP, NPP = MixedDims<N>::NPP;
+  if (s < 0) {
+#pragma unroll
+    for (int r = 0; r < NP; ++r) a.rhsOut[off + r * sK] = rhs[r];
+  } else {
+    double dtk;
+    if (a.localDT) {
+      dtk = dtLocal;
+      if (n == 0) a.DT[k] = dtk;
+    } else {
+      const double gm = __longlong_as_double(static_cast<long long>(a.sc->gmax[s]));
+      dtk = a.cfl / gm;
+      const double t = a.sc->time;
+      if (t + dtk > a.finalTime) dtk = a.finalTime - t;
+      if (k == 0 && n == 0) a.sc->dt[s] = dtk;
+    }
+    const float dt = static_cast<float>(dtk);
+    float dn[NP];
+    if (s == 0) {
+#pragma unroll
+      for (int r = 0; r < NP; ++r) dn[r] = kSspC0 * (dt * rhs[r]);
+    } else if (s == 1) {
+#pragma unroll
+      for (int r = 0; r < NP; ++r) dn[r] = kSspB1 * ds[r] + kSspC1 * (dt * rhs[r]);
+    } else if (s == 2) {
+#pragma unroll
+      for (int r = 0; r < NP; ++r) dn[r] = kSspB2 * ds[r] + kSspC2 * (dt * rhs[r]);
+    } else if (s == 3) {
+#pragma unroll
+      for (int r = 0; r < NP; ++r) {
+        a.R3[off + r * sK] = rhs[r];
+        dn[r] = kSspB3 * ds[r] + kSspC3 * (dt * rhs[r]);
+      }
+    }
+    if (s < 4) {
+      float* dst = a.D[s + 1] + off;
+#pragma unroll
+      for (int r = 0; r < NP; ++r) dst[r * sK] = dn[r];
+      float dqn[NPP];
+#pragma unroll
+      for (int r = 0; r < NPP; ++r) dqn[r] = (r < NP) ? dq0[r] + (dn[r] - dn[0]) : 0.0f;
+      write_faces<N>(a, sI, eslot, n, dqn);
+      float h = a.Qhi[off], l = a.Qlo[off];
+      df_add(h, l, dn[0]);
+      a.base[static_cast<size_t>(k) * 4 + n] = make_float2(h, l);
+    } else {
+      // Final increment and the compensated accumulation (rkAdvance stage 4).
+      float qh[NP], ql[NP];
+#pragma unroll
+      for (int r = 0; r < NP; ++r) {
+        const float inc = kSspA2 * a.D[2][off + r * sK] + kSspA3 * a.D[3][off + r * sK] + kSspA4 * ds[r] +
+                          kSspR3 * (dt * a.R3[off + r * sK]) + kSspC4 * (dt * rhs[r]);
+        qh[r] = a.Qhi[off + r * sK];
+        ql[r] = a.Qlo[off + r * sK];
+        df_add(qh[r], ql[r], inc);
+        a.Qhi[off + r * sK] = qh[r];
+        a.Qlo[off + r * sK] = ql[r];
+        rmax = fmaxf(rmax, inc);
+        rabs = fmaxf(rabs, fabsf(inc));
+        rs2 = fmaf(inc, inc, rs2);
+        if (inc != inc) rabs = inc;
+      }
+      // Prepare the next step's stage 0 from the new state.
+      float dqn[NPP];
+#pragma unroll
+      for (int r = 0; r < NPP; ++r) dqn[r] = 0.0f;
+#pragma unroll
+      for (int r = 0; r < NP; ++r) {
+        dqn[r] = df_diff(qh[r], ql[r], qh[0], ql[0]);
+        a.dQ0[off + r * sK] = dqn[r];
+      }
+      write_faces<N>(a, sI, eslot, n, dqn);
+      a.base[static_cast<size_t>(k) * 4 + n] = make_float2(qh[0], ql[0]);
+    }
+  }
+}
+
 // (b)+(e): delta-form divergence, SSP stage update on the FP32 increments, and
 // the next stage's faces / reference states.  stage -1 writes the RHS only.
 template <int N>
@@ -635,80 +723,7 @@ __global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
     float rhs[NP];
 #pragma unroll
     for (int r = 0; r < NP; ++r) rhs[r] = -acc[r] * ooJ;
-    if (s < 0) {
-#pragma unroll
-      for (int r = 0; r < NP; ++r) a.rhsOut[off + r * sK] = rhs[r];
-    } else {
-      double dtk;
-      if (a.localDT) {
-        dtk = dtLocal;
-        if (n == 0) a.DT[k] = dtk;
-      } else {
-        const double gm = __longlong_as_double(static_cast<long long>(a.sc->gmax[s]));
-        dtk = a.cfl / gm;
-        const double t = a.sc->time;
-        if (t + dtk > a.finalTime) dtk = a.finalTime - t;
-        if (k == 0 && n == 0) a.sc->dt[s] = dtk;
-      }
-      const float dt = static_cast<float>(dtk);
-      float dn[NP];
-      if (s == 0) {
-#pragma unroll
-        for (int r = 0; r < NP; ++r) dn[r] = kSspC0 * (dt * rhs[r]);
-      } else if (s == 1) {
-#pragma unroll
-        for (int r = 0; r < NP; ++r) dn[r] = kSspB1 * ds[r] + kSspC1 * (dt * rhs[r]);
-      } else if (s == 2) {
-#pragma unroll
-        for (int r = 0; r < NP; ++r) dn[r] = kSspB2 * ds[r] + kSspC2 * (dt * rhs[r]);
-      } else if (s == 3) {
-#pragma unroll
-        for (int r = 0; r < NP; ++r) {
-          a.R3[off + r * sK] = rhs[r];
-          dn[r] = kSspB3 * ds[r] + kSspC3 * (dt * rhs[r]);
-        }
-      }
-      if (s < 4) {
-        float* dst = a.D[s + 1] + off;
-#pragma unroll
-        for (int r = 0; r < NP; ++r) dst[r * sK] = dn[r];
-        float dqn[NPP];
-#pragma unroll
-        for (int r = 0; r < NPP; ++r) dqn[r] = (r < NP) ? dq0[r] + (dn[r] - dn[0]) : 0.0f;
-        write_faces<N>(a, sI, eslot, n, dqn);
-        float h = a.Qhi[off], l = a.Qlo[off];
-        df_add(h, l, dn[0]);
-        a.base[static_cast<size_t>(k) * 4 + n] = make_float2(h, l);
-      } else {
-        // Final increment and the compensated accumulation (rkAdvance stage 4).
-        float qh[NP], ql[NP];
-#pragma unroll
-        for (int r = 0; r < NP; ++r) {
-          const float inc = kSspA2 * a.D[2][off + r * sK] + kSspA3 * a.D[3][off + r * sK] + kSspA4 * ds[r] +
-                            kSspR3 * (dt * a.R3[off + r * sK]) + kSspC4 * (dt * rhs[r]);
-          qh[r] = a.Qhi[off + r * sK];
-          ql[r] = a.Qlo[off + r * sK];
-          df_add(qh[r], ql[r], inc);
-          a.Qhi[off + r * sK] = qh[r];
-          a.Qlo[off + r * sK] = ql[r];
-          rmax = fmaxf(rmax, inc);
-          rabs = fmaxf(rabs, fabsf(inc));
-          rs2 = fmaf(inc, inc, rs2);
-          if (inc != inc) rabs = inc;
-        }
-        // Prepare the next step's stage 0 from the new state.
-        float dqn[NPP];
-#pragma unroll
-        for (int r = 0; r < NPP; ++r) dqn[r] = 0.0f;
-#pragma unroll
-        for (int r = 0; r < NP; ++r) {
-          dqn[r] = df_diff(qh[r], ql[r], qh[0], ql[0]);
-          a.dQ0[off + r * sK] = dqn[r];
-        }
-        write_faces<N>(a, sI, eslot, n, dqn);
-        a.base[static_cast<size_t>(k) * 4 + n] = make_float2(qh[0], ql[0]);
-      }
-    }
+    stage_tail<N>(a, sI, eslot, n, k, off, sK, s, rhs, dq0, ds, dtLocal, rmax, rabs, rs2);
   }
   if (s == 4) {
     const unsigned long long km = warp_max_u64(order_key(static_cast<double>(rmax)));

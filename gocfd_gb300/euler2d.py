@@ -30,7 +30,7 @@ from .meshes import Mesh, read_mesh
 FLUX_TYPES = {"average": 0, "lax": 1, "roe": 2, "roe-er": 3}          # fluxes.go:25-33
 INIT_TYPES = {"freestream": 0, "ivortex": 1, "shocktube": 2}          # initialization.go:22-31
 LIMITERS = {"": 0, "perssonc0": 1, "persson c0": 1}                   # filter.go:29-35
-PRECISIONS = {"fp64": 0, "fp32": 1}
+PRECISIONS = {"fp64": 0, "fp32": 1, "tf32x3": 2}
 
 
 @dataclass

@@ -42,9 +42,11 @@ enum { GCFD_FLUX_AVERAGE = 0, GCFD_FLUX_LAX = 1, GCFD_FLUX_ROE = 2, GCFD_FLUX_RO
 enum { GCFD_INIT_FREESTREAM = 0, GCFD_INIT_IVORTEX = 1, GCFD_INIT_SHOCKTUBE = 2 };
 /* Limiter names of model_problems/Euler2D/filter.go:10-23. */
 enum { GCFD_LIMITER_NONE = 0, GCFD_LIMITER_PERSSON_C0 = 1 };
-/* Arithmetic of the RHS.  FP64 is the drop-in; the others keep the conserved
- * state, the RK accumulation and the residual norms in FP64. */
-enum { GCFD_PREC_FP64 = 0, GCFD_PREC_FP32 = 1 };
+/* Arithmetic of the RHS.  FP64 is the drop-in.  FP32 is the delta-form mixed
+ * path (FP32 arithmetic, compensated FP32 conserved state, FP64 dt and
+ * residual scalars); TF32X3 is the same path with the divergence GEMM on the
+ * tensor cores as three TF32 products (hi*hi + hi*lo + lo*hi). */
+enum { GCFD_PREC_FP64 = 0, GCFD_PREC_FP32 = 1, GCFD_PREC_TF32X3 = 2 };
 /* BC flags, numbered as types.BCFLAG (types/cfd.go:11-26). */
 enum {
   GCFD_BC_NONE = 0, GCFD_BC_IN = 1, GCFD_BC_FAR = 4, GCFD_BC_WALL = 5, GCFD_BC_CYL = 6,

@@ -128,9 +128,10 @@ def test_local_time_stepping_parity():
 
 
 @pytest.mark.parametrize("N", [1, 2, 3, 4])
-def test_rhs_mixed_vortex(N):
+@pytest.mark.parametrize("precision", ["fp32", "tf32x3"])
+def test_rhs_mixed_vortex(N, precision):
     mesh = meshes.vortex_box(16, jitter=0.1)
-    gpu, ora = make_pair(mesh, N, init="ivortex", vortex_center=(0.0, 0.0), precision="fp32")
+    gpu, ora = make_pair(mesh, N, init="ivortex", vortex_center=(0.0, 0.0), precision=precision)
     r = gpu.rhs_global(ora.Q, 0.1)
     ref = ora.rhs(ora.Q, 0.1)
     err = rel_l2(r, ref)
@@ -140,10 +141,11 @@ def test_rhs_mixed_vortex(N):
 
 
 @pytest.mark.parametrize("N", [2, 4])
-def test_rhs_mixed_resolved_vortex(N):
+@pytest.mark.parametrize("precision", ["fp32", "tf32x3"])
+def test_rhs_mixed_resolved_vortex(N, precision):
     """64x64 jittered mesh: the vortex is resolved, deltas are small."""
     mesh = meshes.vortex_box(64, jitter=0.1, seed=2)
-    gpu, ora = make_pair(mesh, N, init="ivortex", vortex_center=(0.0, 0.0), precision="fp32")
+    gpu, ora = make_pair(mesh, N, init="ivortex", vortex_center=(0.0, 0.0), precision=precision)
     r = gpu.rhs_global(ora.Q, 0.05)
     ref = ora.rhs(ora.Q, 0.05)
     err = rel_l2(r, ref)
@@ -153,9 +155,10 @@ def test_rhs_mixed_resolved_vortex(N):
 
 
 @pytest.mark.parametrize("flux", ["average", "lax", "roe", "roe-er"])
-def test_rhs_mixed_bc_mesh(flux):
+@pytest.mark.parametrize("precision", ["fp32", "tf32x3"])
+def test_rhs_mixed_bc_mesh(flux, precision):
     mesh = meshes.read_mesh(fixture("fstepA001.neu"))
-    gpu, ora = make_pair(mesh, 3, flux=flux, minf=0.5, alpha=10.0, precision="fp32")
+    gpu, ora = make_pair(mesh, 3, flux=flux, minf=0.5, alpha=10.0, precision=precision)
     Q = perturbed(ora.Q, seed=3, amp=0.01)
     err = rel_l2(gpu.rhs_global(Q), ora.rhs(Q))
     print(f"mixed RHS rel L2 {flux}: {err:.3e}")
@@ -164,18 +167,20 @@ def test_rhs_mixed_bc_mesh(flux):
 
 
 @pytest.mark.parametrize("N", range(5))
-def test_freestream_exact_mixed(N):
+@pytest.mark.parametrize("precision", ["fp32", "tf32x3"])
+def test_freestream_exact_mixed(N, precision):
     """Delta form: a uniform state has zero deltas, so the RHS is exactly zero."""
     mesh = meshes.read_mesh(fixture("test_tris_6_nowall.neu"))
-    gpu, _ = make_pair(mesh, N, flux="roe", minf=2.0, precision="fp32")
+    gpu, _ = make_pair(mesh, N, flux="roe", minf=2.0, precision=precision)
     r = gpu.rhs_global(gpu.get_global_state())
     assert np.abs(r).max() < 1e-12
     gpu.close()
 
 
-def test_step_mixed_vortex():
+@pytest.mark.parametrize("precision", ["fp32", "tf32x3"])
+def test_step_mixed_vortex(precision):
     mesh = meshes.vortex_box(20)
-    gpu, ora = make_pair(mesh, 2, init="ivortex", vortex_center=(0.0, 0.0), precision="fp32")
+    gpu, ora = make_pair(mesh, 2, init="ivortex", vortex_center=(0.0, 0.0), precision=precision)
     info = gpu.step(100)
     t, _, _ = ora.step(100)
     err = rel_l2(gpu.get_global_state(), ora.Q)
@@ -185,10 +190,11 @@ def test_step_mixed_vortex():
     gpu.close()
 
 
-def test_step_mixed_local_dt_and_restart():
+@pytest.mark.parametrize("precision", ["fp32", "tf32x3"])
+def test_step_mixed_local_dt_and_restart(precision):
     """Local time stepping, and set_state between steps (stage-0 rebuild)."""
     mesh = meshes.wedge_channel(24, 12)
-    gpu, ora = make_pair(mesh, 2, flux="roe", minf=2.0, local_dt=True, cfl=0.5, precision="fp32")
+    gpu, ora = make_pair(mesh, 2, flux="roe", minf=2.0, local_dt=True, cfl=0.5, precision=precision)
     gpu.step(5)
     ora.step(5)
     gpu.set_global_state(ora.Q)
