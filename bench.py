@@ -52,7 +52,7 @@ def args_parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--precision", choices=["fp32", "tf32x3", "fp64"], default="fp32")
-    p.add_argument("--workload", choices=sorted(WORKLOADS), default="vortex256")
+    p.add_argument("--workload", choices=sorted(WORKLOADS), default="vortex1024")
     p.add_argument("--fp64-steps", type=int, default=100)
     p.add_argument("--adj-steps", type=int, default=20, help="steps of the FP64 adjoint timing (0: skip)")
     p.add_argument("--e2e-steps", type=int, default=50)
@@ -203,7 +203,7 @@ def ncu_traffic_per_element(kernel, precision, N):
 
 
 # --------------------------------------------------------------------------- CPU oracle
-def cpu_baseline(wl, mesh, seconds, steps=None, warmup=0):
+def cpu_baseline(wl, mesh, seconds, steps=None, warmup=0, max_steps=200):
     """The oracle (C++ FP64, OpenMP on all host cores) on the same workload."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
@@ -216,7 +216,7 @@ def cpu_baseline(wl, mesh, seconds, steps=None, warmup=0):
     ora.step(1)
     t1 = time.perf_counter()
     done, el = 1, t1 - t0
-    target = steps if steps is not None else max(1, min(200, int(seconds / max(el, 1e-6))))
+    target = steps if steps is not None else max(1, min(max_steps, int(seconds / max(el, 1e-6))))
     while done < target:
         ora.step(1)
         done += 1
@@ -448,39 +448,9 @@ def run_ours(a, world, rank, local):
         dist.destroy_process_group()
 
 
-def exact_vortex_error(solver, t, vortex=(5.0, 0.0, 0.0, 1.4)):
-    """Relative L2 (over all points and variables) of the state against the
-    exact isentropic vortex translated to time t, at the solution points."""
-    import math
-    g = solver
-    beta, x0, y0, gamma = vortex
-    Q = g.get_global_state()
-    xs, ys = solution_points_xy(g)
-    GM1 = gamma - 1.0
-    xm, ym = xs - t, ys
-    r2 = (xm - x0) ** 2 + (ym - y0) ** 2
-    ex1r = np.exp(1 - r2)
-    u = 1.0 - beta * ex1r * (ym - y0) / (2 * math.pi)
-    v = beta * ex1r * (xm - x0) / (2 * math.pi)
-    rho = (1.0 - GM1 * beta * beta * np.exp(2 * (1 - r2)) / (16 * gamma * math.pi ** 2)) ** (1 / GM1)
-    p = rho ** gamma
-    ex = np.stack([rho, rho * u, rho * v, p / GM1 + 0.5 * rho * (u * u + v * v)])
-    return float(np.linalg.norm(Q - ex) / np.linalg.norm(ex))
-
-
-def solution_points_xy(g):
-    from gocfd_gb300 import _lib
-    rs = _lib.host_operator(g.ip.PolynomialOrder, 4)
-    v = g.mesh.EToV
-    VX, VY = g.mesh.VX, g.mesh.VY
-    r, s = rs[:, 0:1], rs[:, 1:2]
-    X = 0.5 * (-(r + s) * VX[v[:, 0]][None] + (r + 1) * VX[v[:, 1]][None] + (s + 1) * VX[v[:, 2]][None])
-    Y = 0.5 * (-(r + s) * VY[v[:, 0]][None] + (r + 1) * VY[v[:, 1]][None] + (s + 1) * VY[v[:, 2]][None])
-    return X, Y
-
-
 def run_accuracy(a, local):
     import torch
+    from gocfd_gb300.configs import exact_vortex_error
     from gocfd_gb300.euler2d import Euler
     torch.cuda.set_device(local)
     wl = WORKLOADS[a.workload]
@@ -492,7 +462,8 @@ def run_accuracy(a, local):
         s = Euler(ip, mesh, 1, precision=prec, device=local, vortex_center=(0.0, 0.0))
         info = s.step(a.accuracy)
         states[prec] = s.get_global_state()
-        res[prec] = {"time": info["time"], "rel_l2_vs_exact": exact_vortex_error(s, info["time"]),
+        l2, linf = exact_vortex_error(s, info["time"])
+        res[prec] = {"time": info["time"], "rel_l2_vs_exact": l2, "rel_linf_vs_exact": linf,
                      "resid_rms": info["resid_rms"]}
         s.close()
     d = states["fp32"] - states["fp64"]
@@ -510,9 +481,11 @@ def run_reference(a, world, rank):
         return
     wl = WORKLOADS[a.workload]
     mesh = make_mesh(wl)
-    r = cpu_baseline(wl, mesh, 0.0, steps=a.steps, warmup=a.warmup)
+    # A bounded sample of the workload: full steps of the whole mesh, as many as
+    # fit in ~60 s of host time (at least one, at most --steps), after one warm-up step.
+    r = cpu_baseline(wl, mesh, 60.0, warmup=min(a.warmup, 1), max_steps=a.steps)
     out = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world,
-           "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * r["seconds"] / r["steps"],
+           "steps": r["steps"], "warmup": min(a.warmup, 1), "ms_per_step": 1e3 * r["seconds"] / r["steps"],
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
            "data": "synthetic (analytic isentropic-vortex initial condition on a generated mesh)",
            "config": {"workload": a.workload, "description": wl["desc"], "N": wl["N"], "flux": "roe",

@@ -1,0 +1,201 @@
+"""The five validation / benchmark configurations of the Euler2D DFR path, with
+a runner that reports each one's errors against its exact solution.
+
+    vortex20      isentropic vortex, [-5,5]^2, 20x20 quads (800 triangles), N=2, 100 steps
+    vortex256     the same on 256x256 quads (131,072 triangles), +-10% node jitter, N=4, 1000 steps
+    sod2000x100   Sod shock tube, [0,1]x[0,0.05], 2000x100 quads (400,000 triangles), N=3,
+                  PerssonC0 (Kappa 5), to t = 0.2, density against the exact solution
+    wedge512x256  Mach 2 over a 15 degree ramp, [0,3]x[0,1], 512x256 quads (262,144 triangles), N=2,
+                  local time stepping, PerssonC0 (Kappa 6), steady march, ramp pressure force
+    vortex1024    the vortex on 1024x1024 quads (2,097,152 triangles), N=4, 1000 steps
+
+Physics, BCs and inputs follow the reference's runs (InitializeSolution,
+euler.go:728-794; test_cases/Euler2D/shock-tube/input-wall.yaml: CFL 5, Roe,
+PerssonC0, Kappa 5; test_cases/Euler2D/Wedge/input.yaml: CFL 1, Roe, Minf 2,
+local time stepping, PerssonC0, Kappa 6, 15000 iterations): vortex boundaries are Wall-tagged and
+become IVortex (exact state through the characteristic BC); the vortex is
+centred at (0, 0) inside the box.  Meshes are generated (gocfd_gb300.meshes);
+the jitter stream is numpy's PCG64 with the stated seed.
+
+Run one:  python -m gocfd_gb300.configs --config sod2000x100 [--precision fp64] [--scale 0.25]
+(--scale shrinks the quad counts for a quick look.)
+"""
+import argparse
+import json
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib, meshes
+from .euler2d import Euler, InputParameters2D
+
+
+@dataclass
+class Config:
+    name: str
+    desc: str
+    mesh: str                      # vortex | sod | wedge
+    nx: int
+    ny: int
+    N: int
+    init: str
+    jitter: float = 0.0
+    seed: int = 0
+    cfl: float = 1.0
+    flux: str = "roe"
+    steps: int = 0                 # fixed step count (vortex)
+    final_time: float = 1e9
+    limiter: str = ""
+    kappa: float = 0.0
+    minf: float = 0.1
+    local_dt: bool = False
+    residual_tol: float = 0.0      # steady march stop: rms(R)/rms(Q) per variable
+    max_steps: int = 0
+    extra: dict = field(default_factory=dict)
+
+
+CONFIGS = {
+    "vortex20": Config("vortex20", "isentropic vortex [-5,5]^2, 20x20 quads -> 800 tris, N=2", "vortex", 20, 20, 2,
+                       "ivortex", steps=100),
+    "vortex256": Config("vortex256", "isentropic vortex [-5,5]^2, 256x256 quads -> 131072 tris, jitter 0.1h seed 0, N=4",
+                        "vortex", 256, 256, 4, "ivortex", jitter=0.1, steps=1000),
+    "sod2000x100": Config("sod2000x100", "Sod shock tube [0,1]x[0,0.05], 2000x100 quads -> 400000 tris, N=3, PerssonC0",
+                          "sod", 2000, 100, 3, "shocktube", cfl=5.0, final_time=0.2, limiter="PerssonC0",
+                          kappa=5.0),
+    "wedge512x256": Config("wedge512x256", "Mach 2 wedge 15 deg, [0,3]x[0,1], 512x256 quads -> 262144 tris, N=2, "
+                           "local dt, PerssonC0", "wedge", 512, 256, 2, "freestream", cfl=1.0, limiter="PerssonC0",
+                           kappa=6.0, minf=2.0, local_dt=True, residual_tol=1e-10, max_steps=15000),
+    "vortex1024": Config("vortex1024", "isentropic vortex [-5,5]^2, 1024x1024 quads -> 2097152 tris, jitter 0.1h "
+                         "seed 0, N=4", "vortex", 1024, 1024, 4, "ivortex", jitter=0.1, steps=1000),
+}
+
+
+def build_mesh(cfg: Config, scale: float = 1.0):
+    nx, ny = max(2, int(round(cfg.nx * scale))), max(2, int(round(cfg.ny * scale)))
+    if cfg.mesh == "vortex":
+        return meshes.vortex_box(nx, jitter=cfg.jitter, seed=cfg.seed)
+    if cfg.mesh == "sod":
+        return meshes.sod_channel(nx, ny)
+    if cfg.mesh == "wedge":
+        return meshes.wedge_channel(nx, ny)
+    raise ValueError(cfg.mesh)
+
+
+def input_params(cfg: Config) -> InputParameters2D:
+    return InputParameters2D(CFL=cfg.cfl, FluxType=cfg.flux, InitType=cfg.init, PolynomialOrder=cfg.N,
+                             FinalTime=cfg.final_time, Minf=cfg.minf, Gamma=1.4, Alpha=0.0,
+                             LocalTimeStepping=cfg.local_dt, MaxIterations=10 ** 9, Limiter=cfg.limiter,
+                             Kappa=cfg.kappa)
+
+
+def solution_points_xy(solver: Euler):
+    """Physical coordinates of the solution points, Np x K each."""
+    rs = _lib.host_operator(solver.ip.PolynomialOrder, 4)
+    v = solver.mesh.EToV
+    VX, VY = solver.mesh.VX, solver.mesh.VY
+    r, s = rs[:, 0:1], rs[:, 1:2]
+    X = 0.5 * (-(r + s) * VX[v[:, 0]][None] + (r + 1) * VX[v[:, 1]][None] + (s + 1) * VX[v[:, 2]][None])
+    Y = 0.5 * (-(r + s) * VY[v[:, 0]][None] + (r + 1) * VY[v[:, 1]][None] + (s + 1) * VY[v[:, 2]][None])
+    return X, Y
+
+
+def exact_vortex(X, Y, t, vortex=(5.0, 0.0, 0.0, 1.4)):
+    """IVortex.GetStateC (isentropic_vortex/analytic_vortex.go:31-82) at (X, Y), 4 x shape."""
+    beta, x0, y0, gamma = vortex
+    GM1 = gamma - 1.0
+    xm, ym = X - t, Y
+    r2 = (xm - x0) ** 2 + (ym - y0) ** 2
+    ex1r = np.exp(1 - r2)
+    u = 1.0 - beta * ex1r * (ym - y0) / (2 * math.pi)
+    v = beta * ex1r * (xm - x0) / (2 * math.pi)
+    rho = (1.0 - GM1 * beta * beta * np.exp(2 * (1 - r2)) / (16 * gamma * math.pi ** 2)) ** (1 / GM1)
+    p = rho ** gamma
+    return np.stack([rho, rho * u, rho * v, p / GM1 + 0.5 * rho * (u * u + v * v)])
+
+
+def exact_vortex_error(solver: Euler, t: float):
+    """(relative L2, relative Linf) over all solution points and variables."""
+    X, Y = solution_points_xy(solver)
+    ex = exact_vortex(X, Y, t)
+    d = solver.get_global_state() - ex
+    return float(np.linalg.norm(d) / np.linalg.norm(ex)), float(np.abs(d).max() / np.abs(ex).max())
+
+
+def sod_density_error(solver: Euler, t: float):
+    """Density at every solution point against the exact Sod solution at its x:
+    (L1 mean, L2 rms, Linf), and the same over points at least 0.02 from the waves."""
+    from .sod import SodExact
+    sod = SodExact(t)
+    X, _ = solution_points_xy(solver)
+    rho = solver.get_global_state()[0]
+    ex = sod.density(X)
+    d = np.abs(rho - ex)
+    waves = np.array([sod.x1, sod.x2, sod.x3, sod.x4])
+    far = np.min(np.abs(X[..., None] - waves), axis=-1) > 0.02
+    return {"l1": float(d.mean()), "l2": float(np.sqrt((d ** 2).mean())), "linf": float(d.max()),
+            "l1_smooth": float(d[far].mean()), "linf_smooth": float(d[far].max()),
+            "shock_x_exact": sod.x4}
+
+
+def run(name: str, precision: str = "fp64", scale: float = 1.0, device: int = 0, max_steps: int = 0,
+        report_every: int = 0):
+    cfg = CONFIGS[name]
+    mesh = build_mesh(cfg, scale)
+    ip = input_params(cfg)
+    center = (0.0, 0.0) if cfg.mesh == "vortex" else (5.0, 0.0)
+    out = {"config": name, "desc": cfg.desc, "scale": scale, "precision": precision}
+    with Euler(ip, mesh, 1, precision=precision, device=device, vortex_center=center) as s:
+        out["K"] = s.K
+        t0 = time.perf_counter()
+        if cfg.mesh == "vortex":
+            info = s.step(cfg.steps)
+            out.update(steps=cfg.steps, time=info["time"])
+            out["rel_l2_vs_exact"], out["rel_linf_vs_exact"] = exact_vortex_error(s, info["time"])
+        elif cfg.mesh == "sod":
+            steps, t = 0, 0.0
+            cap = max_steps or 10 ** 7
+            while t < cfg.final_time * (1 - 1e-12) and steps < cap:
+                info = s.step(100)
+                steps += 100
+                t = info["time"]
+            out.update(steps=steps, time=t)
+            out["density_error"] = sod_density_error(s, t)
+        else:  # steady march
+            steps, hist = 0, []
+            # per-variable RMS of the state, floored so that a variable that is zero
+            # in the initial state (v-momentum at zero incidence) is measured on the others' scale
+            qn = np.sqrt(np.mean(s.get_global_state() ** 2, axis=(1, 2)))
+            qn = np.maximum(qn, 1e-3 * qn.max())
+            cap = max_steps or cfg.max_steps
+            rel = np.inf
+            while steps < cap:
+                info = s.step(50)
+                steps += 50
+                rel = float(np.max(np.array(info["resid_rms"]) / qn))
+                if report_every and steps % report_every == 0:
+                    hist.append((steps, rel))
+                if rel < cfg.residual_tol:
+                    break
+            out.update(steps=steps, residual_rel_rms=rel, converged=bool(rel < cfg.residual_tol), history=hist)
+            out["ramp_force_x"], _, _ = s.functional("wall_force_x")
+            out["ramp_force_y"], _, _ = s.functional("wall_force_y")
+        out["seconds"] = time.perf_counter() - t0
+    return out
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    p.add_argument("--config", choices=sorted(CONFIGS), required=True)
+    p.add_argument("--precision", choices=["fp64", "fp32", "tf32x3"], default="fp64")
+    p.add_argument("--scale", type=float, default=1.0)
+    p.add_argument("--max-steps", type=int, default=0)
+    p.add_argument("--report-every", type=int, default=0)
+    a = p.parse_args(argv)
+    print(json.dumps(run(a.config, a.precision, a.scale, max_steps=a.max_steps, report_every=a.report_every)),
+          flush=True)
+
+
+if __name__ == "__main__":
+    main()

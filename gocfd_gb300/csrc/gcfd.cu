@@ -1446,10 +1446,33 @@ std::vector<double> edge_weights(const gcfd_ctx* c) {
   return w;
 }
 
+// Buffers of gcfd_functional (any path): the state adjoint, face adjoints,
+// scalars, solution-point coordinates, edge weights and FP64 faces.
+int func_init(gcfd_ctx* c) {
+  if (c->adjS) return GCFD_OK;
+  const size_t S = static_cast<size_t>(4) * c->Np * c->K;
+  const size_t F = static_cast<size_t>(4) * 3 * c->NE * c->K;
+  int rc;
+  if (!c->QF) {  // the mixed path keeps its faces elsewhere
+    double* qf = nullptr;
+    if ((rc = dalloc(c, &qf, F))) return rc;
+    c->QF = qf;
+  }
+  if ((rc = dalloc(c, &c->Qb[0], S))) return rc;
+  if ((rc = dalloc(c, &c->QFb, F))) return rc;
+  if ((rc = upload(c, &c->dXs, c->geo.xSol))) return rc;
+  if ((rc = upload(c, &c->dYs, c->geo.ySol))) return rc;
+  if ((rc = upload(c, &c->edgeW, edge_weights(c)))) return rc;
+  if ((rc = dalloc(c, &c->adjS, 16))) return rc;
+  GCFD_CUDA(c, cudaMemsetAsync(c->adjS, 0, sizeof(double) * 16, c->stream));
+  return GCFD_OK;
+}
+
 int adj_init(gcfd_ctx* c) {
   if (c->adjReady) return GCFD_OK;
   int rc = adj_check(c);
   if (rc) return rc;
+  if ((rc = func_init(c))) return rc;
   const size_t S = static_cast<size_t>(4) * c->Np * c->K;
   const size_t F = static_cast<size_t>(4) * 3 * c->NE * c->K;
   const int nE = c->nInt + c->nBC;
@@ -1458,23 +1481,17 @@ int adj_init(gcfd_ctx* c) {
     if ((rc = dalloc(c, &c->tapeES[s], static_cast<size_t>(nE)))) return rc;
     if ((rc = dalloc(c, &c->tapeDT[s], static_cast<size_t>(c->K)))) return rc;
     if ((rc = dalloc(c, &c->tapeQF[s], F))) return rc;
-    if ((rc = dalloc(c, &c->Qb[s], S))) return rc;
+    if (s > 0 && (rc = dalloc(c, &c->Qb[s], S))) return rc;
   }
   if ((rc = dalloc(c, &c->tapeSc0, 1))) return rc;
   if ((rc = dalloc(c, &c->tapeSc, 1))) return rc;
   if ((rc = dalloc(c, &c->Qbf, S))) return rc;
   if ((rc = dalloc(c, &c->Rb3, S))) return rc;
-  if ((rc = dalloc(c, &c->QFb, F))) return rc;
   if ((rc = dalloc(c, &c->FEb, F))) return rc;
   if ((rc = dalloc(c, &c->carry, static_cast<size_t>(c->K)))) return rc;
   if ((rc = dalloc(c, &c->dtOwnK, static_cast<size_t>(c->K)))) return rc;
   if ((rc = dalloc(c, &c->esBar, static_cast<size_t>(nE)))) return rc;
-  if ((rc = dalloc(c, &c->adjS, 16))) return rc;
   if ((rc = dalloc(c, &c->argEdge, 8))) return rc;
-  if ((rc = upload(c, &c->dXs, c->geo.xSol))) return rc;
-  if ((rc = upload(c, &c->dYs, c->geo.ySol))) return rc;
-  if ((rc = upload(c, &c->edgeW, edge_weights(c)))) return rc;
-  GCFD_CUDA(c, cudaMemsetAsync(c->adjS, 0, sizeof(double) * 16, c->stream));
   c->adjReady = true;
   return GCFD_OK;
 }
@@ -1499,9 +1516,10 @@ int gcfd_functional(gcfd_ctx* c, int32_t kind, double* J, int32_t nshards, const
   if (!c || !J) return c ? fail(c, GCFD_ERR_ARG, "null J") : GCFD_ERR_ARG;
   if (kind < GCFD_FUNC_WALL_FORCE_X || kind > GCFD_FUNC_VORTEX_ERROR)
     return fail(c, GCFD_ERR_ARG, "unknown functional kind");
-  int rc = adj_init(c);
+  int rc = func_init(c);
   if (rc) return rc;
   if (Qbar && (rc = check_shards(c, nshards, Kmax))) return rc;
+  if ((rc = sync_fp64_state(c))) return rc;
   AdjOps o;
   select_adj_ops(c->N, &o);
   GCFD_CUDA(c, cudaMemsetAsync(c->adjS + 9, 0, sizeof(double) * 3, c->stream));

@@ -302,3 +302,21 @@ def test_adjoint_rejects_mixed_and_dissipation():
         with pytest.raises(_lib.GcfdError) as e:
             gpu.record(1)
         assert e.value.code == -7
+
+
+@pytest.mark.parametrize("precision,limiter", [("fp32", ""), ("fp64", "PerssonC0")])
+def test_functional_on_paths_without_adjoint(precision, limiter):
+    """The functionals need no adjoint: the mixed path and the PerssonC0 path evaluate them too."""
+    mesh = meshes.wedge_channel(8, 4)
+    ip = InputParameters2D(CFL=0.5, FluxType="roe", InitType="freestream", PolynomialOrder=2, FinalTime=1e9,
+                           Minf=2.0, Gamma=1.4, Limiter=limiter, Kappa=6.0)
+    gpu, ora = make_pair(mesh, 2, minf=2.0)
+    Q = perturbed(ora.Q, 12, 0.05)
+    gpu.set_global_state(Q)
+    J_ref, _, _ = gpu.functional("wall_force_x")
+    gpu.close()
+    with Euler(ip, mesh, 1, precision=precision) as other:
+        other.set_global_state(Q)
+        J, Qb, _ = other.functional("wall_force_x")
+    assert abs(J - J_ref) <= 1e-12 * abs(J_ref)
+    assert np.all(np.isfinite(Qb))
