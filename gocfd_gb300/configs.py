@@ -18,7 +18,10 @@ centred at (0, 0) inside the box.  Meshes are generated (gocfd_gb300.meshes);
 the jitter stream is numpy's PCG64 with the stated seed.
 
 Run one:  python -m gocfd_gb300.configs --config sod2000x100 [--precision fp64] [--scale 0.25]
-(--scale shrinks the quad counts for a quick look.)
+(--scale shrinks the quad counts for a quick look.)  The vortex1024 adjoint
+(1000 mixed-precision steps, then the field-error adjoint through 200 FP64
+steps with a checkpoint every 10):
+          python -m gocfd_gb300.configs --config vortex1024 --warm-steps 1000 --adjoint-steps 200
 """
 import argparse
 import json
@@ -185,6 +188,56 @@ def run(name: str, precision: str = "fp64", scale: float = 1.0, device: int = 0,
     return out
 
 
+def adjoint(name: str, steps: int, every: int, warm_steps: int = 0, warm_precision: str = "fp32",
+            fd_h: float = 1e-8, device: int = 0, seed: int = 0):
+    """The field-error adjoint of a vortex configuration: advance warm_steps in
+    warm_precision, then record `steps` FP64 steps with a checkpoint every
+    `every` steps, take J = sum (Q - Q_exact(t))^2 at the end and run the
+    adjoint back to the window's start.  The gradient is checked along one
+    random direction against central differences of the FP64 forward
+    (the GPU FP64 path, which tracks the oracle to 1e-10)."""
+    cfg = CONFIGS[name]
+    assert cfg.mesh == "vortex"
+    mesh = build_mesh(cfg)
+    ip = input_params(cfg)
+    out = {"config": name, "warm_steps": warm_steps, "warm_precision": warm_precision, "adjoint_steps": steps,
+           "checkpoint_every": every}
+    with Euler(ip, mesh, 1, precision="fp64", device=device, vortex_center=(0.0, 0.0)) as s:
+        if warm_steps:
+            with Euler(ip, mesh, 1, precision=warm_precision, device=device, vortex_center=(0.0, 0.0)) as w:
+                info = w.step(warm_steps)
+                s.set_global_state(w.get_global_state())
+                s.time = info["time"]
+        Q0, t0 = s.get_global_state(), s.time
+        t1 = time.perf_counter()
+        s.record(steps, every)
+        t2 = time.perf_counter()
+        J, Qbf, tbf = s.functional("vortex_error")
+        t3 = time.perf_counter()
+        Qb0, qinfb, tb0 = s.step_vjp(Qbf, tbf)
+        t4 = time.perf_counter()
+        out.update(J=J, grad_norm=float(np.linalg.norm(Qb0)), time_bar0=tb0,
+                   record_s=t2 - t1, vjp_s=t4 - t3, vjp_over_record=(t4 - t3) / (t2 - t1))
+        if fd_h > 0:
+            rng = np.random.default_rng(seed)
+            d = rng.standard_normal(Q0.shape) * np.abs(Q0)
+
+            def Jat(q):
+                s.set_global_state(q)
+                s.time = t0
+                s.step(steps)
+                return s.functional("vortex_error")[0]
+            ad = float(np.sum(Qb0 * d))
+            out.update(directional_adjoint=ad, fd={})
+            # d has norm ~ sqrt(#DOF) |Q|: the step h must keep h |d| small against the
+            # error the functional measures, or the cubic term of the central
+            # difference dominates; two steps show the convergence.
+            for h in (fd_h, fd_h / 10):
+                fd = (Jat(Q0 + h * d) - Jat(Q0 - h * d)) / (2 * h)
+                out["fd"][f"{h:g}"] = {"directional_fd": fd, "rel_diff": abs(ad - fd) / max(abs(fd), 1e-300)}
+    return out
+
+
 def main(argv=None):
     p = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     p.add_argument("--config", choices=sorted(CONFIGS), required=True)
@@ -192,9 +245,18 @@ def main(argv=None):
     p.add_argument("--scale", type=float, default=1.0)
     p.add_argument("--max-steps", type=int, default=0)
     p.add_argument("--report-every", type=int, default=0)
+    p.add_argument("--adjoint-steps", type=int, default=0,
+                   help="vortex configs: run the field-error adjoint through this many steps instead")
+    p.add_argument("--checkpoint-every", type=int, default=10)
+    p.add_argument("--warm-steps", type=int, default=0)
+    p.add_argument("--fd-h", type=float, default=1e-8, help="central-difference step of the adjoint check (0: skip)")
     a = p.parse_args(argv)
-    print(json.dumps(run(a.config, a.precision, a.scale, max_steps=a.max_steps, report_every=a.report_every)),
-          flush=True)
+    if a.adjoint_steps:
+        res = adjoint(a.config, a.adjoint_steps, a.checkpoint_every, a.warm_steps,
+                      a.precision if a.precision != "fp64" else "fp32", fd_h=a.fd_h)
+    else:
+        res = run(a.config, a.precision, a.scale, max_steps=a.max_steps, report_every=a.report_every)
+    print(json.dumps(res), flush=True)
 
 
 if __name__ == "__main__":

@@ -320,3 +320,30 @@ def test_functional_on_paths_without_adjoint(precision, limiter):
         J, Qb, _ = other.functional("wall_force_x")
     assert abs(J - J_ref) <= 1e-12 * abs(J_ref)
     assert np.all(np.isfinite(Qb))
+
+
+@pytest.mark.parametrize("center", [(0.0, 0.0), (5.0, 0.0)])
+def test_step_vjp_field_error_functional(center):
+    """J = sum (Q_final - Q_exact(t_final))^2: the final time's adjoint enters through tfinal_bar."""
+    mesh = meshes.vortex_box(4, jitter=0.1)
+    gpu, ora = make_pair(mesh, 2, init="ivortex", cfl=1.0, vortex_center=center)
+    Q0 = perturbed(ora.Q, 13, 0.01)
+    nsteps = 6
+    gpu.set_global_state(Q0)
+    gpu.record(nsteps, 4)
+    J, Qbf, tbf = gpu.functional("vortex_error")
+    Qb0, _, _ = gpu.step_vjp(Qbf, tbf)
+    rng = np.random.default_rng(14)
+    d = rng.standard_normal(Q0.shape) * np.abs(Q0)
+    vortex = (5.0, center[0], center[1], 1.4)
+    X, Y = ora.geo.SolX, ora.geo.SolY
+
+    def Jat(sign, h=1e-6):
+        ora.Q = np.ascontiguousarray(Q0 + sign * h * d)
+        ora.time = 0.0
+        ora.step(nsteps)
+        return float(np.sum((ora.Q - oracle.ivortex_state(vortex, ora.time, X, Y)) ** 2))
+    assert abs(Jat(0.0) - J) <= 1e-10 * J
+    fd = (Jat(1.0) - Jat(-1.0)) / 2e-6
+    assert_close(float(np.sum(Qb0 * d)), fd)
+    gpu.close()
