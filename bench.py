@@ -458,7 +458,7 @@ def run_accuracy(a, local):
     ip = input_params(wl["N"])
     res = {"workload": a.workload, "steps": a.accuracy}
     states = {}
-    for prec in ("fp64", "fp32"):
+    for prec in ("fp64", "fp32", "tf32x3"):
         s = Euler(ip, mesh, 1, precision=prec, device=local, vortex_center=(0.0, 0.0))
         info = s.step(a.accuracy)
         states[prec] = s.get_global_state()
@@ -466,11 +466,12 @@ def run_accuracy(a, local):
         res[prec] = {"time": info["time"], "rel_l2_vs_exact": l2, "rel_linf_vs_exact": linf,
                      "resid_rms": info["resid_rms"]}
         s.close()
-    d = states["fp32"] - states["fp64"]
-    res["fp32_vs_fp64_rel_l2"] = float(np.linalg.norm(d) / np.linalg.norm(states["fp64"]))
-    res["fp32_vs_fp64_rel_linf"] = float(np.abs(d).max() / np.abs(states["fp64"]).max())
-    res["fp32_vs_fp64_rel_l2_per_var"] = [float(np.linalg.norm(d[n]) / np.linalg.norm(states["fp64"][n]))
-                                         for n in range(4)]
+    for prec in ("fp32", "tf32x3"):
+        d = states[prec] - states["fp64"]
+        res[f"{prec}_vs_fp64_rel_l2"] = float(np.linalg.norm(d) / np.linalg.norm(states["fp64"]))
+        res[f"{prec}_vs_fp64_rel_linf"] = float(np.abs(d).max() / np.abs(states["fp64"]).max())
+        res[f"{prec}_vs_fp64_rel_l2_per_var"] = [float(np.linalg.norm(d[n]) / np.linalg.norm(states["fp64"][n]))
+                                                for n in range(4)]
     print(json.dumps(res), flush=True)
 
 
