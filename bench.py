@@ -4,8 +4,9 @@ SSP(5,4) step on GB300, against the CPU restatement timed on the host cores.
 
 One "step" is one 5-stage SSP-RK step over the whole mesh.  DOF-updates per
 step = K * Np * 4 * 5.  Default workload: isentropic vortex on [-5,5]^2,
-256 x 256 quads split into 131,072 triangles with +-10% h interior jitter
-(seed 0), N = 4 (Np = 15), Roe flux, CFL 1, far-field exact-state BCs.
+1024 x 1024 quads split into 2,097,152 triangles with +-10% h interior jitter
+(seed 0), N = 4 (Np = 15), Roe flux, CFL 1, far-field exact-state BCs
+(--workload vortex256: 256 x 256 quads, 131,072 triangles).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -226,6 +227,24 @@ def cpu_baseline(wl, mesh, seconds, steps=None, warmup=0, max_steps=200):
                 sample=f"{done} full SSP-RK steps of the same {ora.K}-element N={wl['N']} workload")
 
 
+# --------------------------------------------------------------------------- ranks
+def max_over_ranks(x: float, world: int, device: str = "cpu") -> float:
+    """The slowest rank's time: all-reduce(max) of x over the process group."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(world: int, units_per_rank: float, seconds: float) -> float:
+    """Whole-job rate of independent replicas: every rank processed units_per_rank
+    in at most `seconds` (the max over ranks)."""
+    return world * units_per_rank / seconds
+
+
 # --------------------------------------------------------------------------- GPU arm
 def run_ours(a, world, rank, local):
     import torch
@@ -271,11 +290,8 @@ def run_ours(a, world, rank, local):
     ms = float(sum(s.elapsed_time(e) for s, e in evs))
     info = solver.step(0)  # raises on a non-finite state
     clk = clocks.summary(t_wall0, t_wall1)
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * dof_per_step * a.steps / (ms / 1e3)
+    ms = max_over_ranks(ms, world, f"cuda:{local}")
+    value = aggregate_rate(world, dof_per_step * a.steps, ms / 1e3)
     nBC_mesh = 4 * wl["n"]
     launches_per_step = 2 + 5 * (3 if a.precision == "fp64" else (2 + (nBC_mesh > 0)))
 
@@ -405,12 +421,9 @@ def run_ours(a, world, rank, local):
         _lib.check(lib, solver.ctx, lib.gcfd_get_state(solver.ctx, 1, km.ctypes.data_as(_lib.PI), ptrs))
     e2e_s = time.perf_counter() - t0
     barrier()
-    if world > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, world, f"cuda:{local}")
     state_bytes = 4 * Np * K * 8
-    e2e = {"value": world * dof_per_step * a.e2e_steps / e2e_s, "unit": UNIT,
+    e2e = {"value": aggregate_rate(world, dof_per_step * a.e2e_steps, e2e_s), "unit": UNIT,
            "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes,
            "steps": a.e2e_steps, "api": "gcfd_set_state + gcfd_step + gcfd_get_state, pinned host shards"}
     clocks.stop()

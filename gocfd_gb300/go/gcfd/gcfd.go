@@ -28,6 +28,14 @@ import (
 const (
 	PrecFP64 = int(C.GCFD_PREC_FP64) // the drop-in
 	PrecFP32 = int(C.GCFD_PREC_FP32) // delta-form FP32 arithmetic, compensated state
+	PrecTF32x3 = int(C.GCFD_PREC_TF32X3) // the same with the divergence GEMM on the tensor cores
+)
+
+// Functionals for the adjoint (GCFD_FUNC_*).
+const (
+	FuncWallForceX  = int(C.GCFD_FUNC_WALL_FORCE_X)
+	FuncWallForceY  = int(C.GCFD_FUNC_WALL_FORCE_Y)
+	FuncVortexError = int(C.GCFD_FUNC_VORTEX_ERROR)
 )
 
 // Params mirrors InputParameters.InputParameters2D plus the arithmetic mode.
@@ -178,4 +186,80 @@ func (c *Context) RHS(t float64, Q, RHS [][4][]float64, Kmax []int) error {
 		kmS[i] = C.int32_t(k)
 	}
 	return status(c.ctx, C.gcfd_rhs(c.ctx, C.double(t), C.int32_t(len(Q)), km, tq, tr))
+}
+
+// kmaxTable fills the C shard-size table that shardTable allocated.
+func kmaxTable(km *C.int32_t, Kmax []int) {
+	kmS := unsafe.Slice(km, len(Kmax))
+	for i, k := range Kmax {
+		kmS[i] = C.int32_t(k)
+	}
+}
+
+// Forward records nsteps steps (Step semantics) with a checkpoint every
+// `every` steps, for a following Backward.
+func (c *Context) Forward(nsteps, every int) (time, dt float64, err error) {
+	var t, d C.double
+	err = status(c.ctx, C.gcfd_record_steps(c.ctx, C.int32_t(nsteps), C.int32_t(every), &t, &d))
+	return float64(t), float64(d), err
+}
+
+// Functional evaluates J on the current state and, with Qbar non-nil, writes
+// dJ/dQ into the shards and returns dJ/dtime.
+func (c *Context) Functional(kind int, Qbar [][4][]float64, Kmax []int) (J, tbar float64, err error) {
+	var j, tb C.double
+	if Qbar == nil {
+		err = status(c.ctx, C.gcfd_functional(c.ctx, C.int32_t(kind), &j, 0, nil, nil, &tb))
+		return float64(j), float64(tb), err
+	}
+	var pin runtime.Pinner
+	defer pin.Unpin()
+	tab, km, free := shardTable(&pin, Qbar)
+	defer free()
+	kmaxTable(km, Kmax)
+	err = status(c.ctx, C.gcfd_functional(c.ctx, C.int32_t(kind), &j, C.int32_t(len(Qbar)), km, tab, &tb))
+	return float64(j), float64(tb), err
+}
+
+// Backward runs the adjoint of the recorded window: from the adjoint of the
+// final state (and time) to that of the initial state, the far-field Qinf and
+// the initial time.
+func (c *Context) Backward(QfinalBar [][4][]float64, tfinalBar float64, Q0Bar [][4][]float64, Kmax []int) (
+	qinfBar [4]float64, t0Bar float64, err error) {
+	var pin runtime.Pinner
+	defer pin.Unpin()
+	tf, km, freeF := shardTable(&pin, QfinalBar)
+	defer freeF()
+	t0, _, free0 := shardTable(&pin, Q0Bar)
+	defer free0()
+	kmaxTable(km, Kmax)
+	var qb [4]C.double
+	var tb C.double
+	err = status(c.ctx, C.gcfd_step_vjp(c.ctx, C.int32_t(len(QfinalBar)), km, tf, C.double(tfinalBar), t0,
+		&qb[0], &tb))
+	for i := range qb {
+		qinfBar[i] = float64(qb[i])
+	}
+	return qinfBar, float64(tb), err
+}
+
+// RHSBackward is the adjoint of RHS at (Q, t): Qbar = (dRHS/dQ)^T RHSbar.
+func (c *Context) RHSBackward(t float64, Q, RHSbar, Qbar [][4][]float64, Kmax []int) (qinfBar [4]float64,
+	tbar float64, err error) {
+	var pin runtime.Pinner
+	defer pin.Unpin()
+	tq, km, freeQ := shardTable(&pin, Q)
+	defer freeQ()
+	tr, _, freeR := shardTable(&pin, RHSbar)
+	defer freeR()
+	tb, _, freeB := shardTable(&pin, Qbar)
+	defer freeB()
+	kmaxTable(km, Kmax)
+	var qb [4]C.double
+	var tt C.double
+	err = status(c.ctx, C.gcfd_rhs_vjp(c.ctx, C.double(t), C.int32_t(len(Q)), km, tq, tr, tb, &qb[0], &tt))
+	for i := range qb {
+		qinfBar[i] = float64(qb[i])
+	}
+	return qinfBar, float64(tt), err
 }
