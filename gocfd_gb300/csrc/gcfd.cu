@@ -19,6 +19,7 @@
 #include "gcfd_mixed_tc.cuh"
 #include "gcfd_diss.cuh"
 #include "gcfd_adjoint.cuh"
+#include "gcfd_adjoint_diss.cuh"
 #include "mesh.hpp"
 
 using namespace gcfd;
@@ -143,9 +144,19 @@ struct gcfd_ctx {
   double* adjS = nullptr;      // [0,5) dt adjoints, [5,9) Qinf adjoint, [9] t-bar current, [10] t-bar next, [11] J
   int* argEdge = nullptr;      // [5]
   double *dXs = nullptr, *dYs = nullptr, *edgeW = nullptr;
+  // adjoint of the dissipation
+  double* tapeQ2pre = nullptr;
+  double* tapeDTV[5] = {};
+  double* tapeVS[5] = {};
+  double* tapeRHSpre[5] = {};
+  double *sigE = nullptr, *epsE = nullptr, *SeE = nullptr, *alphaBar = nullptr, *carryV = nullptr;
+  double *sigVbar = nullptr, *epsVbar = nullptr, *VFbar = nullptr, *DissXbar = nullptr, *DissYbar = nullptr;
+  double *RbE = nullptr, *vsBar = nullptr;
+  int *sigArg = nullptr, *epsArg = nullptr, *argVisc = nullptr;
   int winSteps = 0, winEvery = 1;
   std::vector<void*> winAllocs;
   double *ckpt = nullptr, *ckptT = nullptr, *segQ = nullptr, *segT = nullptr, *endQ = nullptr;
+  double *ckptV = nullptr, *segV = nullptr, *endV = nullptr;  // DTVisc (dissipation), K per entry
   Scalars* endSc = nullptr;
   std::vector<int> edgeOrder;             // device edge i -> topology edge
   std::vector<double> hnx, hny, hoohK;    // per device edge
@@ -283,6 +294,7 @@ struct Launch {
     a.DTVisc = c->DTVisc;
     a.cdiff = 1.0 / (double(c->N + 1) * double(c->N + 1));
     a.tapeRHS = nullptr;
+    a.tapeRHSpre = nullptr;
     return a;
   }
   static DissArgs diss_args(gcfd_ctx* c, int stage, double* Qs) {
@@ -329,6 +341,7 @@ struct Launch {
     a.eps0 = 5.0 / 1.5;
     a.S0 = 4.0 / std::pow(double(c->N + 1), 4.0);
     a.omega = double(c->N * c->N);
+    a.sigE = a.epsE = a.SeE = nullptr;
     return a;
   }
   static int grid(int n) { return (n + 127) / 128; }
@@ -595,28 +608,49 @@ struct AdjLaunch {
   }
   // Forward step with the tape: the same launches as L::step (so the states
   // are bit-identical to the recorded trajectory), plus per-stage copies of
-  // the edge speeds and local dt, and the stage RHS written by k_div_update.
+  // the edge speeds, local dt and faces, the stage RHS written by the update
+  // kernel, and with the dissipation the rkStep-2 state before the limiter,
+  // DTVisc before each stage, the viscous speeds and the pre-filter RHS.
   static void tape_step(gcfd_ctx* c) {
     cudaMemcpyAsync(c->tapeSc0, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream);
     k_step_begin<<<1, 32, 0, c->stream>>>(c->sc);
     void* faces = c->QF;
+    const size_t SB = sizeof(double) * 4 * c->Np * static_cast<size_t>(c->K);
     for (int s = 0; s < 5; ++s) {
       c->QF = c->tapeQF[s];  // the stage's faces stay on the tape
-      L::interp(c, c->Q[s]);
+      if (c->diss) {
+        if (s == 2) cudaMemcpyAsync(c->tapeQ2pre, c->Q[2], SB, cudaMemcpyDeviceToDevice, c->stream);
+        cudaMemcpyAsync(c->tapeDTV[s], c->DTVisc, sizeof(double) * c->K, cudaMemcpyDeviceToDevice, c->stream);
+        L::diss_front(c, s, c->Q[s]);
+      } else {
+        L::interp(c, c->Q[s]);
+      }
       L::edge(c, &c->sc->time, &c->sc->gmax[s]);
+      if (c->diss) {
+        L::diss_middle(c, s, c->Q[s]);
+        cudaMemcpyAsync(c->tapeVS[s], c->viscSpeed, sizeof(double) * c->nEdges, cudaMemcpyDeviceToDevice,
+                        c->stream);
+      }
       c->QF = faces;
       cudaMemcpyAsync(c->tapeES[s], c->edgeSpeed, sizeof(double) * c->nEdges, cudaMemcpyDeviceToDevice,
                       c->stream);
-      UpdateArgs<double> u = L::update_args(c, s, c->Q[s]);
-      u.tapeRHS = c->tapeRHS[s];
-      k_div_update<N, double><<<grid(c->K), 128, 0, c->stream>>>(u);
+      if (c->diss) {
+        k_div_update<N, double><<<grid(c->K), 128, 0, c->stream>>>(L::update_args(c, -1, c->Q[s]));
+        UpdateArgs<double> u = L::update_args(c, s, c->Q[s]);
+        u.tapeRHS = c->tapeRHS[s];
+        u.tapeRHSpre = c->tapeRHSpre[s];
+        k_diss_update<N><<<grid(c->K), 128, 0, c->stream>>>(u);
+      } else {
+        UpdateArgs<double> u = L::update_args(c, s, c->Q[s]);
+        u.tapeRHS = c->tapeRHS[s];
+        k_div_update<N, double><<<grid(c->K), 128, 0, c->stream>>>(u);
+      }
       if (c->prm.local_time_stepping)
         cudaMemcpyAsync(c->tapeDT[s], c->DT, sizeof(double) * c->K, cudaMemcpyDeviceToDevice, c->stream);
     }
     k_step_end<<<1, 32, 0, c->stream>>>(c->sc, c->prm.local_time_stepping);
     cudaMemcpyAsync(c->tapeSc, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream);
   }
-  // The reverse of stage s.  Q0 is the step's initial state.
   static void edges(gcfd_ctx* c, const EdgeArgs<double>& e, const AdjEdgeArgs& x) {
     if (c->nInt > 0) {
       if (e.flux == kFluxRoe && x.useManualRoe)
@@ -626,16 +660,84 @@ struct AdjLaunch {
     }
     if (c->nBC > 0) k_adj_edge_bc<N><<<grid(c->nBC * Dims<N>::NE), 128, 0, c->stream>>>(e, x);
   }
+  static AdjDissArgs adj_diss_args(gcfd_ctx* c, const double* Qsens, int s) {
+    AdjDissArgs x;
+    x.nverts = c->nverts;
+    x.Qsens = Qsens;
+    x.rhsPre = c->tapeRHSpre[s < 0 ? 0 : s];
+    x.RbE = c->RbE;
+    x.alphaBar = c->alphaBar;
+    x.sigVbar = c->sigVbar;
+    x.epsVbar = c->epsVbar;
+    x.VFbar = c->VFbar;
+    x.DissXbar = c->DissXbar;
+    x.DissYbar = c->DissYbar;
+    x.QFb = c->QFb;
+    x.vsBar = c->vsBar;
+    x.sigArg = c->sigArg;
+    x.epsArg = c->epsArg;
+    x.sigE = c->sigE;
+    x.SeE = c->SeE;
+    x.Q2pre = c->tapeQ2pre;
+    x.Qlim = c->Qb[2];
+    return x;
+  }
+  // Dissipation, reverse, part 1 (before the Euler part): recompute the
+  // stage's sensor and vertex maxima, then the update / filter / AddDissipation
+  // adjoint; the Euler RHS adjoint is left in RbE.
+  static void diss_reverse_update(gcfd_ctx* c, int s, const double* Qs, const double* Qsens, const double* Qbn,
+                                  double* Qbs, const double* faces) {
+    cudaMemsetAsync(c->sigV, 0, sizeof(unsigned long long) * c->nverts, c->stream);
+    cudaMemsetAsync(c->epsV, 0, sizeof(unsigned long long) * c->nverts, c->stream);
+    DissArgs d = L::diss_args(c, s, const_cast<double*>(Qsens));
+    d.sigE = c->sigE;
+    d.epsE = c->epsE;
+    d.SeE = c->SeE;
+    k_diss_sensor<N><<<grid(c->K), 128, 0, c->stream>>>(d);
+    cudaMemsetAsync(c->sigArg, 0x7f, sizeof(int) * c->nverts, c->stream);
+    cudaMemsetAsync(c->epsArg, 0x7f, sizeof(int) * c->nverts, c->stream);
+    k_diss_argmax<<<grid(c->K), 128, 0, c->stream>>>(d, c->sigE, c->epsE, c->sigArg, c->epsArg);
+    cudaMemsetAsync(c->sigVbar, 0, sizeof(double) * c->nverts, c->stream);
+    cudaMemsetAsync(c->epsVbar, 0, sizeof(double) * c->nverts, c->stream);
+    cudaMemsetAsync(c->VFbar, 0, sizeof(double) * (c->nInt + c->nBC) * 4 * c->NE, c->stream);
+    d.Qs = Qs;
+    d.QF = const_cast<double*>(faces);
+    k_adj_diss_update<N><<<grid(c->K), 128, 0, c->stream>>>(d, adj_args(c, s, Qs, Qbn, Qbs),
+                                                             adj_diss_args(c, Qsens, s));
+  }
+  // Dissipation, reverse, part 2 (after the Euler edge and speed adjoints):
+  // viscous edges, gradient, face transpose, limiter (rkStep 2), sensor.
+  static void diss_reverse_rest(gcfd_ctx* c, int s, const double* Qs, const double* Qsens, double* Qbs,
+                                const double* faces) {
+    DissArgs d = L::diss_args(c, s, const_cast<double*>(Qs));
+    d.QF = const_cast<double*>(faces);
+    const AdjDissArgs x = adj_diss_args(c, Qsens, s);
+    k_adj_diss_edge<N><<<grid(c->nInt + c->nBC), 128, 0, c->stream>>>(d, x);
+    constexpr int NF = Dims<N>::NF;
+    k_adj_diss_grad<N><<<grid(c->K), 128, sizeof(double) * (NF * NF + NF * 3), c->stream>>>(d, x, Qbs);
+    k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, Qbs, c->K);
+    if (s == 2) k_adj_diss_limit<N><<<grid(4 * c->K), 128, 0, c->stream>>>(d, x);
+    k_adj_diss_alpha<<<grid(c->K), 128, 0, c->stream>>>(d, x);
+    k_adj_diss_sensor<N><<<grid(c->K), 128, 0, c->stream>>>(d, x, Qbs);
+  }
+  // The reverse of stage s.  Q0 is the step's initial state.
   static void reverse_stage(gcfd_ctx* c, int s, const double* Q0) {
     const double* Qs = (s == 0) ? Q0 : c->Q[s];
     const double* Qbn = (s == 4) ? c->Qbf : c->Qb[s + 1];
-    k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, s, Qs, Qbn, c->Qb[s]));
+    const double* Qsens = (s == 2) ? c->tapeQ2pre : Qs;
+    if (c->diss) {
+      diss_reverse_update(c, s, Qs, Qsens, Qbn, c->Qb[s], c->tapeQF[s]);
+      k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, -1, Qs, c->RbE, c->Qb[s]));
+    } else {
+      k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, s, Qs, Qbn, c->Qb[s]));
+    }
     EdgeArgs<double> e = edge_args(c, &c->tapeSc0->time);
     e.QF = c->tapeQF[s];
     const AdjEdgeArgs x = adj_edge_args(c);
     const int nE = c->nInt + c->nBC;
     edges(c, e, x);
     cudaMemsetAsync(c->esBar, 0, sizeof(double) * nE, c->stream);
+    if (c->diss) cudaMemsetAsync(c->vsBar, 0, sizeof(double) * nE, c->stream);
     AdjDtArgs d;
     d.K = c->K;
     d.stage = s;
@@ -654,22 +756,38 @@ struct AdjLaunch {
     d.elemEdge = c->elemEdge;
     d.dtOwnK = c->dtOwnK;
     d.carry = c->carry;
+    d.diss = c->diss ? 1 : 0;
+    d.cdiff = 1.0 / (double(c->N + 1) * double(c->N + 1));
+    d.gviscS = reinterpret_cast<const double*>(c->tapeSc->gvisc);
+    d.argVisc = c->argVisc + s;
+    d.vsBar = c->vsBar;
+    d.dtvPrev = c->diss ? c->tapeDTV[s] : nullptr;
+    d.viscSpeed = c->diss ? c->tapeVS[s] : nullptr;
+    d.carryV = c->carryV;
     if (c->prm.local_time_stepping) {
       k_adj_lts<<<grid(c->K), 128, 0, c->stream>>>(d);
     } else {
       cudaMemsetAsync(c->argEdge + s, 0x7f, sizeof(int), c->stream);
       k_adj_argmax<<<grid(nE), 128, 0, c->stream>>>(c->tapeES[s], d.gmaxS, s, nE, c->argEdge + s);
+      if (c->diss) {
+        cudaMemsetAsync(c->argVisc + s, 0x7f, sizeof(int), c->stream);
+        k_adj_argmax<<<grid(nE), 128, 0, c->stream>>>(c->tapeVS[s], d.gviscS, s, nE, c->argVisc + s);
+      }
       k_adj_gsel<<<1, 32, 0, c->stream>>>(d);
     }
     k_adj_speed<N><<<grid(nE), 128, 0, c->stream>>>(e, x);
-    k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[s], c->K);
+    if (c->diss)
+      diss_reverse_rest(c, s, Qs, Qsens, c->Qb[s], c->tapeQF[s]);
+    else
+      k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[s], c->K);
   }
   // Adjoint of one step whose initial state is Q0 (already in c->Q[0]) and
   // time is in c->sc.  In: Qbf, adjS[10] (t-bar of the step's end).  Out:
-  // Qbf <- adjoint of Q0, adjS[10] <- t-bar of the step's start.
+  // Qbf <- adjoint of Q0, adjS[10] <- t-bar of the step's start.  carryV (the
+  // DTVisc adjoint) runs on across steps.
   static void reverse_step(gcfd_ctx* c, const double* Q0) {
     tape_step(c);
-    // no zeroing of the stage adjoints: k_adj_div's first write to each is a store
+    // no zeroing of the stage adjoints: the first write to each is a store
     cudaMemsetAsync(c->adjS, 0, sizeof(double) * 5, c->stream);
     cudaMemcpyAsync(c->adjS + 9, c->adjS + 10, sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
     cudaMemsetAsync(c->carry, 0, sizeof(double) * c->K, c->stream);
@@ -679,13 +797,36 @@ struct AdjLaunch {
   }
   // RHS adjoint at c->Qtmp and sc->rhs_time: Qb[0] <- J^T Qbf.
   static void rhs_vjp(gcfd_ctx* c) {
-    L::interp(c, c->Qtmp);
     const size_t S = sizeof(double) * 4 * c->Np * static_cast<size_t>(c->K);
+    void* faces = c->QF;
+    if (c->diss) {  // the forward RHS once more, keeping the pre-filter RHS
+      c->QF = c->tapeQF[0];
+      L::diss_front(c, -1, c->Qtmp);
+      L::edge(c, &c->sc->rhs_time, &c->sc->gmax[0]);
+      L::diss_middle(c, -1, c->Qtmp);
+      k_div_update<N, double><<<grid(c->K), 128, 0, c->stream>>>(L::update_args(c, -1, c->Qtmp));
+      UpdateArgs<double> u = L::update_args(c, -1, c->Qtmp);
+      u.tapeRHSpre = c->tapeRHSpre[0];
+      k_diss_update<N><<<grid(c->K), 128, 0, c->stream>>>(u);
+    } else {
+      L::interp(c, c->Qtmp);
+    }
     cudaMemsetAsync(c->Qb[0], 0, S, c->stream);
-    k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, -1, c->Qtmp, c->Qbf, c->Qb[0]));
     const EdgeArgs<double> e = edge_args(c, &c->sc->rhs_time);
+    if (c->diss) {
+      diss_reverse_update(c, -1, c->Qtmp, c->Qtmp, c->Qbf, c->Qb[0], static_cast<const double*>(c->QF));
+      k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, -1, c->Qtmp, c->RbE, c->Qb[0]));
+    } else {
+      k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, -1, c->Qtmp, c->Qbf, c->Qb[0]));
+    }
     edges(c, e, adj_edge_args(c));
-    k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[0], c->K);
+    if (c->diss) {
+      cudaMemsetAsync(c->vsBar, 0, sizeof(double) * (c->nInt + c->nBC), c->stream);
+      diss_reverse_rest(c, -1, c->Qtmp, c->Qtmp, c->Qb[0], static_cast<const double*>(c->QF));
+      c->QF = faces;
+    } else {
+      k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[0], c->K);
+    }
   }
   // Functionals of the current state Q[0]: J into adjS[11], dJ/dQ into Qb[0],
   // dJ/dt into adjS[9].
@@ -1409,7 +1550,6 @@ namespace {
 
 int adj_check(gcfd_ctx* c) {
   if (c->fp32) return fail(c, GCFD_ERR_UNSUPPORTED, "the adjoint runs on the FP64 path only");
-  if (c->diss) return fail(c, GCFD_ERR_UNSUPPORTED, "the adjoint does not cover the PerssonC0 dissipation");
   return GCFD_OK;
 }
 
@@ -1492,6 +1632,27 @@ int adj_init(gcfd_ctx* c) {
   if ((rc = dalloc(c, &c->dtOwnK, static_cast<size_t>(c->K)))) return rc;
   if ((rc = dalloc(c, &c->esBar, static_cast<size_t>(nE)))) return rc;
   if ((rc = dalloc(c, &c->argEdge, 8))) return rc;
+  if (c->diss) {
+    const size_t NR = static_cast<size_t>(c->Np) + 3 * c->NE;
+    if ((rc = dalloc(c, &c->tapeQ2pre, S))) return rc;
+    for (int s = 0; s < 5; ++s) {
+      if ((rc = dalloc(c, &c->tapeDTV[s], static_cast<size_t>(c->K)))) return rc;
+      if ((rc = dalloc(c, &c->tapeVS[s], static_cast<size_t>(nE)))) return rc;
+      if ((rc = dalloc(c, &c->tapeRHSpre[s], S))) return rc;
+    }
+    for (double** p : {&c->sigE, &c->epsE, &c->SeE, &c->alphaBar, &c->carryV})
+      if ((rc = dalloc(c, p, static_cast<size_t>(c->K)))) return rc;
+    if ((rc = dalloc(c, &c->sigVbar, static_cast<size_t>(c->nverts)))) return rc;
+    if ((rc = dalloc(c, &c->epsVbar, static_cast<size_t>(c->nverts)))) return rc;
+    if ((rc = dalloc(c, &c->VFbar, static_cast<size_t>(nE) * 4 * c->NE))) return rc;
+    if ((rc = dalloc(c, &c->DissXbar, 4 * NR * c->K))) return rc;
+    if ((rc = dalloc(c, &c->DissYbar, 4 * NR * c->K))) return rc;
+    if ((rc = dalloc(c, &c->RbE, S))) return rc;
+    if ((rc = dalloc(c, &c->vsBar, static_cast<size_t>(nE)))) return rc;
+    if ((rc = dalloc(c, &c->sigArg, static_cast<size_t>(c->nverts)))) return rc;
+    if ((rc = dalloc(c, &c->epsArg, static_cast<size_t>(c->nverts)))) return rc;
+    if ((rc = dalloc(c, &c->argVisc, 8))) return rc;
+  }
   c->adjReady = true;
   return GCFD_OK;
 }
@@ -1574,6 +1735,12 @@ int gcfd_record_steps(gcfd_ctx* c, int32_t nsteps, int32_t every, double* time, 
   if ((rc = win_alloc(c, &c->segQ, S * std::min(every, nsteps)))) return rc;
   if ((rc = win_alloc(c, &c->segT, static_cast<size_t>(std::min(every, nsteps))))) return rc;
   if ((rc = win_alloc(c, &c->endQ, S))) return rc;
+  const size_t KV = c->diss ? static_cast<size_t>(c->K) : 0;  // DTVisc persists across steps
+  if (c->diss) {
+    if ((rc = win_alloc(c, &c->ckptV, KV * nck))) return rc;
+    if ((rc = win_alloc(c, &c->segV, KV * std::min(every, nsteps)))) return rc;
+    if ((rc = win_alloc(c, &c->endV, KV))) return rc;
+  }
   double* sc = nullptr;
   if ((rc = win_alloc(c, &sc, (sizeof(Scalars) + 7) / 8))) return rc;
   c->endSc = reinterpret_cast<Scalars*>(sc);
@@ -1584,10 +1751,15 @@ int gcfd_record_steps(gcfd_ctx* c, int32_t nsteps, int32_t every, double* time, 
                                    c->stream));
       GCFD_CUDA(c, cudaMemcpyAsync(c->ckptT + j, &c->sc->time, sizeof(double), cudaMemcpyDeviceToDevice,
                                    c->stream));
+      if (c->diss)
+        GCFD_CUDA(c, cudaMemcpyAsync(c->ckptV + KV * j, c->DTVisc, KV * sizeof(double), cudaMemcpyDeviceToDevice,
+                                     c->stream));
     }
     GCFD_CUDA(c, cudaGraphLaunch(c->graphExec, c->stream));
   }
   GCFD_CUDA(c, cudaMemcpyAsync(c->endQ, c->Q[0], S * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  if (c->diss)
+    GCFD_CUDA(c, cudaMemcpyAsync(c->endV, c->DTVisc, KV * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
   GCFD_CUDA(c, cudaMemcpyAsync(c->endSc, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream));
   Scalars h;
   GCFD_CUDA(c, cudaMemcpyAsync(&h, c->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
@@ -1613,6 +1785,8 @@ int gcfd_step_vjp(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doubl
   if ((rc = copy_shards(c, c->Qbf, nshards, Kmax, Qfinal_bar, true, nullptr))) return rc;
   GCFD_CUDA(c, cudaMemsetAsync(c->adjS, 0, sizeof(double) * 12, c->stream));
   GCFD_CUDA(c, cudaMemcpyAsync(c->adjS + 10, &tfinal_bar, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  const size_t KV = c->diss ? static_cast<size_t>(c->K) : 0;
+  if (c->diss) GCFD_CUDA(c, cudaMemsetAsync(c->carryV, 0, KV * sizeof(double), c->stream));
   const int every = c->winEvery, nsteps = c->winSteps;
   const int nseg = (nsteps + every - 1) / every;
   for (int seg = nseg - 1; seg >= 0; --seg) {
@@ -1620,16 +1794,25 @@ int gcfd_step_vjp(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doubl
     GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], c->ckpt + S * seg, SB, cudaMemcpyDeviceToDevice, c->stream));
     GCFD_CUDA(c, cudaMemcpyAsync(&c->sc->time, c->ckptT + seg, sizeof(double), cudaMemcpyDeviceToDevice,
                                  c->stream));
+    if (c->diss)
+      GCFD_CUDA(c, cudaMemcpyAsync(c->DTVisc, c->ckptV + KV * seg, KV * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   c->stream));
     for (int i = 0; i < m; ++i) {
       GCFD_CUDA(c, cudaMemcpyAsync(c->segQ + S * i, c->Q[0], SB, cudaMemcpyDeviceToDevice, c->stream));
       GCFD_CUDA(c, cudaMemcpyAsync(c->segT + i, &c->sc->time, sizeof(double), cudaMemcpyDeviceToDevice,
                                    c->stream));
+      if (c->diss)
+        GCFD_CUDA(c, cudaMemcpyAsync(c->segV + KV * i, c->DTVisc, KV * sizeof(double), cudaMemcpyDeviceToDevice,
+                                     c->stream));
       if (i + 1 < m) GCFD_CUDA(c, cudaGraphLaunch(c->graphExec, c->stream));
     }
     for (int i = m - 1; i >= 0; --i) {
       GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], c->segQ + S * i, SB, cudaMemcpyDeviceToDevice, c->stream));
       GCFD_CUDA(c, cudaMemcpyAsync(&c->sc->time, c->segT + i, sizeof(double), cudaMemcpyDeviceToDevice,
                                    c->stream));
+      if (c->diss)
+        GCFD_CUDA(c, cudaMemcpyAsync(c->DTVisc, c->segV + KV * i, KV * sizeof(double), cudaMemcpyDeviceToDevice,
+                                     c->stream));
       o.reverse_step(c, c->segQ + S * i);
       GCFD_CUDA(c, cudaGetLastError());
     }
@@ -1640,6 +1823,8 @@ int gcfd_step_vjp(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doubl
   // back to the window's end
   GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], c->endQ, SB, cudaMemcpyDeviceToDevice, c->stream));
   GCFD_CUDA(c, cudaMemcpyAsync(c->sc, c->endSc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream));
+  if (c->diss)
+    GCFD_CUDA(c, cudaMemcpyAsync(c->DTVisc, c->endV, KV * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
   GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
   if (qinf_bar4)
     for (int i = 0; i < 4; ++i) qinf_bar4[i] = h[i];

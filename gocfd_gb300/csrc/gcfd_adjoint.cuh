@@ -525,6 +525,15 @@ struct AdjDtArgs {
   const int* elemEdge;     // [3][K]
   const double* dtOwnK;
   double* carry;           // [K]: adjoint carried to the previous stage's dt
+  // viscous limit of the PerssonC0 dissipation (diss != 0)
+  int diss;
+  double cdiff;            // 1 / (N + 1)^2
+  const double* gviscS;    // taped per-stage max viscous speed [5]
+  const int* argVisc;      // global: the edge that set it
+  double* vsBar;           // per edge: adjoint of the viscous speed
+  const double* dtvPrev;   // local: taped DTVisc before this stage [K]
+  const double* viscSpeed; // local: taped viscous speeds of this stage
+  double* carryV;          // [K]: adjoint of DTVisc carried to the previous stage (and step)
 };
 
 // Global: dt = min-clip(CFL / gmax) (calculateGlobalDT, euler.go:945-971).
@@ -534,9 +543,16 @@ __global__ void k_adj_gsel(AdjDtArgs a) {
   double dtb = a.dtbarG[s];
   if (s == 4) dtb += *a.tbarNext;  // Time += GlobalDT of the last stage
   const double gm = a.gmaxS[s];
-  const double dtU = a.cfl / gm;
+  const double dtC = a.cfl / gm;
+  const double gv = a.diss ? a.gviscS[s] : 0.0;
+  const double dtV = a.diss ? a.cdiff / gv : 0.0;
+  const bool visc = a.diss && fmin(dtC, dtV) == dtV && dtV < dtC;
+  const double dtU = a.diss ? fmin(dtC, dtV) : dtC;
   if (*a.tn + dtU > a.finalTime) {
     *a.tbarCur -= dtb;  // dt = FinalTime - t
+  } else if (visc) {
+    const int g = *a.argVisc;
+    if (g >= 0 && g < a.nEdges) a.vsBar[g] += -a.cdiff / (gv * gv) * dtb;
   } else {
     const int g = *a.argEdge;
     if (g >= 0 && g < a.nEdges) a.esBar[g] += -a.cfl / (gm * gm) * dtb;
@@ -559,7 +575,33 @@ __global__ void k_adj_lts(AdjDtArgs a) {
     const double w = a.edgeSpeed[eg[e]];
     if (w > v) { v = w; arg = e; }
   }
-  const double dtb = a.dtOwnK[k] + a.carry[k];
+  double dtb = a.dtOwnK[k] + a.carry[k];
+  if (a.diss) {
+    // dv = max(DTVisc, viscous speeds); DTVisc <- Cdiff / dv when dv > 1e-9, and
+    // dt = min(CFL / v, DTVisc) (CalculateLocalDT with the dissipation).
+    double dv = a.dtvPrev[k];
+    int argv = -1;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      const double w = a.viscSpeed[eg[e]];
+      if (w > dv) { dv = w; argv = e; }
+    }
+    double dvnb = a.carryV[k];
+    if (dv > 1.e-9) {
+      const double dvn = a.cdiff / dv;
+      if (dvn < a.cfl / v) {  // the viscous limit set dt
+        dvnb += dtb;
+        dtb = 0.0;
+      }
+      dvnb = -a.cdiff / (dv * dv) * dvnb;
+    }
+    if (argv < 0) {
+      a.carryV[k] = dvnb;
+    } else {
+      a.carryV[k] = 0.0;
+      if (dvnb != 0.0) atomicAdd(&a.vsBar[eg[argv]], dvnb);
+    }
+  }
   const double vb = -a.cfl / (v * v) * dtb;
   if (arg < 0) {
     a.carry[k] = (s == 0) ? 0.0 : vb;

@@ -58,6 +58,9 @@ struct DissArgs {
   double* viscSpeed;          // per edge
   unsigned long long* gvisc;  // per stage max viscous speed
   double kappa, eps0, S0, omega;
+  double* sigE;               // optional (adjoint recompute): element sigma, eps and Se
+  double* epsE;
+  double* SeE;
 };
 
 template <int N>
@@ -101,6 +104,11 @@ __global__ void __launch_bounds__(128) k_diss_sensor(DissArgs a) {
   else if (se >= left && se <= right) sigma = 0.5 * (1.0 + sin(3.14159265358979323846 * (0.5 / a.kappa) * (se - a.S0)));
   else if (se > right) sigma = 1.0;
   const double eps = a.eps0 * a.hK[k] * sigma;
+  if (a.sigE) {
+    a.sigE[k] = sigma;
+    a.epsE[k] = eps;
+    a.SeE[k] = se;
+  }
 #pragma unroll
   for (int v = 0; v < 3; ++v) {
     const int vert = a.etov[v * sK + k];
@@ -395,14 +403,20 @@ __global__ void __launch_bounds__(128) k_diss_update(UpdateArgs<double> a) {
       }
 #pragma unroll
       for (int r = 0; r < NP; ++r) u[r] = a.rhsOut[(n * NP + r) * sK + k] + oojd * u[r];
+      if (a.tapeRHSpre) {
+#pragma unroll
+        for (int r = 0; r < NP; ++r) a.tapeRHSpre[(n * NP + r) * sK + k] = u[r];
+      }
       limit_filter_modal<NP>(u, sV, sVi, smf, alpha);
       if (a.stage < 0) {
 #pragma unroll
         for (int r = 0; r < NP; ++r) a.rhsOut[(n * NP + r) * sK + k] = u[r];
       } else {
 #pragma unroll
-        for (int r = 0; r < NP; ++r)
+        for (int r = 0; r < NP; ++r) {
+          if (a.tapeRHS) a.tapeRHS[(n * NP + r) * sK + k] = u[r];
           ssp_stage_update(a, (n * NP + r) * sK + k, u[r], dtk, rloc_max[n], rloc_abs[n], rloc_s2[n]);
+        }
       }
     }
   }

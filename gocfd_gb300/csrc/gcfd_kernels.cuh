@@ -276,6 +276,7 @@ struct UpdateArgs {
   double* DTVisc;            // K, persistent (CalcElementMaxWaveSpeed never resets it)
   double cdiff;              // 1/(N+1)^2
   double* tapeRHS;           // when set, the stage's RHS is stored there (adjoint tape)
+  double* tapeRHSpre;        // k_diss_update: the RHS before the modal filter (adjoint tape)
 };
 
 __constant__ double kSSP[5][6] = {

@@ -347,3 +347,73 @@ def test_step_vjp_field_error_functional(center):
     fd = (Jat(1.0) - Jat(-1.0)) / 2e-6
     assert_close(float(np.sum(Qb0 * d)), fd)
     gpu.close()
+
+
+# ----------------------------------------------------------------------------- with PerssonC0
+def diss_pair(mesh, N, *, kappa=0.0, local_dt=False, cfl=0.5):
+    ip = InputParameters2D(CFL=cfl, FluxType="roe", InitType="shocktube", PolynomialOrder=N, FinalTime=1e9,
+                           Minf=0.5, Gamma=1.4, LocalTimeStepping=local_dt, MaxIterations=10 ** 9,
+                           Limiter="PerssonC0", Kappa=kappa)
+    gpu = Euler(ip, mesh, 1, precision="fp64")
+    ora = oracle.OracleSolver(N, mesh.VX, mesh.VY, mesh.EToV, mesh.bc_edges, flux="roe", init="shocktube",
+                              cfl=cfl, final_time=1e9, minf=0.5, local_dt=local_dt, limiter="PerssonC0",
+                              kappa=kappa)
+    return gpu, ora
+
+
+def smooth_tube(ora, width):
+    h = 0.5 * (1.0 + np.tanh((ora.geo.SolX - 0.5) / width))
+    Q = np.zeros((4,) + h.shape)
+    Q[0] = 1.0 + (0.125 - 1.0) * h
+    Q[3] = (1.0 + (0.1 - 1.0) * h) / 0.4
+    return Q
+
+
+@pytest.mark.parametrize("N,kappa", [(1, 0.0), (2, 0.0), (2, 3.0), (3, 0.0)])
+def test_rhs_vjp_with_dissipation(N, kappa):
+    mesh = meshes.sod_channel(25, 3)
+    gpu, ora = diss_pair(mesh, N, kappa=kappa)
+    rng = np.random.default_rng(20 + N)
+    Q = smooth_tube(ora, 0.02 if N == 1 else 0.008)
+    Q = np.ascontiguousarray(Q * (1.0 + 0.01 * rng.uniform(-1, 1, Q.shape)))
+    sig = ora.sensor(Q)[1]
+    assert ((sig > 0) & (sig < 1)).any()  # the ramp is live somewhere
+    Rb = rng.standard_normal(Q.shape)
+    d = rng.standard_normal(Q.shape) * np.abs(Q)
+    Qb, _, _ = gpu.rhs_vjp_global(Q, Rb)
+    ad = float(np.sum(Qb * d))
+    # The vertex maxima and the ramp's ends are kinks; a central difference
+    # that straddles one disagrees with the one-sided adjoint, so the check
+    # takes the best of three step sizes (a kink cannot sit inside all three).
+    errs = []
+    for h in (1e-6, 1e-7, 1e-8):
+        fd = (np.sum(Rb * ora.rhs(Q + h * d)) - np.sum(Rb * ora.rhs(Q - h * d))) / (2 * h)
+        errs.append(abs(ad - fd) / max(abs(ad), abs(fd)))
+    assert min(errs) <= FD_RTOL, errs
+    gpu.close()
+
+
+@pytest.mark.parametrize("N,local_dt", [(2, False), (2, True), (3, False)])
+def test_step_vjp_with_dissipation(N, local_dt):
+    mesh = meshes.sod_channel(24, 3)
+    gpu, ora = diss_pair(mesh, N, local_dt=local_dt)
+    rng = np.random.default_rng(30 + N)
+    Q0 = smooth_tube(ora, 0.01)
+    Q0 = np.ascontiguousarray(Q0 * (1.0 + 0.005 * rng.uniform(-1, 1, Q0.shape)))
+    nsteps = 4
+    gpu.set_global_state(Q0)
+    gpu.record(nsteps, 2)
+    Qbf = rng.standard_normal(Q0.shape)
+    Qb0, _, _ = gpu.step_vjp(Qbf)
+    d = rng.standard_normal(Q0.shape) * np.abs(Q0)
+
+    def J(sign, h=1e-7):
+        ora.Q = np.ascontiguousarray(Q0 + sign * h * d)
+        ora.time = 0.0
+        ora.DT[:] = 0.0
+        ora.DTVisc[:] = 0.0
+        ora.step(nsteps)
+        return float(np.sum(Qbf * ora.Q))
+    fd = (J(1.0) - J(-1.0)) / 2e-7
+    assert_close(float(np.sum(Qb0 * d)), fd)
+    gpu.close()
