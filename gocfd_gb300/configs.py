@@ -22,6 +22,8 @@ Run one:  python -m gocfd_gb300.configs --config sod2000x100 [--precision fp64] 
 (1000 mixed-precision steps, then the field-error adjoint through 200 FP64
 steps with a checkpoint every 10):
           python -m gocfd_gb300.configs --config vortex1024 --warm-steps 1000 --adjoint-steps 200
+The wedge's ramp-force sensitivity to Minf and the flow angle through 500 steps:
+          python -m gocfd_gb300.configs --config wedge512x256 --adjoint-steps 500 --fd-h 1e-6
 """
 import argparse
 import json
@@ -238,6 +240,51 @@ def adjoint(name: str, steps: int, every: int, warm_steps: int = 0, warm_precisi
     return out
 
 
+def wedge_sensitivity(steps: int = 500, every: int = 10, scale: float = 1.0, fd_h: float = 1e-6, device: int = 0):
+    """Ramp pressure force after `steps` local-dt steps from the freestream state,
+    and its derivatives with respect to the inflow Mach number and the flow
+    angle by the adjoint (recorded window, checkpoint every `every` steps),
+    against central differences of the FP64 forward at Minf +- h, alpha +- h.
+    The freestream enters both the far-field BC (Qinf adjoint) and the initial
+    state (its adjoint summed over the mesh): dQinf/dM = (0, cos a, sin a, M),
+    dQinf/da = (0, -M sin a, M cos a, 0) per radian (NewFreeStream, fluids.go:245-262)."""
+    cfg = CONFIGS["wedge512x256"]
+    mesh = build_mesh(cfg, scale)
+
+    def solver(minf, alpha_deg):
+        ip = input_params(cfg)
+        ip.Minf, ip.Alpha = minf, alpha_deg
+        return Euler(ip, mesh, 1, precision="fp64", device=device)
+
+    M, A = cfg.minf, 0.0
+    out = {"config": "wedge512x256", "scale": scale, "steps": steps, "checkpoint_every": every}
+    with solver(M, A) as s:
+        out["K"] = s.K
+        t0 = time.perf_counter()
+        s.record(steps, every)
+        t1 = time.perf_counter()
+        J, Qbf, _ = s.functional("wall_force_x")
+        Qb0, qinfb, _ = s.step_vjp(Qbf)
+        t2 = time.perf_counter()
+    a = math.radians(A)
+    dq_dM = np.array([0.0, math.cos(a), math.sin(a), M])
+    dq_da = np.array([0.0, -M * math.sin(a), M * math.cos(a), 0.0]) * (math.pi / 180.0)  # per degree
+    ic = Qb0.sum(axis=(1, 2))  # the initial state is Qinf at every point
+    out.update(J=J, dJ_dMinf=float(qinfb @ dq_dM + ic @ dq_dM), dJ_dalpha_deg=float(qinfb @ dq_da + ic @ dq_da),
+               record_s=t1 - t0, vjp_s=t2 - t1)
+
+    def J_at(minf, alpha_deg):
+        with solver(minf, alpha_deg) as s2:
+            s2.step(steps)
+            return s2.functional("wall_force_x")[0]
+    if fd_h > 0:
+        out["fd_dJ_dMinf"] = (J_at(M + fd_h, A) - J_at(M - fd_h, A)) / (2 * fd_h)
+        out["fd_dJ_dalpha_deg"] = (J_at(M, A + fd_h) - J_at(M, A - fd_h)) / (2 * fd_h)
+        out["rel_diff_Minf"] = abs(out["dJ_dMinf"] - out["fd_dJ_dMinf"]) / abs(out["fd_dJ_dMinf"])
+        out["rel_diff_alpha"] = abs(out["dJ_dalpha_deg"] - out["fd_dJ_dalpha_deg"]) / abs(out["fd_dJ_dalpha_deg"])
+    return out
+
+
 def main(argv=None):
     p = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     p.add_argument("--config", choices=sorted(CONFIGS), required=True)
@@ -251,7 +298,9 @@ def main(argv=None):
     p.add_argument("--warm-steps", type=int, default=0)
     p.add_argument("--fd-h", type=float, default=1e-8, help="central-difference step of the adjoint check (0: skip)")
     a = p.parse_args(argv)
-    if a.adjoint_steps:
+    if a.adjoint_steps and a.config.startswith("wedge"):
+        res = wedge_sensitivity(a.adjoint_steps, a.checkpoint_every, a.scale, fd_h=a.fd_h)
+    elif a.adjoint_steps:
         res = adjoint(a.config, a.adjoint_steps, a.checkpoint_every, a.warm_steps,
                       a.precision if a.precision != "fp64" else "fp32", fd_h=a.fd_h)
     else:

@@ -36,3 +36,11 @@ def test_wedge_reduced_march():
     out = configs.run("wedge512x256", scale=1 / 32, max_steps=300)   # 16 x 8 quads
     assert np.isfinite(out["residual_rel_rms"])
     assert out["ramp_force_x"] > 0.0   # the ramp pushes back on the flow: +x pressure force on the wall
+
+
+def test_wedge_force_sensitivities_reduced():
+    """dJ/dMinf and dJ/dalpha of the ramp force (PerssonC0, local dt) by the adjoint
+    against central differences of the FP64 forward."""
+    out = configs.wedge_sensitivity(steps=20, every=5, scale=1 / 32, fd_h=1e-5)
+    assert out["rel_diff_Minf"] <= 1e-6, out
+    assert out["rel_diff_alpha"] <= 1e-6, out
