@@ -17,6 +17,7 @@
 #include "gcfd_kernels.cuh"
 #include "gcfd_mixed.cuh"
 #include "gcfd_mixed_tc.cuh"
+#include "gcfd_mixed_diss.cuh"
 #include "gcfd_diss.cuh"
 #include "gcfd_adjoint.cuh"
 #include "gcfd_adjoint_diss.cuh"
@@ -480,6 +481,9 @@ struct MixedLaunch {
     a.rhsOut = c->rhsOut;
     a.Btc = c->mBtc;
     a.err = reinterpret_cast<unsigned int*>(&c->sc->errFlags);
+    a.rhsOnly = 0;
+    a.gviscS = nullptr;
+    a.cdiff = 0.0;
     return a;
   }
   static int gridE(gcfd_ctx* c) { return (c->K + 31) / 32; }
@@ -539,6 +543,10 @@ struct MixedLaunch {
     mark(1);
     acc(3, 0, 1);
     for (int s = 0; s < 5; ++s) {
+      if (c->diss) {  // dissipation: no per-family split
+        diss_stage(c, s);
+        continue;
+      }
       mark(2);
       edges(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s], ev == nullptr);
       mark(3);
@@ -554,8 +562,36 @@ struct MixedLaunch {
   }
   static void rhs(gcfd_ctx* c) {
     prepare(c, c->Qtmp);
+    if (c->diss) Launch<N, double>::diss_front(c, -1, c->Qtmp);
     edges(c, -1, c->Qtmp, &c->sc->rhs_time, &c->sc->gmax[0], false);
+    if (c->diss) Launch<N, double>::diss_middle(c, -1, c->Qtmp);
     stage_kernel(c, args(c, -1, c->Qtmp, &c->sc->rhs_time, &c->sc->gmax[0]));
+    if (c->diss)
+      k_mixed_diss_update<N><<<gridE(c), 128, 0, c->stream>>>(args(c, -1, c->Qtmp, &c->sc->rhs_time,
+                                                                    &c->sc->gmax[0]),
+                                                               Launch<N, double>::update_args(c, -1, c->Qtmp));
+  }
+  // One stage with the PerssonC0 dissipation: FP64 stage state for the
+  // dissipation kernels (Q[1] is free on the mixed path), the Euler RHS of the
+  // stage from the delta-form kernel, then the dissipated update.
+  static void diss_stage(gcfd_ctx* c, int s) {
+    using L = Launch<N, double>;
+    double* Qs64 = c->Q[1];
+    k_mixed_form_stage<N><<<gridE(c), 128, 0, c->stream>>>(args(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]),
+                                                           Qs64);
+    L::diss_front(c, s, Qs64);
+    if (s == 2)
+      k_mixed_relimit<N><<<gridE(c), 128, 0, c->stream>>>(args(c, 2, c->Q[0], &c->sc->time, &c->sc->gmax[2]),
+                                                          Qs64);
+    edges(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s], true);
+    L::diss_middle(c, s, Qs64);
+    MixedArgs m = args(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]);
+    m.rhsOnly = 1;
+    stage_kernel(c, m);
+    MixedArgs m2 = args(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]);
+    m2.gviscS = c->sc->gvisc;
+    m2.cdiff = 1.0 / (double(c->N + 1) * double(c->N + 1));
+    k_mixed_diss_update<N><<<gridE(c), 128, 0, c->stream>>>(m2, L::update_args(c, s, Qs64));
   }
   static void prep_state(gcfd_ctx* c) { prepare(c, c->Q[0]); }
 };
@@ -1163,8 +1199,6 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
   // the sensor ramp takes Kappa when given, else 5 (dissipation.go:140-147).
   c->diss = (p.limiter == GCFD_LIMITER_PERSSON_C0) && p.N > 0;
   c->dissKappa = (p.kappa != 0.0) ? p.kappa : 5.0;
-  if (c->diss && c->fp32)
-    return fail(c, GCFD_ERR_UNSUPPORTED, "PerssonC0 dissipation runs on the FP64 path only in this build");
   try {
     c->el = build_dfr_element(p.N);
   } catch (const std::exception& e) {
@@ -1266,8 +1300,13 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
     char* fe = nullptr;
     if ((rc = dalloc(c, &fe, nFace * tsz))) return rc;
     c->FE = fe;
-  } else if ((rc = build_mixed(c))) {
-    return rc;
+  } else {
+    if ((rc = build_mixed(c))) return rc;
+    if (c->diss) {  // the FP64 dissipation kernels need FP64 faces
+      double* qf = nullptr;
+      if ((rc = dalloc(c, &qf, nFace))) return rc;
+      c->QF = qf;
+    }
   }
   if (c->diss && (rc = build_diss(c, m))) return rc;
   if ((rc = upload(c, &c->Iop, c->el.FluxEdgeInterp.v))) return rc;

@@ -239,7 +239,10 @@ struct MixedArgs {
   double gammaD;
   FreeStreamT<double> fsFar, fsIn, fsOut;
   double vbeta, vx0, vy0, vgamma;
-  double* rhsOut;             // stage -1: RHS in FP64 [n][i][k]
+  double* rhsOut;             // stage -1 (or rhsOnly): RHS in FP64 [n][i][k]
+  int rhsOnly;                // write the RHS of stage `stage` to rhsOut instead of updating
+  const unsigned long long* gviscS;  // per-stage max viscous speed when the dissipation limits dt
+  double cdiff;
   const float* Btc;           // tensor-core path: DivInt split hi / lo in the shared-memory operand layout
   unsigned int* err;          // error flags (bit 0: a tensor-core wait ran out)
 };
@@ -513,6 +516,32 @@ __global__ void __launch_bounds__(8 * MixedDims<N>::NE) k_mixed_edge_bc(MixedArg
   }
 }
 
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
+}
+
+// L2 prefetch of what stage_tail will read: the compensated state at point 0
+// (stages 0-3), or the whole compensated state, the stage-2/3 increments and
+// the stage-3 RHS (stage 4).
+template <int N>
+__device__ __forceinline__ void stage_tail_prefetch(const MixedArgs& a, size_t off, size_t sK, int s) {
+  constexpr int NP = MixedDims<N>::NP;
+  if (s < 0) return;
+  if (s < 4) {
+    prefetch_l2(a.Qhi + off);
+    prefetch_l2(a.Qlo + off);
+    return;
+  }
+#pragma unroll
+  for (int r = 0; r < NP; ++r) {
+    prefetch_l2(a.Qhi + off + r * sK);
+    prefetch_l2(a.Qlo + off + r * sK);
+    prefetch_l2(a.D[2] + off + r * sK);
+    prefetch_l2(a.D[3] + off + r * sK);
+    prefetch_l2(a.R3 + off + r * sK);
+  }
+}
+
 // The stage update after the divergence (shared by the FMA and tensor-core
 // stage kernels): the RHS goes to rhsOut (stage -1) or into the SSP increments,
 // the next stage's faces and reference state, and at stage 4 the compensated
@@ -523,7 +552,7 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const float* sI, 
                                            const float ds[], double dtLocal, float& rmax, float& rabs,
                                            float& rs2) {
   constexpr int NP = MixedDims<N>::NP, NPP = MixedDims<N>::NPP;
-  if (s < 0) {
+  if (s < 0 || a.rhsOnly) {
 #pragma unroll
     for (int r = 0; r < NP; ++r) a.rhsOut[off + r * sK] = rhs[r];
   } else {
@@ -534,6 +563,7 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const float* sI, 
     } else {
       const double gm = __longlong_as_double(static_cast<long long>(a.sc->gmax[s]));
       dtk = a.cfl / gm;
+      if (a.gviscS) dtk = fmin(dtk, a.cdiff / __longlong_as_double(static_cast<long long>(a.gviscS[s])));
       const double t = a.sc->time;
       if (t + dtk > a.finalTime) dtk = a.finalTime - t;
       if (k == 0 && n == 0) a.sc->dt[s] = dtk;
@@ -643,6 +673,10 @@ __global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
     }
     asm volatile("cp.async.commit_group;\n" ::);
   }
+  // The stage update's own inputs are needed only at the end: prefetch them
+  // into L2 now so their DRAM latency overlaps the flux and divergence work
+  // (the kernel is bound by load latency, not bandwidth).
+  if (active) stage_tail_prefetch<N>(a, off, sK, s);
   // Stage input deltas relative to point 0 of the stage state.
   float dq0[NP], ds[NP];
   if (active) {
@@ -662,7 +696,7 @@ __global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
   // Local time step of this stage: DT persists across stages, so every thread
   // of the element reads it before the barrier and one writes it after.
   double dtLocal = 0.0;
-  if (active && a.localDT && s >= 0) {
+  if (active && a.localDT && s >= 0 && !a.rhsOnly) {
     double v = (s == 0) ? -100.0 : a.DT[k];
 #pragma unroll
     for (int e = 0; e < 3; ++e) v = fmax(v, a.edgeSpeed[eslot[e] >> 1]);
@@ -725,7 +759,7 @@ __global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
     for (int r = 0; r < NP; ++r) rhs[r] = -acc[r] * ooJ;
     stage_tail<N>(a, sI, eslot, n, k, off, sK, s, rhs, dq0, ds, dtLocal, rmax, rabs, rs2);
   }
-  if (s == 4) {
+  if (s == 4 && !a.rhsOnly) {
     const unsigned long long km = warp_max_u64(order_key(static_cast<double>(rmax)));
     const double am = warp_max(static_cast<double>(rabs));
     const double s2 = warp_sum(static_cast<double>(rs2));

@@ -1,0 +1,170 @@
+// PerssonC0 shock capturing on the mixed path: the Euler RHS stays in the
+// FP32 delta form (k_mixed_stage with rhsOnly), the dissipation runs in FP64
+// on the stage state (the FP64 kernels of gcfd_diss.cuh: sensor, vertex
+// maxima, limiter, RT gradient, viscous edges), and k_mixed_diss_update adds
+// AddDissipation, applies the modal filter and the viscous time-step limit,
+// then performs the mixed stage update (stage_tail).  The conserved state
+// keeps its compensated FP32 accumulation.
+#pragma once
+#include "gcfd_diss.cuh"
+#include "gcfd_mixed.cuh"
+
+namespace gcfd {
+
+// FP64 stage state Q_s = (hi + lo) + D_s (stage 0: hi + lo), one thread per
+// (element, variable) as the stage kernel.
+template <int N>
+__global__ void __launch_bounds__(128) k_mixed_form_stage(MixedArgs a, double* Qs64) {
+  constexpr int NP = MixedDims<N>::NP;
+  const int n = threadIdx.x >> 5;
+  const int k = blockIdx.x * 32 + (threadIdx.x & 31);
+  if (k >= a.K) return;
+  const size_t sK = static_cast<size_t>(a.K);
+  const size_t off = static_cast<size_t>(n) * NP * sK + k;
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    const size_t ind = off + i * sK;
+    double q = static_cast<double>(a.Qhi[ind]) + static_cast<double>(a.Qlo[ind]);
+    if (a.stage >= 1) q += static_cast<double>(a.D[a.stage][ind]);
+    Qs64[ind] = q;
+  }
+}
+
+// After the rkStep-2 limiter changed the FP64 stage state: the stage-2
+// increment, faces and reference state of the mixed path from it.
+template <int N>
+__global__ void __launch_bounds__(128) k_mixed_relimit(MixedArgs a, const double* Qs64) {
+  constexpr int NP = MixedDims<N>::NP, NE3 = MixedDims<N>::NE3, NPP = MixedDims<N>::NPP;
+  __shared__ __align__(16) float sI[NE3 * NPP];
+  for (int i = threadIdx.x; i < NE3 * NPP; i += blockDim.x) sI[i] = a.Iop[i];
+  __syncthreads();
+  const int n = threadIdx.x >> 5;
+  const int k = blockIdx.x * 32 + (threadIdx.x & 31);
+  if (k >= a.K) return;
+  const size_t sK = static_cast<size_t>(a.K);
+  const size_t off = static_cast<size_t>(n) * NP * sK + k;
+  float dn[NP], dqn[NPP];
+#pragma unroll
+  for (int r = 0; r < NP; ++r) {
+    const size_t ind = off + r * sK;
+    dn[r] = static_cast<float>(Qs64[ind] - (static_cast<double>(a.Qhi[ind]) + static_cast<double>(a.Qlo[ind])));
+    a.D[2][ind] = dn[r];
+  }
+#pragma unroll
+  for (int r = 0; r < NPP; ++r) dqn[r] = (r < NP) ? a.dQ0[off + r * sK] + (dn[r] - dn[0]) : 0.0f;
+  int es[3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) es[e] = a.eslot[e * sK + k];
+  write_faces<N>(a, sI, es, n, dqn);
+  float h = a.Qhi[off], l = a.Qlo[off];
+  df_add(h, l, dn[0]);
+  a.base[static_cast<size_t>(k) * 4 + n] = make_float2(h, l);
+}
+
+// RHS = F(a) (RHS_Euler + DivInt DOF(DissX, DissY, VF) / |J|), the viscous
+// time-step limit, then the mixed stage update.  One thread per (element,
+// variable); stage -1 writes the dissipated, filtered RHS to rhsOut.
+template <int N>
+__global__ void __launch_bounds__(128) k_mixed_diss_update(MixedArgs a, UpdateArgs<double> u) {
+  constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NE3 = MixedDims<N>::NE3;
+  constexpr int NF = MixedDims<N>::NF, NPP = MixedDims<N>::NPP, NR = NP + NE3;
+  __shared__ double sD[NP * NF], sV[NP * NP], sVi[NP * NP], smf[NP];
+  __shared__ __align__(16) float sI[NE3 * NPP];
+  const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = blockIdx.x * 32 + lane;
+  const bool active = k < a.K;
+  const size_t sK = static_cast<size_t>(a.K);
+  const size_t off = static_cast<size_t>(n) * NP * sK + k;
+  const int s = a.stage;
+  // Local dt with the viscous limit (CalculateLocalDT; DT and DTVisc persist):
+  // every variable's thread reads them before the barrier, one writes after.
+  double dtLocal = 0.0, dvNew = 0.0;
+  if (active && a.localDT && s >= 0) {
+    double v = (s == 0) ? -100.0 : a.DT[k];
+    double dv = u.DTVisc[k];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      const int g = u.elemEdge[e * sK + k];
+      v = fmax(v, a.edgeSpeed[g]);
+      dv = fmax(dv, u.viscSpeed[g]);
+    }
+    dtLocal = a.cfl / v;
+    if (dv > 1.e-9) {
+      dv = u.cdiff / dv;
+      dtLocal = fmin(dtLocal, dv);
+    }
+    dvNew = dv;
+  }
+  stage_operator(sD, u.Div, NP * NF);
+  stage_operator(sV, u.V, NP * NP);
+  stage_operator(sVi, u.Vinv, NP * NP);
+  stage_operator(smf, u.mf, NP);
+  for (int i = threadIdx.x; i < NE3 * NPP; i += blockDim.x) sI[i] = a.Iop[i];
+  __syncthreads();
+  float rmax = -3.4028235e38f, rabs = 0.0f, rs2 = 0.0f;
+  if (active) {
+    const double Jd = u.Jdet[k], oojd = 1.0 / Jd;
+    const double J0 = u.Jinv[k], J1 = u.Jinv[sK + k], J2 = u.Jinv[2 * sK + k], J3 = u.Jinv[3 * sK + k];
+    double sig = 0.0;
+#pragma unroll
+    for (int v = 0; v < 3; ++v) sig = sig + __longlong_as_double(static_cast<long long>(u.sigV[u.etov[v * sK + k]]));
+    const double alpha = sin(0.5 * 3.14159265358979323846 * (sig / 3.0));
+    int eg[3], eslot[3];
+    double esg[3];
+    bool own[3];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      eg[e] = u.elemEdge[e * sK + k];
+      own[e] = u.ekL[eg[e]] == k && (u.eLR[eg[e]] & 3) == e;
+      esg[e] = (own[e] ? 1.0 : -1.0) * u.IIE[e * sK + k];
+      eslot[e] = a.eslot[e * sK + k];
+    }
+    double w[NP];
+#pragma unroll
+    for (int r = 0; r < NP; ++r) w[r] = 0.0;
+#pragma unroll 1
+    for (int j = 0; j < NP; ++j) {
+      const size_t ind = (n * NR + j) * sK + k;
+      const double dx = u.DissX[ind], dy = u.DissY[ind];
+      const double fr = Jd * (J0 * dx + J1 * dy), fs = Jd * (J2 * dx + J3 * dy);
+#pragma unroll
+      for (int r = 0; r < NP; ++r) w[r] += sD[r * NF + j] * fr + sD[r * NF + NP + j] * fs;
+    }
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      const double* vf = u.VF + (static_cast<size_t>(eg[e]) * 4 + n) * NE;
+#pragma unroll
+      for (int p = 0; p < NE; ++p) {
+        const double f = vf[own[e] ? p : NE - 1 - p] * esg[e];
+#pragma unroll
+        for (int r = 0; r < NP; ++r) w[r] += sD[r * NF + 2 * NP + e * NE + p] * f;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < NP; ++r) w[r] = a.rhsOut[off + r * sK] + oojd * w[r];
+    limit_filter_modal<NP>(w, sV, sVi, smf, alpha);
+    float rhs[NP];
+#pragma unroll
+    for (int r = 0; r < NP; ++r) rhs[r] = static_cast<float>(w[r]);
+    if (a.localDT && s >= 0 && n == 0) u.DTVisc[k] = dvNew;
+    float dq0[NP], ds[NP];
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+      dq0[i] = a.dQ0[off + i * sK];
+      ds[i] = (s >= 1) ? a.D[s][off + i * sK] : 0.0f;
+    }
+    stage_tail<N>(a, sI, eslot, n, k, off, sK, s, rhs, dq0, ds, dtLocal, rmax, rabs, rs2);
+  }
+  if (s == 4) {
+    const unsigned long long km = warp_max_u64(order_key(static_cast<double>(rmax)));
+    const double am = warp_max(static_cast<double>(rabs));
+    const double s2 = warp_sum(static_cast<double>(rs2));
+    if (lane == 0) {
+      atomicMax(&a.sc->rmax[n], km);
+      atomicMax(&a.sc->rabs[n], static_cast<unsigned long long>(__double_as_longlong(am)));
+      atomicAdd(&a.sc->rsum2[n], s2);
+    }
+  }
+}
+
+}  // namespace gcfd

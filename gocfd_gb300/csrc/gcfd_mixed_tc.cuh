@@ -84,6 +84,7 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
     }
     asm volatile("cp.async.commit_group;\n" ::);
   }
+  if (active) stage_tail_prefetch<N>(a, off, sK, s);
   float dq0[NP], ds[NP];
   if (active) {
 #pragma unroll
@@ -100,7 +101,7 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
     sbase[n][lane] = a.base[static_cast<size_t>(k) * 4 + n].x;
   }
   double dtLocal = 0.0;
-  if (active && a.localDT && s >= 0) {
+  if (active && a.localDT && s >= 0 && !a.rhsOnly) {
     double v = (s == 0) ? -100.0 : a.DT[k];
 #pragma unroll
     for (int e = 0; e < 3; ++e) v = fmax(v, a.edgeSpeed[eslot[e] >> 1]);
@@ -217,7 +218,7 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
     tc::fence_after();
     tc::dealloc(tbase, NCOLS);
   }
-  if (s == 4) {
+  if (s == 4 && !a.rhsOnly) {
     const unsigned long long km = warp_max_u64(order_key(static_cast<double>(rmax)));
     const double am = warp_max(static_cast<double>(rabs));
     const double s2 = warp_sum(static_cast<double>(rs2));

@@ -111,8 +111,33 @@ def test_step_parity_limiter_state_vortex():
     gpu.close()
 
 
-def test_dissipation_needs_fp64_path():
-    mesh = meshes.sod_channel(8, 2)
-    with pytest.raises(_lib.GcfdError) as e:
-        make_pair(mesh, 2, precision="fp32")
-    assert e.value.code == -7  # GCFD_ERR_UNSUPPORTED
+@pytest.mark.parametrize("N", [2, 3])
+def test_rhs_mixed_with_dissipation(N):
+    """Mixed path: FP32 delta-form Euler RHS plus the FP64 dissipation and filter."""
+    mesh = meshes.sod_channel(25, 3)
+    gpu, ora = make_pair(mesh, N, precision="fp32")
+    rng = np.random.default_rng(N)
+    Q = smooth_tube(ora, 0.005)
+    Q = np.ascontiguousarray(Q * (1.0 + 0.01 * rng.uniform(-1, 1, Q.shape)))
+    r = gpu.rhs_global(Q)
+    ref = ora.rhs(Q)
+    err = rel_l2(r, ref)
+    print(f"mixed + dissipation RHS rel L2 N={N}: {err:.3e}")
+    assert err <= 5e-4
+    gpu.close()
+
+
+@pytest.mark.parametrize("local_dt", [False, True])
+def test_step_mixed_with_dissipation(local_dt):
+    mesh = meshes.sod_channel(40, 4)
+    gpu, ora = make_pair(mesh, 2, local_dt=local_dt, precision="fp32")
+    ora.Q = np.ascontiguousarray(smooth_tube(ora))
+    gpu.set_global_state(ora.Q)
+    gpu.step(10)
+    ora.step(10)
+    Q = gpu.get_global_state()
+    err = rel_l2(Q, ora.Q)
+    print(f"mixed + dissipation 10-step rel L2 (local dt {local_dt}): {err:.3e}")
+    assert np.all(np.isfinite(Q))
+    assert err <= 1e-6
+    gpu.close()
