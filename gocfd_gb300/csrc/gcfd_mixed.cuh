@@ -632,7 +632,7 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const float* sI, 
 // (b)+(e): delta-form divergence, SSP stage update on the FP32 increments, and
 // the next stage's faces / reference states.  stage -1 writes the RHS only.
 template <int N>
-__global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
+__global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
   constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NE3 = MixedDims<N>::NE3;
   constexpr int NF = MixedDims<N>::NF, NPP = MixedDims<N>::NPP, NEP = MixedDims<N>::NEP;
   __shared__ __align__(16) float sD[NF * NPP];
@@ -677,21 +677,23 @@ __global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
   // into L2 now so their DRAM latency overlaps the flux and divergence work
   // (the kernel is bound by load latency, not bandwidth).
   if (active) stage_tail_prefetch<N>(a, off, sK, s);
-  // Stage input deltas relative to point 0 of the stage state.
-  float dq0[NP], ds[NP];
+  // Stage input deltas relative to point 0 of the stage state (the update
+  // re-reads dQ0 and D_s at the end, from cache, rather than keeping them live).
+  // Geometry is loaded here too, before the barrier, so its latency overlaps.
+  float Jd = 0.f, J0 = 0.f, J1 = 0.f, J2 = 0.f, J3 = 0.f, ooJ = 0.f;
   if (active) {
+    const float* dsrc = (s >= 1) ? a.D[s] + off : nullptr;
+    const float ds0 = dsrc ? dsrc[0] : 0.0f;
 #pragma unroll
-    for (int i = 0; i < NP; ++i) dq0[i] = a.dQ0[off + i * sK];
-    if (s >= 1) {
-#pragma unroll
-      for (int i = 0; i < NP; ++i) ds[i] = a.D[s][off + i * sK];
-    } else {
-#pragma unroll
-      for (int i = 0; i < NP; ++i) ds[i] = 0.0f;
-    }
-#pragma unroll
-    for (int i = 0; i < NP; ++i) sdq[n][i][lane] = dq0[i] + (ds[i] - ds[0]);
+    for (int i = 0; i < NP; ++i)
+      sdq[n][i][lane] = a.dQ0[off + i * sK] + (dsrc ? dsrc[i * sK] - ds0 : 0.0f);
     sbase[n][lane] = a.base[static_cast<size_t>(k) * 4 + n].x;
+    Jd = a.geo[k];
+    J0 = a.geo[sK + k];
+    J1 = a.geo[2 * sK + k];
+    J2 = a.geo[3 * sK + k];
+    J3 = a.geo[4 * sK + k];
+    ooJ = a.geo[5 * sK + k];
   }
   // Local time step of this stage: DT persists across stages, so every thread
   // of the element reads it before the barrier and one writes it after.
@@ -705,8 +707,6 @@ __global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
   __syncthreads();
   float rmax = -3.4028235e38f, rabs = 0.0f, rs2 = 0.0f;
   if (active) {
-    const float Jd = a.geo[k], J0 = a.geo[sK + k], J1 = a.geo[2 * sK + k];
-    const float J2 = a.geo[3 * sK + k], J3 = a.geo[4 * sK + k], ooJ = a.geo[5 * sK + k];
     const float bq[4] = {sbase[0][lane], sbase[1][lane], sbase[2][lane], sbase[3][lane]};
     const float gm1 = a.gamma - 1.0f;
     const BasePrim b = base_prim(bq, gm1);
@@ -754,9 +754,13 @@ __global__ void __launch_bounds__(128, 6) k_mixed_stage(MixedArgs a) {
         }
       }
     }
-    float rhs[NP];
+    float rhs[NP], dq0[NP], ds[NP];
 #pragma unroll
-    for (int r = 0; r < NP; ++r) rhs[r] = -acc[r] * ooJ;
+    for (int r = 0; r < NP; ++r) {
+      rhs[r] = -acc[r] * ooJ;
+      dq0[r] = a.dQ0[off + r * sK];
+      ds[r] = (s >= 1) ? a.D[s][off + r * sK] : 0.0f;
+    }
     stage_tail<N>(a, sI, eslot, n, k, off, sK, s, rhs, dq0, ds, dtLocal, rmax, rabs, rs2);
   }
   if (s == 4 && !a.rhsOnly) {
