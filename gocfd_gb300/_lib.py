@@ -29,7 +29,8 @@ ERRORS = {
 EXPORTS = [
     "gcfd_create", "gcfd_destroy", "gcfd_last_error", "gcfd_dims", "gcfd_set_state",
     "gcfd_get_state", "gcfd_set_state_device", "gcfd_get_state_device", "gcfd_set_time",
-    "gcfd_get_time", "gcfd_rhs", "gcfd_step", "gcfd_enqueue_steps", "gcfd_get_stream", "gcfd_profile_step",
+    "gcfd_get_time", "gcfd_rhs", "gcfd_step", "gcfd_enqueue_steps", "gcfd_get_stream", "gcfd_set_option",
+    "gcfd_get_option", "gcfd_profile_step",
     "gcfd_host_operator", "gcfd_residual_norms_static", "gcfd_functional", "gcfd_rhs_vjp",
     "gcfd_record_steps", "gcfd_step_vjp",
 ]
@@ -95,6 +96,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         lib.gcfd_step.argtypes = [C.c_void_p, C.c_int32, PD, PD, PD, PD, PD]
         lib.gcfd_enqueue_steps.argtypes = [C.c_void_p, C.c_int32]
         lib.gcfd_get_stream.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+        lib.gcfd_set_option.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+        lib.gcfd_get_option.argtypes = [C.c_void_p, C.c_int32, PI]
         lib.gcfd_profile_step.argtypes = [C.c_void_p, PD, PI]
         lib.gcfd_host_operator.argtypes = [C.c_int32, C.c_int32, PD, PI, PI]
         lib.gcfd_residual_norms_static.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, PD, PD, PD]

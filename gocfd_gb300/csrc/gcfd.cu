@@ -17,6 +17,7 @@
 #include "gcfd_kernels.cuh"
 #include "gcfd_mixed.cuh"
 #include "gcfd_mixed_tc.cuh"
+#include "gcfd_mixed_pipe.cuh"
 #include "gcfd_mixed_diss.cuh"
 #include "gcfd_diss.cuh"
 #include "gcfd_adjoint.cuh"
@@ -114,13 +115,18 @@ struct gcfd_ctx {
   bool fp64Stale = false;  // mixed path: Q[0] lags the compensated state
   cudaStream_t stream2 = nullptr;
   cudaEvent_t evFork = nullptr, evJoin = nullptr;
-  float *mDivT = nullptr, *mIop = nullptr, *mgeo = nullptr, *mII = nullptr;
+  float *mgeo = nullptr, *mII = nullptr;
   int* meslot = nullptr;
   float *mnx = nullptr, *mny = nullptr, *moohK = nullptr;
   bool dirty = true;  // Q0 changed outside a step: the stage-0 data must be rebuilt
   bool tc = false;     // mixed path with the divergence GEMM on the tensor cores (3xTF32)
   float* mBtc = nullptr;
   int tcDynSmem = 0;   // dynamic shared memory that caps the stage kernel's CTAs per SM to its TMEM share
+  // persistent TMA-pipelined stage kernel (needs K % 4 == 0 for 16-byte row strides)
+  bool pipe = false;   // built and usable
+  bool pipeOn = false;  // selected (gcfd_set_option)
+  int pipeGrid = 0, pipeSmem = 0;
+  StageMaps pipeMaps{};
   // artificial dissipation (PerssonC0, FP64 path)
   bool diss = false;
   unsigned long long *sigV = nullptr, *epsV = nullptr;
@@ -446,8 +452,6 @@ struct MixedLaunch {
     a.fhat = c->mfhat;
     a.corr = c->mcorr;
     a.base = c->mbase;
-    a.Div = c->mDivT;
-    a.Iop = c->mIop;
     a.geo = c->mgeo;
     a.II = c->mII;
     a.eslot = c->meslot;
@@ -488,6 +492,14 @@ struct MixedLaunch {
   }
   static int gridE(gcfd_ctx* c) { return (c->K + 31) / 32; }
   static void stage_kernel(gcfd_ctx* c, const MixedArgs& a) {
+    if (c->pipe && c->pipeOn) {
+      const int g = std::min(c->pipeGrid, gridE(c));
+      if (c->tc)
+        k_mixed_stage_pipe<N, true><<<g, 128, c->pipeSmem, c->stream>>>(c->pipeMaps, a);
+      else
+        k_mixed_stage_pipe<N, false><<<g, 128, c->pipeSmem, c->stream>>>(c->pipeMaps, a);
+      return;
+    }
     if (c->tc)
       k_mixed_stage_tc<N><<<gridE(c), 128, c->tcDynSmem, c->stream>>>(a);
     else
@@ -1125,6 +1137,106 @@ int build_tc(gcfd_ctx* c) {
   }
 }
 
+// cuTensorMapEncodeTiled, resolved through the runtime so the library needs no libcuda link.
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// Tensor maps and launch shape of the persistent stage kernel.  K % 4 != 0
+// (row strides not a multiple of 16 bytes) keeps the one-block kernels.
+template <int N, bool TC>
+int build_pipe_n(gcfd_ctx* c) {
+  c->pipe = false;
+  if (c->K % 4 != 0) return GCFD_OK;
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q{};
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+          cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || fn == nullptr) {
+    cudaGetLastError();
+    return fail(c, GCFD_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  }
+  const auto enc = reinterpret_cast<EncodeTiledFn>(fn);
+  const cuuint64_t K = static_cast<cuuint64_t>(c->K), NP = static_cast<cuuint64_t>(c->Np);
+  const cuuint32_t es[3] = {1, 1, 1};
+  auto map3 = [&](CUtensorMap* m, float* p, cuuint32_t rows) {
+    const cuuint64_t dims[3] = {K, NP, 4};
+    const cuuint64_t strides[2] = {K * 4, NP * K * 4};
+    const cuuint32_t box[3] = {32, rows, 4};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, p, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  };
+  auto map2 = [&](CUtensorMap* m, CUtensorMapDataType t, void* p, cuuint64_t d0, cuuint64_t d1, cuuint64_t stride,
+                  cuuint32_t b0, cuuint32_t b1) {
+    const cuuint64_t dims[2] = {d0, d1};
+    const cuuint64_t strides[1] = {stride};
+    const cuuint32_t box[2] = {b0, b1};
+    return enc(m, t, 2, p, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  };
+  StageMaps& M = c->pipeMaps;
+  const cuuint32_t np = static_cast<cuuint32_t>(c->Np);
+  bool ok = map3(&M.dQ0, c->dQ0, np);
+  for (int i = 1; i <= 4; ++i) ok = ok && map3(&M.D[i], c->Dk[i], np);
+  M.D[0] = M.D[1];
+  ok = ok && map3(&M.R3, c->R3, np) && map3(&M.Qhi, c->Qhi, np) && map3(&M.Qlo, c->Qlo, np) &&
+       map3(&M.QhiRow, c->Qhi, 1) && map3(&M.QloRow, c->Qlo, 1);
+  ok = ok && map2(&M.geo, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, c->mgeo, K, 6, K * 4, 32, 6) &&
+       map2(&M.eslot, CU_TENSOR_MAP_DATA_TYPE_INT32, c->meslot, K, 3, K * 4, 32, 3) &&
+       map2(&M.II, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, c->mII, K, 3, K * 4, 32, 3) &&
+       map2(&M.base, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, c->mbase, 8, K, 32, 8, 32);
+  if (!ok) return fail(c, GCFD_ERR_CUDA, "tensor map encoding failed for the stage kernel");
+  int smem = PipeLayout<N, TC>::BYTES;
+  if (TC) {
+    // Pad the footprint so no more CTAs share an SM than its Tensor Memory holds.
+    const int perSM = 512 / TcDims<N>::NCOLS;
+    int smemPerSM = 0, reserved = 0;
+    GCFD_CUDA(c, cudaDeviceGetAttribute(&smemPerSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->prm.device));
+    GCFD_CUDA(c, cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, c->prm.device));
+    smem = std::max(smem, smemPerSM / (perSM + 1) + 1 - reserved);
+  }
+  GCFD_CUDA(c, cudaFuncSetAttribute(k_mixed_stage_pipe<N, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  int occ = 0, sms = 0;
+  GCFD_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mixed_stage_pipe<N, TC>, 128, smem));
+  if (TC) occ = std::min(occ, 512 / TcDims<N>::NCOLS);
+  if (occ < 1) return fail(c, GCFD_ERR_CUDA, "stage kernel: no CTA fits on an SM");
+  GCFD_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->prm.device));
+  c->pipeGrid = sms * occ;
+  c->pipeSmem = smem;
+  c->pipe = true;
+  return GCFD_OK;
+}
+
+int build_pipe(gcfd_ctx* c) {
+  switch (c->N) {
+    case 0: return c->tc ? build_pipe_n<0, true>(c) : build_pipe_n<0, false>(c);
+    case 1: return c->tc ? build_pipe_n<1, true>(c) : build_pipe_n<1, false>(c);
+    case 2: return c->tc ? build_pipe_n<2, true>(c) : build_pipe_n<2, false>(c);
+    case 3: return c->tc ? build_pipe_n<3, true>(c) : build_pipe_n<3, false>(c);
+    case 4: return c->tc ? build_pipe_n<4, true>(c) : build_pipe_n<4, false>(c);
+    default: return GCFD_OK;
+  }
+}
+
+// The mixed path's FP32 operators into the per-order constant-memory copies
+// (identical for every context of the same order, so concurrent contexts agree).
+int upload_const_ops(gcfd_ctx* c, const std::vector<float>& divT, const std::vector<float>& iopT) {
+  const void* d = nullptr;
+  const void* i = nullptr;
+  switch (c->N) {
+    case 0: d = &cDivT0; i = &cIopT0; break;
+    case 1: d = &cDivT1; i = &cIopT1; break;
+    case 2: d = &cDivT2; i = &cIopT2; break;
+    case 3: d = &cDivT3; i = &cIopT3; break;
+    case 4: d = &cDivT4; i = &cIopT4; break;
+    default: return fail(c, GCFD_ERR_UNSUPPORTED, "mixed path: N <= 4");
+  }
+  GCFD_CUDA(c, cudaMemcpyToSymbol(d, divT.data(), divT.size() * sizeof(float)));
+  GCFD_CUDA(c, cudaMemcpyToSymbol(i, iopT.data(), iopT.size() * sizeof(float)));
+  return GCFD_OK;
+}
+
 // Buffers and FP32 operator / geometry copies of the mixed path.
 int build_mixed(gcfd_ctx* c) {
   const int K = c->K, Np = c->Np, NE = c->NE, NF = c->NF;
@@ -1150,14 +1262,15 @@ int build_mixed(gcfd_ctx* c) {
   GCFD_CUDA(c, cudaMemset(c->mfhat, 0, sizeof(float) * c->nEdges * 4 * NEP));
   GCFD_CUDA(c, cudaMemset(c->mcorr, 0, sizeof(float) * c->nEdges * 4));
   // DivInt^T, rows = flux DOF j, cols = output point r padded to NPP.
-  std::vector<float> divT(static_cast<size_t>(NF) * NPP, 0.f), iop(static_cast<size_t>(3 * NE) * NPP, 0.f);
+  // FluxEdgeInterp^T, rows = solution point i, cols = face point padded to NE3P.
+  const int NE3P = (3 * NE + 3) & ~3;
+  std::vector<float> divT(static_cast<size_t>(NF) * NPP, 0.f), iop(static_cast<size_t>(NPP) * NE3P, 0.f);
   for (int j = 0; j < NF; ++j)
     for (int r = 0; r < Np; ++r) divT[static_cast<size_t>(j) * NPP + r] = static_cast<float>(c->el.DivInt(r, j));
   for (int j = 0; j < 3 * NE; ++j)
-    for (int i = 0; i < Np; ++i) iop[static_cast<size_t>(j) * NPP + i] = static_cast<float>(c->el.FluxEdgeInterp(j, i));
-  if ((rc = upload(c, &c->mDivT, divT))) return rc;
+    for (int i = 0; i < Np; ++i) iop[static_cast<size_t>(i) * NE3P + j] = static_cast<float>(c->el.FluxEdgeInterp(j, i));
+  if ((rc = upload_const_ops(c, divT, iop))) return rc;
   if (c->tc && (rc = build_tc(c))) return rc;
-  if ((rc = upload(c, &c->mIop, iop))) return rc;
   const Geometry& g = c->geo;
   std::vector<float> geo(static_cast<size_t>(6) * K), ii(static_cast<size_t>(3) * K);
   for (int k = 0; k < K; ++k) {
@@ -1187,7 +1300,7 @@ int build_mixed(gcfd_ctx* c) {
   if ((rc = upload(c, &c->mnx, nx))) return rc;
   if ((rc = upload(c, &c->mny, ny))) return rc;
   if ((rc = upload(c, &c->moohK, oh))) return rc;
-  return GCFD_OK;
+  return build_pipe(c);
 }
 
 int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
@@ -1506,8 +1619,12 @@ int gcfd_step(gcfd_ctx* c, int32_t nsteps, double* time, double* dt_last, double
     if (resid_rms4) resid_rms4[n] = rms;
     if (nsteps > 0 && !(std::isfinite(am) && std::isfinite(rms))) finite = false;
   }
+  if (h.errFlags & 2u)
+    return fail(c, GCFD_ERR_CUDA, "stage kernel: dynamic shared memory is not 128-byte aligned");
   if (h.errFlags)
-    return fail(c, GCFD_ERR_TIMEOUT, "a tensor-core completion wait ran out of its iteration bound");
+    return fail(c, GCFD_ERR_TIMEOUT,
+                (h.errFlags & 4u) ? "a TMA copy of the stage kernel did not complete within its wait bound"
+                                  : "a tensor-core completion wait ran out of its iteration bound");
   if (!finite) return fail(c, GCFD_ERR_NAN, "non-finite RK increment (solution diverged)");
   return GCFD_OK;
 }
@@ -1525,6 +1642,27 @@ int gcfd_enqueue_steps(gcfd_ctx* c, int32_t nsteps) {
 int gcfd_get_stream(gcfd_ctx* c, void** stream) {
   if (!c || !stream) return GCFD_ERR_ARG;
   *stream = static_cast<void*>(c->stream);
+  return GCFD_OK;
+}
+
+int gcfd_set_option(gcfd_ctx* c, int32_t option, int32_t value) {
+  if (!c) return GCFD_ERR_ARG;
+  if (option != GCFD_OPT_STAGE_PIPELINE) return fail(c, GCFD_ERR_ARG, "unknown option");
+  if (value != 0 && value != 1) return fail(c, GCFD_ERR_ARG, "GCFD_OPT_STAGE_PIPELINE takes 0 or 1");
+  if (c->pipeOn == (value == 1)) return GCFD_OK;
+  GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->pipeOn = (value == 1);
+  if (c->graphExec) GCFD_CUDA(c, cudaGraphExecDestroy(c->graphExec));
+  if (c->graph) GCFD_CUDA(c, cudaGraphDestroy(c->graph));
+  c->graphExec = nullptr;
+  c->graph = nullptr;
+  return capture_graph(c);
+}
+
+int gcfd_get_option(const gcfd_ctx* c, int32_t option, int32_t* value) {
+  if (!c || !value) return GCFD_ERR_ARG;
+  if (option != GCFD_OPT_STAGE_PIPELINE) return GCFD_ERR_ARG;
+  *value = (c->fp32 && c->pipe && c->pipeOn) ? 1 : 0;
   return GCFD_OK;
 }
 

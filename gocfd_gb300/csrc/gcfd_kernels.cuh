@@ -35,7 +35,8 @@ struct Scalars {
   double rsum2[4];              // sum R^2
   unsigned long long gvisc[5];  // per stage max viscous wave speed (artificial dissipation)
   int steps;
-  unsigned int errFlags;        // sticky device error bits (1: a tensor-core wait ran out)
+  unsigned int errFlags;        // sticky device error bits (1: a tensor-core wait ran out, 2: misaligned
+                                //   dynamic shared memory, 4: a TMA copy wait ran out)
 };
 
 __device__ __forceinline__ unsigned long long order_key(double x) {

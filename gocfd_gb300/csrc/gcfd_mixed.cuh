@@ -212,8 +212,6 @@ struct MixedArgs {
   float* fhat;                // [g][4][NE]
   float* corr;                // [g][4]
   float2* base;               // [k][4] (hi, lo) reference state; updated in place per stage
-  const float* Div;           // DivInt^T padded: [NF][NPP]
-  const float* Iop;           // FluxEdgeInterp padded: [NE3][NPP]
   const float* geo;           // [6][K]: Jdet, Jinv0..3, 1/Jdet
   const float* II;            // [3][K] IInII
   const int* eslot;           // [3][K] edge id * 2 + side
@@ -264,44 +262,71 @@ struct MixedDims {
   // Edge-major stride per (slot, variable): NpEdge rounded up to even, so every
   // (slot, variable) run starts 8-byte aligned and moves as float2.
   static constexpr int NEP = (NE + 1) & ~1;
+  // Face interpolation operator, transposed: [NPP][NE3P], face points padded to float4.
+  static constexpr int NE3P = (NE3 + 3) & ~3;
+  static constexpr int ISZ = NPP * NE3P;
+  static constexpr int DSZ = NF * NPP;
 };
 
-// Writes the element's 3 edges of face deltas for variable n (rows e*NE + p).
+// The FP32 operators of the mixed path live in constant memory, one copy per
+// order N (they depend on N only): DivInt^T [NF][NPP] and FluxEdgeInterp^T
+// [NPP][NE3P].  Every warp reads the same entry at the same time, so with the
+// loops unrolled each entry is an immediate constant-bank operand of its FMA
+// and the element kernels issue no shared-memory loads for them.
+__constant__ float cDivT0[MixedDims<0>::DSZ], cDivT1[MixedDims<1>::DSZ], cDivT2[MixedDims<2>::DSZ],
+    cDivT3[MixedDims<3>::DSZ], cDivT4[MixedDims<4>::DSZ];
+__constant__ float cIopT0[MixedDims<0>::ISZ], cIopT1[MixedDims<1>::ISZ], cIopT2[MixedDims<2>::ISZ],
+    cIopT3[MixedDims<3>::ISZ], cIopT4[MixedDims<4>::ISZ];
+
+// DivInt[r][j] = div_op<N>(j * NPP + r).
 template <int N>
-__device__ __forceinline__ void write_faces(const MixedArgs& a, const float* sI, const int eslot[3],
-                                            int n, const float dq[]) {
-  constexpr int NE = MixedDims<N>::NE, NPP = MixedDims<N>::NPP, NEP = MixedDims<N>::NEP;
+__device__ __forceinline__ float div_op(int idx) {
+  if constexpr (N == 0) return cDivT0[idx];
+  else if constexpr (N == 1) return cDivT1[idx];
+  else if constexpr (N == 2) return cDivT2[idx];
+  else if constexpr (N == 3) return cDivT3[idx];
+  else return cDivT4[idx];
+}
+// FluxEdgeInterp[q][i] = iop_op<N>(i * NE3P + q).
+template <int N>
+__device__ __forceinline__ float iop_op(int idx) {
+  if constexpr (N == 0) return cIopT0[idx];
+  else if constexpr (N == 1) return cIopT1[idx];
+  else if constexpr (N == 2) return cIopT2[idx];
+  else if constexpr (N == 3) return cIopT3[idx];
+  else return cIopT4[idx];
+}
+
+// Writes the element's 3 edges of face deltas for variable n (face point
+// q = e*NE + p): out_q = sum_i FluxEdgeInterp[q][i] dq[i], accumulated over i
+// in order.
+template <int N>
+__device__ __forceinline__ void write_faces(const MixedArgs& a, const int eslot[3], int n, const float dq[]) {
+  constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NEP = MixedDims<N>::NEP;
+  constexpr int NE3 = MixedDims<N>::NE3, NE3P = MixedDims<N>::NE3P;
+  float out[NE3];
+#pragma unroll
+  for (int q = 0; q < NE3; ++q) out[q] = 0.0f;
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+#pragma unroll
+    for (int q = 0; q < NE3; ++q) out[q] = fmaf(iop_op<N>(i * NE3P + q), dq[i], out[q]);
+  }
 #pragma unroll
   for (int e = 0; e < 3; ++e) {
     float* dst = a.faces + (static_cast<size_t>(eslot[e]) * 4 + n) * NEP;
-    float out[NE];
-#pragma unroll
-    for (int p = 0; p < NE; ++p) {
-      const float4* row = reinterpret_cast<const float4*>(sI + (e * NE + p) * NPP);
-      float acc = 0.0f;
-#pragma unroll
-      for (int i4 = 0; i4 < NPP / 4; ++i4) {
-        const float4 w = row[i4];
-        acc = fmaf(w.x, dq[4 * i4 + 0], acc);
-        acc = fmaf(w.y, dq[4 * i4 + 1], acc);
-        acc = fmaf(w.z, dq[4 * i4 + 2], acc);
-        acc = fmaf(w.w, dq[4 * i4 + 3], acc);
-      }
-      out[p] = acc;
-    }
     // (slot*4 + n) * NEP floats with NEP even: 8-byte aligned, pairs go out as float2.
 #pragma unroll
-    for (int p = 0; p + 1 < NE; p += 2) reinterpret_cast<float2*>(dst)[p / 2] = make_float2(out[p], out[p + 1]);
-    if (NE & 1) dst[NE - 1] = out[NE - 1];
+    for (int p = 0; p + 1 < NE; p += 2)
+      reinterpret_cast<float2*>(dst)[p / 2] = make_float2(out[e * NE + p], out[e * NE + p + 1]);
+    if (NE & 1) dst[NE - 1] = out[e * NE + NE - 1];
   }
 }
 
 // Stage-0 preparation from the FP64 state: hi/lo split, dQ0, faces, reference states.
 template <int N>
 __global__ void __launch_bounds__(128) k_mixed_prepare(MixedArgs a) {
-  constexpr int NP = MixedDims<N>::NP, NE3 = MixedDims<N>::NE3, NPP = MixedDims<N>::NPP;
-  __shared__ __align__(16) float sI[NE3 * NPP];
-  for (int i = threadIdx.x; i < NE3 * NPP; i += blockDim.x) sI[i] = a.Iop[i];
+  constexpr int NP = MixedDims<N>::NP, NPP = MixedDims<N>::NPP;
   __syncthreads();
   const int n = threadIdx.x >> 5;
   const int k = blockIdx.x * 32 + (threadIdx.x & 31);
@@ -326,7 +351,7 @@ __global__ void __launch_bounds__(128) k_mixed_prepare(MixedArgs a) {
   int es[3];
 #pragma unroll
   for (int e = 0; e < 3; ++e) es[e] = a.eslot[e * sK + k];
-  write_faces<N>(a, sI, es, n, dq);
+  write_faces<N>(a, es, n, dq);
 }
 
 // FP64 copy of the compensated state, for gcfd_get_state.
@@ -547,7 +572,7 @@ __device__ __forceinline__ void stage_tail_prefetch(const MixedArgs& a, size_t o
 // the next stage's faces and reference state, and at stage 4 the compensated
 // state and the residual partials.
 template <int N>
-__device__ __forceinline__ void stage_tail(const MixedArgs& a, const float* sI, const int eslot[3], int n, int k,
+__device__ __forceinline__ void stage_tail(const MixedArgs& a, const int eslot[3], int n, int k,
                                            size_t off, size_t sK, int s, const float rhs[], const float dq0[],
                                            const float ds[], double dtLocal, float& rmax, float& rabs,
                                            float& rs2) {
@@ -593,7 +618,7 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const float* sI, 
       float dqn[NPP];
 #pragma unroll
       for (int r = 0; r < NPP; ++r) dqn[r] = (r < NP) ? dq0[r] + (dn[r] - dn[0]) : 0.0f;
-      write_faces<N>(a, sI, eslot, n, dqn);
+      write_faces<N>(a, eslot, n, dqn);
       float h = a.Qhi[off], l = a.Qlo[off];
       df_add(h, l, dn[0]);
       a.base[static_cast<size_t>(k) * 4 + n] = make_float2(h, l);
@@ -623,7 +648,7 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const float* sI, 
         dqn[r] = df_diff(qh[r], ql[r], qh[0], ql[0]);
         a.dQ0[off + r * sK] = dqn[r];
       }
-      write_faces<N>(a, sI, eslot, n, dqn);
+      write_faces<N>(a, eslot, n, dqn);
       a.base[static_cast<size_t>(k) * 4 + n] = make_float2(qh[0], ql[0]);
     }
   }
@@ -634,15 +659,11 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const float* sI, 
 template <int N>
 __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
   constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NE3 = MixedDims<N>::NE3;
-  constexpr int NF = MixedDims<N>::NF, NPP = MixedDims<N>::NPP, NEP = MixedDims<N>::NEP;
-  __shared__ __align__(16) float sD[NF * NPP];
-  __shared__ __align__(16) float sI[NE3 * NPP];
+  constexpr int NPP = MixedDims<N>::NPP, NEP = MixedDims<N>::NEP;
   __shared__ float sdq[4][NP][33];
   __shared__ float sbase[4][32];
   __shared__ float sfh[4][NE3][32];   // this element's edge fluxes, prefetched
   __shared__ float scorr[4][3][32];
-  for (int i = threadIdx.x; i < NF * NPP; i += blockDim.x) sD[i] = a.Div[i];
-  for (int i = threadIdx.x; i < NE3 * NPP; i += blockDim.x) sI[i] = a.Iop[i];
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = blockIdx.x * 32 + lane;
   const bool active = k < a.K;
@@ -710,11 +731,11 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
     const float bq[4] = {sbase[0][lane], sbase[1][lane], sbase[2][lane], sbase[3][lane]};
     const float gm1 = a.gamma - 1.0f;
     const BasePrim b = base_prim(bq, gm1);
-    float acc[NPP];
+    float acc[NP];
 #pragma unroll
-    for (int r = 0; r < NPP; ++r) acc[r] = 0.0f;
+    for (int r = 0; r < NP; ++r) acc[r] = 0.0f;
     // Interior transformed delta fluxes, DivInt columns 0..2NP-1.
-#pragma unroll 3
+#pragma unroll
     for (int i = 0; i < NP; ++i) {
       const float d[4] = {sdq[0][i][lane], sdq[1][i][lane], sdq[2][i][lane], sdq[3][i][lane]};
       const DeltaPrim q = delta_prim(b, d, gm1);
@@ -722,16 +743,9 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
       delta_flux_c(n, b, d, q, &fx, &fy);
       const float Fr = Jd * (J0 * fx + J1 * fy);
       const float Fs = Jd * (J2 * fx + J3 * fy);
-      const float4* cr = reinterpret_cast<const float4*>(sD + i * NPP);
-      const float4* cs = reinterpret_cast<const float4*>(sD + (NP + i) * NPP);
 #pragma unroll
-      for (int r4 = 0; r4 < NPP / 4; ++r4) {
-        const float4 x = cr[r4], y = cs[r4];
-        acc[4 * r4 + 0] = fmaf(x.x, Fr, fmaf(y.x, Fs, acc[4 * r4 + 0]));
-        acc[4 * r4 + 1] = fmaf(x.y, Fr, fmaf(y.y, Fs, acc[4 * r4 + 1]));
-        acc[4 * r4 + 2] = fmaf(x.z, Fr, fmaf(y.z, Fs, acc[4 * r4 + 2]));
-        acc[4 * r4 + 3] = fmaf(x.w, Fr, fmaf(y.w, Fs, acc[4 * r4 + 3]));
-      }
+      for (int r = 0; r < NP; ++r)
+        acc[r] = fmaf(div_op<N>(i * NPP + r), Fr, fmaf(div_op<N>((NP + i) * NPP + r), Fs, acc[r]));
     }
     // Edge DOFs: IInII * (s fhat - n_e.F(Qb)), owner order / reversed for the right side.
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
@@ -743,15 +757,8 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
 #pragma unroll
       for (int p = 0; p < NE; ++p) {
         const float dof = right ? -(sfh[n][e * NE + NE - 1 - p][lane] - cc) * ii : sfh[n][e * NE + p][lane] * ii;
-        const float4* col = reinterpret_cast<const float4*>(sD + (2 * NP + e * NE + p) * NPP);
 #pragma unroll
-        for (int r4 = 0; r4 < NPP / 4; ++r4) {
-          const float4 x = col[r4];
-          acc[4 * r4 + 0] = fmaf(x.x, dof, acc[4 * r4 + 0]);
-          acc[4 * r4 + 1] = fmaf(x.y, dof, acc[4 * r4 + 1]);
-          acc[4 * r4 + 2] = fmaf(x.z, dof, acc[4 * r4 + 2]);
-          acc[4 * r4 + 3] = fmaf(x.w, dof, acc[4 * r4 + 3]);
-        }
+        for (int r = 0; r < NP; ++r) acc[r] = fmaf(div_op<N>((2 * NP + e * NE + p) * NPP + r), dof, acc[r]);
       }
     }
     float rhs[NP], dq0[NP], ds[NP];
@@ -761,7 +768,7 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
       dq0[r] = a.dQ0[off + r * sK];
       ds[r] = (s >= 1) ? a.D[s][off + r * sK] : 0.0f;
     }
-    stage_tail<N>(a, sI, eslot, n, k, off, sK, s, rhs, dq0, ds, dtLocal, rmax, rabs, rs2);
+    stage_tail<N>(a, eslot, n, k, off, sK, s, rhs, dq0, ds, dtLocal, rmax, rabs, rs2);
   }
   if (s == 4 && !a.rhsOnly) {
     const unsigned long long km = warp_max_u64(order_key(static_cast<double>(rmax)));

@@ -34,9 +34,7 @@ __global__ void __launch_bounds__(128) k_mixed_form_stage(MixedArgs a, double* Q
 // increment, faces and reference state of the mixed path from it.
 template <int N>
 __global__ void __launch_bounds__(128) k_mixed_relimit(MixedArgs a, const double* Qs64) {
-  constexpr int NP = MixedDims<N>::NP, NE3 = MixedDims<N>::NE3, NPP = MixedDims<N>::NPP;
-  __shared__ __align__(16) float sI[NE3 * NPP];
-  for (int i = threadIdx.x; i < NE3 * NPP; i += blockDim.x) sI[i] = a.Iop[i];
+  constexpr int NP = MixedDims<N>::NP, NPP = MixedDims<N>::NPP;
   __syncthreads();
   const int n = threadIdx.x >> 5;
   const int k = blockIdx.x * 32 + (threadIdx.x & 31);
@@ -55,7 +53,7 @@ __global__ void __launch_bounds__(128) k_mixed_relimit(MixedArgs a, const double
   int es[3];
 #pragma unroll
   for (int e = 0; e < 3; ++e) es[e] = a.eslot[e * sK + k];
-  write_faces<N>(a, sI, es, n, dqn);
+  write_faces<N>(a, es, n, dqn);
   float h = a.Qhi[off], l = a.Qlo[off];
   df_add(h, l, dn[0]);
   a.base[static_cast<size_t>(k) * 4 + n] = make_float2(h, l);
@@ -67,9 +65,8 @@ __global__ void __launch_bounds__(128) k_mixed_relimit(MixedArgs a, const double
 template <int N>
 __global__ void __launch_bounds__(128) k_mixed_diss_update(MixedArgs a, UpdateArgs<double> u) {
   constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NE3 = MixedDims<N>::NE3;
-  constexpr int NF = MixedDims<N>::NF, NPP = MixedDims<N>::NPP, NR = NP + NE3;
+  constexpr int NF = MixedDims<N>::NF, NR = NP + NE3;
   __shared__ double sD[NP * NF], sV[NP * NP], sVi[NP * NP], smf[NP];
-  __shared__ __align__(16) float sI[NE3 * NPP];
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = blockIdx.x * 32 + lane;
   const bool active = k < a.K;
@@ -99,7 +96,6 @@ __global__ void __launch_bounds__(128) k_mixed_diss_update(MixedArgs a, UpdateAr
   stage_operator(sV, u.V, NP * NP);
   stage_operator(sVi, u.Vinv, NP * NP);
   stage_operator(smf, u.mf, NP);
-  for (int i = threadIdx.x; i < NE3 * NPP; i += blockDim.x) sI[i] = a.Iop[i];
   __syncthreads();
   float rmax = -3.4028235e38f, rabs = 0.0f, rs2 = 0.0f;
   if (active) {
@@ -153,7 +149,7 @@ __global__ void __launch_bounds__(128) k_mixed_diss_update(MixedArgs a, UpdateAr
       dq0[i] = a.dQ0[off + i * sK];
       ds[i] = (s >= 1) ? a.D[s][off + i * sK] : 0.0f;
     }
-    stage_tail<N>(a, sI, eslot, n, k, off, sK, s, rhs, dq0, ds, dtLocal, rmax, rabs, rs2);
+    stage_tail<N>(a, eslot, n, k, off, sK, s, rhs, dq0, ds, dtLocal, rmax, rabs, rs2);
   }
   if (s == 4) {
     const unsigned long long km = warp_max_u64(order_key(static_cast<double>(rmax)));

@@ -39,10 +39,9 @@ inline int tc_b_index(int r, int j, int NFP) { return (r / 8) * (NFP / 4) * 32 +
 template <int N>
 __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
   constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NE3 = MixedDims<N>::NE3;
-  constexpr int NPP = MixedDims<N>::NPP, NEP = MixedDims<N>::NEP;
+  constexpr int NEP = MixedDims<N>::NEP;
   constexpr int NFP = TcDims<N>::NFP, NCOLS = TcDims<N>::NCOLS, BSZ = TcDims<N>::BSZ;
   __shared__ __align__(128) float sB[2 * BSZ];
-  __shared__ __align__(16) float sI[NE3 * NPP];
   __shared__ float sdq[4][NP][33];
   __shared__ float sbase[4][32];
   __shared__ float sfh[4][NE3][32];
@@ -50,7 +49,6 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base;
   for (int i = threadIdx.x; i < 2 * BSZ; i += blockDim.x) sB[i] = a.Btc[i];
-  for (int i = threadIdx.x; i < NE3 * NPP; i += blockDim.x) sI[i] = a.Iop[i];
   tc::fence_proxy_async();  // sB is read by the tensor core
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) tc::mbar_init(&mbar, 1);
@@ -210,7 +208,7 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
     float rhs[NP];
 #pragma unroll
     for (int r = 0; r < NP; ++r) rhs[r] = -__uint_as_float(dv[r]) * ooJ;
-    stage_tail<N>(a, sI, eslot, n, k, off, sK, s, rhs, dq0, ds, dtLocal, rmax, rabs, rs2);
+    stage_tail<N>(a, eslot, n, k, off, sK, s, rhs, dq0, ds, dtLocal, rmax, rabs, rs2);
   }
   tc::fence_before();
   __syncthreads();

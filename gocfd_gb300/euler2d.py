@@ -358,6 +358,19 @@ class Euler:
         _lib.check(self.lib, self.ctx, self.lib.gcfd_get_stream(self.ctx, C.byref(s)))
         return s.value or 0
 
+    # GCFD_OPT_STAGE_PIPELINE of gcfd.h
+    OPT_STAGE_PIPELINE = 1
+
+    def set_stage_pipeline(self, on: bool) -> None:
+        """Select the persistent TMA-pipelined stage kernel (default) or the one-block kernel."""
+        _lib.check(self.lib, self.ctx, self.lib.gcfd_set_option(self.ctx, self.OPT_STAGE_PIPELINE, int(bool(on))))
+
+    def stage_pipeline(self) -> bool:
+        """True while the mixed path's stage update runs as the pipelined kernel."""
+        v = C.c_int32()
+        _lib.check(self.lib, self.ctx, self.lib.gcfd_get_option(self.ctx, self.OPT_STAGE_PIPELINE, C.byref(v)))
+        return bool(v.value)
+
 
 def parse_yaml_file(path: str) -> InputParameters2D:
     return InputParameters2D.from_file(path)

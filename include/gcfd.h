@@ -140,6 +140,16 @@ int gcfd_enqueue_steps(gcfd_ctx* ctx, int32_t nsteps);
 /* The CUDA stream (cudaStream_t) all work of the context is ordered on. */
 int gcfd_get_stream(gcfd_ctx* ctx, void** stream);
 
+/* Implementation choices of a context; no counterpart in the reference.
+ * GCFD_OPT_STAGE_PIPELINE: 1 (the default) runs the mixed path's stage update
+ * as the persistent kernel whose element inputs are double-buffered by TMA
+ * copies (used when K % 4 == 0); 0 selects the one-block-per-CTA kernel.
+ * Setting an option records the per-step CUDA graph again.  Reading
+ * GCFD_OPT_STAGE_PIPELINE gives 1 only while the pipelined kernel runs. */
+#define GCFD_OPT_STAGE_PIPELINE 1
+int gcfd_set_option(gcfd_ctx* ctx, int32_t option, int32_t value);
+int gcfd_get_option(const gcfd_ctx* ctx, int32_t option, int32_t* value);
+
 /* Run one step launch by launch with CUDA events around each kernel and
  * return the summed device time per kernel family (ms): [0] face
  * interpolation, [1] edge flux + BCs, [2] divergence + RK update, [3] step

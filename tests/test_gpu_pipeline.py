@@ -1,0 +1,135 @@
+"""The persistent TMA-pipelined stage kernel against the one-block stage kernel
+and the FP64 oracle.
+
+Both kernels run the same arithmetic per element (delta-form fluxes, the same
+FMA or 3xTF32 tensor-core divergence, the same stage update); the compiler may
+fuse a multiply-add differently in the two, so their states agree to FP32
+round-off of the mixed path, which at N = 1 (DivInt entries ~1e3) reaches
+~1e-6 after 20 steps.  The bar, written in each test: the pipelined kernel's
+distance to the oracle is at most twice the one-block kernel's (plus 1e-12),
+and the two kernels' states differ by no more than that either.  Meshes
+cover K % 32 != 0 (a partial last block), K large enough that every CTA walks
+several blocks through both pipeline buffers, local time stepping, the
+PerssonC0 dissipation (stage kernel in RHS-only mode) and the RHS call
+(stage -1).  K % 4 != 0 keeps the one-block kernel.
+"""
+import numpy as np
+import pytest
+
+from conftest import fixture
+import oracle
+from gocfd_gb300 import meshes
+from gocfd_gb300.euler2d import Euler, InputParameters2D
+
+pytestmark = pytest.mark.gpu
+
+
+def assert_as_accurate(q_pipe, q_one, q_ref, label):
+    e_p, e_o, d = rel_l2(q_pipe, q_ref), rel_l2(q_one, q_ref), rel_l2(q_pipe, q_one)
+    print(f"{label}: pipelined-oracle {e_p:.3e}, one-block-oracle {e_o:.3e}, pipelined-one-block {d:.3e}")
+    assert np.all(np.isfinite(q_pipe))
+    assert e_p <= 2.0 * e_o + 1e-12
+    assert d <= 2.0 * e_o + 1e-12
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def make(mesh, N, precision, *, init="ivortex", flux="roe", local_dt=False, cfl=1.0, minf=0.5,
+         limiter="", vortex_center=(0.0, 0.0)):
+    ip = InputParameters2D(CFL=cfl, FluxType=flux, InitType=init, PolynomialOrder=N, FinalTime=1e9,
+                           Minf=minf, Gamma=1.4, Alpha=0.0, LocalTimeStepping=local_dt, MaxIterations=10 ** 9,
+                           Limiter=limiter)
+    return Euler(ip, mesh, 1, precision=precision, vortex_center=vortex_center)
+
+
+def oracle_run(mesh, N, steps, Q0=None, *, init="ivortex", flux="roe", local_dt=False, cfl=1.0, minf=0.5,
+               limiter="", vortex_center=(0.0, 0.0)):
+    ora = oracle.OracleSolver(N, mesh.VX, mesh.VY, mesh.EToV, mesh.bc_edges, flux=flux, init=init, cfl=cfl,
+                              final_time=1e9, minf=minf, gamma=1.4, alpha=0.0, local_dt=local_dt,
+                              vortex_center=vortex_center, limiter=limiter)
+    if Q0 is not None:
+        ora.Q = np.ascontiguousarray(Q0)
+    ora.step(steps)
+    return ora.Q
+
+
+def run_both(mesh, N, precision, steps, Q0=None, **kw):
+    out = []
+    for pipe in (True, False):
+        g = make(mesh, N, precision, **kw)
+        g.set_stage_pipeline(pipe)
+        assert g.stage_pipeline() == pipe
+        if Q0 is not None:
+            g.set_global_state(Q0)
+        info = g.step(steps)
+        out.append((g.get_global_state(), info))
+        g.close()
+    return out
+
+
+def test_pipeline_option():
+    g = make(meshes.vortex_box(16), 2, "fp32")
+    assert not g.stage_pipeline()  # the one-block kernel is the default
+    g.set_stage_pipeline(True)
+    assert g.stage_pipeline()
+    g.set_stage_pipeline(False)
+    assert not g.stage_pipeline()
+    g.close()
+    g = make(meshes.read_mesh(fixture("test_tris_6_nowall.neu")), 2, "fp32", init="freestream")
+    g.set_stage_pipeline(True)
+    assert not g.stage_pipeline()  # K = 6: row strides are not multiples of 16 bytes
+    g.close()
+    g = make(meshes.vortex_box(16), 2, "fp64")
+    g.set_stage_pipeline(True)
+    assert not g.stage_pipeline()  # the FP64 path has its own kernels
+    g.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "tf32x3"])
+@pytest.mark.parametrize("N", [0, 1, 2, 3, 4])
+def test_pipeline_matches_one_block_partial_block(precision, N):
+    mesh = meshes.vortex_box(10, jitter=0.1, seed=4)  # K = 200 = 6 x 32 + 8
+    (qa, ia), (qb, ib) = run_both(mesh, N, precision, 20)
+    assert_as_accurate(qa, qb, oracle_run(mesh, N, 20), f"K={mesh.K} N={N} {precision}")
+    assert ia["time"] == pytest.approx(ib["time"], rel=1e-6)
+    assert np.allclose(ia["resid_rms"], ib["resid_rms"], rtol=1e-3, atol=0)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "tf32x3"])
+def test_pipeline_matches_one_block_many_blocks_per_cta(precision):
+    # K = 51,200: 1,600 blocks, more than two per CTA on any GB300-sized grid.
+    mesh = meshes.vortex_box(160, jitter=0.1, seed=5)
+    (qa, _), (qb, _) = run_both(mesh, 4, precision, 5)
+    assert_as_accurate(qa, qb, oracle_run(mesh, 4, 5), f"K={mesh.K} N=4 {precision}")
+
+
+@pytest.mark.parametrize("precision", ["fp32", "tf32x3"])
+def test_pipeline_matches_one_block_local_dt(precision):
+    mesh = meshes.wedge_channel(24, 12)  # K = 576
+    kw = dict(init="freestream", minf=2.0, local_dt=True, cfl=0.5)
+    (qa, _), (qb, _) = run_both(mesh, 2, precision, 10, **kw)
+    assert_as_accurate(qa, qb, oracle_run(mesh, 2, 10, **kw), f"local dt {precision}")
+
+
+def test_pipeline_matches_one_block_with_dissipation():
+    mesh = meshes.sod_channel(40, 4)  # K = 320
+    kw = dict(init="shocktube", limiter="PerssonC0", cfl=0.5)
+    (qa, _), (qb, _) = run_both(mesh, 2, "fp32", 10, **kw)
+    assert_as_accurate(qa, qb, oracle_run(mesh, 2, 10, **kw), "PerssonC0")
+
+
+@pytest.mark.parametrize("precision", ["fp32", "tf32x3"])
+def test_pipeline_rhs_matches_one_block(precision):
+    mesh = meshes.vortex_box(12, jitter=0.1, seed=6)  # K = 288
+    g = make(mesh, 3, precision)
+    Q = g.get_global_state()
+    Q = np.ascontiguousarray(Q * (1.0 + 0.01 * np.random.default_rng(7).uniform(-1, 1, Q.shape)))
+    ra = g.rhs_global(Q, 0.1)
+    g.set_stage_pipeline(False)
+    rb = g.rhs_global(Q, 0.1)
+    g.close()
+    ora = oracle.OracleSolver(3, mesh.VX, mesh.VY, mesh.EToV, mesh.bc_edges, flux="roe", init="ivortex", cfl=1.0,
+                              final_time=1e9, minf=0.5, gamma=1.4, alpha=0.0, vortex_center=(0.0, 0.0))
+    assert_as_accurate(ra, rb, ora.rhs(Q, 0.1), f"RHS {precision}")
