@@ -65,7 +65,7 @@ struct DeltaPrim {
 };
 __device__ __forceinline__ DeltaPrim delta_prim(const BasePrim& b, const float d[4], float gm1) {
   DeltaPrim r;
-  const float ir = 1.0f / (b.rho + d[0]);
+  const float ir = __fdividef(1.0f, b.rho + d[0]);  // ~1 ulp; it only scales deltas
   r.du = (d[1] - b.u * d[0]) * ir;
   r.dv = (d[2] - b.v * d[0]) * ir;
   r.dp = gm1 * (d[3] - 0.5f * (b.m * r.du + d[1] * b.u + d[1] * r.du + b.n * r.dv + d[2] * b.v +
@@ -364,16 +364,47 @@ __global__ void k_mixed_to_fp64(const float* __restrict__ hi, const float* __res
 
 // (c) interior-edge fluxes in delta form, one thread per mesh edge.  RoeER
 // instantiates the Roe-ER flux in FP64 (fluxes.go:415-503 has no delta form).
+// A block's 128 edges own a contiguous run of the edge-major face array, which
+// is copied into shared memory with coalesced 16-byte cp.async (the copy
+// overlaps the base-state loads); the fluxes leave the same way, through a
+// shared-memory record per edge and coalesced 16-byte stores.
+template <int N>
+struct EdgeDims {
+  static constexpr int NEP = MixedDims<N>::NEP;
+  static constexpr int FW = 8 * NEP;                  // floats of one edge's faces (2 sides x 4 variables)
+  static constexpr int FWP = FW + ((FW % 8) ? 0 : 4);  // record stride = 4 mod 8 words: no bank conflicts
+  static constexpr int OW = 4 * NEP + 4;               // fhat (4 x NEP) and corr (4)
+  static constexpr int OWP = OW + ((OW % 8) ? 0 : 4);
+};
+
 template <int N, bool RoeER>
-__global__ void __launch_bounds__(128) k_mixed_edge(MixedArgs a) {
+__global__ void __launch_bounds__(128, RoeER ? 1 : 5) k_mixed_edge(MixedArgs a) {
   constexpr int NE = MixedDims<N>::NE, NEP = MixedDims<N>::NEP;
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr int FW = EdgeDims<N>::FW, FWP = EdgeDims<N>::FWP, OWP = EdgeDims<N>::OWP;
+  static_assert(FW % 4 == 0 && FWP % 4 == 0 && OWP % 4 == 0, "16-byte records");
+  __shared__ __align__(16) float sf[128 * FWP];
+  __shared__ __align__(16) float so[128 * OWP];
+  const int g0 = blockIdx.x * 128;
+  const int nE = min(128, a.nInt - g0);
+  {
+    const float* src = a.faces + static_cast<size_t>(g0) * FW;
+    for (int i = threadIdx.x; i < nE * (FW / 4); i += 128) {
+      const int e = i / (FW / 4), c = i - e * (FW / 4);
+      const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(&sf[e * FWP + 4 * c]));
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src + 4 * i));
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+  }
+  const int g = g0 + threadIdx.x;
+  const bool active = g < a.nInt;
   double smax = 0.0;
-  if (g < a.nInt) {
+  float bh[4] = {1.f, 0.f, 0.f, 1.f}, bl[4] = {0.f, 0.f, 0.f, 0.f}, dB[4] = {0.f, 0.f, 0.f, 0.f};
+  float nx = 0.f, ny = 0.f, oohK = 0.f;
+  if (active) {
     const int kL = a.ekL[g], kR = a.ekR[g];
-    const float nx = a.enx[g], ny = a.eny[g];
-    const float oohK = a.eoohK[g];
-    float bh[4], bl[4], dB[4];
+    nx = a.enx[g];
+    ny = a.eny[g];
+    oohK = a.eoohK[g];
     const float4* pL = reinterpret_cast<const float4*>(a.base + static_cast<size_t>(kL) * 4);
     const float4* pR = reinterpret_cast<const float4*>(a.base + static_cast<size_t>(kR) * 4);
     const float4 L01 = pL[0], L23 = pL[1], R01 = pR[0], R23 = pR[1];
@@ -383,21 +414,22 @@ __global__ void __launch_bounds__(128) k_mixed_edge(MixedArgs a) {
     dB[1] = df_diff(R01.z, R01.w, bh[1], bl[1]);
     dB[2] = df_diff(R23.x, R23.y, bh[2], bl[2]);
     dB[3] = df_diff(R23.z, R23.w, bh[3], bl[3]);
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncthreads();
+  if (active) {
     const float gm1 = a.gamma - 1.0f;
     const BasePrim b = base_prim(bh, gm1);
     const Gas<float> gf{a.gamma, gm1, 1.0f / gm1};
-    const float* fL = a.faces + static_cast<size_t>(g) * 2 * 4 * NEP;
-    const float* fR = fL + 4 * NEP;
-    float dl[4][NEP], dr[4][NEP];
+    float fr[FW];  // [side][variable][NEP]
+    const float4* rec = reinterpret_cast<const float4*>(&sf[threadIdx.x * FWP]);
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-#pragma unroll
-      for (int p = 0; p < NEP; p += 2) {
-        const float2 l = reinterpret_cast<const float2*>(fL + c * NEP)[p / 2];
-        const float2 r = reinterpret_cast<const float2*>(fR + c * NEP)[p / 2];
-        dl[c][p] = l.x; dl[c][p + 1] = l.y;
-        dr[c][p] = r.x; dr[c][p + 1] = r.y;
-      }
+    for (int c = 0; c < FW / 4; ++c) {
+      const float4 v = rec[c];
+      fr[4 * c] = v.x;
+      fr[4 * c + 1] = v.y;
+      fr[4 * c + 2] = v.z;
+      fr[4 * c + 3] = v.w;
     }
     float fo[4][NE];
     float sm = 0.0f;
@@ -406,8 +438,8 @@ __global__ void __launch_bounds__(128) k_mixed_edge(MixedArgs a) {
       float ql[4], qr[4], f[4];
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        ql[c] = dl[c][p];
-        qr[c] = dr[c][NE - 1 - p] + dB[c];
+        ql[c] = fr[c * NEP + p];
+        qr[c] = fr[4 * NEP + c * NEP + NE - 1 - p] + dB[c];
       }
       if (RoeER) {
         double QLd[4], QRd[4], fd[4], Fx[4], Fy[4], bd[4];
@@ -432,19 +464,27 @@ __global__ void __launch_bounds__(128) k_mixed_edge(MixedArgs a) {
       const float QL[4] = {b.rho + ql[0], b.m + ql[1], b.n + ql[2], b.E + ql[3]};
       sm = fmaxf(sm, oohK * (speed(QL[0], QL[1], QL[2]) + sound_speed(gf, QL[0], QL[1], QL[2], QL[3])));
     }
-    float* out = a.fhat + static_cast<size_t>(g) * 4 * NEP;
+    float cr[4];
+    delta_normal_flux(b, dB, nx, ny, gm1, cr);
+    float* o = &so[threadIdx.x * OWP];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
 #pragma unroll
-      for (int p = 0; p + 1 < NE; p += 2)
-        reinterpret_cast<float2*>(out + c * NEP)[p / 2] = make_float2(fo[c][p], fo[c][p + 1]);
-      if (NE & 1) out[c * NEP + NE - 1] = fo[c][NE - 1];
+      for (int p = 0; p < NEP; ++p) o[c * NEP + p] = (p < NE) ? fo[c][p < NE ? p : 0] : 0.0f;
+      o[4 * NEP + c] = cr[c];
     }
-    float cr[4];
-    delta_normal_flux(b, dB, nx, ny, gm1, cr);
-    reinterpret_cast<float4*>(a.corr)[g] = make_float4(cr[0], cr[1], cr[2], cr[3]);
     smax = static_cast<double>(sm);
     a.edgeSpeed[g] = smax;
+  }
+  __syncthreads();
+  {
+    float* fdst = a.fhat + static_cast<size_t>(g0) * 4 * NEP;
+    for (int i = threadIdx.x; i < nE * NEP; i += 128) {
+      const int e = i / NEP, c = i - e * NEP;
+      reinterpret_cast<float4*>(fdst)[i] = *reinterpret_cast<const float4*>(&so[e * OWP + 4 * c]);
+    }
+    if (active)
+      reinterpret_cast<float4*>(a.corr)[g] = *reinterpret_cast<const float4*>(&so[threadIdx.x * OWP + 4 * NEP]);
   }
   smax = warp_max(smax);
   if ((threadIdx.x & 31) == 0)
@@ -545,52 +585,80 @@ __device__ __forceinline__ void prefetch_l2(const void* p) {
   asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
 }
 
-// L2 prefetch of what stage_tail will read: the compensated state at point 0
-// (stages 0-3), or the whole compensated state, the stage-2/3 increments and
-// the stage-3 RHS (stage 4).
+// L2 prefetch of what stage_tail will read for block blk, issued by one warp
+// per variable n: the compensated state at point 0 (stages 0-3), or the whole
+// compensated state, the stage-2/3 increments and the stage-3 RHS (stage 4).
+// With K % 4 == 0 every row of the block is 128 contiguous, 16-byte aligned
+// bytes and lane j bulk-prefetches rows j, j+32, ...; otherwise each thread
+// prefetches its own element's lines.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(p), "r"(bytes) : "memory");
+}
 template <int N>
-__device__ __forceinline__ void stage_tail_prefetch(const MixedArgs& a, size_t off, size_t sK, int s) {
+__device__ __forceinline__ void stage_tail_prefetch(const MixedArgs& a, int blk, int n, int lane, size_t sK, int s) {
   constexpr int NP = MixedDims<N>::NP;
-  if (s < 0) return;
-  if (s < 4) {
-    prefetch_l2(a.Qhi + off);
-    prefetch_l2(a.Qlo + off);
+  if (s < 0 || a.rhsOnly) return;
+  const size_t base = static_cast<size_t>(n) * NP * sK + static_cast<size_t>(blk) * 32;
+  const bool full = (a.K & 3) == 0 && blk * 32 + 32 <= a.K;
+  if (!full) {
+    const int k = blk * 32 + lane;
+    if (k >= a.K) return;
+    const int rows = (s < 4) ? 1 : NP;
+    for (int r = 0; r < rows; ++r) {
+      prefetch_l2(a.Qhi + base + lane + r * sK);
+      prefetch_l2(a.Qlo + base + lane + r * sK);
+      if (s == 4) {
+        prefetch_l2(a.D[2] + base + lane + r * sK);
+        prefetch_l2(a.D[3] + base + lane + r * sK);
+        prefetch_l2(a.R3 + base + lane + r * sK);
+      }
+    }
     return;
   }
-#pragma unroll
-  for (int r = 0; r < NP; ++r) {
-    prefetch_l2(a.Qhi + off + r * sK);
-    prefetch_l2(a.Qlo + off + r * sK);
-    prefetch_l2(a.D[2] + off + r * sK);
-    prefetch_l2(a.D[3] + off + r * sK);
-    prefetch_l2(a.R3 + off + r * sK);
+  if (s < 4) {
+    if (lane < 2) bulk_prefetch_l2((lane ? a.Qlo : a.Qhi) + base, 128);
+    return;
   }
+  for (int it = lane; it < 5 * NP; it += 32) {
+    const int arr = it / NP, r = it - arr * NP;
+    const float* p = arr == 0 ? a.Qhi : arr == 1 ? a.Qlo : arr == 2 ? a.D[2] : arr == 3 ? a.D[3] : a.R3;
+    bulk_prefetch_l2(p + base + r * sK, 128);
+  }
+}
+
+// The stage's global time step (calculateGlobalDT, euler.go:945-971, with the
+// viscous cap and the FinalTime clip), computed once per CTA.
+__device__ __forceinline__ double global_stage_dt(const MixedArgs& a, int s) {
+  const double gm = __longlong_as_double(static_cast<long long>(a.sc->gmax[s]));
+  double dtk = a.cfl / gm;
+  if (a.gviscS) dtk = fmin(dtk, a.cdiff / __longlong_as_double(static_cast<long long>(a.gviscS[s])));
+  const double t = a.sc->time;
+  if (t + dtk > a.finalTime) dtk = a.finalTime - t;
+  return dtk;
+}
+// Whether a stage kernel needs the global time step.
+__device__ __forceinline__ bool needs_global_dt(const MixedArgs& a, int s) {
+  return s >= 0 && !a.rhsOnly && !a.localDT;
 }
 
 // The stage update after the divergence (shared by the FMA and tensor-core
 // stage kernels): the RHS goes to rhsOut (stage -1) or into the SSP increments,
 // the next stage's faces and reference state, and at stage 4 the compensated
-// state and the residual partials.
+// state and the residual partials.  dtk is the element's time step: its local
+// one with local time stepping, else the stage's global one.
 template <int N>
 __device__ __forceinline__ void stage_tail(const MixedArgs& a, const int eslot[3], int n, int k,
                                            size_t off, size_t sK, int s, const float rhs[], const float dq0[],
-                                           const float ds[], double dtLocal, float& rmax, float& rabs,
+                                           const float ds[], double dtk, float& rmax, float& rabs,
                                            float& rs2) {
   constexpr int NP = MixedDims<N>::NP, NPP = MixedDims<N>::NPP;
   if (s < 0 || a.rhsOnly) {
 #pragma unroll
     for (int r = 0; r < NP; ++r) a.rhsOut[off + r * sK] = rhs[r];
   } else {
-    double dtk;
     if (a.localDT) {
-      dtk = dtLocal;
       if (n == 0) a.DT[k] = dtk;
     } else {
-      const double gm = __longlong_as_double(static_cast<long long>(a.sc->gmax[s]));
-      dtk = a.cfl / gm;
-      if (a.gviscS) dtk = fmin(dtk, a.cdiff / __longlong_as_double(static_cast<long long>(a.gviscS[s])));
-      const double t = a.sc->time;
-      if (t + dtk > a.finalTime) dtk = a.finalTime - t;
       if (k == 0 && n == 0) a.sc->dt[s] = dtk;
     }
     const float dt = static_cast<float>(dtk);
@@ -656,23 +724,34 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const int eslot[3
 
 // (b)+(e): delta-form divergence, SSP stage update on the FP32 increments, and
 // the next stage's faces / reference states.  stage -1 writes the RHS only.
+//
+// One CTA = 32 elements x 4 variables.  The element's stage inputs (dQ0, D_s)
+// are staged in shared memory by coalesced row loads; its three edge records
+// (fhat, 4 x NEP floats, and corr, 4 floats, per edge) are gathered as 16-byte
+// cp.async chunks shared out over the element's four threads, waited for after
+// the interior flux work.
+template <int N>
+struct StageDims {
+  static constexpr int NEP = MixedDims<N>::NEP;
+  static constexpr int CH = NEP + 1;    // 16-byte chunks per edge record
+  static constexpr int RW = 3 * CH * 4;  // floats per element's three records
+};
+
 template <int N>
 __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
-  constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NE3 = MixedDims<N>::NE3;
-  constexpr int NPP = MixedDims<N>::NPP, NEP = MixedDims<N>::NEP;
-  __shared__ float sdq[4][NP][33];
+  constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NPP = MixedDims<N>::NPP;
+  constexpr int NEP = MixedDims<N>::NEP, CH = StageDims<N>::CH, RW = StageDims<N>::RW;
+  __shared__ float sq0[4][NP][33];
+  __shared__ float sds[4][NP][33];
   __shared__ float sbase[4][32];
-  __shared__ float sfh[4][NE3][32];   // this element's edge fluxes, prefetched
-  __shared__ float scorr[4][3][32];
+  __shared__ __align__(16) float srec[32 * RW];
+  __shared__ double sdt;
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = blockIdx.x * 32 + lane;
   const bool active = k < a.K;
   const size_t sK = static_cast<size_t>(a.K);
   const size_t off = static_cast<size_t>(n) * NP * sK + k;
   const int s = a.stage;
-  // Prefetch the element's edge fluxes (a gather: 3 edges x NpEdge per
-  // variable) into shared memory asynchronously; the interior work below hides
-  // the latency.  Each thread later reads only what it copied itself.
   int eslot[3] = {0, 0, 0};
   float eII[3] = {0.f, 0.f, 0.f};
   if (active) {
@@ -680,34 +759,30 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
     for (int e = 0; e < 3; ++e) {
       eslot[e] = a.eslot[e * sK + k];
       eII[e] = a.II[e * sK + k];
-      const float* fh = a.fhat + (static_cast<size_t>(eslot[e] >> 1) * 4 + n) * NEP;
+    }
+    // Chunks c = n, n+4, ... of the element's 3 x CH record chunks.
 #pragma unroll
-      for (int p = 0; p < NE; ++p) {
-        const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(&sfh[n][e * NE + p][lane]));
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(fh + p));
-      }
-      if (eslot[e] & 1) {
-        const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(&scorr[n][e][lane]));
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst),
-                     "l"(a.corr + static_cast<size_t>(eslot[e] >> 1) * 4 + n));
+    for (int t = 0; t < (3 * CH + 3) / 4; ++t) {
+      const int c = n + 4 * t;
+      if (c < 3 * CH) {
+        const int e = c / CH, j = c - e * CH;
+        const size_t g = static_cast<size_t>((e == 0 ? eslot[0] : (e == 1 ? eslot[1] : eslot[2])) >> 1);
+        const float* src = (j < NEP) ? a.fhat + g * 4 * NEP + 4 * j : a.corr + g * 4;
+        const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(&srec[lane * RW + 4 * c]));
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src));
       }
     }
-    asm volatile("cp.async.commit_group;\n" ::);
   }
-  // The stage update's own inputs are needed only at the end: prefetch them
-  // into L2 now so their DRAM latency overlaps the flux and divergence work
-  // (the kernel is bound by load latency, not bandwidth).
-  if (active) stage_tail_prefetch<N>(a, off, sK, s);
-  // Stage input deltas relative to point 0 of the stage state (the update
-  // re-reads dQ0 and D_s at the end, from cache, rather than keeping them live).
-  // Geometry is loaded here too, before the barrier, so its latency overlaps.
+  asm volatile("cp.async.commit_group;\n" ::);
+  stage_tail_prefetch<N>(a, blockIdx.x, n, lane, sK, s);
   float Jd = 0.f, J0 = 0.f, J1 = 0.f, J2 = 0.f, J3 = 0.f, ooJ = 0.f;
   if (active) {
-    const float* dsrc = (s >= 1) ? a.D[s] + off : nullptr;
-    const float ds0 = dsrc ? dsrc[0] : 0.0f;
 #pragma unroll
-    for (int i = 0; i < NP; ++i)
-      sdq[n][i][lane] = a.dQ0[off + i * sK] + (dsrc ? dsrc[i * sK] - ds0 : 0.0f);
+    for (int i = 0; i < NP; ++i) sq0[n][i][lane] = a.dQ0[off + i * sK];
+    if (s >= 1) {
+#pragma unroll
+      for (int i = 0; i < NP; ++i) sds[n][i][lane] = a.D[s][off + i * sK];
+    }
     sbase[n][lane] = a.base[static_cast<size_t>(k) * 4 + n].x;
     Jd = a.geo[k];
     J0 = a.geo[sK + k];
@@ -718,26 +793,33 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
   }
   // Local time step of this stage: DT persists across stages, so every thread
   // of the element reads it before the barrier and one writes it after.
-  double dtLocal = 0.0;
+  double dtk = 0.0;
   if (active && a.localDT && s >= 0 && !a.rhsOnly) {
     double v = (s == 0) ? -100.0 : a.DT[k];
 #pragma unroll
     for (int e = 0; e < 3; ++e) v = fmax(v, a.edgeSpeed[eslot[e] >> 1]);
-    dtLocal = a.cfl / v;
+    dtk = a.cfl / v;
   }
+  if (threadIdx.x == 0 && needs_global_dt(a, s)) sdt = global_stage_dt(a, s);
   __syncthreads();
-  float rmax = -3.4028235e38f, rabs = 0.0f, rs2 = 0.0f;
+  if (needs_global_dt(a, s)) dtk = sdt;
+  float acc[NP];
+#pragma unroll
+  for (int r = 0; r < NP; ++r) acc[r] = 0.0f;
   if (active) {
     const float bq[4] = {sbase[0][lane], sbase[1][lane], sbase[2][lane], sbase[3][lane]};
     const float gm1 = a.gamma - 1.0f;
     const BasePrim b = base_prim(bq, gm1);
-    float acc[NP];
+    float d0[4];
 #pragma unroll
-    for (int r = 0; r < NP; ++r) acc[r] = 0.0f;
-    // Interior transformed delta fluxes, DivInt columns 0..2NP-1.
+    for (int c = 0; c < 4; ++c) d0[c] = (s >= 1) ? sds[c][0][lane] : 0.0f;
+    // Interior transformed delta fluxes, DivInt columns 0..2NP-1; the stage
+    // delta relative to point 0 is dQ0 + (D_s - D_s(point 0)).
 #pragma unroll
     for (int i = 0; i < NP; ++i) {
-      const float d[4] = {sdq[0][i][lane], sdq[1][i][lane], sdq[2][i][lane], sdq[3][i][lane]};
+      float d[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) d[c] = sq0[c][i][lane] + ((s >= 1) ? sds[c][i][lane] - d0[c] : 0.0f);
       const DeltaPrim q = delta_prim(b, d, gm1);
       float fx, fy;
       delta_flux_c(n, b, d, q, &fx, &fy);
@@ -747,16 +829,29 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
       for (int r = 0; r < NP; ++r)
         acc[r] = fmaf(div_op<N>(i * NPP + r), Fr, fmaf(div_op<N>((NP + i) * NPP + r), Fs, acc[r]));
     }
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncthreads();  // every thread's record chunks
+  float rmax = -3.4028235e38f, rabs = 0.0f, rs2 = 0.0f;
+  if (active) {
     // Edge DOFs: IInII * (s fhat - n_e.F(Qb)), owner order / reversed for the right side.
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
+      const float* rec = &srec[lane * RW + e * CH * 4];
       const bool right = eslot[e] & 1;
       const float ii = eII[e];
-      const float cc = right ? scorr[n][e][lane] : 0.0f;
+      const float cc = right ? rec[4 * NEP + n] : 0.0f;
+      float v[NEP];
+      const float2* rp = reinterpret_cast<const float2*>(rec + n * NEP);
+#pragma unroll
+      for (int q = 0; q < NEP / 2; ++q) {
+        const float2 t = rp[q];
+        v[2 * q] = t.x;
+        v[2 * q + 1] = t.y;
+      }
 #pragma unroll
       for (int p = 0; p < NE; ++p) {
-        const float dof = right ? -(sfh[n][e * NE + NE - 1 - p][lane] - cc) * ii : sfh[n][e * NE + p][lane] * ii;
+        const float dof = right ? -(v[NE - 1 - p] - cc) * ii : v[p] * ii;
 #pragma unroll
         for (int r = 0; r < NP; ++r) acc[r] = fmaf(div_op<N>((2 * NP + e * NE + p) * NPP + r), dof, acc[r]);
       }
@@ -765,10 +860,10 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
 #pragma unroll
     for (int r = 0; r < NP; ++r) {
       rhs[r] = -acc[r] * ooJ;
-      dq0[r] = a.dQ0[off + r * sK];
-      ds[r] = (s >= 1) ? a.D[s][off + r * sK] : 0.0f;
+      dq0[r] = sq0[n][r][lane];
+      ds[r] = (s >= 1) ? sds[n][r][lane] : 0.0f;
     }
-    stage_tail<N>(a, eslot, n, k, off, sK, s, rhs, dq0, ds, dtLocal, rmax, rabs, rs2);
+    stage_tail<N>(a, eslot, n, k, off, sK, s, rhs, dq0, ds, dtk, rmax, rabs, rs2);
   }
   if (s == 4 && !a.rhsOnly) {
     const unsigned long long km = warp_max_u64(order_key(static_cast<double>(rmax)));

@@ -66,7 +66,7 @@ template <int N>
 __global__ void __launch_bounds__(128) k_mixed_diss_update(MixedArgs a, UpdateArgs<double> u) {
   constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NE3 = MixedDims<N>::NE3;
   constexpr int NF = MixedDims<N>::NF, NR = NP + NE3;
-  __shared__ double sD[NP * NF], sV[NP * NP], sVi[NP * NP], smf[NP];
+  __shared__ double sD[NP * NF], sV[NP * NP], sVi[NP * NP], smf[NP], sdt;
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = blockIdx.x * 32 + lane;
   const bool active = k < a.K;
@@ -96,7 +96,9 @@ __global__ void __launch_bounds__(128) k_mixed_diss_update(MixedArgs a, UpdateAr
   stage_operator(sV, u.V, NP * NP);
   stage_operator(sVi, u.Vinv, NP * NP);
   stage_operator(smf, u.mf, NP);
+  if (threadIdx.x == 0 && needs_global_dt(a, s)) sdt = global_stage_dt(a, s);
   __syncthreads();
+  if (needs_global_dt(a, s)) dtLocal = sdt;
   float rmax = -3.4028235e38f, rabs = 0.0f, rs2 = 0.0f;
   if (active) {
     const double Jd = u.Jdet[k], oojd = 1.0 / Jd;

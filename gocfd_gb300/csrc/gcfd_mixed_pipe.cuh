@@ -111,6 +111,7 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_pipe(const __grid_consta
   }
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + L::BAR);  // [0], [1]: tile copies; [2]: MMA
   uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + L::BAR + 32);
+  double* sdt = reinterpret_cast<double*>(sm + L::BAR + 40);
   float* sOps = reinterpret_cast<float*>(sm + L::OPS);
   float* sfh = reinterpret_cast<float*>(sm + L::FH);      // [4][NE3][32]
   float* scorr = reinterpret_cast<float*>(sm + L::CORR);  // [4][3][32]
@@ -127,7 +128,9 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_pipe(const __grid_consta
     tc::alloc(tslot, NCOLS);
     tc::fence_before();
   }
+  if (threadIdx.x == 0 && needs_global_dt(a, s)) *sdt = global_stage_dt(a, s);
   __syncthreads();
+  const double dtGlobal = needs_global_dt(a, s) ? *sdt : 0.0;
   if (TC) tc::fence_after();
   const uint32_t tbase = TC ? *tslot : 0u;
   const uint32_t trow = tbase + (static_cast<uint32_t>(n * 32) << 16);  // this warp's TMEM lanes
@@ -225,7 +228,7 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_pipe(const __grid_consta
     asm volatile("cp.async.commit_group;\n" ::);
     // Local time step (DT persists across stages; warp 0 rewrites it in the
     // update, after a CTA barrier).
-    double dtLocal = 0.0;
+    double dtLocal = dtGlobal;
     if (active && a.localDT && s >= 0 && !a.rhsOnly) {
       double v = (s == 0) ? -100.0 : a.DT[k];
 #pragma unroll

@@ -48,6 +48,7 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
   __shared__ float scorr[4][3][32];
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base;
+  __shared__ double sdt;
   for (int i = threadIdx.x; i < 2 * BSZ; i += blockDim.x) sB[i] = a.Btc[i];
   tc::fence_proxy_async();  // sB is read by the tensor core
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -82,7 +83,7 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
     }
     asm volatile("cp.async.commit_group;\n" ::);
   }
-  if (active) stage_tail_prefetch<N>(a, off, sK, s);
+  stage_tail_prefetch<N>(a, blockIdx.x, n, lane, sK, s);
   float dq0[NP], ds[NP];
   if (active) {
 #pragma unroll
@@ -98,14 +99,16 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
     for (int i = 0; i < NP; ++i) sdq[n][i][lane] = dq0[i] + (ds[i] - ds[0]);
     sbase[n][lane] = a.base[static_cast<size_t>(k) * 4 + n].x;
   }
-  double dtLocal = 0.0;
+  double dtk = 0.0;
   if (active && a.localDT && s >= 0 && !a.rhsOnly) {
     double v = (s == 0) ? -100.0 : a.DT[k];
 #pragma unroll
     for (int e = 0; e < 3; ++e) v = fmax(v, a.edgeSpeed[eslot[e] >> 1]);
-    dtLocal = a.cfl / v;
+    dtk = a.cfl / v;
   }
+  if (threadIdx.x == 0 && needs_global_dt(a, s)) sdt = global_stage_dt(a, s);
   __syncthreads();
+  if (needs_global_dt(a, s)) dtk = sdt;
   tc::fence_after();
   const uint32_t tbase = tmem_base;
   const uint32_t trow = tbase + (static_cast<uint32_t>(n * 32) << 16);  // this warp's 32 TMEM lanes
@@ -208,7 +211,7 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
     float rhs[NP];
 #pragma unroll
     for (int r = 0; r < NP; ++r) rhs[r] = -__uint_as_float(dv[r]) * ooJ;
-    stage_tail<N>(a, eslot, n, k, off, sK, s, rhs, dq0, ds, dtLocal, rmax, rabs, rs2);
+    stage_tail<N>(a, eslot, n, k, off, sK, s, rhs, dq0, ds, dtk, rmax, rabs, rs2);
   }
   tc::fence_before();
   __syncthreads();
