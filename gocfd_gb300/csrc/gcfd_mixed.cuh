@@ -62,10 +62,12 @@ __device__ __forceinline__ BasePrim base_prim(const float b[4], float gm1) {
 // Velocity and pressure deltas of state Qb + d relative to Qb.
 struct DeltaPrim {
   float du, dv, dp;
+  float ir;  // 1 / (rho_b + d_rho)
 };
 __device__ __forceinline__ DeltaPrim delta_prim(const BasePrim& b, const float d[4], float gm1) {
   DeltaPrim r;
   const float ir = __fdividef(1.0f, b.rho + d[0]);  // ~1 ulp; it only scales deltas
+  r.ir = ir;
   r.du = (d[1] - b.u * d[0]) * ir;
   r.dv = (d[2] - b.v * d[0]) * ir;
   r.dp = gm1 * (d[3] - 0.5f * (b.m * r.du + d[1] * b.u + d[1] * r.du + b.n * r.dv + d[2] * b.v +
@@ -173,6 +175,64 @@ __device__ __forceinline__ void riemann_delta(int kind, const BasePrim& b, const
   f[1] += nx * d1 - ny * d2;
   f[2] += ny * d1 + nx * d2;
   f[3] += d3;
+}
+
+// RoeFlux (fluxes.go:284-413) in delta form, as riemann_delta's Roe branch,
+// with one reciprocal per quantity instead of a division per use (the Roe
+// averages, 1/C and 1/C^2 each once), plus the left state's wave speed
+// |u| + c for the time step from the same primitives.
+__device__ __forceinline__ void roe_delta_fast(const BasePrim& b, const float dL[4], const float dR[4],
+                                               float nx, float ny, float gamma, float f[4], float* waveL) {
+  const float gm1 = gamma - 1.0f;
+  const DeltaPrim qL = delta_prim(b, dL, gm1), qR = delta_prim(b, dR, gm1);
+  float cL[4], cR[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    float fx, fy;
+    delta_flux_c(c, b, dL, qL, &fx, &fy);
+    cL[c] = nx * fx + ny * fy;
+    delta_flux_c(c, b, dR, qR, &fx, &fy);
+    cR[c] = nx * fx + ny * fy;
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) f[c] = 0.5f * (cL[c] + cR[c]);
+  const float rhoL = b.rho + dL[0], rhoR = b.rho + dR[0];
+  const float uxL = b.u + qL.du, uyL = b.v + qL.dv, uxR = b.u + qR.du, uyR = b.v + qR.dv;
+  const float uL = uxL * nx + uyL * ny, vL = -uxL * ny + uyL * nx;
+  const float uR = uxR * nx + uyR * ny, vR = -uxR * ny + uyR * nx;
+  const float pL = b.p + qL.dp, pR = b.p + qR.dp;
+  const float hL = (b.E + dL[3] + pL) * qL.ir, hR = (b.E + dR[3] + pR) * qR.ir;
+  const float rLs = sqrtf(rhoL), rRs = sqrtf(rhoR);
+  const float irs = __fdividef(1.0f, rLs + rRs);
+  const float rho = rLs * rRs;
+  const float u = (rLs * uL + rRs * uR) * irs;
+  const float v = (rLs * vL + rRs * vR) * irs;
+  const float h = (rLs * hL + rRs * hR) * irs;
+  const float c2 = gm1 * (h - 0.5f * (u * u + v * v));
+  const float C = sqrtf(c2);
+  const float iC = __fdividef(1.0f, C), ic2 = iC * iC;
+  const float dun = (qR.du - qL.du) * nx + (qR.dv - qL.dv) * ny;     // uR - uL
+  const float dvt = -(qR.du - qL.du) * ny + (qR.dv - qL.dv) * nx;    // vR - vL
+  const float dpj = qR.dp - qL.dp;                                    // pR - pL
+  const float drj = dR[0] - dL[0];                                    // rhoR - rhoL
+  const float t1 = 0.5f * (rho * dun) * iC, t2 = 0.5f * dpj * ic2;
+  float dW1 = t2 - t1;
+  float dW2 = drj - dpj * ic2;
+  float dW3 = rho * dvt;
+  float dW4 = t1 + t2;
+  dW1 = fabsf(u - C) * dW1;
+  dW2 = fabsf(u) * dW2;
+  dW3 = fabsf(u) * dW3;
+  dW4 = fabsf(u + C) * dW4;
+  const float d0 = -0.5f * (dW1 + dW2 + dW4);
+  const float d1 = -0.5f * (dW1 * (u - C) + dW2 * u + dW4 * (u + C));
+  const float d2 = -0.5f * (dW1 * v + dW2 * v + dW3 + dW4 * v);
+  const float d3 = -0.5f * (dW1 * (h - u * C) + 0.5f * dW2 * (u * u + v * v) + dW3 * v + dW4 * (h + u * C));
+  f[0] += d0;
+  f[1] += nx * d1 - ny * d2;
+  f[2] += ny * d1 + nx * d2;
+  f[3] += d3;
+  *waveL = sqrtf(uxL * uxL + uyL * uyL) + sqrtf(fabsf(gamma * pL * qL.ir));
 }
 
 // ---------------------------------------------------------------------------
@@ -456,13 +516,19 @@ __global__ void __launch_bounds__(128, RoeER ? 1 : 5) k_mixed_edge(MixedArgs a) 
 #pragma unroll
         for (int c = 0; c < 4; ++c)
           f[c] = static_cast<float>(fd[c] - (static_cast<double>(nx) * Fx[c] + static_cast<double>(ny) * Fy[c]));
+      } else if (a.flux == kFluxRoe) {
+        float w;
+        roe_delta_fast(b, ql, qr, nx, ny, a.gamma, f, &w);
+        sm = fmaxf(sm, oohK * w);
       } else {
         riemann_delta(a.flux, b, ql, qr, nx, ny, a.gamma, f);
       }
 #pragma unroll
       for (int c = 0; c < 4; ++c) fo[c][p] = f[c];
-      const float QL[4] = {b.rho + ql[0], b.m + ql[1], b.n + ql[2], b.E + ql[3]};
-      sm = fmaxf(sm, oohK * (speed(QL[0], QL[1], QL[2]) + sound_speed(gf, QL[0], QL[1], QL[2], QL[3])));
+      if (RoeER || a.flux != kFluxRoe) {
+        const float QL[4] = {b.rho + ql[0], b.m + ql[1], b.n + ql[2], b.E + ql[3]};
+        sm = fmaxf(sm, oohK * (speed(QL[0], QL[1], QL[2]) + sound_speed(gf, QL[0], QL[1], QL[2], QL[3])));
+      }
     }
     float cr[4];
     delta_normal_flux(b, dB, nx, ny, gm1, cr);
