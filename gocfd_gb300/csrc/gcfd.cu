@@ -576,12 +576,19 @@ struct MixedLaunch {
     prepare(c, c->Qtmp);
     if (c->diss) Launch<N, double>::diss_front(c, -1, c->Qtmp);
     edges(c, -1, c->Qtmp, &c->sc->rhs_time, &c->sc->gmax[0], false);
-    if (c->diss) Launch<N, double>::diss_middle(c, -1, c->Qtmp);
+    if (c->diss) diss_middle(c, -1, c->Qtmp);
     stage_kernel(c, args(c, -1, c->Qtmp, &c->sc->rhs_time, &c->sc->gmax[0]));
     if (c->diss)
       k_mixed_diss_update<N><<<gridE(c), 128, 0, c->stream>>>(args(c, -1, c->Qtmp, &c->sc->rhs_time,
                                                                     &c->sc->gmax[0]),
                                                                Launch<N, double>::update_args(c, -1, c->Qtmp));
+  }
+  // The RT gradient in FP32 (delta form), then the FP64 viscous edge fluxes.
+  static void diss_middle(gcfd_ctx* c, int stage, double* Qs) {
+    const DissArgs d = Launch<N, double>::diss_args(c, stage, Qs);
+    constexpr int NF = Dims<N>::NF;
+    k_diss_grad_mixed<N><<<(c->K + 127) / 128, 128, sizeof(float) * (NF * NF + NF * 3), c->stream>>>(d);
+    k_diss_edge<N><<<(c->nInt + c->nBC + 127) / 128, 128, 0, c->stream>>>(d);
   }
   // One stage with the PerssonC0 dissipation: FP64 stage state for the
   // dissipation kernels (Q[1] is free on the mixed path), the Euler RHS of the
@@ -596,7 +603,7 @@ struct MixedLaunch {
       k_mixed_relimit<N><<<gridE(c), 128, 0, c->stream>>>(args(c, 2, c->Q[0], &c->sc->time, &c->sc->gmax[2]),
                                                           Qs64);
     edges(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s], true);
-    L::diss_middle(c, s, Qs64);
+    diss_middle(c, s, Qs64);
     MixedArgs m = args(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]);
     m.rhsOnly = 1;
     stage_kernel(c, m);

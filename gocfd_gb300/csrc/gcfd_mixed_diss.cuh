@@ -1,10 +1,11 @@
 // PerssonC0 shock capturing on the mixed path: the Euler RHS stays in the
-// FP32 delta form (k_mixed_stage with rhsOnly), the dissipation runs in FP64
-// on the stage state (the FP64 kernels of gcfd_diss.cuh: sensor, vertex
-// maxima, limiter, RT gradient, viscous edges), and k_mixed_diss_update adds
-// AddDissipation, applies the modal filter and the viscous time-step limit,
-// then performs the mixed stage update (stage_tail).  The conserved state
-// keeps its compensated FP32 accumulation.
+// FP32 delta form (k_mixed_stage with rhsOnly); the sensor, vertex maxima,
+// limiter and viscous edge fluxes run in FP64 on the stage state (the kernels
+// of gcfd_diss.cuh); the two heavy parts run in FP32: the RT gradient
+// (k_diss_grad_mixed, on the element's deltas U - U_0) and k_mixed_diss_update,
+// which adds AddDissipation, applies the modal filter and the viscous time-step
+// limit, then performs the mixed stage update (stage_tail).  The conserved
+// state keeps its compensated FP32 accumulation.
 #pragma once
 #include "gcfd_diss.cuh"
 #include "gcfd_mixed.cuh"
@@ -59,6 +60,102 @@ __global__ void __launch_bounds__(128) k_mixed_relimit(MixedArgs a, const double
   a.base[static_cast<size_t>(k) * 4 + n] = make_float2(h, l);
 }
 
+// limit_filter_modal in FP32.
+template <int NP>
+__device__ __forceinline__ void limit_filter_modal_f(float u[NP], const float* sV, const float* sVi,
+                                                     const float* mf, float alpha) {
+  float m[NP];
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int j = 0; j < NP; ++j) acc = fmaf(sVi[i * NP + j], u[j], acc);
+    m[i] = acc;
+  }
+#pragma unroll
+  for (int i = 1; i < NP; ++i) m[i] *= mf[i] * (1.0f - alpha);
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int j = 0; j < NP; ++j) acc = fmaf(sV[i * NP + j], m[j], acc);
+    u[i] = acc;
+  }
+}
+
+// eps * grad(Q) at the interior and edge flux points (k_diss_grad,
+// CalculateEpsilonGradient, dissipation.go:244-272) in FP32.  The RT gradient
+// of a constant field is zero, so it is taken of U - U_0 (U_0 the element's
+// value at solution point 0, subtracted in FP64): the rounding then scales with
+// the variation of U across the element, not with U.  FP64 inputs and outputs.
+template <int N>
+__global__ void __launch_bounds__(128) k_diss_grad_mixed(DissArgs a) {
+  constexpr int NP = DissDims<N>::NP, NE = DissDims<N>::NE, NE3 = DissDims<N>::NE3;
+  constexpr int NF = DissDims<N>::NF, NR = DissDims<N>::NR;
+  extern __shared__ float smf32[];
+  float* sDiv = smf32;          // NF x NF
+  float* sB = smf32 + NF * NF;  // NF x 3
+  stage_operator(sDiv, a.Div, NF * NF);
+  stage_operator(sB, a.Bary, NF * 3);
+  __syncthreads();
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.K) return;
+  const size_t sK = static_cast<size_t>(a.K);
+  const float J0 = static_cast<float>(a.Jinv[k]), J1 = static_cast<float>(a.Jinv[sK + k]);
+  const float J2 = static_cast<float>(a.Jinv[2 * sK + k]), J3 = static_cast<float>(a.Jinv[3 * sK + k]);
+  const double ooJd = 1.0 / a.Jdet[k];
+  float ev[3], mx[3], my[3];
+  int eg[3], eLn[3];
+  bool own[3];
+#pragma unroll
+  for (int v = 0; v < 3; ++v) ev[v] = static_cast<float>(vdouble(a.epsV, a.etov[v * sK + k]));
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    eg[e] = a.elemEdge[e * sK + k];
+    own[e] = a.ekL[eg[e]] == k && (a.eLR[eg[e]] & 3) == e;
+    eLn[e] = a.eLR[eg[e]] & 3;
+    const double ii = a.IIE[e * sK + k];
+    mx[e] = static_cast<float>(ooJd * a.nxE[e * sK + k] * ii);
+    my[e] = static_cast<float>(ooJd * a.nyE[e * sK + k] * ii);
+  }
+#pragma unroll 1
+  for (int n = 0; n < 4; ++n) {
+    const double u0 = a.Qs[(n * NP) * sK + k];
+    float U[NP], Ue[NE3];
+#pragma unroll
+    for (int i = 0; i < NP; ++i) U[i] = static_cast<float>(a.Qs[(n * NP + i) * sK + k] - u0);
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      const int kl = a.ekL[eg[e]];
+#pragma unroll
+      for (int p = 0; p < NE; ++p) {
+        const int ii = own[e] ? p : NE - 1 - p;  // stored left states, this element's order
+        Ue[e * NE + p] = static_cast<float>(a.QF[(n * NE3 + eLn[e] * NE + ii) * sK + kl] - u0);
+      }
+    }
+#pragma unroll 1
+    for (int rr = 0; rr < NR; ++rr) {
+      const int r = rr < NP ? rr : 2 * NP + (rr - NP);
+      const float* row = sDiv + r * NF;
+      float A = 0.0f, B = 0.0f, C[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int j = 0; j < NP; ++j) {
+        A = fmaf(row[j], U[j], A);
+        B = fmaf(row[NP + j], U[j], B);
+      }
+#pragma unroll
+      for (int e = 0; e < 3; ++e)
+#pragma unroll
+        for (int p = 0; p < NE; ++p) C[e] = fmaf(row[2 * NP + e * NE + p], Ue[e * NE + p], C[e]);
+      const float gx = J0 * A + J2 * B + mx[0] * C[0] + mx[1] * C[1] + mx[2] * C[2];
+      const float gy = J1 * A + J3 * B + my[0] * C[0] + my[1] * C[1] + my[2] * C[2];
+      const float epsr = sB[r * 3] * ev[0] + sB[r * 3 + 1] * ev[1] + sB[r * 3 + 2] * ev[2];
+      a.DissX[(n * NR + rr) * sK + k] = static_cast<double>(gx * epsr);
+      a.DissY[(n * NR + rr) * sK + k] = static_cast<double>(gy * epsr);
+    }
+  }
+}
+
 // RHS = F(a) (RHS_Euler + DivInt DOF(DissX, DissY, VF) / |J|), the viscous
 // time-step limit, then the mixed stage update.  One thread per (element,
 // variable); stage -1 writes the dissipated, filtered RHS to rhsOut.
@@ -66,7 +163,8 @@ template <int N>
 __global__ void __launch_bounds__(128) k_mixed_diss_update(MixedArgs a, UpdateArgs<double> u) {
   constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NE3 = MixedDims<N>::NE3;
   constexpr int NF = MixedDims<N>::NF, NR = NP + NE3;
-  __shared__ double sD[NP * NF], sV[NP * NP], sVi[NP * NP], smf[NP], sdt;
+  __shared__ float sD[NP * NF], sV[NP * NP], sVi[NP * NP], smf[NP];
+  __shared__ double sdt;
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = blockIdx.x * 32 + lane;
   const bool active = k < a.K;
@@ -101,49 +199,52 @@ __global__ void __launch_bounds__(128) k_mixed_diss_update(MixedArgs a, UpdateAr
   if (needs_global_dt(a, s)) dtLocal = sdt;
   float rmax = -3.4028235e38f, rabs = 0.0f, rs2 = 0.0f;
   if (active) {
-    const double Jd = u.Jdet[k], oojd = 1.0 / Jd;
-    const double J0 = u.Jinv[k], J1 = u.Jinv[sK + k], J2 = u.Jinv[2 * sK + k], J3 = u.Jinv[3 * sK + k];
+    const double Jdd = u.Jdet[k];
+    const float Jd = static_cast<float>(Jdd), oojd = static_cast<float>(1.0 / Jdd);
+    const float J0 = static_cast<float>(u.Jinv[k]), J1 = static_cast<float>(u.Jinv[sK + k]);
+    const float J2 = static_cast<float>(u.Jinv[2 * sK + k]), J3 = static_cast<float>(u.Jinv[3 * sK + k]);
     double sig = 0.0;
 #pragma unroll
     for (int v = 0; v < 3; ++v) sig = sig + __longlong_as_double(static_cast<long long>(u.sigV[u.etov[v * sK + k]]));
-    const double alpha = sin(0.5 * 3.14159265358979323846 * (sig / 3.0));
+    const float alpha = static_cast<float>(sin(0.5 * 3.14159265358979323846 * (sig / 3.0)));
     int eg[3], eslot[3];
-    double esg[3];
+    float esg[3];
     bool own[3];
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
       eg[e] = u.elemEdge[e * sK + k];
       own[e] = u.ekL[eg[e]] == k && (u.eLR[eg[e]] & 3) == e;
-      esg[e] = (own[e] ? 1.0 : -1.0) * u.IIE[e * sK + k];
+      esg[e] = static_cast<float>((own[e] ? 1.0 : -1.0) * u.IIE[e * sK + k]);
       eslot[e] = a.eslot[e * sK + k];
     }
-    double w[NP];
+    // AddDissipation (dissipation.go:274-346) in FP32.
+    float w[NP];
 #pragma unroll
-    for (int r = 0; r < NP; ++r) w[r] = 0.0;
+    for (int r = 0; r < NP; ++r) w[r] = 0.0f;
 #pragma unroll 1
     for (int j = 0; j < NP; ++j) {
       const size_t ind = (n * NR + j) * sK + k;
-      const double dx = u.DissX[ind], dy = u.DissY[ind];
-      const double fr = Jd * (J0 * dx + J1 * dy), fs = Jd * (J2 * dx + J3 * dy);
+      const float dx = static_cast<float>(u.DissX[ind]), dy = static_cast<float>(u.DissY[ind]);
+      const float fr = Jd * (J0 * dx + J1 * dy), fs = Jd * (J2 * dx + J3 * dy);
 #pragma unroll
-      for (int r = 0; r < NP; ++r) w[r] += sD[r * NF + j] * fr + sD[r * NF + NP + j] * fs;
+      for (int r = 0; r < NP; ++r) w[r] = fmaf(sD[r * NF + j], fr, fmaf(sD[r * NF + NP + j], fs, w[r]));
     }
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
       const double* vf = u.VF + (static_cast<size_t>(eg[e]) * 4 + n) * NE;
 #pragma unroll
       for (int p = 0; p < NE; ++p) {
-        const double f = vf[own[e] ? p : NE - 1 - p] * esg[e];
+        const float f = static_cast<float>(vf[own[e] ? p : NE - 1 - p]) * esg[e];
 #pragma unroll
-        for (int r = 0; r < NP; ++r) w[r] += sD[r * NF + 2 * NP + e * NE + p] * f;
+        for (int r = 0; r < NP; ++r) w[r] = fmaf(sD[r * NF + 2 * NP + e * NE + p], f, w[r]);
       }
     }
 #pragma unroll
-    for (int r = 0; r < NP; ++r) w[r] = a.rhsOut[off + r * sK] + oojd * w[r];
-    limit_filter_modal<NP>(w, sV, sVi, smf, alpha);
+    for (int r = 0; r < NP; ++r) w[r] = static_cast<float>(a.rhsOut[off + r * sK]) + oojd * w[r];
+    limit_filter_modal_f<NP>(w, sV, sVi, smf, alpha);
     float rhs[NP];
 #pragma unroll
-    for (int r = 0; r < NP; ++r) rhs[r] = static_cast<float>(w[r]);
+    for (int r = 0; r < NP; ++r) rhs[r] = w[r];
     if (a.localDT && s >= 0 && n == 0) u.DTVisc[k] = dvNew;
     float dq0[NP], ds[NP];
 #pragma unroll
