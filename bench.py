@@ -436,8 +436,8 @@ def run_ours(a, world, rank, local):
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": {"fp64": "fp64", "fp32": "fp32 (fp64 state/RK)",
-                                                  "tf32x3": "3xtf32 tensor-core GEMM, fp32 elsewhere (fp64 state/RK)"}[a.precision],
+            "vs_baseline": None, "dtype": {"fp64": "fp64", "fp32": "fp32 (compensated fp32 state)",
+                                                  "tf32x3": "3xtf32 tensor-core GEMM, fp32 elsewhere (compensated fp32 state)"}[a.precision],
             "data": "synthetic (analytic isentropic-vortex initial condition on a generated mesh)",
             "config": {"workload": a.workload, "description": wl["desc"], "K": K, "N": wl["N"], "Np": Np,
                        "dof_updates_per_step": dof_per_step, "flux": "roe", "cfl": 1.0,

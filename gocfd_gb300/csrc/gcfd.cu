@@ -519,10 +519,13 @@ struct MixedLaunch {
     if (c->nBC > 0)
       k_mixed_edge_bc<N><<<(c->nBC + 7) / 8, dim3(8, MixedDims<N>::NE), 0, sb>>>(a);
     if (c->nInt > 0) {
-      if (c->prm.flux_type == GCFD_FLUX_ROE_ER)
-        k_mixed_edge<N, true><<<(c->nInt + 127) / 128, 128, 0, c->stream>>>(a);
-      else
-        k_mixed_edge<N, false><<<(c->nInt + 127) / 128, 128, 0, c->stream>>>(a);
+      const int nb = (c->nInt + 127) / 128;
+      switch (c->prm.flux_type) {
+        case GCFD_FLUX_ROE_ER: k_mixed_edge<N, kFluxRoeER><<<nb, 128, 0, c->stream>>>(a); break;
+        case GCFD_FLUX_ROE: k_mixed_edge<N, kFluxRoe><<<nb, 128, 0, c->stream>>>(a); break;
+        case GCFD_FLUX_LAX: k_mixed_edge<N, kFluxLax><<<nb, 128, 0, c->stream>>>(a); break;
+        default: k_mixed_edge<N, kFluxAverage><<<nb, 128, 0, c->stream>>>(a); break;
+      }
     }
     if (fork && c->nBC > 0) {
       cudaEventRecord(c->evJoin, c->stream2);

@@ -422,8 +422,9 @@ __global__ void k_mixed_to_fp64(const float* __restrict__ hi, const float* __res
     q[i] = static_cast<double>(hi[i]) + static_cast<double>(lo[i]);
 }
 
-// (c) interior-edge fluxes in delta form, one thread per mesh edge.  RoeER
-// instantiates the Roe-ER flux in FP64 (fluxes.go:415-503 has no delta form).
+// (c) interior-edge fluxes in delta form, one thread per mesh edge, one
+// instantiation per flux kind FK; Roe-ER runs in FP64 (fluxes.go:415-503 has
+// no delta form).
 // A block's 128 edges own a contiguous run of the edge-major face array, which
 // is copied into shared memory with coalesced 16-byte cp.async (the copy
 // overlaps the base-state loads); the fluxes leave the same way, through a
@@ -437,8 +438,9 @@ struct EdgeDims {
   static constexpr int OWP = OW + ((OW % 8) ? 0 : 4);
 };
 
-template <int N, bool RoeER>
-__global__ void __launch_bounds__(128, RoeER ? 1 : 5) k_mixed_edge(MixedArgs a) {
+template <int N, int FK>
+__global__ void __launch_bounds__(128, FK == kFluxRoeER ? 1 : 5) k_mixed_edge(MixedArgs a) {
+  constexpr bool RoeER = (FK == kFluxRoeER);
   constexpr int NE = MixedDims<N>::NE, NEP = MixedDims<N>::NEP;
   constexpr int FW = EdgeDims<N>::FW, FWP = EdgeDims<N>::FWP, OWP = EdgeDims<N>::OWP;
   static_assert(FW % 4 == 0 && FWP % 4 == 0 && OWP % 4 == 0, "16-byte records");
@@ -457,7 +459,7 @@ __global__ void __launch_bounds__(128, RoeER ? 1 : 5) k_mixed_edge(MixedArgs a) 
   }
   const int g = g0 + threadIdx.x;
   const bool active = g < a.nInt;
-  double smax = 0.0;
+  float smax = 0.0f;
   float bh[4] = {1.f, 0.f, 0.f, 1.f}, bl[4] = {0.f, 0.f, 0.f, 0.f}, dB[4] = {0.f, 0.f, 0.f, 0.f};
   float nx = 0.f, ny = 0.f, oohK = 0.f;
   if (active) {
@@ -501,7 +503,7 @@ __global__ void __launch_bounds__(128, RoeER ? 1 : 5) k_mixed_edge(MixedArgs a) 
         ql[c] = fr[c * NEP + p];
         qr[c] = fr[4 * NEP + c * NEP + NE - 1 - p] + dB[c];
       }
-      if (RoeER) {
+      if constexpr (RoeER) {
         double QLd[4], QRd[4], fd[4], Fx[4], Fy[4], bd[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
@@ -516,16 +518,16 @@ __global__ void __launch_bounds__(128, RoeER ? 1 : 5) k_mixed_edge(MixedArgs a) 
 #pragma unroll
         for (int c = 0; c < 4; ++c)
           f[c] = static_cast<float>(fd[c] - (static_cast<double>(nx) * Fx[c] + static_cast<double>(ny) * Fy[c]));
-      } else if (a.flux == kFluxRoe) {
+      } else if constexpr (FK == kFluxRoe) {
         float w;
         roe_delta_fast(b, ql, qr, nx, ny, a.gamma, f, &w);
         sm = fmaxf(sm, oohK * w);
       } else {
-        riemann_delta(a.flux, b, ql, qr, nx, ny, a.gamma, f);
+        riemann_delta(FK, b, ql, qr, nx, ny, a.gamma, f);
       }
 #pragma unroll
       for (int c = 0; c < 4; ++c) fo[c][p] = f[c];
-      if (RoeER || a.flux != kFluxRoe) {
+      if constexpr (FK != kFluxRoe) {
         const float QL[4] = {b.rho + ql[0], b.m + ql[1], b.n + ql[2], b.E + ql[3]};
         sm = fmaxf(sm, oohK * (speed(QL[0], QL[1], QL[2]) + sound_speed(gf, QL[0], QL[1], QL[2], QL[3])));
       }
@@ -539,8 +541,8 @@ __global__ void __launch_bounds__(128, RoeER ? 1 : 5) k_mixed_edge(MixedArgs a) 
       for (int p = 0; p < NEP; ++p) o[c * NEP + p] = (p < NE) ? fo[c][p < NE ? p : 0] : 0.0f;
       o[4 * NEP + c] = cr[c];
     }
-    smax = static_cast<double>(sm);
-    a.edgeSpeed[g] = smax;
+    smax = sm;
+    a.edgeSpeed[g] = static_cast<double>(sm);
   }
   __syncthreads();
   {
@@ -552,9 +554,9 @@ __global__ void __launch_bounds__(128, RoeER ? 1 : 5) k_mixed_edge(MixedArgs a) 
     if (active)
       reinterpret_cast<float4*>(a.corr)[g] = *reinterpret_cast<const float4*>(&so[threadIdx.x * OWP + 4 * NEP]);
   }
-  smax = warp_max(smax);
+  smax = warp_max(smax);  // wave speeds are >= 0: their FP64 bit patterns order like integers
   if ((threadIdx.x & 31) == 0)
-    atomicMax(a.gmax, static_cast<unsigned long long>(__double_as_longlong(smax)));
+    atomicMax(a.gmax, static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(smax))));
 }
 
 // (c) boundary edges: face state, characteristic / wall / exact-state BC and
@@ -689,6 +691,19 @@ __device__ __forceinline__ void stage_tail_prefetch(const MixedArgs& a, int blk,
     const int arr = it / NP, r = it - arr * NP;
     const float* p = arr == 0 ? a.Qhi : arr == 1 ? a.Qlo : arr == 2 ? a.D[2] : arr == 3 ? a.D[3] : a.R3;
     bulk_prefetch_l2(p + base + r * sK, 128);
+  }
+}
+
+// One warp's residual partials of the final stage (FP32 warp reductions; the
+// FP64 pipe is narrow), folded into the per-variable scalars by lane 0.
+__device__ __forceinline__ void residual_commit(Scalars* sc, int n, int lane, float rmax, float rabs, float rs2) {
+  rmax = warp_max(rmax);
+  rabs = warp_max(rabs);
+  rs2 = warp_sum_f(rs2);
+  if (lane == 0) {
+    atomicMax(&sc->rmax[n], order_key(static_cast<double>(rmax)));
+    atomicMax(&sc->rabs[n], static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(rabs))));
+    atomicAdd(&sc->rsum2[n], static_cast<double>(rs2));
   }
 }
 
@@ -932,14 +947,7 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
     stage_tail<N>(a, eslot, n, k, off, sK, s, rhs, dq0, ds, dtk, rmax, rabs, rs2);
   }
   if (s == 4 && !a.rhsOnly) {
-    const unsigned long long km = warp_max_u64(order_key(static_cast<double>(rmax)));
-    const double am = warp_max(static_cast<double>(rabs));
-    const double s2 = warp_sum(static_cast<double>(rs2));
-    if (lane == 0) {
-      atomicMax(&a.sc->rmax[n], km);
-      atomicMax(&a.sc->rabs[n], static_cast<unsigned long long>(__double_as_longlong(am)));
-      atomicAdd(&a.sc->rsum2[n], s2);
-    }
+    residual_commit(a.sc, n, lane, rmax, rabs, rs2);
   }
 }
 

@@ -255,14 +255,7 @@ __global__ void __launch_bounds__(128) k_mixed_diss_update(MixedArgs a, UpdateAr
     stage_tail<N>(a, eslot, n, k, off, sK, s, rhs, dq0, ds, dtLocal, rmax, rabs, rs2);
   }
   if (s == 4) {
-    const unsigned long long km = warp_max_u64(order_key(static_cast<double>(rmax)));
-    const double am = warp_max(static_cast<double>(rabs));
-    const double s2 = warp_sum(static_cast<double>(rs2));
-    if (lane == 0) {
-      atomicMax(&a.sc->rmax[n], km);
-      atomicMax(&a.sc->rabs[n], static_cast<unsigned long long>(__double_as_longlong(am)));
-      atomicAdd(&a.sc->rsum2[n], s2);
-    }
+    residual_commit(a.sc, n, lane, rmax, rabs, rs2);
   }
 }
 

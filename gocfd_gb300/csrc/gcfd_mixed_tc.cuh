@@ -220,14 +220,7 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
     tc::dealloc(tbase, NCOLS);
   }
   if (s == 4 && !a.rhsOnly) {
-    const unsigned long long km = warp_max_u64(order_key(static_cast<double>(rmax)));
-    const double am = warp_max(static_cast<double>(rabs));
-    const double s2 = warp_sum(static_cast<double>(rs2));
-    if (lane == 0) {
-      atomicMax(&a.sc->rmax[n], km);
-      atomicMax(&a.sc->rabs[n], static_cast<unsigned long long>(__double_as_longlong(am)));
-      atomicAdd(&a.sc->rsum2[n], s2);
-    }
+    residual_commit(a.sc, n, lane, rmax, rabs, rs2);
   }
 }
 
