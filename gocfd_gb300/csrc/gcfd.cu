@@ -349,6 +349,9 @@ struct Launch {
     a.S0 = 4.0 / std::pow(double(c->N + 1), 4.0);
     a.omega = double(c->N * c->N);
     a.sigE = a.epsE = a.SeE = nullptr;
+    a.faces32 = c->mfaces;
+    a.base32 = c->mbase;
+    a.eslot32 = c->meslot;
     return a;
   }
   static int grid(int n) { return (n + 127) / 128; }
@@ -577,7 +580,7 @@ struct MixedLaunch {
   }
   static void rhs(gcfd_ctx* c) {
     prepare(c, c->Qtmp);
-    if (c->diss) Launch<N, double>::diss_front(c, -1, c->Qtmp);
+    if (c->diss) diss_front(c, -1, c->Qtmp);
     edges(c, -1, c->Qtmp, &c->sc->rhs_time, &c->sc->gmax[0], false);
     if (c->diss) diss_middle(c, -1, c->Qtmp);
     stage_kernel(c, args(c, -1, c->Qtmp, &c->sc->rhs_time, &c->sc->gmax[0]));
@@ -586,12 +589,22 @@ struct MixedLaunch {
                                                                     &c->sc->gmax[0]),
                                                                Launch<N, double>::update_args(c, -1, c->Qtmp));
   }
-  // The RT gradient in FP32 (delta form), then the FP64 viscous edge fluxes.
+  // Sensor, vertex smoothing and the rkStep-2 limiter; the face states the
+  // dissipation needs are the mixed path's own (k_mixed_relimit rebuilds them
+  // after the limiter), so no FP64 interpolation.
+  static void diss_front(gcfd_ctx* c, int stage, double* Qs) {
+    cudaMemsetAsync(c->sigV, 0, sizeof(unsigned long long) * c->nverts, c->stream);
+    cudaMemsetAsync(c->epsV, 0, sizeof(unsigned long long) * c->nverts, c->stream);
+    const DissArgs d = Launch<N, double>::diss_args(c, stage, Qs);
+    k_diss_sensor<N><<<(c->K + 127) / 128, 128, 0, c->stream>>>(d);
+    if (stage == 2) k_diss_limit<N><<<(4 * c->K + 127) / 128, 128, 0, c->stream>>>(d);
+  }
+  // The RT gradient in FP32 (delta form), then the viscous edge fluxes.
   static void diss_middle(gcfd_ctx* c, int stage, double* Qs) {
     const DissArgs d = Launch<N, double>::diss_args(c, stage, Qs);
     constexpr int NF = Dims<N>::NF;
     k_diss_grad_mixed<N><<<(c->K + 127) / 128, 128, sizeof(float) * (NF * NF + NF * 3), c->stream>>>(d);
-    k_diss_edge<N><<<(c->nInt + c->nBC + 127) / 128, 128, 0, c->stream>>>(d);
+    k_diss_edge<N, true><<<(c->nInt + c->nBC + 127) / 128, 128, 0, c->stream>>>(d);
   }
   // One stage with the PerssonC0 dissipation: FP64 stage state for the
   // dissipation kernels (Q[1] is free on the mixed path), the Euler RHS of the
@@ -601,7 +614,7 @@ struct MixedLaunch {
     double* Qs64 = c->Q[1];
     k_mixed_form_stage<N><<<gridE(c), 128, 0, c->stream>>>(args(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]),
                                                            Qs64);
-    L::diss_front(c, s, Qs64);
+    diss_front(c, s, Qs64);
     if (s == 2)
       k_mixed_relimit<N><<<gridE(c), 128, 0, c->stream>>>(args(c, 2, c->Q[0], &c->sc->time, &c->sc->gmax[2]),
                                                           Qs64);
@@ -1425,11 +1438,6 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
     c->FE = fe;
   } else {
     if ((rc = build_mixed(c))) return rc;
-    if (c->diss) {  // the FP64 dissipation kernels need FP64 faces
-      double* qf = nullptr;
-      if ((rc = dalloc(c, &qf, nFace))) return rc;
-      c->QF = qf;
-    }
   }
   if (c->diss && (rc = build_diss(c, m))) return rc;
   if ((rc = upload(c, &c->Iop, c->el.FluxEdgeInterp.v))) return rc;

@@ -61,6 +61,11 @@ struct DissArgs {
   double* sigE;               // optional (adjoint recompute): element sigma, eps and Se
   double* epsE;
   double* SeE;
+  // Mixed path: edge-major FP32 face deltas [edge][side][n][NEP] and their
+  // reference states [k][n] (hi, lo) stand in for QF.
+  const float* faces32;
+  const float2* base32;
+  const int* eslot32;         // [3][K] edge * 2 + side
 };
 
 template <int N>
@@ -247,8 +252,10 @@ __global__ void __launch_bounds__(128) k_diss_grad(DissArgs a) {
   }
 }
 
-// Stage 5: viscous normal flux and viscous wave speed per mesh edge.
-template <int N>
+// Stage 5: viscous normal flux and viscous wave speed per mesh edge.  MF:
+// the penalty's face states come from the mixed path's FP32 face deltas (the
+// two states of the jump share their reference state, which cancels).
+template <int N, bool MF = false>
 __global__ void __launch_bounds__(128) k_diss_edge(DissArgs a) {
   constexpr int NP = DissDims<N>::NP, NE = DissDims<N>::NE, NE3 = DissDims<N>::NE3;
   constexpr int NF = DissDims<N>::NF, NR = DissDims<N>::NR;
@@ -303,9 +310,15 @@ __global__ void __launch_bounds__(128) k_diss_edge(DissArgs a) {
           const int rR = 2 * NP + eR * NE + (NE - 1 - p);
           const double epsR = sB[rR * 3] * evR[0] + sB[rR * 3 + 1] * evR[1] + sB[rR * 3 + 2] * evR[2];
           const double lam = 0.5 * (epsL[p] + epsR);
-          const double qa = a.QF[(n * NE3 + eL * NE + p) * sK + kL];
-          const double qb = a.QF[(n * NE3 + eL * NE + (NE - 1 - p)) * sK + kL];
-          v -= (a.omega * lam * ooLen) * (qa - qb);
+          double jump;
+          if constexpr (MF) {
+            constexpr int NEP = (NE + 1) & ~1;
+            const float* fl = a.faces32 + (static_cast<size_t>(g) * 8 + n) * NEP;  // side 0: left element
+            jump = static_cast<double>(fl[p] - fl[NE - 1 - p]);
+          } else {
+            jump = a.QF[(n * NE3 + eL * NE + p) * sK + kL] - a.QF[(n * NE3 + eL * NE + (NE - 1 - p)) * sK + kL];
+          }
+          v -= (a.omega * lam * ooLen) * jump;
           vf[n * NE + p] = v;
         }
     }

@@ -104,16 +104,18 @@ __global__ void __launch_bounds__(128) k_diss_grad_mixed(DissArgs a) {
   const float J0 = static_cast<float>(a.Jinv[k]), J1 = static_cast<float>(a.Jinv[sK + k]);
   const float J2 = static_cast<float>(a.Jinv[2 * sK + k]), J3 = static_cast<float>(a.Jinv[3 * sK + k]);
   const double ooJd = 1.0 / a.Jdet[k];
+  constexpr int NEP = (NE + 1) & ~1;
   float ev[3], mx[3], my[3];
-  int eg[3], eLn[3];
+  int eg[3], kl[3];
   bool own[3];
 #pragma unroll
   for (int v = 0; v < 3; ++v) ev[v] = static_cast<float>(vdouble(a.epsV, a.etov[v * sK + k]));
 #pragma unroll
   for (int e = 0; e < 3; ++e) {
-    eg[e] = a.elemEdge[e * sK + k];
-    own[e] = a.ekL[eg[e]] == k && (a.eLR[eg[e]] & 3) == e;
-    eLn[e] = a.eLR[eg[e]] & 3;
+    const int slot = a.eslot32[e * sK + k];
+    eg[e] = slot >> 1;
+    own[e] = (slot & 1) == 0;
+    kl[e] = a.ekL[eg[e]];
     const double ii = a.IIE[e * sK + k];
     mx[e] = static_cast<float>(ooJd * a.nxE[e * sK + k] * ii);
     my[e] = static_cast<float>(ooJd * a.nyE[e * sK + k] * ii);
@@ -124,14 +126,15 @@ __global__ void __launch_bounds__(128) k_diss_grad_mixed(DissArgs a) {
     float U[NP], Ue[NE3];
 #pragma unroll
     for (int i = 0; i < NP; ++i) U[i] = static_cast<float>(a.Qs[(n * NP + i) * sK + k] - u0);
+    // The stored left states (the left element's faces, this element's order):
+    // its reference state plus its FP32 face deltas.
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
-      const int kl = a.ekL[eg[e]];
+      const float2 bl = a.base32[static_cast<size_t>(kl[e]) * 4 + n];
+      const float shift = static_cast<float>((static_cast<double>(bl.x) + static_cast<double>(bl.y)) - u0);
+      const float* fl = a.faces32 + (static_cast<size_t>(eg[e]) * 8 + n) * NEP;
 #pragma unroll
-      for (int p = 0; p < NE; ++p) {
-        const int ii = own[e] ? p : NE - 1 - p;  // stored left states, this element's order
-        Ue[e * NE + p] = static_cast<float>(a.QF[(n * NE3 + eLn[e] * NE + ii) * sK + kl] - u0);
-      }
+      for (int p = 0; p < NE; ++p) Ue[e * NE + p] = shift + fl[own[e] ? p : NE - 1 - p];
     }
 #pragma unroll 1
     for (int rr = 0; rr < NR; ++rr) {
