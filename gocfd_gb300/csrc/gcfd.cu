@@ -596,8 +596,8 @@ struct MixedLaunch {
     cudaMemsetAsync(c->sigV, 0, sizeof(unsigned long long) * c->nverts, c->stream);
     cudaMemsetAsync(c->epsV, 0, sizeof(unsigned long long) * c->nverts, c->stream);
     const DissArgs d = Launch<N, double>::diss_args(c, stage, Qs);
-    k_diss_sensor<N><<<(c->K + 127) / 128, 128, 0, c->stream>>>(d);
-    if (stage == 2) k_diss_limit<N><<<(4 * c->K + 127) / 128, 128, 0, c->stream>>>(d);
+    k_diss_sensor_mixed<N><<<(c->K + 127) / 128, 128, 0, c->stream>>>(d);
+    if (stage == 2) k_diss_limit_mixed<N><<<(4 * c->K + 127) / 128, 128, 0, c->stream>>>(d);
   }
   // The RT gradient in FP32 (delta form), then the viscous edge fluxes.
   static void diss_middle(gcfd_ctx* c, int stage, double* Qs) {

@@ -83,6 +83,79 @@ __device__ __forceinline__ void limit_filter_modal_f(float u[NP], const float* s
   }
 }
 
+// The shock sensor (k_diss_sensor: UpdateSeMoment, UpdateShockFinderSigma,
+// CalculateElementViscosity) with its three Np x Np products in FP32; the
+// moment's log10 and the sigma ramp stay in FP64.  FP32 rounding perturbs the
+// high-mode energy by ~1e-7 of the density's, i.e. only moments far below the
+// ramp (sigma = 0 there either way).
+template <int N>
+__global__ void __launch_bounds__(128) k_diss_sensor_mixed(DissArgs a) {
+  constexpr int NP = DissDims<N>::NP;
+  __shared__ float sP[NP * NP], sM[NP * NP], sDq[NP * NP];
+  stage_operator(sP, a.SensP, NP * NP);
+  stage_operator(sM, a.Mass, NP * NP);
+  stage_operator(sDq, a.SensD, NP * NP);
+  __syncthreads();
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.K) return;
+  const size_t sK = static_cast<size_t>(a.K);
+  float rho[NP];
+#pragma unroll
+  for (int j = 0; j < NP; ++j) rho[j] = static_cast<float>(a.Qs[j * sK + k]);
+  float num = 0.0f, den = 0.0f;
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    float x = 0.0f, y = 0.0f, dq = 0.0f;
+#pragma unroll
+    for (int j = 0; j < NP; ++j) {
+      x = fmaf(sP[i * NP + j], rho[j], x);
+      y = fmaf(sM[i * NP + j], rho[j], y);
+      dq = fmaf(sDq[i * NP + j], rho[j], dq);
+    }
+    num = fmaf(dq, x, num);
+    den = fmaf(rho[i], y, den);
+  }
+  const double se = log10(static_cast<double>(num) / static_cast<double>(den));
+  const double left = a.S0 - a.kappa, right = a.S0 + a.kappa;
+  double sigma = 0.0;  // a NaN moment keeps sigma = 0
+  if (se < left) sigma = 0.0;
+  else if (se >= left && se <= right) sigma = 0.5 * (1.0 + sin(3.14159265358979323846 * (0.5 / a.kappa) * (se - a.S0)));
+  else if (se > right) sigma = 1.0;
+  const double eps = a.eps0 * a.hK[k] * sigma;
+#pragma unroll
+  for (int v = 0; v < 3; ++v) {
+    const int vert = a.etov[v * sK + k];
+    atomicMax(&a.sigV[vert], static_cast<unsigned long long>(__double_as_longlong(sigma)));
+    atomicMax(&a.epsV[vert], static_cast<unsigned long long>(__double_as_longlong(eps)));
+  }
+}
+
+// The rkStep-2 modal limiter (k_diss_limit, limitAndFilterSolution) on the
+// FP64 stage state, in FP32 on the deltas U - U_0: the filter keeps mode 0 (the
+// constant), so filter(U) = U_0 + filter(U - U_0).  One thread per (variable,
+// element).
+template <int N>
+__global__ void __launch_bounds__(128) k_diss_limit_mixed(DissArgs a) {
+  constexpr int NP = DissDims<N>::NP;
+  __shared__ float sV[NP * NP], sVi[NP * NP], smf[NP];
+  stage_operator(sV, a.V, NP * NP);
+  stage_operator(sVi, a.Vinv, NP * NP);
+  stage_operator(smf, a.mf, NP);
+  __syncthreads();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 4 * a.K) return;
+  const int n = t / a.K, k = t - n * a.K;
+  const size_t sK = static_cast<size_t>(a.K);
+  const float alpha = static_cast<float>(sin(0.5 * 3.14159265358979323846 * element_sigma(a, k, sK)));
+  const double u0 = a.Qlim[(n * NP) * sK + k];
+  float q[NP];
+#pragma unroll
+  for (int i = 0; i < NP; ++i) q[i] = static_cast<float>(a.Qlim[(n * NP + i) * sK + k] - u0);
+  limit_filter_modal_f<NP>(q, sV, sVi, smf, alpha);
+#pragma unroll
+  for (int i = 0; i < NP; ++i) a.Qlim[(n * NP + i) * sK + k] = u0 + static_cast<double>(q[i]);
+}
+
 // eps * grad(Q) at the interior and edge flux points (k_diss_grad,
 // CalculateEpsilonGradient, dissipation.go:244-272) in FP32.  The RT gradient
 // of a constant field is zero, so it is taken of U - U_0 (U_0 the element's
