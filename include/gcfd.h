@@ -162,13 +162,15 @@ int gcfd_profile_step(gcfd_ctx* ctx, double* kernel_ms4, int32_t* launches4);
  * 5 flux-point r,s (NpFlux x 2).  With out == NULL only rows/cols are set. */
 int gcfd_host_operator(int32_t N, int32_t which, double* out, int32_t* rows, int32_t* cols);
 
-/* ---- Adjoint (vector-Jacobian products), FP64 path without PerssonC0 ----
+/* ---- Adjoint (vector-Jacobian products), FP64 path ----
  * The reference has no adjoint; these transpose its discrete RHS and step
  * exactly, including the time step's dependence on the state (the global max
  * wave speed of calculateGlobalDT, euler.go:945-971, with the FinalTime clip;
- * the running max of CalculateLocalDT, euler.go:973-1002) and the IVortex
- * boundary state's dependence on the solver time.  The mixed path and the
- * PerssonC0 dissipation return GCFD_ERR_UNSUPPORTED. */
+ * the running max of CalculateLocalDT, euler.go:973-1002), the IVortex
+ * boundary state's dependence on the solver time and, with the PerssonC0
+ * limiter, the sensor, vertex maxima, limiter, RT gradient, viscous fluxes and
+ * viscous time-step limit.  A mixed-precision context returns
+ * GCFD_ERR_UNSUPPORTED (its state is handed to an FP64 context instead). */
 
 /* Functionals of the current state: the wall pressure force, summed over Wall
  * and Cyl boundary edges as |edge| sum_p w_p p n_x (or n_y), with the
