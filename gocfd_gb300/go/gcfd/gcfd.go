@@ -173,6 +173,17 @@ func (c *Context) Step(nsteps int) (time, dt float64, resid [4]float64, err erro
 	return float64(t), float64(d), resid, err
 }
 
+// SetStagePipeline selects the mixed path's persistent TMA-pipelined stage
+// kernel (true) or the one-block kernel (false, the default);
+// GCFD_OPT_STAGE_PIPELINE of gcfd.h.
+func (c *Context) SetStagePipeline(on bool) error {
+	v := C.int32_t(0)
+	if on {
+		v = 1
+	}
+	return status(c.ctx, C.gcfd_set_option(c.ctx, C.GCFD_OPT_STAGE_PIPELINE, v))
+}
+
 // RHS evaluates the right-hand side of Q at BC time t into RHS (same shards).
 func (c *Context) RHS(t float64, Q, RHS [][4][]float64, Kmax []int) error {
 	var pin runtime.Pinner
