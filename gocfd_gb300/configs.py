@@ -155,15 +155,17 @@ def run(name: str, precision: str = "fp64", scale: float = 1.0, device: int = 0,
         out["K"] = s.K
         t0 = time.perf_counter()
         if cfg.mesh == "vortex":
-            info = s.step(cfg.steps)
-            out.update(steps=cfg.steps, time=info["time"])
+            n = min(cfg.steps, max_steps) if max_steps else cfg.steps
+            info = s.step(n)
+            out.update(steps=n, time=info["time"])
             out["rel_l2_vs_exact"], out["rel_linf_vs_exact"] = exact_vortex_error(s, info["time"])
         elif cfg.mesh == "sod":
             steps, t = 0, 0.0
             cap = max_steps or 10 ** 7
             while t < cfg.final_time * (1 - 1e-12) and steps < cap:
-                info = s.step(100)
-                steps += 100
+                n = min(100, cap - steps)
+                info = s.step(n)
+                steps += n
                 t = info["time"]
             out.update(steps=steps, time=t)
             out["density_error"] = sod_density_error(s, t)

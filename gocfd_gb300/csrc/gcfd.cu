@@ -115,6 +115,7 @@ struct gcfd_ctx {
   bool fp64Stale = false;  // mixed path: Q[0] lags the compensated state
   cudaStream_t stream2 = nullptr;
   cudaEvent_t evFork = nullptr, evJoin = nullptr;
+  cudaEvent_t evChunk[8] = {};  // chunked state copies (mixed path)
   float *mgeo = nullptr, *mII = nullptr;
   int* meslot = nullptr;
   float *mnx = nullptr, *mny = nullptr, *moohK = nullptr;
@@ -179,6 +180,8 @@ struct gcfd_ctx {
       if (e) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
     for (void* p : winAllocs) cudaFree(p);
+    for (auto& e : evChunk)
+      if (e) cudaEventDestroy(e);
     if (evFork) cudaEventDestroy(evFork);
     if (evJoin) cudaEventDestroy(evJoin);
     if (stream2) cudaStreamDestroy(stream2);
@@ -535,8 +538,10 @@ struct MixedLaunch {
       cudaStreamWaitEvent(c->stream, c->evJoin, 0);
     }
   }
-  static void prepare(gcfd_ctx* c, double* Q0) {
-    k_mixed_prepare<N><<<gridE(c), 128, 0, c->stream>>>(args(c, 0, Q0, nullptr, nullptr));
+  static void prepare(gcfd_ctx* c, double* Q0) { prepare_range(c, Q0, 0, c->K); }
+  static void prepare_range(gcfd_ctx* c, double* Q0, int k0, int k1) {
+    if (k1 <= k0) return;
+    k_mixed_prepare<N><<<(k1 - k0 + 31) / 32, 128, 0, c->stream>>>(args(c, 0, Q0, nullptr, nullptr), k0, k1);
   }
   static void step(gcfd_ctx* c, cudaEvent_t* ev, double* ms, int* launches) {
     auto mark = [&](int i) {
@@ -629,6 +634,7 @@ struct MixedLaunch {
     k_mixed_diss_update<N><<<gridE(c), 128, 0, c->stream>>>(m2, L::update_args(c, s, Qs64));
   }
   static void prep_state(gcfd_ctx* c) { prepare(c, c->Q[0]); }
+  static void prep_state_range(gcfd_ctx* c, int k0, int k1) { prepare_range(c, c->Q[0], k0, k1); }
 };
 
 // Adjoint launchers (FP64 path).
@@ -945,26 +951,64 @@ bool select_adj_ops(int N, AdjOps* o) {
 }
 
 // Mixed path: rebuild the FP64 state Q[0] from the compensated pair.
+void to_fp64_range(gcfd_ctx* c, int k0, int k1) {
+  if (k1 <= k0) return;
+  const size_t n = static_cast<size_t>(4) * c->Np * (k1 - k0);
+  k_mixed_to_fp64<<<static_cast<int>(std::min<size_t>((n + 255) / 256, 152 * 16)), 256, 0, c->stream>>>(
+      c->Qhi, c->Qlo, c->Q[0], c->K, 4 * c->Np, k0, k1);
+}
+
 int sync_fp64_state(gcfd_ctx* c) {
   if (!c->fp32 || !c->fp64Stale) return GCFD_OK;
-  const size_t n = static_cast<size_t>(4) * c->Np * c->K;
-  k_mixed_to_fp64<<<static_cast<int>(std::min<size_t>((n + 255) / 256, 152 * 16)), 256, 0, c->stream>>>(
-      c->Qhi, c->Qlo, c->Q[0], n);
+  to_fp64_range(c, 0, c->K);
   GCFD_CUDA(c, cudaGetLastError());
   c->fp64Stale = false;
   return GCFD_OK;
 }
 
+// Host <-> device state copies of the element range [k0, k1) of the sharded
+// host state (shard np covers [S_np, S_np + Kmax[np])) on the given stream.
+int copy_shards_range(gcfd_ctx* c, int nshards, const int32_t* Kmax, const double* const* Qin,
+                      double* const* Qout, bool toDevice, int k0, int k1, cudaStream_t st) {
+  const size_t pitch = static_cast<size_t>(c->K) * sizeof(double);
+  long long s0 = 0;
+  for (int np = 0; np < nshards; ++np) {
+    const long long a = std::max<long long>(s0, k0), b = std::min<long long>(s0 + Kmax[np], k1);
+    if (b > a) {
+      const size_t hp = static_cast<size_t>(Kmax[np]) * sizeof(double), w = static_cast<size_t>(b - a) * sizeof(double);
+      for (int n = 0; n < 4; ++n) {
+        double* d = c->Q[0] + static_cast<size_t>(n) * c->Np * c->K + a;
+        if (toDevice) {
+          if (!Qin[np * 4 + n]) return fail(c, GCFD_ERR_ARG, "null state pointer");
+          GCFD_CUDA(c, cudaMemcpy2DAsync(d, pitch, Qin[np * 4 + n] + (a - s0), hp, w, c->Np, cudaMemcpyHostToDevice,
+                                         st));
+        } else {
+          if (!Qout[np * 4 + n]) return fail(c, GCFD_ERR_ARG, "null state pointer");
+          GCFD_CUDA(c, cudaMemcpy2DAsync(Qout[np * 4 + n] + (a - s0), hp, d, pitch, w, c->Np,
+                                         cudaMemcpyDeviceToHost, st));
+        }
+      }
+    }
+    s0 += Kmax[np];
+  }
+  return GCFD_OK;
+}
+
+
+
 struct Ops {
   void (*step)(gcfd_ctx*, cudaEvent_t*, double*, int*);
   void (*rhs)(gcfd_ctx*);
   void (*prep)(gcfd_ctx*);  // rebuild stage-0 data from Q0 (mixed path), or nullptr
+  void (*prep_range)(gcfd_ctx*, int, int);  // the same for elements [k0, k1)
 };
 
 template <int N>
 Ops ops_for(bool fp32) {
-  if (fp32) return Ops{&MixedLaunch<N>::step, &MixedLaunch<N>::rhs, &MixedLaunch<N>::prep_state};
-  return Ops{&Launch<N, double>::step, &Launch<N, double>::rhs, nullptr};
+  if (fp32)
+    return Ops{&MixedLaunch<N>::step, &MixedLaunch<N>::rhs, &MixedLaunch<N>::prep_state,
+               &MixedLaunch<N>::prep_state_range};
+  return Ops{&Launch<N, double>::step, &Launch<N, double>::rhs, nullptr, nullptr};
 }
 
 bool select_ops(int N, bool fp32, Ops* o) {
@@ -976,6 +1020,49 @@ bool select_ops(int N, bool fp32, Ops* o) {
     case 4: *o = ops_for<4>(fp32); return true;
     default: return false;
   }
+}
+
+// Mixed path: the state moves in kStateChunks element ranges, and each range's
+// conversion (hi/lo split, dQ0, faces, reference states on the way in; hi + lo
+// to FP64 on the way out) runs on the compute stream while the next range's copy
+// is in flight on the second stream.
+constexpr int kStateChunks = 8;
+
+int set_state_overlapped(gcfd_ctx* c, int nshards, const int32_t* Kmax, const double* const* Q) {
+  Ops o;
+  select_ops(c->N, c->fp32, &o);
+  const int step = ((c->K + kStateChunks - 1) / kStateChunks + 31) & ~31;
+  GCFD_CUDA(c, cudaEventRecord(c->evFork, c->stream));  // earlier work on Q0 first
+  GCFD_CUDA(c, cudaStreamWaitEvent(c->stream2, c->evFork, 0));
+  for (int j = 0, k0 = 0; k0 < c->K; ++j, k0 += step) {
+    const int k1 = std::min(c->K, k0 + step);
+    int rc = copy_shards_range(c, nshards, Kmax, Q, nullptr, true, k0, k1, c->stream2);
+    if (rc) return rc;
+    GCFD_CUDA(c, cudaEventRecord(c->evChunk[j], c->stream2));
+    GCFD_CUDA(c, cudaStreamWaitEvent(c->stream, c->evChunk[j], 0));
+    o.prep_range(c, k0, k1);
+  }
+  GCFD_CUDA(c, cudaGetLastError());
+  c->dirty = false;
+  c->fp64Stale = false;
+  return GCFD_OK;
+}
+
+int get_state_overlapped(gcfd_ctx* c, int nshards, const int32_t* Kmax, double* const* Q) {
+  const int step = ((c->K + kStateChunks - 1) / kStateChunks + 31) & ~31;
+  for (int j = 0, k0 = 0; k0 < c->K; ++j, k0 += step) {
+    const int k1 = std::min(c->K, k0 + step);
+    to_fp64_range(c, k0, k1);
+    GCFD_CUDA(c, cudaEventRecord(c->evChunk[j], c->stream));
+    GCFD_CUDA(c, cudaStreamWaitEvent(c->stream2, c->evChunk[j], 0));
+    int rc = copy_shards_range(c, nshards, Kmax, nullptr, Q, false, k0, k1, c->stream2);
+    if (rc) return rc;
+  }
+  GCFD_CUDA(c, cudaGetLastError());
+  GCFD_CUDA(c, cudaEventRecord(c->evJoin, c->stream2));
+  GCFD_CUDA(c, cudaStreamWaitEvent(c->stream, c->evJoin, 0));
+  c->fp64Stale = false;
+  return GCFD_OK;
 }
 
 int capture_graph(gcfd_ctx* c) {
@@ -1280,6 +1367,7 @@ int build_mixed(gcfd_ctx* c) {
   GCFD_CUDA(c, cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
   GCFD_CUDA(c, cudaEventCreateWithFlags(&c->evFork, cudaEventDisableTiming));
   GCFD_CUDA(c, cudaEventCreateWithFlags(&c->evJoin, cudaEventDisableTiming));
+  for (auto& e : c->evChunk) GCFD_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   if ((rc = dalloc(c, &c->mexBC, static_cast<size_t>(std::max(c->nBC, 1)) * NE * 4))) return rc;
   GCFD_CUDA(c, cudaMemset(c->mfaces, 0, sizeof(float) * c->nEdges * 2 * 4 * NEP));
   GCFD_CUDA(c, cudaMemset(c->mfhat, 0, sizeof(float) * c->nEdges * 4 * NEP));
@@ -1534,9 +1622,13 @@ int gcfd_set_state(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doub
   if (!c || !Q) return c ? fail(c, GCFD_ERR_ARG, "null state") : GCFD_ERR_ARG;
   int rc = check_shards(c, nshards, Kmax);
   if (rc) return rc;
-  if ((rc = copy_shards(c, c->Q[0], nshards, Kmax, Q, true, nullptr))) return rc;
-  c->dirty = true;
-  c->fp64Stale = false;
+  if (c->fp32) {
+    if ((rc = set_state_overlapped(c, nshards, Kmax, Q))) return rc;
+  } else {
+    if ((rc = copy_shards(c, c->Q[0], nshards, Kmax, Q, true, nullptr))) return rc;
+    c->dirty = true;
+    c->fp64Stale = false;
+  }
   GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
   return GCFD_OK;
 }
@@ -1545,8 +1637,12 @@ int gcfd_get_state(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, double* co
   if (!c || !Q) return c ? fail(c, GCFD_ERR_ARG, "null state") : GCFD_ERR_ARG;
   int rc = check_shards(c, nshards, Kmax);
   if (rc) return rc;
-  if ((rc = sync_fp64_state(c))) return rc;
-  if ((rc = copy_shards(c, c->Q[0], nshards, Kmax, nullptr, false, Q))) return rc;
+  if (c->fp32 && c->fp64Stale) {
+    if ((rc = get_state_overlapped(c, nshards, Kmax, Q))) return rc;
+  } else {
+    if ((rc = sync_fp64_state(c))) return rc;
+    if ((rc = copy_shards(c, c->Q[0], nshards, Kmax, nullptr, false, Q))) return rc;
+  }
   GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
   return GCFD_OK;
 }

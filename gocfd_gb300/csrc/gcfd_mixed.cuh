@@ -384,13 +384,13 @@ __device__ __forceinline__ void write_faces(const MixedArgs& a, const int eslot[
 }
 
 // Stage-0 preparation from the FP64 state: hi/lo split, dQ0, faces, reference states.
+// Elements [k0, k1).
 template <int N>
-__global__ void __launch_bounds__(128) k_mixed_prepare(MixedArgs a) {
+__global__ void __launch_bounds__(128) k_mixed_prepare(MixedArgs a, int k0, int k1) {
   constexpr int NP = MixedDims<N>::NP, NPP = MixedDims<N>::NPP;
-  __syncthreads();
   const int n = threadIdx.x >> 5;
-  const int k = blockIdx.x * 32 + (threadIdx.x & 31);
-  if (k >= a.K) return;
+  const int k = k0 + blockIdx.x * 32 + (threadIdx.x & 31);
+  if (k >= k1) return;
   const size_t sK = static_cast<size_t>(a.K);
   const size_t off = static_cast<size_t>(n) * NP * sK + k;
   const double q0 = a.Q0[off];
@@ -415,11 +415,16 @@ __global__ void __launch_bounds__(128) k_mixed_prepare(MixedArgs a) {
 }
 
 // FP64 copy of the compensated state, for gcfd_get_state.
+// FP64 state = hi + lo for elements [k0, k1) of every [n][i] row (rows x K).
 __global__ void k_mixed_to_fp64(const float* __restrict__ hi, const float* __restrict__ lo,
-                                double* __restrict__ q, size_t n) {
-  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<size_t>(gridDim.x) * blockDim.x)
+                                double* __restrict__ q, int K, int rows, int k0, int k1) {
+  const int w = k1 - k0;
+  const size_t n = static_cast<size_t>(rows) * w;
+  for (size_t t = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; t < n;
+       t += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const size_t r = t / w, i = r * K + k0 + (t - r * w);
     q[i] = static_cast<double>(hi[i]) + static_cast<double>(lo[i]);
+  }
 }
 
 // (c) interior-edge fluxes in delta form, one thread per mesh edge, one

@@ -218,6 +218,27 @@ def test_shard_layout_roundtrip():
     gpu.close()
 
 
+@pytest.mark.parametrize("precision", ["fp32", "tf32x3"])
+def test_shard_layout_roundtrip_mixed(precision):
+    """The mixed path moves the state in element chunks (copy of one chunk
+    overlapping the conversion of the previous): uneven shards that straddle the
+    chunk boundaries, K not a multiple of 32."""
+    mesh = meshes.vortex_box(30, jitter=0.1, seed=8)  # K = 1800: 8 chunks of 256 elements, the last of 8
+    gpu, ora = make_pair(mesh, 3, init="ivortex", vortex_center=(0.0, 0.0), proc_limit=7, precision=precision)
+    Q = perturbed(ora.Q, seed=6)
+    gpu.set_global_state(Q)
+    # hi + lo holds ~48 bits: the round trip is exact to ~1e-14 relative
+    assert rel_l2(gpu.get_global_state(), Q) <= 1e-13
+    # state set through the chunked path, then stepped, against the oracle
+    ora.Q = Q
+    gpu.step(5)
+    ora.step(5)
+    err = rel_l2(gpu.get_global_state(), ora.Q)
+    print(f"chunked set_state + 5 mixed steps on a 2%-perturbed state: rel L2 {err:.3e}")
+    assert err <= 1e-6  # deltas of the perturbed state are ~100x the smooth field's
+    gpu.close()
+
+
 def test_errors_are_status_codes():
     mesh = meshes.vortex_box(4)
     gpu, _ = make_pair(mesh, 1, init="ivortex", vortex_center=(0.0, 0.0))
