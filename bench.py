@@ -289,6 +289,7 @@ def run_ours(a, world, rank, local):
     barrier()
     ms = float(sum(s.elapsed_time(e) for s, e in evs))
     info = solver.step(0)  # raises on a non-finite state
+    clocks.stop()  # samples cover the timed region; nvidia-smi's queries would perturb the host-API timings below
     clk = clocks.summary(t_wall0, t_wall1)
     ms = max_over_ranks(ms, world, f"cuda:{local}")
     value = aggregate_rate(world, dof_per_step * a.steps, ms / 1e3)
@@ -426,7 +427,6 @@ def run_ours(a, world, rank, local):
     e2e = {"value": aggregate_rate(world, dof_per_step * a.e2e_steps, e2e_s), "unit": UNIT,
            "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes,
            "steps": a.e2e_steps, "api": "gcfd_set_state + gcfd_step + gcfd_get_state, pinned host shards"}
-    clocks.stop()
 
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
