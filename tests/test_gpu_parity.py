@@ -1,6 +1,6 @@
 """GPU parity of the CUDA path (through the C ABI) against the FP64 oracle.
 
-Tolerances, written here and stated in the design doc:
+Tolerances, written here:
   FP64 path   RHS: max |d| <= 1e-9 * amp * max|RHS|, amp = max|DivInt| / 50 (>= 1),
               covering the two FP64 constructions of DivInt (they agree to ~1e-13
               relative to its entries); steps: rel L2 of the state <= 1e-10
