@@ -355,6 +355,9 @@ struct Launch {
     a.faces32 = c->mfaces;
     a.base32 = c->mbase;
     a.eslot32 = c->meslot;
+    a.DissX32 = reinterpret_cast<float*>(c->DissX);  // mixed path only; half of the FP64 arrays' memory
+    a.DissY32 = reinterpret_cast<float*>(c->DissY);
+    a.VF32 = reinterpret_cast<float*>(c->VF);
     return a;
   }
   static int grid(int n) { return (n + 127) / 128; }
@@ -490,6 +493,9 @@ struct MixedLaunch {
     a.vgamma = c->vgamma;
     a.rhsOut = c->rhsOut;
     a.Btc = c->mBtc;
+    a.DissX32 = reinterpret_cast<const float*>(c->DissX);
+    a.DissY32 = reinterpret_cast<const float*>(c->DissY);
+    a.VF32 = reinterpret_cast<const float*>(c->VF);
     a.err = reinterpret_cast<unsigned int*>(&c->sc->errFlags);
     a.rhsOnly = 0;
     a.gviscS = nullptr;

@@ -66,6 +66,10 @@ struct DissArgs {
   const float* faces32;
   const float2* base32;
   const int* eslot32;         // [3][K] edge * 2 + side
+  // Mixed path: the gradient rows and viscous fluxes in FP32 (in the FP64 arrays' memory).
+  float* DissX32;
+  float* DissY32;
+  float* VF32;
 };
 
 template <int N>
@@ -283,13 +287,20 @@ __global__ void __launch_bounds__(128) k_diss_edge(DissArgs a) {
     vmax = vm;
     a.viscSpeed[g] = vm;
     double* vf = a.VF + static_cast<size_t>(g) * 4 * NE;
+    float* vf32 = MF ? a.VF32 + static_cast<size_t>(g) * 4 * NE : nullptr;
+    auto dx = [&](size_t i) { return MF ? static_cast<double>(a.DissX32[i]) : a.DissX[i]; };
+    auto dy = [&](size_t i) { return MF ? static_cast<double>(a.DissY32[i]) : a.DissY[i]; };
+    auto put = [&](int i, double v) {
+      if constexpr (MF) vf32[i] = static_cast<float>(v);
+      else vf[i] = v;
+    };
     if (g >= a.nInt) {
 #pragma unroll
       for (int n = 0; n < 4; ++n)
 #pragma unroll
         for (int p = 0; p < NE; ++p) {
           const size_t ind = (n * NR + NP + eL * NE + p) * sK + kL;
-          vf[n * NE + p] = nx * a.DissX[ind] + ny * a.DissY[ind];
+          put(n * NE + p, nx * dx(ind) + ny * dy(ind));
         }
     } else {
       const int kR = a.ekR[g], eR = a.eLR[g] >> 2;
@@ -304,8 +315,8 @@ __global__ void __launch_bounds__(128) k_diss_edge(DissArgs a) {
         for (int p = 0; p < NE; ++p) {
           const size_t indL = (n * NR + NP + eL * NE + p) * sK + kL;
           const size_t indR = (n * NR + NP + eR * NE + (NE - 1 - p)) * sK + kR;
-          const double vFL = nx * a.DissX[indL] + ny * a.DissY[indL];
-          const double vFR = nx * a.DissX[indR] + ny * a.DissY[indR];
+          const double vFL = nx * dx(indL) + ny * dy(indL);
+          const double vFR = nx * dx(indR) + ny * dy(indR);
           double v = 0.5 * (vFL + vFR);
           const int rR = 2 * NP + eR * NE + (NE - 1 - p);
           const double epsR = sB[rR * 3] * evR[0] + sB[rR * 3 + 1] * evR[1] + sB[rR * 3 + 2] * evR[2];
@@ -319,7 +330,7 @@ __global__ void __launch_bounds__(128) k_diss_edge(DissArgs a) {
             jump = a.QF[(n * NE3 + eL * NE + p) * sK + kL] - a.QF[(n * NE3 + eL * NE + (NE - 1 - p)) * sK + kL];
           }
           v -= (a.omega * lam * ooLen) * jump;
-          vf[n * NE + p] = v;
+          put(n * NE + p, v);
         }
     }
   }

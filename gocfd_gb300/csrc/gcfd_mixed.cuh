@@ -302,6 +302,9 @@ struct MixedArgs {
   const unsigned long long* gviscS;  // per-stage max viscous speed when the dissipation limits dt
   double cdiff;
   const float* Btc;           // tensor-core path: DivInt split hi / lo in the shared-memory operand layout
+  const float* DissX32;       // PerssonC0: FP32 eps-gradient rows [4][NR][K] and viscous fluxes [edge][4][NE]
+  const float* DissY32;
+  const float* VF32;
   unsigned int* err;          // error flags (bit 0: a tensor-core wait ran out)
 };
 

@@ -160,7 +160,8 @@ __global__ void __launch_bounds__(128) k_diss_limit_mixed(DissArgs a) {
 // CalculateEpsilonGradient, dissipation.go:244-272) in FP32.  The RT gradient
 // of a constant field is zero, so it is taken of U - U_0 (U_0 the element's
 // value at solution point 0, subtracted in FP64): the rounding then scales with
-// the variation of U across the element, not with U.  FP64 inputs and outputs.
+// the variation of U across the element, not with U.  FP64 state in, FP32 rows
+// out (DissX32 / DissY32).
 template <int N>
 __global__ void __launch_bounds__(128) k_diss_grad_mixed(DissArgs a) {
   constexpr int NP = DissDims<N>::NP, NE = DissDims<N>::NE, NE3 = DissDims<N>::NE3;
@@ -226,8 +227,8 @@ __global__ void __launch_bounds__(128) k_diss_grad_mixed(DissArgs a) {
       const float gx = J0 * A + J2 * B + mx[0] * C[0] + mx[1] * C[1] + mx[2] * C[2];
       const float gy = J1 * A + J3 * B + my[0] * C[0] + my[1] * C[1] + my[2] * C[2];
       const float epsr = sB[r * 3] * ev[0] + sB[r * 3 + 1] * ev[1] + sB[r * 3 + 2] * ev[2];
-      a.DissX[(n * NR + rr) * sK + k] = static_cast<double>(gx * epsr);
-      a.DissY[(n * NR + rr) * sK + k] = static_cast<double>(gy * epsr);
+      a.DissX32[(n * NR + rr) * sK + k] = gx * epsr;
+      a.DissY32[(n * NR + rr) * sK + k] = gy * epsr;
     }
   }
 }
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(128) k_diss_grad_mixed(DissArgs a) {
 // time-step limit, then the mixed stage update.  One thread per (element,
 // variable); stage -1 writes the dissipated, filtered RHS to rhsOut.
 template <int N>
-__global__ void __launch_bounds__(128) k_mixed_diss_update(MixedArgs a, UpdateArgs<double> u) {
+__global__ void __launch_bounds__(128, N >= 4 ? 3 : 5) k_mixed_diss_update(MixedArgs a, UpdateArgs<double> u) {
   constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NE3 = MixedDims<N>::NE3;
   constexpr int NF = MixedDims<N>::NF, NR = NP + NE3;
   __shared__ float sD[NP * NF], sV[NP * NP], sVi[NP * NP], smf[NP];
@@ -300,17 +301,17 @@ __global__ void __launch_bounds__(128) k_mixed_diss_update(MixedArgs a, UpdateAr
 #pragma unroll 1
     for (int j = 0; j < NP; ++j) {
       const size_t ind = (n * NR + j) * sK + k;
-      const float dx = static_cast<float>(u.DissX[ind]), dy = static_cast<float>(u.DissY[ind]);
+      const float dx = a.DissX32[ind], dy = a.DissY32[ind];
       const float fr = Jd * (J0 * dx + J1 * dy), fs = Jd * (J2 * dx + J3 * dy);
 #pragma unroll
       for (int r = 0; r < NP; ++r) w[r] = fmaf(sD[r * NF + j], fr, fmaf(sD[r * NF + NP + j], fs, w[r]));
     }
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
-      const double* vf = u.VF + (static_cast<size_t>(eg[e]) * 4 + n) * NE;
+      const float* vf = a.VF32 + (static_cast<size_t>(eg[e]) * 4 + n) * NE;
 #pragma unroll
       for (int p = 0; p < NE; ++p) {
-        const float f = static_cast<float>(vf[own[e] ? p : NE - 1 - p]) * esg[e];
+        const float f = vf[own[e] ? p : NE - 1 - p] * esg[e];
 #pragma unroll
         for (int r = 0; r < NP; ++r) w[r] = fmaf(sD[r * NF + 2 * NP + e * NE + p], f, w[r]);
       }
