@@ -615,7 +615,7 @@ struct MixedLaunch {
     const DissArgs d = Launch<N, double>::diss_args(c, stage, Qs);
     constexpr int NF = Dims<N>::NF;
     k_diss_grad_mixed<N><<<(c->K + 127) / 128, 128, sizeof(float) * (NF * NF + NF * 3), c->stream>>>(d);
-    k_diss_edge<N, true><<<(c->nInt + c->nBC + 127) / 128, 128, 0, c->stream>>>(d);
+    k_diss_edge_mixed<N><<<(c->nInt + c->nBC + 127) / 128, 128, 0, c->stream>>>(d);
   }
   // One stage with the PerssonC0 dissipation: FP64 stage state for the
   // dissipation kernels (Q[1] is free on the mixed path), the Euler RHS of the

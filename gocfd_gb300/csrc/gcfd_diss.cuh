@@ -256,10 +256,8 @@ __global__ void __launch_bounds__(128) k_diss_grad(DissArgs a) {
   }
 }
 
-// Stage 5: viscous normal flux and viscous wave speed per mesh edge.  MF:
-// the penalty's face states come from the mixed path's FP32 face deltas (the
-// two states of the jump share their reference state, which cancels).
-template <int N, bool MF = false>
+// Stage 5: viscous normal flux and viscous wave speed per mesh edge.
+template <int N>
 __global__ void __launch_bounds__(128) k_diss_edge(DissArgs a) {
   constexpr int NP = DissDims<N>::NP, NE = DissDims<N>::NE, NE3 = DissDims<N>::NE3;
   constexpr int NF = DissDims<N>::NF, NR = DissDims<N>::NR;
@@ -287,20 +285,13 @@ __global__ void __launch_bounds__(128) k_diss_edge(DissArgs a) {
     vmax = vm;
     a.viscSpeed[g] = vm;
     double* vf = a.VF + static_cast<size_t>(g) * 4 * NE;
-    float* vf32 = MF ? a.VF32 + static_cast<size_t>(g) * 4 * NE : nullptr;
-    auto dx = [&](size_t i) { return MF ? static_cast<double>(a.DissX32[i]) : a.DissX[i]; };
-    auto dy = [&](size_t i) { return MF ? static_cast<double>(a.DissY32[i]) : a.DissY[i]; };
-    auto put = [&](int i, double v) {
-      if constexpr (MF) vf32[i] = static_cast<float>(v);
-      else vf[i] = v;
-    };
     if (g >= a.nInt) {
 #pragma unroll
       for (int n = 0; n < 4; ++n)
 #pragma unroll
         for (int p = 0; p < NE; ++p) {
           const size_t ind = (n * NR + NP + eL * NE + p) * sK + kL;
-          put(n * NE + p, nx * dx(ind) + ny * dy(ind));
+          vf[n * NE + p] = nx * a.DissX[ind] + ny * a.DissY[ind];
         }
     } else {
       const int kR = a.ekR[g], eR = a.eLR[g] >> 2;
@@ -315,22 +306,16 @@ __global__ void __launch_bounds__(128) k_diss_edge(DissArgs a) {
         for (int p = 0; p < NE; ++p) {
           const size_t indL = (n * NR + NP + eL * NE + p) * sK + kL;
           const size_t indR = (n * NR + NP + eR * NE + (NE - 1 - p)) * sK + kR;
-          const double vFL = nx * dx(indL) + ny * dy(indL);
-          const double vFR = nx * dx(indR) + ny * dy(indR);
+          const double vFL = nx * a.DissX[indL] + ny * a.DissY[indL];
+          const double vFR = nx * a.DissX[indR] + ny * a.DissY[indR];
           double v = 0.5 * (vFL + vFR);
           const int rR = 2 * NP + eR * NE + (NE - 1 - p);
           const double epsR = sB[rR * 3] * evR[0] + sB[rR * 3 + 1] * evR[1] + sB[rR * 3 + 2] * evR[2];
           const double lam = 0.5 * (epsL[p] + epsR);
-          double jump;
-          if constexpr (MF) {
-            constexpr int NEP = (NE + 1) & ~1;
-            const float* fl = a.faces32 + (static_cast<size_t>(g) * 8 + n) * NEP;  // side 0: left element
-            jump = static_cast<double>(fl[p] - fl[NE - 1 - p]);
-          } else {
-            jump = a.QF[(n * NE3 + eL * NE + p) * sK + kL] - a.QF[(n * NE3 + eL * NE + (NE - 1 - p)) * sK + kL];
-          }
-          v -= (a.omega * lam * ooLen) * jump;
-          put(n * NE + p, v);
+          const double qa = a.QF[(n * NE3 + eL * NE + p) * sK + kL];
+          const double qb = a.QF[(n * NE3 + eL * NE + (NE - 1 - p)) * sK + kL];
+          v -= (a.omega * lam * ooLen) * (qa - qb);
+          vf[n * NE + p] = v;
         }
     }
   }

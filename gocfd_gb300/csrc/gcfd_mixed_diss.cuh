@@ -233,6 +233,76 @@ __global__ void __launch_bounds__(128) k_diss_grad_mixed(DissArgs a) {
   }
 }
 
+// Viscous normal flux and viscous wave speed per mesh edge (k_diss_edge,
+// StoreEdgeViscousFlux edges.go:151-244) in FP32 from the FP32 gradient rows;
+// the penalty's jump comes from the FP32 face deltas of the left element (its
+// reference state cancels).  The wave-speed maximum is stored as FP64.
+template <int N>
+__global__ void __launch_bounds__(128) k_diss_edge_mixed(DissArgs a) {
+  constexpr int NP = DissDims<N>::NP, NE = DissDims<N>::NE;
+  constexpr int NF = DissDims<N>::NF, NR = DissDims<N>::NR, NEP = (NE + 1) & ~1;
+  __shared__ float sB[NF * 3];
+  stage_operator(sB, a.Bary, NF * 3);
+  __syncthreads();
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  float vmax = 0.0f;
+  if (g < a.nInt + a.nBC) {
+    const size_t sK = static_cast<size_t>(a.K);
+    const int kL = a.ekL[g], eL = a.eLR[g] & 3;
+    const float nx = static_cast<float>(a.enx[g]), ny = static_cast<float>(a.eny[g]);
+    const float oohK = static_cast<float>(a.eoohK[g]);
+    float evL[3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) evL[v] = static_cast<float>(vdouble(a.epsV, a.etov[v * sK + kL]));
+    float epsL[NE];
+    float vm = -3.4028235e38f;
+#pragma unroll
+    for (int p = 0; p < NE; ++p) {
+      const int r = 2 * NP + eL * NE + p;
+      epsL[p] = sB[r * 3] * evL[0] + sB[r * 3 + 1] * evL[1] + sB[r * 3 + 2] * evL[2];
+      vm = fmaxf(oohK * oohK * epsL[p], vm);
+    }
+    vmax = vm;
+    a.viscSpeed[g] = static_cast<double>(vm);
+    float* vf = a.VF32 + static_cast<size_t>(g) * 4 * NE;
+    if (g >= a.nInt) {
+#pragma unroll
+      for (int n = 0; n < 4; ++n)
+#pragma unroll
+        for (int p = 0; p < NE; ++p) {
+          const size_t ind = (n * NR + NP + eL * NE + p) * sK + kL;
+          vf[n * NE + p] = nx * a.DissX32[ind] + ny * a.DissY32[ind];
+        }
+    } else {
+      const int kR = a.ekR[g], eR = a.eLR[g] >> 2;
+      float evR[3];
+#pragma unroll
+      for (int v = 0; v < 3; ++v) evR[v] = static_cast<float>(vdouble(a.epsV, a.etov[v * sK + kR]));
+      const double len = (eL == 1) ? 2.0 * sqrt(2.0) * a.eIIL[g] : 2.0 * a.eIIL[g];
+      const float pen = static_cast<float>(a.omega / len);
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+        const float* fl = a.faces32 + (static_cast<size_t>(g) * 8 + n) * NEP;  // side 0: left element
+#pragma unroll
+        for (int p = 0; p < NE; ++p) {
+          const size_t indL = (n * NR + NP + eL * NE + p) * sK + kL;
+          const size_t indR = (n * NR + NP + eR * NE + (NE - 1 - p)) * sK + kR;
+          const float vFL = nx * a.DissX32[indL] + ny * a.DissY32[indL];
+          const float vFR = nx * a.DissX32[indR] + ny * a.DissY32[indR];
+          const int rR = 2 * NP + eR * NE + (NE - 1 - p);
+          const float epsR = sB[rR * 3] * evR[0] + sB[rR * 3 + 1] * evR[1] + sB[rR * 3 + 2] * evR[2];
+          const float lam = 0.5f * (epsL[p] + epsR);
+          vf[n * NE + p] = 0.5f * (vFL + vFR) - (pen * lam) * (fl[p] - fl[NE - 1 - p]);
+        }
+      }
+    }
+  }
+  vmax = warp_max(vmax);
+  if ((threadIdx.x & 31) == 0)
+    atomicMax(a.gvisc,
+              static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(fmaxf(vmax, 0.0f)))));
+}
+
 // RHS = F(a) (RHS_Euler + DivInt DOF(DissX, DissY, VF) / |J|), the viscous
 // time-step limit, then the mixed stage update.  One thread per (element,
 // variable); stage -1 writes the dissipated, filtered RHS to rhsOut.
