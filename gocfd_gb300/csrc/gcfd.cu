@@ -600,21 +600,22 @@ struct MixedLaunch {
                                                                     &c->sc->gmax[0]),
                                                                Launch<N, double>::update_args(c, -1, c->Qtmp));
   }
-  // Sensor, vertex smoothing and the rkStep-2 limiter; the face states the
-  // dissipation needs are the mixed path's own (k_mixed_relimit rebuilds them
-  // after the limiter), so no FP64 interpolation.
+  // Sensor, vertex smoothing and the rkStep-2 limiter on the mixed state (the
+  // limiter rewrites D2, the faces and the reference states it changes).
   static void diss_front(gcfd_ctx* c, int stage, double* Qs) {
     cudaMemsetAsync(c->sigV, 0, sizeof(unsigned long long) * c->nverts, c->stream);
     cudaMemsetAsync(c->epsV, 0, sizeof(unsigned long long) * c->nverts, c->stream);
     const DissArgs d = Launch<N, double>::diss_args(c, stage, Qs);
-    k_diss_sensor_mixed<N><<<(c->K + 127) / 128, 128, 0, c->stream>>>(d);
-    if (stage == 2) k_diss_limit_mixed<N><<<(4 * c->K + 127) / 128, 128, 0, c->stream>>>(d);
+    const MixedArgs m = args(c, stage, c->Q[0], &c->sc->time, &c->sc->gmax[stage < 0 ? 0 : stage]);
+    k_diss_sensor_mixed<N><<<(c->K + 127) / 128, 128, 0, c->stream>>>(d, m);
+    if (stage == 2) k_mixed_limit<N><<<gridE(c), 128, 0, c->stream>>>(d, m);
   }
   // The RT gradient in FP32 (delta form), then the viscous edge fluxes.
   static void diss_middle(gcfd_ctx* c, int stage, double* Qs) {
     const DissArgs d = Launch<N, double>::diss_args(c, stage, Qs);
+    const MixedArgs m = args(c, stage, c->Q[0], &c->sc->time, &c->sc->gmax[stage < 0 ? 0 : stage]);
     constexpr int NF = Dims<N>::NF;
-    k_diss_grad_mixed<N><<<(c->K + 127) / 128, 128, sizeof(float) * (NF * NF + NF * 3), c->stream>>>(d);
+    k_diss_grad_mixed<N><<<(c->K + 127) / 128, 128, sizeof(float) * (NF * NF + NF * 3), c->stream>>>(d, m);
     k_diss_edge_mixed<N><<<(c->nInt + c->nBC + 127) / 128, 128, 0, c->stream>>>(d);
   }
   // One stage with the PerssonC0 dissipation: FP64 stage state for the
@@ -622,13 +623,8 @@ struct MixedLaunch {
   // stage from the delta-form kernel, then the dissipated update.
   static void diss_stage(gcfd_ctx* c, int s) {
     using L = Launch<N, double>;
-    double* Qs64 = c->Q[1];
-    k_mixed_form_stage<N><<<gridE(c), 128, 0, c->stream>>>(args(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]),
-                                                           Qs64);
+    double* Qs64 = c->Q[1];  // not read: the dissipation kernels take the mixed state
     diss_front(c, s, Qs64);
-    if (s == 2)
-      k_mixed_relimit<N><<<gridE(c), 128, 0, c->stream>>>(args(c, 2, c->Q[0], &c->sc->time, &c->sc->gmax[2]),
-                                                          Qs64);
     edges(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s], true);
     diss_middle(c, s, Qs64);
     MixedArgs m = args(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]);

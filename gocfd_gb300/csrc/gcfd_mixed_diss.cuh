@@ -1,64 +1,17 @@
-// PerssonC0 shock capturing on the mixed path: the Euler RHS stays in the
-// FP32 delta form (k_mixed_stage with rhsOnly); the sensor, vertex maxima,
-// limiter and viscous edge fluxes run in FP64 on the stage state (the kernels
-// of gcfd_diss.cuh); the two heavy parts run in FP32: the RT gradient
-// (k_diss_grad_mixed, on the element's deltas U - U_0) and k_mixed_diss_update,
-// which adds AddDissipation, applies the modal filter and the viscous time-step
-// limit, then performs the mixed stage update (stage_tail).  The conserved
-// state keeps its compensated FP32 accumulation.
+// PerssonC0 shock capturing on the mixed path, on the compensated FP32 state
+// itself (no FP64 stage state): the Euler RHS stays in the FP32 delta form
+// (k_mixed_stage with rhsOnly); the sensor's products (on the stage density),
+// the rkStep-2 limiter and the RT gradient work on the element deltas
+// dq = dQ0 + D_s - D_s(point 0); the viscous edge fluxes, AddDissipation and
+// the modal RHS filter run in FP32; the sensor's log10 and sine ramp and the
+// vertex maxima stay FP64.  k_mixed_diss_update adds the dissipation, filters,
+// applies the viscous time-step limit and performs the mixed stage update
+// (stage_tail).
 #pragma once
 #include "gcfd_diss.cuh"
 #include "gcfd_mixed.cuh"
 
 namespace gcfd {
-
-// FP64 stage state Q_s = (hi + lo) + D_s (stage 0: hi + lo), one thread per
-// (element, variable) as the stage kernel.
-template <int N>
-__global__ void __launch_bounds__(128) k_mixed_form_stage(MixedArgs a, double* Qs64) {
-  constexpr int NP = MixedDims<N>::NP;
-  const int n = threadIdx.x >> 5;
-  const int k = blockIdx.x * 32 + (threadIdx.x & 31);
-  if (k >= a.K) return;
-  const size_t sK = static_cast<size_t>(a.K);
-  const size_t off = static_cast<size_t>(n) * NP * sK + k;
-#pragma unroll
-  for (int i = 0; i < NP; ++i) {
-    const size_t ind = off + i * sK;
-    double q = static_cast<double>(a.Qhi[ind]) + static_cast<double>(a.Qlo[ind]);
-    if (a.stage >= 1) q += static_cast<double>(a.D[a.stage][ind]);
-    Qs64[ind] = q;
-  }
-}
-
-// After the rkStep-2 limiter changed the FP64 stage state: the stage-2
-// increment, faces and reference state of the mixed path from it.
-template <int N>
-__global__ void __launch_bounds__(128) k_mixed_relimit(MixedArgs a, const double* Qs64) {
-  constexpr int NP = MixedDims<N>::NP, NPP = MixedDims<N>::NPP;
-  __syncthreads();
-  const int n = threadIdx.x >> 5;
-  const int k = blockIdx.x * 32 + (threadIdx.x & 31);
-  if (k >= a.K) return;
-  const size_t sK = static_cast<size_t>(a.K);
-  const size_t off = static_cast<size_t>(n) * NP * sK + k;
-  float dn[NP], dqn[NPP];
-#pragma unroll
-  for (int r = 0; r < NP; ++r) {
-    const size_t ind = off + r * sK;
-    dn[r] = static_cast<float>(Qs64[ind] - (static_cast<double>(a.Qhi[ind]) + static_cast<double>(a.Qlo[ind])));
-    a.D[2][ind] = dn[r];
-  }
-#pragma unroll
-  for (int r = 0; r < NPP; ++r) dqn[r] = (r < NP) ? a.dQ0[off + r * sK] + (dn[r] - dn[0]) : 0.0f;
-  int es[3];
-#pragma unroll
-  for (int e = 0; e < 3; ++e) es[e] = a.eslot[e * sK + k];
-  write_faces<N>(a, es, n, dqn);
-  float h = a.Qhi[off], l = a.Qlo[off];
-  df_add(h, l, dn[0]);
-  a.base[static_cast<size_t>(k) * 4 + n] = make_float2(h, l);
-}
 
 // limit_filter_modal in FP32.
 template <int NP>
@@ -83,13 +36,27 @@ __device__ __forceinline__ void limit_filter_modal_f(float u[NP], const float* s
   }
 }
 
+// The stage-s deltas of variable n of element k relative to its stage state
+// at solution point 0: dQ0 + (D_s - D_s(point 0)), as the stage kernel forms
+// them (stage <= 0: dQ0).
+template <int N>
+__device__ __forceinline__ void stage_deltas(const MixedArgs& a, int n, int k, size_t sK,
+                                             float dq[MixedDims<N>::NP]) {
+  constexpr int NP = MixedDims<N>::NP;
+  const size_t off = static_cast<size_t>(n) * NP * sK + k;
+  const float* ds = (a.stage >= 1) ? a.D[a.stage] + off : nullptr;
+  const float d0 = ds ? ds[0] : 0.0f;
+#pragma unroll
+  for (int i = 0; i < NP; ++i) dq[i] = a.dQ0[off + i * sK] + (ds ? ds[i * sK] - d0 : 0.0f);
+}
+
 // The shock sensor (k_diss_sensor: UpdateSeMoment, UpdateShockFinderSigma,
 // CalculateElementViscosity) with its three Np x Np products in FP32; the
 // moment's log10 and the sigma ramp stay in FP64.  FP32 rounding perturbs the
 // high-mode energy by ~1e-7 of the density's, i.e. only moments far below the
 // ramp (sigma = 0 there either way).
 template <int N>
-__global__ void __launch_bounds__(128) k_diss_sensor_mixed(DissArgs a) {
+__global__ void __launch_bounds__(128) k_diss_sensor_mixed(DissArgs a, MixedArgs m) {
   constexpr int NP = DissDims<N>::NP;
   __shared__ float sP[NP * NP], sM[NP * NP], sDq[NP * NP];
   stage_operator(sP, a.SensP, NP * NP);
@@ -99,9 +66,12 @@ __global__ void __launch_bounds__(128) k_diss_sensor_mixed(DissArgs a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= a.K) return;
   const size_t sK = static_cast<size_t>(a.K);
-  float rho[NP];
+  // The stage density from the mixed state: reference state plus deltas.
+  float dq[NP], rho[NP];
+  stage_deltas<N>(m, 0, k, sK, dq);
+  const float2 b0 = m.base[static_cast<size_t>(k) * 4];
 #pragma unroll
-  for (int j = 0; j < NP; ++j) rho[j] = static_cast<float>(a.Qs[j * sK + k]);
+  for (int j = 0; j < NP; ++j) rho[j] = b0.x + (b0.y + dq[j]);
   float num = 0.0f, den = 0.0f;
 #pragma unroll
   for (int i = 0; i < NP; ++i) {
@@ -131,39 +101,54 @@ __global__ void __launch_bounds__(128) k_diss_sensor_mixed(DissArgs a) {
 }
 
 // The rkStep-2 modal limiter (k_diss_limit, limitAndFilterSolution) on the
-// FP64 stage state, in FP32 on the deltas U - U_0: the filter keeps mode 0 (the
-// constant), so filter(U) = U_0 + filter(U - U_0).  One thread per (variable,
-// element).
+// mixed stage state, in FP32 on the deltas dq = U - U_0: the filter keeps mode
+// 0 (the constant), so filter(U) = U_0 + filter(dq).  The limited state goes
+// back into the stage-2 increment, D2'_i = D2_0 + dq'_i - dQ0_i, with the
+// faces and reference state rebuilt from it.  One thread per (element,
+// variable), 32 x 4 per CTA.
 template <int N>
-__global__ void __launch_bounds__(128) k_diss_limit_mixed(DissArgs a) {
-  constexpr int NP = DissDims<N>::NP;
+__global__ void __launch_bounds__(128) k_mixed_limit(DissArgs d, MixedArgs a) {
+  constexpr int NP = DissDims<N>::NP, NPP = MixedDims<N>::NPP;
   __shared__ float sV[NP * NP], sVi[NP * NP], smf[NP];
-  stage_operator(sV, a.V, NP * NP);
-  stage_operator(sVi, a.Vinv, NP * NP);
-  stage_operator(smf, a.mf, NP);
+  stage_operator(sV, d.V, NP * NP);
+  stage_operator(sVi, d.Vinv, NP * NP);
+  stage_operator(smf, d.mf, NP);
   __syncthreads();
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 4 * a.K) return;
-  const int n = t / a.K, k = t - n * a.K;
+  const int n = threadIdx.x >> 5;
+  const int k = blockIdx.x * 32 + (threadIdx.x & 31);
+  if (k >= a.K) return;
   const size_t sK = static_cast<size_t>(a.K);
-  const float alpha = static_cast<float>(sin(0.5 * 3.14159265358979323846 * element_sigma(a, k, sK)));
-  const double u0 = a.Qlim[(n * NP) * sK + k];
-  float q[NP];
+  const size_t off = static_cast<size_t>(n) * NP * sK + k;
+  const float alpha = static_cast<float>(sin(0.5 * 3.14159265358979323846 * element_sigma(d, k, sK)));
+  float dq[NP];
+  stage_deltas<N>(a, n, k, sK, dq);
+  limit_filter_modal_f<NP>(dq, sV, sVi, smf, alpha);
+  const float d20 = a.D[2][off];
+  float dqn[NPP];
 #pragma unroll
-  for (int i = 0; i < NP; ++i) q[i] = static_cast<float>(a.Qlim[(n * NP + i) * sK + k] - u0);
-  limit_filter_modal_f<NP>(q, sV, sVi, smf, alpha);
+  for (int r = 0; r < NPP; ++r) dqn[r] = 0.0f;
 #pragma unroll
-  for (int i = 0; i < NP; ++i) a.Qlim[(n * NP + i) * sK + k] = u0 + static_cast<double>(q[i]);
+  for (int r = 0; r < NP; ++r) {
+    a.D[2][off + r * sK] = d20 + (dq[r] - a.dQ0[off + r * sK]);
+    dqn[r] = dq[r] - dq[0];
+  }
+  int es[3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) es[e] = a.eslot[e * sK + k];
+  write_faces<N>(a, es, n, dqn);
+  float h = a.Qhi[off], l = a.Qlo[off];
+  df_add(h, l, d20 + (dq[0] - a.dQ0[off]));
+  a.base[static_cast<size_t>(k) * 4 + n] = make_float2(h, l);
 }
 
 // eps * grad(Q) at the interior and edge flux points (k_diss_grad,
 // CalculateEpsilonGradient, dissipation.go:244-272) in FP32.  The RT gradient
 // of a constant field is zero, so it is taken of U - U_0 (U_0 the element's
 // value at solution point 0, subtracted in FP64): the rounding then scales with
-// the variation of U across the element, not with U.  FP64 state in, FP32 rows
-// out (DissX32 / DissY32).
+// the variation of U across the element, not with U; the deltas are the mixed
+// state's own (dQ0 + D_s - D_s(point 0)).  FP32 rows out (DissX32 / DissY32).
 template <int N>
-__global__ void __launch_bounds__(128) k_diss_grad_mixed(DissArgs a) {
+__global__ void __launch_bounds__(128) k_diss_grad_mixed(DissArgs a, MixedArgs m) {
   constexpr int NP = DissDims<N>::NP, NE = DissDims<N>::NE, NE3 = DissDims<N>::NE3;
   constexpr int NF = DissDims<N>::NF, NR = DissDims<N>::NR;
   extern __shared__ float smf32[];
@@ -196,10 +181,10 @@ __global__ void __launch_bounds__(128) k_diss_grad_mixed(DissArgs a) {
   }
 #pragma unroll 1
   for (int n = 0; n < 4; ++n) {
-    const double u0 = a.Qs[(n * NP) * sK + k];
+    const float2 b0 = m.base[static_cast<size_t>(k) * 4 + n];
+    const double u0 = static_cast<double>(b0.x) + static_cast<double>(b0.y);
     float U[NP], Ue[NE3];
-#pragma unroll
-    for (int i = 0; i < NP; ++i) U[i] = static_cast<float>(a.Qs[(n * NP + i) * sK + k] - u0);
+    stage_deltas<N>(m, n, k, sK, U);
     // The stored left states (the left element's faces, this element's order):
     // its reference state plus its FP32 face deltas.
 #pragma unroll
