@@ -1346,6 +1346,20 @@ int upload_const_ops(gcfd_ctx* c, const std::vector<float>& divT, const std::vec
   }
   GCFD_CUDA(c, cudaMemcpyToSymbol(d, divT.data(), divT.size() * sizeof(float)));
   GCFD_CUDA(c, cudaMemcpyToSymbol(i, iopT.data(), iopT.size() * sizeof(float)));
+  // The modal filter's operators (PerssonC0 on the mixed path).
+  const void* sv[5] = {&cV0, &cV1, &cV2, &cV3, &cV4};
+  const void* svi[5] = {&cVi0, &cVi1, &cVi2, &cVi3, &cVi4};
+  const void* smf[5] = {&cMf0, &cMf1, &cMf2, &cMf3, &cMf4};
+  const int np = c->Np;
+  std::vector<float> V(static_cast<size_t>(np) * np), Vi(V.size()), mf(np);
+  for (size_t q = 0; q < V.size(); ++q) {
+    V[q] = static_cast<float>(c->el.V.v[q]);
+    Vi[q] = static_cast<float>(c->el.Vinv.v[q]);
+  }
+  for (int q = 0; q < np; ++q) mf[q] = static_cast<float>(c->el.ModeFilter[q]);
+  GCFD_CUDA(c, cudaMemcpyToSymbol(sv[c->N], V.data(), V.size() * sizeof(float)));
+  GCFD_CUDA(c, cudaMemcpyToSymbol(svi[c->N], Vi.data(), Vi.size() * sizeof(float)));
+  GCFD_CUDA(c, cudaMemcpyToSymbol(smf[c->N], mf.data(), mf.size() * sizeof(float)));
   return GCFD_OK;
 }
 

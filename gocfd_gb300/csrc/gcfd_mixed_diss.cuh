@@ -13,6 +13,62 @@
 
 namespace gcfd {
 
+// The modal filter's operators (V, V^-1, the mode filter) in constant memory,
+// one copy per order N, for the same reason as the divergence operator.
+__constant__ float cV0[Dims<0>::NP * Dims<0>::NP], cV1[Dims<1>::NP * Dims<1>::NP],
+    cV2[Dims<2>::NP * Dims<2>::NP], cV3[Dims<3>::NP * Dims<3>::NP], cV4[Dims<4>::NP * Dims<4>::NP];
+__constant__ float cVi0[Dims<0>::NP * Dims<0>::NP], cVi1[Dims<1>::NP * Dims<1>::NP],
+    cVi2[Dims<2>::NP * Dims<2>::NP], cVi3[Dims<3>::NP * Dims<3>::NP], cVi4[Dims<4>::NP * Dims<4>::NP];
+__constant__ float cMf0[Dims<0>::NP], cMf1[Dims<1>::NP], cMf2[Dims<2>::NP], cMf3[Dims<3>::NP],
+    cMf4[Dims<4>::NP];
+template <int N>
+__device__ __forceinline__ float v_op(int i) {
+  if constexpr (N == 0) return cV0[i];
+  else if constexpr (N == 1) return cV1[i];
+  else if constexpr (N == 2) return cV2[i];
+  else if constexpr (N == 3) return cV3[i];
+  else return cV4[i];
+}
+template <int N>
+__device__ __forceinline__ float vi_op(int i) {
+  if constexpr (N == 0) return cVi0[i];
+  else if constexpr (N == 1) return cVi1[i];
+  else if constexpr (N == 2) return cVi2[i];
+  else if constexpr (N == 3) return cVi3[i];
+  else return cVi4[i];
+}
+template <int N>
+__device__ __forceinline__ float mf_op(int i) {
+  if constexpr (N == 0) return cMf0[i];
+  else if constexpr (N == 1) return cMf1[i];
+  else if constexpr (N == 2) return cMf2[i];
+  else if constexpr (N == 3) return cMf3[i];
+  else return cMf4[i];
+}
+// limitAndFilterSolution's filter u <- V diag(mf (1 - alpha)) V^-1 u for
+// modes >= 1, in FP32 with constant-bank operators.
+template <int N>
+__device__ __forceinline__ void limit_filter_modal_c(float u[Dims<N>::NP], float alpha) {
+  constexpr int NP = Dims<N>::NP;
+  float m[NP];
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int j = 0; j < NP; ++j) acc = fmaf(vi_op<N>(i * NP + j), u[j], acc);
+    m[i] = acc;
+  }
+#pragma unroll
+  for (int i = 1; i < NP; ++i) m[i] *= mf_op<N>(i) * (1.0f - alpha);
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int j = 0; j < NP; ++j) acc = fmaf(v_op<N>(i * NP + j), m[j], acc);
+    u[i] = acc;
+  }
+}
+
 // limit_filter_modal in FP32.
 template <int NP>
 __device__ __forceinline__ void limit_filter_modal_f(float u[NP], const float* sV, const float* sVi,
@@ -109,11 +165,6 @@ __global__ void __launch_bounds__(128) k_diss_sensor_mixed(DissArgs a, MixedArgs
 template <int N>
 __global__ void __launch_bounds__(128) k_mixed_limit(DissArgs d, MixedArgs a) {
   constexpr int NP = DissDims<N>::NP, NPP = MixedDims<N>::NPP;
-  __shared__ float sV[NP * NP], sVi[NP * NP], smf[NP];
-  stage_operator(sV, d.V, NP * NP);
-  stage_operator(sVi, d.Vinv, NP * NP);
-  stage_operator(smf, d.mf, NP);
-  __syncthreads();
   const int n = threadIdx.x >> 5;
   const int k = blockIdx.x * 32 + (threadIdx.x & 31);
   if (k >= a.K) return;
@@ -122,7 +173,7 @@ __global__ void __launch_bounds__(128) k_mixed_limit(DissArgs d, MixedArgs a) {
   const float alpha = static_cast<float>(sin(0.5 * 3.14159265358979323846 * element_sigma(d, k, sK)));
   float dq[NP];
   stage_deltas<N>(a, n, k, sK, dq);
-  limit_filter_modal_f<NP>(dq, sV, sVi, smf, alpha);
+  limit_filter_modal_c<N>(dq, alpha);
   const float d20 = a.D[2][off];
   float dqn[NPP];
 #pragma unroll
@@ -295,7 +346,6 @@ template <int N>
 __global__ void __launch_bounds__(128, N >= 4 ? 3 : 5) k_mixed_diss_update(MixedArgs a, UpdateArgs<double> u) {
   constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NE3 = MixedDims<N>::NE3;
   constexpr int NF = MixedDims<N>::NF, NR = NP + NE3;
-  __shared__ float sD[NP * NF], sV[NP * NP], sVi[NP * NP], smf[NP];
   __shared__ double sdt;
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = blockIdx.x * 32 + lane;
@@ -322,10 +372,6 @@ __global__ void __launch_bounds__(128, N >= 4 ? 3 : 5) k_mixed_diss_update(Mixed
     }
     dvNew = dv;
   }
-  stage_operator(sD, u.Div, NP * NF);
-  stage_operator(sV, u.V, NP * NP);
-  stage_operator(sVi, u.Vinv, NP * NP);
-  stage_operator(smf, u.mf, NP);
   if (threadIdx.x == 0 && needs_global_dt(a, s)) sdt = global_stage_dt(a, s);
   __syncthreads();
   if (needs_global_dt(a, s)) dtLocal = sdt;
@@ -353,13 +399,15 @@ __global__ void __launch_bounds__(128, N >= 4 ? 3 : 5) k_mixed_diss_update(Mixed
     float w[NP];
 #pragma unroll
     for (int r = 0; r < NP; ++r) w[r] = 0.0f;
-#pragma unroll 1
+    constexpr int NPP = MixedDims<N>::NPP;  // DivInt[r][j] = div_op<N>(j * NPP + r)
+#pragma unroll
     for (int j = 0; j < NP; ++j) {
       const size_t ind = (n * NR + j) * sK + k;
       const float dx = a.DissX32[ind], dy = a.DissY32[ind];
       const float fr = Jd * (J0 * dx + J1 * dy), fs = Jd * (J2 * dx + J3 * dy);
 #pragma unroll
-      for (int r = 0; r < NP; ++r) w[r] = fmaf(sD[r * NF + j], fr, fmaf(sD[r * NF + NP + j], fs, w[r]));
+      for (int r = 0; r < NP; ++r)
+        w[r] = fmaf(div_op<N>(j * NPP + r), fr, fmaf(div_op<N>((NP + j) * NPP + r), fs, w[r]));
     }
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
@@ -368,12 +416,12 @@ __global__ void __launch_bounds__(128, N >= 4 ? 3 : 5) k_mixed_diss_update(Mixed
       for (int p = 0; p < NE; ++p) {
         const float f = vf[own[e] ? p : NE - 1 - p] * esg[e];
 #pragma unroll
-        for (int r = 0; r < NP; ++r) w[r] = fmaf(sD[r * NF + 2 * NP + e * NE + p], f, w[r]);
+        for (int r = 0; r < NP; ++r) w[r] = fmaf(div_op<N>((2 * NP + e * NE + p) * NPP + r), f, w[r]);
       }
     }
 #pragma unroll
     for (int r = 0; r < NP; ++r) w[r] = static_cast<float>(a.rhsOut[off + r * sK]) + oojd * w[r];
-    limit_filter_modal_f<NP>(w, sV, sVi, smf, alpha);
+    limit_filter_modal_c<N>(w, alpha);
     float rhs[NP];
 #pragma unroll
     for (int r = 0; r < NP; ++r) rhs[r] = w[r];
