@@ -31,7 +31,7 @@ EXPORTS = [
     "gcfd_get_state", "gcfd_set_state_device", "gcfd_get_state_device", "gcfd_set_time",
     "gcfd_get_time", "gcfd_rhs", "gcfd_step", "gcfd_enqueue_steps", "gcfd_get_stream", "gcfd_set_option",
     "gcfd_get_option", "gcfd_profile_step",
-    "gcfd_host_operator", "gcfd_residual_norms_static", "gcfd_functional", "gcfd_rhs_vjp",
+    "gcfd_host_operator", "gcfd_read_mesh", "gcfd_free_mesh", "gcfd_residual_norms_static", "gcfd_functional", "gcfd_rhs_vjp",
     "gcfd_record_steps", "gcfd_step_vjp",
 ]
 
@@ -100,6 +100,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         lib.gcfd_get_option.argtypes = [C.c_void_p, C.c_int32, PI]
         lib.gcfd_profile_step.argtypes = [C.c_void_p, PD, PI]
         lib.gcfd_host_operator.argtypes = [C.c_int32, C.c_int32, PD, PI, PI]
+        lib.gcfd_read_mesh.argtypes = [C.c_char_p, C.POINTER(Mesh)]
+        lib.gcfd_free_mesh.argtypes = [C.POINTER(Mesh)]
+        lib.gcfd_free_mesh.restype = None
         lib.gcfd_residual_norms_static.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, PD, PD, PD]
         lib.gcfd_functional.argtypes = [C.c_void_p, C.c_int32, PD, C.c_int32, PI, C.POINTER(PD), PD]
         lib.gcfd_rhs_vjp.argtypes = [C.c_void_p, C.c_double, C.c_int32, PI, C.POINTER(PD), C.POINTER(PD),
@@ -114,6 +117,22 @@ def check(lib, ctx, rc: int):
     if rc != GCFD_OK:
         msg = lib.gcfd_last_error(ctx)
         raise GcfdError(rc, msg.decode() if msg else "")
+
+
+def read_mesh(path: str):
+    """A Gambit (.neu) or SU2 (.su2) mesh read by the library's C++ reader:
+    (VX, VY, EToV (K x 3, 0-based), bc_edges [(v1, v2, flag)]).  No GPU needed."""
+    lib = load()
+    m = Mesh()
+    check(lib, None, lib.gcfd_read_mesh(os.fsencode(path), C.byref(m)))
+    try:
+        vx = np.ctypeslib.as_array(m.vx, shape=(m.nverts,)).copy()
+        vy = np.ctypeslib.as_array(m.vy, shape=(m.nverts,)).copy()
+        etov = np.ctypeslib.as_array(m.etov, shape=(m.K * 3,)).reshape(m.K, 3).copy()
+        bc = [(int(m.bc_v1[i]), int(m.bc_v2[i]), int(m.bc_flag[i])) for i in range(m.nbc)]
+    finally:
+        lib.gcfd_free_mesh(C.byref(m))
+    return vx, vy, etov, bc
 
 
 def host_operator(N: int, which: int) -> np.ndarray:

@@ -1619,6 +1619,40 @@ int gcfd_destroy(gcfd_ctx* ctx) {
   return GCFD_OK;
 }
 
+int gcfd_read_mesh(const char* path, gcfd_mesh* out) {
+  if (!path || !out) return fail(nullptr, GCFD_ERR_ARG, "null argument");
+  MeshFile m;
+  const std::string msg = read_mesh_file(path, &m);
+  if (!msg.empty()) return fail(nullptr, GCFD_ERR_ARG, msg);
+  auto copy = [](const auto& v) {
+    using T = typename std::decay_t<decltype(v)>::value_type;
+    T* p = new T[std::max<size_t>(v.size(), 1)];
+    std::copy(v.begin(), v.end(), p);
+    return p;
+  };
+  out->nverts = static_cast<int32_t>(m.vx.size());
+  out->vx = copy(m.vx);
+  out->vy = copy(m.vy);
+  out->K = static_cast<int32_t>(m.etov.size() / 3);
+  out->etov = copy(m.etov);
+  out->nbc = static_cast<int32_t>(m.bc_flag.size());
+  out->bc_v1 = copy(m.bc_v1);
+  out->bc_v2 = copy(m.bc_v2);
+  out->bc_flag = copy(m.bc_flag);
+  return GCFD_OK;
+}
+
+void gcfd_free_mesh(gcfd_mesh* m) {
+  if (!m) return;
+  delete[] m->vx;
+  delete[] m->vy;
+  delete[] m->etov;
+  delete[] m->bc_v1;
+  delete[] m->bc_v2;
+  delete[] m->bc_flag;
+  *m = gcfd_mesh{};
+}
+
 const char* gcfd_last_error(const gcfd_ctx* ctx) {
   return ctx ? ctx->err.c_str() : g_create_error.c_str();
 }

@@ -2,7 +2,12 @@
 // each piece follows.
 #include "mesh.hpp"
 
+#include <algorithm>
+#include <cctype>
 #include <cmath>
+#include <fstream>
+#include <sstream>
+#include <stdexcept>
 #include <unordered_map>
 
 namespace gcfd {
@@ -128,6 +133,187 @@ void build_geometry(const DFRElement& el, const Topology& t, const double* vx, c
   };
   local(el.rFlux, el.sFlux, &g->xFlux, &g->yFlux);
   local(el.r, el.s, &g->xSol, &g->ySol);
+}
+
+// ---------------------------------------------------------------------------
+// Mesh files.
+
+int bc_flag_of_tag(const std::string& tag) {
+  std::string base;
+  for (char ch : tag) base.push_back(static_cast<char>(std::tolower(static_cast<unsigned char>(ch))));
+  const auto b = base.find_first_not_of(" \t"), e = base.find_last_not_of(" \t");
+  base = (b == std::string::npos) ? std::string() : base.substr(b, e - b + 1);
+  const auto dash = base.find('-');
+  if (dash != std::string::npos && dash > 0) base = base.substr(0, dash);
+  static const std::unordered_map<std::string, int> flags = {
+      {"inflow", 1}, {"in", 1}, {"dirichlet", 2}, {"slip", 3}, {"far", 4}, {"wall", 5}, {"cyl", 6},
+      {"neuman", 7}, {"out", 8}, {"outflow", 8}, {"ivortex", 9}, {"periodic", 10}, {"periodicreversed", 11}};
+  const auto it = flags.find(base);
+  return it == flags.end() ? -1 : it->second;
+}
+
+namespace {
+
+std::vector<std::string> split_ws(const std::string& line) {
+  std::istringstream is(line);
+  std::vector<std::string> t;
+  std::string w;
+  while (is >> w) t.push_back(w);
+  return t;
+}
+
+// Throws std::runtime_error on malformed input; the caller turns it into a status.
+struct Lines {
+  std::vector<std::string> v;
+  const std::string& at(size_t i) const {
+    if (i >= v.size()) throw std::runtime_error("unexpected end of file");
+    return v[i];
+  }
+  std::vector<std::string> tok(size_t i, size_t need) const {
+    auto t = split_ws(at(i));
+    if (t.size() < need) throw std::runtime_error("malformed line " + std::to_string(i + 1) + ": [" + v[i] + "]");
+    return t;
+  }
+};
+
+void add_bc(MeshFile* m, const std::string& tag, int a, int b) {
+  const int f = bc_flag_of_tag(tag);
+  if (f < 0) throw std::runtime_error("unable to find BC with base name, full tag: [" + tag + "]");
+  m->bc_v1.push_back(a);
+  m->bc_v2.push_back(b);
+  m->bc_flag.push_back(f);
+}
+
+void read_gambit(const Lines& L, MeshFile* m) {
+  size_t pos = 6;
+  auto h = L.tok(pos, 5);
+  const int Nv = std::stoi(h[0]), K = std::stoi(h[1]), Nmats = std::stoi(h[2]), Nbcs = std::stoi(h[3]);
+  if (std::stoi(h[4]) != 2) throw std::runtime_error("only 2D Gambit meshes are supported");
+  pos += 3;
+  m->vx.assign(Nv, 0.0);
+  m->vy.assign(Nv, 0.0);
+  for (int i = 0; i < Nv; ++i) {
+    auto t = L.tok(pos + i, 3);
+    const int ind = std::stoi(t[0]) - 1;
+    if (ind < 0 || ind >= Nv) throw std::runtime_error("vertex index out of range");
+    m->vx[ind] = std::stod(t[1]);
+    m->vy[ind] = std::stod(t[2]);
+  }
+  pos += Nv + 2;
+  m->etov.assign(static_cast<size_t>(K) * 3, 0);
+  for (int i = 0; i < K; ++i) {
+    auto t = L.tok(pos + i, 6);
+    const int k = std::stoi(t[0]) - 1;
+    if (k < 0 || k >= K) throw std::runtime_error("element index out of range");
+    for (int c = 0; c < 3; ++c) m->etov[3 * k + c] = std::stoi(t[3 + c]) - 1;
+  }
+  pos += K + 2;
+  for (int g = 0; g < Nmats; ++g) {
+    const std::string& ln = L.at(pos);
+    const auto at = ln.find("ELEMENTS:");
+    if (at == std::string::npos) throw std::runtime_error("malformed element group header");
+    const int nel = std::stoi(split_ws(ln.substr(at + 9)).at(0));
+    pos += 3 + (nel + 9) / 10 + 2;
+  }
+  for (int b = 0; b < Nbcs; ++b) {
+    if (b != 0) ++pos;
+    auto head = L.tok(pos, 3);
+    const std::string& tag = head[0];
+    std::string low;
+    for (char ch : tag) low.push_back(static_cast<char>(std::tolower(static_cast<unsigned char>(ch))));
+    const int nfaces = (low == "cyl" && head.size() > 3) ? std::stoi(head[3]) : std::stoi(head[2]);
+    ++pos;
+    for (int i = 0; i < nfaces; ++i) {
+      auto t = L.tok(pos + i, 3);
+      const int k = std::stoi(t[0]) - 1, face = std::stoi(t[2]);
+      if (k < 0 || k >= K || face < 1 || face > 3) throw std::runtime_error("boundary face out of range");
+      const int32_t* v = &m->etov[3 * k];
+      const int a = v[face - 1], c = v[face % 3];
+      add_bc(m, tag, a, c);
+    }
+    pos += nfaces + 1;
+  }
+}
+
+void read_su2(const Lines& raw, MeshFile* m) {
+  Lines L;
+  for (const auto& ln : raw.v) {
+    const auto b = ln.find_first_not_of(" \t\r");
+    if (b == std::string::npos || ln[b] == '%') continue;
+    const auto e = ln.find_last_not_of(" \t\r");
+    L.v.push_back(ln.substr(b, e - b + 1));
+  }
+  size_t pos = 0;
+  auto token = [&]() {
+    const std::string& ln = L.at(pos++);
+    const auto eq = ln.find('=');
+    if (eq == std::string::npos) throw std::runtime_error("badly formed input line [" + ln + "], should have an =");
+    auto v = ln.substr(eq + 1);
+    const auto b = v.find_first_not_of(" \t");
+    return b == std::string::npos ? std::string() : v.substr(b);
+  };
+  if (std::stoi(token()) != 2) throw std::runtime_error("only 2D SU2 meshes are supported");
+  const int K = std::stoi(token());
+  m->etov.assign(static_cast<size_t>(K) * 3, 0);
+  for (int k = 0; k < K; ++k) {
+    auto t = L.tok(pos + k, 4);
+    if (std::stoi(t[0]) != 5) throw std::runtime_error("unable to deal with non-triangular elements right now");
+    for (int c = 0; c < 3; ++c) m->etov[3 * k + c] = std::stoi(t[1 + c]);
+  }
+  pos += K;
+  const int Nv = std::stoi(token());
+  m->vx.assign(Nv, 0.0);
+  m->vy.assign(Nv, 0.0);
+  for (int i = 0; i < Nv; ++i) {
+    auto t = L.tok(pos + i, 2);
+    m->vx[i] = std::stod(t[0]);
+    m->vy[i] = std::stod(t[1]);
+  }
+  pos += Nv;
+  const int nmark = std::stoi(token());
+  for (int b = 0; b < nmark; ++b) {
+    const std::string tag = split_ws(token()).at(0);
+    const int ne = std::stoi(token());
+    for (int i = 0; i < ne; ++i) {
+      auto t = L.tok(pos + i, 3);
+      if (std::stoi(t[0]) != 3) throw std::runtime_error("BCs should only contain line elements in 2D");
+      add_bc(m, tag, std::stoi(t[1]), std::stoi(t[2]));
+    }
+    pos += ne;
+  }
+}
+
+bool ends_with(const std::string& s, const std::string& suf) {
+  return s.size() >= suf.size() && s.compare(s.size() - suf.size(), suf.size(), suf) == 0;
+}
+
+}  // namespace
+
+std::string read_mesh_file(const std::string& path, MeshFile* out) {
+  std::string p = path;
+  while (!p.empty() && std::isspace(static_cast<unsigned char>(p.back()))) p.pop_back();
+  const bool neu = ends_with(p, ".neu"), su2 = ends_with(p, ".su2");
+  if (!neu && !su2) return "unsupported file type: " + path;
+  std::ifstream f(p);
+  if (!f) return "cannot open " + p;
+  Lines L;
+  std::string ln;
+  while (std::getline(f, ln)) {
+    if (!ln.empty() && ln.back() == '\r') ln.pop_back();
+    L.v.push_back(ln);
+  }
+  MeshFile m;
+  try {
+    if (neu) read_gambit(L, &m);
+    else read_su2(L, &m);
+  } catch (const std::exception& e) {
+    return p + ": " + e.what();
+  }
+  const int Nv = static_cast<int>(m.vx.size());
+  for (int32_t v : m.etov)
+    if (v < 0 || v >= Nv) return p + ": element vertex out of range";
+  *out = std::move(m);
+  return std::string();
 }
 
 }  // namespace gcfd

@@ -57,4 +57,22 @@ std::string build_topology(int Nv, int K, const int32_t* etov, int nbc, const in
 void build_geometry(const DFRElement& el, const Topology& topo, const double* vx,
                     const double* vy, const int32_t* etov, Geometry* geo);
 
+// A mesh file's vertices, triangles (0-based) and boundary edges with their
+// BCFLAG, as the reference's readers produce them.
+struct MeshFile {
+  std::vector<double> vx, vy;
+  std::vector<int32_t> etov;  // K x 3
+  std::vector<int32_t> bc_v1, bc_v2, bc_flag;
+};
+
+// BC tag -> BCFLAG as types.BCNameMap (types/cfd.go:28-73): the part of the tag
+// before a '-' selects the flag; -1 for an unknown name.
+int bc_flag_of_tag(const std::string& tag);
+
+// Gambit neutral (readfiles/readGambitGrid.go:21-165,223-363) or SU2
+// (readfiles/readSU2Grid.go:27-177) 2D triangle mesh, chosen by the file
+// extension as getFileTypeFromExtension (DG2D/dfr_startup.go:184-204).
+// Returns an empty string on success, else the error.
+std::string read_mesh_file(const std::string& path, MeshFile* out);
+
 }  // namespace gcfd

@@ -91,6 +91,17 @@ typedef struct {
 
 typedef struct gcfd_ctx gcfd_ctx;
 
+/* Host-only (no GPU needed): reads a Gambit neutral (.neu) or SU2 (.su2) 2D
+ * triangle mesh with the reference's conventions (ReadGambit2d,
+ * readfiles/readGambitGrid.go:21-165,223-363; ReadSU2,
+ * readfiles/readSU2Grid.go:27-177; chosen by extension as
+ * getFileTypeFromExtension, DG2D/dfr_startup.go:184-204): 0-based triangles,
+ * boundary edges with the BCFLAG of their tag (types/cfd.go:28-73).  The arrays
+ * are owned by the library until gcfd_free_mesh.  Errors: GCFD_ERR_ARG with
+ * gcfd_last_error(NULL). */
+int gcfd_read_mesh(const char* path, gcfd_mesh* out);
+void gcfd_free_mesh(gcfd_mesh* mesh);
+
 /* Replaces Euler2D.NewEuler (model_problems/Euler2D/euler.go:61-136): builds
  * the DFR operators and FP64 geometry on the host, uploads them, sets the
  * initial condition (InitializeSolution, euler.go:728-794) on the device and

@@ -115,6 +115,33 @@ def test_mesh_readers_on_reference_fixtures():
         meshes.read_mesh("mesh.msh")
 
 
+@pytest.mark.parametrize("name", sorted(f for f in os.listdir(os.path.join(os.path.dirname(__file__), "fixtures"))
+                                        if f.endswith((".neu", ".su2"))))
+def test_native_mesh_reader_matches_python_reader(name):
+    """gcfd_read_mesh (C++) against the Python readers on every fixture mesh."""
+    m = meshes.read_mesh(fixture(name))
+    vx, vy, etov, bc = _lib.read_mesh(fixture(name))
+    assert np.array_equal(vx, m.VX) and np.array_equal(vy, m.VY)
+    assert np.array_equal(etov, m.EToV)
+    assert bc == [tuple(int(x) for x in e) for e in m.bc_edges]
+
+
+def test_native_mesh_reader_errors(tmp_path):
+    with pytest.raises(_lib.GcfdError):
+        _lib.read_mesh(str(tmp_path / "mesh.msh"))        # unsupported extension
+    with pytest.raises(_lib.GcfdError):
+        _lib.read_mesh(str(tmp_path / "missing.neu"))     # no such file
+    src = open(fixture("fstepA001.neu")).read()
+    bad = tmp_path / "badtag.neu"
+    bad.write_text(src.replace("Wall  ", "nosuchbc", 1))
+    with pytest.raises(_lib.GcfdError, match="nosuchbc"):
+        _lib.read_mesh(str(bad))
+    cut = tmp_path / "cut.neu"
+    cut.write_text("\n".join(src.splitlines()[:40]))       # truncated
+    with pytest.raises(_lib.GcfdError):
+        _lib.read_mesh(str(cut))
+
+
 def test_structured_mesh_is_ccw_and_roundtrips(tmp_path):
     m = meshes.vortex_box(6, jitter=0.1, seed=3)
     v = m.EToV
