@@ -1509,8 +1509,8 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
       flag[b] = t.bc[en];
       for (int q = 0; q < NE; ++q) {
         const size_t row = static_cast<size_t>(2 * Np + t.eL[en] * NE + q);
-        bx[static_cast<size_t>(b) * NE + q] = g.xFlux[row * K + t.kL[en]];
-        by[static_cast<size_t>(b) * NE + q] = g.yFlux[row * K + t.kL[en]];
+        element_point(m->etov, m->vx, m->vy, t.kL[en], c->el.rFlux[row], c->el.sFlux[row],
+                      &bx[static_cast<size_t>(b) * NE + q], &by[static_cast<size_t>(b) * NE + q]);
       }
     }
   }

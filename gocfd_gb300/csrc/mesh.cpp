@@ -118,21 +118,15 @@ void build_geometry(const DFRElement& el, const Topology& t, const double* vx, c
     g->edgeLenMax[k] = g->Jdet[k] / mx;
     g->hK[k] = g->edgeLenMax[k] / np12;
   }
-  auto local = [&](const std::vector<double>& R, const std::vector<double>& S,
-                   std::vector<double>* X, std::vector<double>* Y) {
-    const int n = static_cast<int>(R.size());
-    X->assign(static_cast<size_t>(n) * K, 0.0);
-    Y->assign(static_cast<size_t>(n) * K, 0.0);
-    for (int i = 0; i < n; ++i)
-      for (int k = 0; k < K; ++k) {
-        const int va = etov[3 * k], vb = etov[3 * k + 1], vc = etov[3 * k + 2];
-        const double a = -(R[i] + S[i]), b = R[i] + 1.0, c = S[i] + 1.0;
-        (*X)[static_cast<size_t>(i) * K + k] = 0.5 * (a * vx[va] + b * vx[vb] + c * vx[vc]);
-        (*Y)[static_cast<size_t>(i) * K + k] = 0.5 * (a * vy[va] + b * vy[vb] + c * vy[vc]);
-      }
-  };
-  local(el.rFlux, el.sFlux, &g->xFlux, &g->yFlux);
-  local(el.r, el.s, &g->xSol, &g->ySol);
+  // Solution-point coordinates (the flux points' are computed where needed, at
+  // boundary edges: element_point).
+  const int n = static_cast<int>(el.r.size());
+  g->xSol.assign(static_cast<size_t>(n) * K, 0.0);
+  g->ySol.assign(static_cast<size_t>(n) * K, 0.0);
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < K; ++k)
+      element_point(etov, vx, vy, k, el.r[i], el.s[i], &g->xSol[static_cast<size_t>(i) * K + k],
+                    &g->ySol[static_cast<size_t>(i) * K + k]);
 }
 
 // ---------------------------------------------------------------------------

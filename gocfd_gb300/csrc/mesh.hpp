@@ -46,7 +46,6 @@ struct Geometry {
   std::vector<double> J, Jinv, Jdet;    // K*4 [xr xs yr ys], K*4 [ys -xs -yr xr]/|J|, K
   std::vector<double> nx, ny, IInII;    // 3*K, index e*K + k (outward unit normal, ||n||)
   std::vector<double> edgeLenMax, hK;   // K
-  std::vector<double> xFlux, yFlux;     // NpFlux*K, row-major (point, element)
   std::vector<double> xSol, ySol;       // Np*K
 };
 
@@ -56,6 +55,16 @@ std::string build_topology(int Nv, int K, const int32_t* etov, int nbc, const in
 
 void build_geometry(const DFRElement& el, const Topology& topo, const double* vx,
                     const double* vy, const int32_t* etov, Geometry* geo);
+
+// Physical coordinates of the reference point (r, s) of element k
+// (CalculateElementLocalGeometry, element_utils.go:163-175).
+inline void element_point(const int32_t* etov, const double* vx, const double* vy, int k, double r, double s,
+                          double* x, double* y) {
+  const int va = etov[3 * k], vb = etov[3 * k + 1], vc = etov[3 * k + 2];
+  const double a = -(r + s), b = r + 1.0, c = s + 1.0;
+  *x = 0.5 * (a * vx[va] + b * vx[vb] + c * vx[vc]);
+  *y = 0.5 * (a * vy[va] + b * vy[vb] + c * vy[vc]);
+}
 
 // A mesh file's vertices, triangles (0-based) and boundary edges with their
 // BCFLAG, as the reference's readers produce them.
