@@ -1,7 +1,8 @@
 // Mixed-precision ("delta form") DFR right-hand side and SSP(5,4) step.
 //
 // Arithmetic: every element carries a reference state Qb = the stage state at
-// its solution point 0 (FP64).  The RT divergence of a constant flux is zero
+// its solution point 0 (a compensated FP32 pair).  The RT divergence of a
+// constant flux is zero
 // (DivInt * dofs(const) = 0), so the RHS is computed from
 //     dF = F(Q) - F(Qb)          at the interior points, and
 //     fhat - n.F(Qb)             at the edge points,
@@ -30,7 +31,8 @@
 //                         edge kernels
 // Element kernels run one thread per (element, variable): a block is 32
 // elements x 4 variables, warp w owns variable w, so every row access is a
-// 128-byte coalesced transaction.
+// 128-byte coalesced transaction.  The operators (DivInt^T, FluxEdgeInterp^T)
+// are constant-memory arrays per order N, read as immediate operands.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
