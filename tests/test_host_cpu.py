@@ -126,6 +126,27 @@ def test_native_mesh_reader_matches_python_reader(name):
     assert bc == [tuple(int(x) for x in e) for e in m.bc_edges]
 
 
+def test_native_mesh_reader_written_meshes(tmp_path):
+    """Gambit files written for the benchmark meshes (all BC groups, several
+    hundred elements) and an SU2 file with dashed marker tags read the same in
+    C++ and Python."""
+    for name, mesh in (("sod.neu", meshes.sod_channel(20, 3)), ("wedge.neu", meshes.wedge_channel(12, 6))):
+        path = str(tmp_path / name)
+        meshes.write_gambit(mesh, path)
+        m = meshes.read_mesh(path)
+        vx, vy, etov, bc = _lib.read_mesh(path)
+        assert np.array_equal(vx, m.VX) and np.array_equal(vy, m.VY) and np.array_equal(etov, m.EToV)
+        assert bc == [tuple(int(x) for x in e) for e in m.bc_edges] and len(bc) == len(mesh.bc_edges)
+    su2 = tmp_path / "tags.su2"
+    su2.write_text("% comment\nNDIME= 2\nNELEM= 2\n5 0 1 2 0\n5 0 2 3 1\nNPOIN= 4\n0 0 0\n1 0 1\n1 1 2\n"
+                   "0 1 3\nNMARK= 2\nMARKER_TAG= far-upstream\nMARKER_ELEMS= 2\n3 0 1\n3 1 2\n"
+                   "MARKER_TAG= Wall-top\nMARKER_ELEMS= 2\n3 2 3\n3 3 0\n")
+    vx, vy, etov, bc = _lib.read_mesh(str(su2))
+    m = meshes.read_mesh(str(su2))
+    assert np.array_equal(etov, m.EToV) and bc == [tuple(int(x) for x in e) for e in m.bc_edges]
+    assert [f for (_, _, f) in bc] == [4, 4, 5, 5]
+
+
 def test_native_mesh_reader_errors(tmp_path):
     with pytest.raises(_lib.GcfdError):
         _lib.read_mesh(str(tmp_path / "mesh.msh"))        # unsupported extension
