@@ -145,13 +145,16 @@ def sod_density_error(solver: Euler, t: float):
 
 
 def run(name: str, precision: str = "fp64", scale: float = 1.0, device: int = 0, max_steps: int = 0,
-        report_every: int = 0):
+        report_every: int = 0, stage_pipeline: bool = False):
     cfg = CONFIGS[name]
     mesh = build_mesh(cfg, scale)
     ip = input_params(cfg)
     center = (0.0, 0.0) if cfg.mesh == "vortex" else (5.0, 0.0)
     out = {"config": name, "desc": cfg.desc, "scale": scale, "precision": precision}
     with Euler(ip, mesh, 1, precision=precision, device=device, vortex_center=center) as s:
+        if stage_pipeline:
+            s.set_stage_pipeline(True)
+            out["stage_pipeline"] = s.stage_pipeline()
         out["K"] = s.K
         t0 = time.perf_counter()
         if cfg.mesh == "vortex":
@@ -294,6 +297,8 @@ def main(argv=None):
     p.add_argument("--scale", type=float, default=1.0)
     p.add_argument("--max-steps", type=int, default=0)
     p.add_argument("--report-every", type=int, default=0)
+    p.add_argument("--stage-pipeline", action="store_true",
+                   help="mixed path: the persistent TMA-pipelined stage kernel instead of the one-block kernel")
     p.add_argument("--adjoint-steps", type=int, default=0,
                    help="vortex configs: run the field-error adjoint through this many steps instead")
     p.add_argument("--checkpoint-every", type=int, default=10)
@@ -306,7 +311,8 @@ def main(argv=None):
         res = adjoint(a.config, a.adjoint_steps, a.checkpoint_every, a.warm_steps,
                       a.precision if a.precision != "fp64" else "fp32", fd_h=a.fd_h)
     else:
-        res = run(a.config, a.precision, a.scale, max_steps=a.max_steps, report_every=a.report_every)
+        res = run(a.config, a.precision, a.scale, max_steps=a.max_steps, report_every=a.report_every,
+                  stage_pipeline=a.stage_pipeline)
     print(json.dumps(res), flush=True)
 
 
