@@ -20,6 +20,13 @@ def fixture(name: str) -> str:
     return os.path.join(FIXTURES, name)
 
 
+def golden(name: str) -> dict:
+    """A known answer of the reference's own tests (tests/golden/reference_known_answers.json)."""
+    import json
+    with open(os.path.join(ROOT, "tests", "golden", "reference_known_answers.json")) as f:
+        return json.load(f)[name]
+
+
 @pytest.fixture(scope="session")
 def has_gpu():
     import torch

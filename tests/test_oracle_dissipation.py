@@ -7,7 +7,7 @@
 import numpy as np
 import pytest
 
-from conftest import fixture
+from conftest import fixture, golden
 import oracle
 from gocfd_gb300 import meshes
 
@@ -26,8 +26,7 @@ def test_shock_finder_pattern(N):
     rho = np.where(x < 0.0, U1[0], U2[0])
     threshold = 0.0075  # ShockSigmaThreshold (dfr_shock_capturing.go:83)
     shocked = [s.shock_indicator(rho[:, k], 3.0) > threshold for k in range(s.K)]
-    F, T = False, True
-    assert shocked == [F, F, T, T, F, F, F, T, T, F]
+    assert shocked == golden("shock_finder_pattern")["pattern"]
 
 
 def test_element_areas_tris_9():

@@ -14,7 +14,7 @@ import math
 import numpy as np
 import pytest
 
-from conftest import fixture
+from conftest import fixture, golden
 import dfr_ops
 import oracle
 from gocfd_gb300 import meshes
@@ -96,24 +96,26 @@ def test_fluid_functions_mach2():
     p = 0.4 * (q[3] - 0.5 * rho * (u * u + v * v))
     c = math.sqrt(abs(1.4 * p / rho))
     vals = [q[0], q[1], q[2], q[3], math.hypot(u, v) / c, p]
-    assert np.allclose(vals, [1, 2, 0, 3.78571, 2, 0.71429], atol=1e-5)
+    g = golden("fluid_functions_mach2")
+    assert np.allclose(vals, g["values"], atol=g["atol"])
 
 
 def test_ivortex_exact_state():
     vortex = (5.0, 5.0, 0.0, 1.4)
     q = oracle.ivortex_state(vortex, 0.0, np.array([5.0]), np.array([0.0]))[:, 0]
-    assert np.allclose(q, [0.361673, 0.361673, 0.0, 0.782817], atol=1e-5)
+    g = golden("ivortex_state_at_5_0")
+    assert np.allclose(q, g["q"], atol=g["atol"])
     rho, rhoU, rhoV, E = q
     u, v = rhoU / rho, rhoV / rho
     p = 0.4 * (E - 0.5 * rho * (u * u + v * v))
     Fx = [rhoU, rhoU * u + p, rhoU * v, u * (E + p)]
     Fy = [rhoV, rhoV * u, rhoV * v + p, v * (E + p)]
-    assert np.allclose(Fx, [0.361673, 0.602465, 0.0, 1.023609], atol=1e-5)
-    assert np.allclose(Fy, [0.0, 0.0, 0.240792, 0.0], atol=1e-5)
+    assert np.allclose(Fx, g["Fx"], atol=g["atol"])
+    assert np.allclose(Fy, g["Fy"], atol=g["atol"])
     # divergence of the y-momentum flux at the centre: d(rho v)/dx (complex step)
     h = 1e-30
     qx = oracle.ivortex_state(vortex, 0.0, np.array([5.0 + 1j * h]), np.array([0.0 + 0j]))
-    assert abs(qx[2, 0].imag / h - 0.782349) < 1e-5
+    assert abs(qx[2, 0].imag / h - g["drhov_dx"]) < g["atol"]
 
 
 def equilateral_triangle(angle_deg):
