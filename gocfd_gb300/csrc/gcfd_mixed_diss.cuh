@@ -69,29 +69,6 @@ __device__ __forceinline__ void limit_filter_modal_c(float u[Dims<N>::NP], float
   }
 }
 
-// limit_filter_modal in FP32.
-template <int NP>
-__device__ __forceinline__ void limit_filter_modal_f(float u[NP], const float* sV, const float* sVi,
-                                                     const float* mf, float alpha) {
-  float m[NP];
-#pragma unroll
-  for (int i = 0; i < NP; ++i) {
-    float acc = 0.0f;
-#pragma unroll
-    for (int j = 0; j < NP; ++j) acc = fmaf(sVi[i * NP + j], u[j], acc);
-    m[i] = acc;
-  }
-#pragma unroll
-  for (int i = 1; i < NP; ++i) m[i] *= mf[i] * (1.0f - alpha);
-#pragma unroll
-  for (int i = 0; i < NP; ++i) {
-    float acc = 0.0f;
-#pragma unroll
-    for (int j = 0; j < NP; ++j) acc = fmaf(sV[i * NP + j], m[j], acc);
-    u[i] = acc;
-  }
-}
-
 // The stage-s deltas of variable n of element k relative to its stage state
 // at solution point 0: dQ0 + (D_s - D_s(point 0)), as the stage kernel forms
 // them (stage <= 0: dQ0).
@@ -345,7 +322,7 @@ __global__ void __launch_bounds__(128) k_diss_edge_mixed(DissArgs a) {
 template <int N>
 __global__ void __launch_bounds__(128, N >= 4 ? 3 : 5) k_mixed_diss_update(MixedArgs a, UpdateArgs<double> u) {
   constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NE3 = MixedDims<N>::NE3;
-  constexpr int NF = MixedDims<N>::NF, NR = NP + NE3;
+  constexpr int NR = NP + NE3;
   __shared__ double sdt;
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = blockIdx.x * 32 + lane;
