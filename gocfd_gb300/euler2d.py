@@ -35,6 +35,8 @@ PRECISIONS = {"fp64": 0, "fp32": 1, "tf32x3": 2}
 
 @dataclass
 class InputParameters2D:
+    """The reference's InputParameters2D (model_problems/Euler2D/input_parameters.go)
+    with its field names and defaults; `parse` / `from_file` read its YAML inputs."""
     Title: str = ""
     CFL: float = 0.0
     FluxType: str = ""
@@ -85,6 +87,7 @@ class InputParameters2D:
 
     @classmethod
     def from_file(cls, path: str) -> "InputParameters2D":
+        """Parse a reference input file (test_cases/Euler2D/*/input*.yaml)."""
         with open(path) as f:
             return cls.parse(f.read())
 
@@ -99,6 +102,7 @@ class PartitionMap:
         self.Partitions = [self.split1d(n) for n in range(parallel_degree)]
 
     def split1d(self, n: int):
+        """Half-open item range of bucket n (PartitionMap.Split1D, utils/parallel_utils.go:172-192)."""
         npart = self.MaxIndex // self.ParallelDegree
         rem = self.MaxIndex % self.ParallelDegree
         start_add, end_add = 0, 0
@@ -111,11 +115,14 @@ class PartitionMap:
         return (b0, b0 + npart + end_add)
 
     def bucket_dimension(self, n: int) -> int:
+        """Number of items in bucket n (GetBucketDimension)."""
         a, b = self.Partitions[n]
         return b - a
 
 
 def set_parallel_degree(proc_limit: int, K: int) -> PartitionMap:
+    """The shard count of Euler.SetParallelDegree (model_problems/Euler2D/parallelism.go:109-114):
+    the process limit if given, else max(NumCPU, K / 185), and 1 when that exceeds K."""
     if proc_limit != 0:
         pd = proc_limit
     else:
@@ -181,6 +188,7 @@ class Euler:
 
     # -- lifetime --------------------------------------------------------------
     def close(self):
+        """Release the device context (gcfd_destroy); idempotent."""
         if getattr(self, "ctx", None):
             self.lib.gcfd_destroy(self.ctx)
             self.ctx = None
@@ -213,10 +221,12 @@ class Euler:
         return arr
 
     def new_sharded(self):
+        """Zeroed shards shaped like the reference's c.Q: per shard, 4 Np x Kmax matrices."""
         return [[np.zeros((self.Np, k)) for _ in range(4)] for k in self._kmax()]
 
     @property
     def Q(self):
+        """The sharded state (c.Q of euler.go:47), copied from the device (gcfd_get_state)."""
         out = self.new_sharded()
         km = self._kmax()
         _lib.check(self.lib, self.ctx, self.lib.gcfd_get_state(self.ctx, len(km), km.ctypes.data_as(_lib.PI),
@@ -225,6 +235,7 @@ class Euler:
 
     @Q.setter
     def Q(self, shards):
+        """Copy a sharded state to the device (gcfd_set_state)."""
         km = self._kmax()
         _lib.check(self.lib, self.ctx, self.lib.gcfd_set_state(self.ctx, len(km), km.ctypes.data_as(_lib.PI),
                                                               self._ptrs(shards)))
@@ -237,27 +248,34 @@ class Euler:
         return out
 
     def unshard(self, shards) -> np.ndarray:
+        """Join the reference's shards into one 4 x Np x K array."""
         return np.stack([np.concatenate([sh[n] for sh in shards], axis=1) for n in range(4)])
 
     def get_global_state(self) -> np.ndarray:
+        """The state as one 4 x Np x K array."""
         return self.unshard(self.Q)
 
     def set_global_state(self, Qg: np.ndarray):
+        """Set the state from one 4 x Np x K array."""
         self.Q = self.shard(np.asarray(Qg, dtype=np.float64))
 
     # -- time ------------------------------------------------------------------------
     @property
     def time(self) -> float:
+        """Solver time (RungeKutta5SSP.Time)."""
         t, s = C.c_double(), C.c_int32()
         _lib.check(self.lib, self.ctx, self.lib.gcfd_get_time(self.ctx, C.byref(t), C.byref(s)))
         return t.value
 
     @time.setter
     def time(self, t: float):
+        """Set the solver time (the BC time of the next step)."""
         _lib.check(self.lib, self.ctx, self.lib.gcfd_set_time(self.ctx, float(t)))
 
     # -- the hot path ------------------------------------------------------------------
     def rhs(self, shards, time: float = 0.0):
+        """One RHS evaluation of a sharded state at BC time `time` (gcfd_rhs: the chain
+        SetRTFluxInternal .. RHSInternalPoints, euler.go:665-726, edges.go:325-488)."""
         out = self.new_sharded()
         km = self._kmax()
         _lib.check(self.lib, self.ctx, self.lib.gcfd_rhs(self.ctx, float(time), len(km), km.ctypes.data_as(_lib.PI),
@@ -265,6 +283,7 @@ class Euler:
         return out
 
     def rhs_global(self, Qg: np.ndarray, time: float = 0.0) -> np.ndarray:
+        """rhs() on a 4 x Np x K array."""
         return self.unshard(self.rhs(self.shard(np.asarray(Qg, dtype=np.float64)), time))
 
     # -- adjoint (FP64 path) --------------------------------------------------------------
@@ -326,6 +345,7 @@ class Euler:
         self.steps += nsteps
 
     def check_if_finished(self, time: float, steps: int) -> bool:
+        """Solve's stopping test (euler.go:796-801): FinalTime reached or MaxIterations steps done."""
         return time >= self.ip.FinalTime or steps >= self.ip.MaxIterations
 
     def solve(self, print_every: int = 100, printer=print):
@@ -349,11 +369,14 @@ class Euler:
         return info
 
     def profile_step(self):
+        """One eagerly launched step with CUDA events around each kernel family (gcfd_profile_step):
+        ([ms] x 4, [launches] x 4) for preparation/interpolation, edge fluxes, stage update, bookkeeping."""
         ms, n = (C.c_double * 4)(), (C.c_int32 * 4)()
         _lib.check(self.lib, self.ctx, self.lib.gcfd_profile_step(self.ctx, ms, n))
         return list(ms), list(n)
 
     def stream_handle(self) -> int:
+        """The context's CUDA stream (cudaStream_t) as an integer, for torch.cuda.ExternalStream."""
         s = C.c_void_p()
         _lib.check(self.lib, self.ctx, self.lib.gcfd_get_stream(self.ctx, C.byref(s)))
         return s.value or 0
@@ -362,7 +385,7 @@ class Euler:
     OPT_STAGE_PIPELINE = 1
 
     def set_stage_pipeline(self, on: bool) -> None:
-        """Select the persistent TMA-pipelined stage kernel (default) or the one-block kernel."""
+        """Select the persistent TMA-pipelined stage kernel (True) or the one-block kernel (False, the default)."""
         _lib.check(self.lib, self.ctx, self.lib.gcfd_set_option(self.ctx, self.OPT_STAGE_PIPELINE, int(bool(on))))
 
     def stage_pipeline(self) -> bool:
@@ -373,5 +396,6 @@ class Euler:
 
 
 def parse_yaml_file(path: str) -> InputParameters2D:
+    """The reference's input-file reader (InputParameters2D.Parse of a YAML file)."""
     return InputParameters2D.from_file(path)
 
