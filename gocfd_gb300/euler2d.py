@@ -35,7 +35,7 @@ PRECISIONS = {"fp64": 0, "fp32": 1, "tf32x3": 2}
 
 @dataclass
 class InputParameters2D:
-    """The reference's InputParameters2D (model_problems/Euler2D/input_parameters.go)
+    """The reference's InputParameters2D (InputParameters/InputParameters.go:11)
     with its field names and defaults; `parse` / `from_file` read its YAML inputs."""
     Title: str = ""
     CFL: float = 0.0
@@ -115,13 +115,13 @@ class PartitionMap:
         return (b0, b0 + npart + end_add)
 
     def bucket_dimension(self, n: int) -> int:
-        """Number of items in bucket n (GetBucketDimension)."""
+        """Number of items in bucket n (GetBucketDimension, utils/parallel_utils.go:160)."""
         a, b = self.Partitions[n]
         return b - a
 
 
 def set_parallel_degree(proc_limit: int, K: int) -> PartitionMap:
-    """The shard count of Euler.SetParallelDegree (model_problems/Euler2D/parallelism.go:109-114):
+    """The shard count of Euler.SetParallelDegree (model_problems/Euler2D/parallelism.go:100-114):
     the process limit if given, else max(NumCPU, K / 185), and 1 when that exceeds K."""
     if proc_limit != 0:
         pd = proc_limit
