@@ -62,6 +62,10 @@ def args_parse():
     p.add_argument("--accuracy", type=int, default=0,
                    help="instead of timing: run this many steps in FP64 and FP32 and report the "
                         "relative L2 differences and the errors against the exact vortex")
+    p.add_argument("--acc-steps", type=int, default=1000,
+                   help="after the timed region: steps of the accuracy leg on vortex256 (0: skip)")
+    p.add_argument("--acc-steps-large", type=int, default=100,
+                   help="after the timed region: steps of the accuracy leg on the benchmarked workload (0: skip)")
     return p.parse_args()
 
 
@@ -75,6 +79,15 @@ def dist_env():
 def make_mesh(wl):
     from gocfd_gb300 import meshes
     return meshes.vortex_box(wl["n"], jitter=wl["jitter"], seed=wl["seed"])
+
+
+def workload_config(name, K, Np):
+    """The workload description both arms print (the same dict, key for key)."""
+    wl = WORKLOADS[name]
+    return {"workload": name, "description": wl["desc"], "K": K, "N": wl["N"], "Np": Np,
+            "dof_updates_per_step": K * Np * 4 * 5, "flux": "roe", "cfl": 1.0,
+            "l2": "state of %.3g GB per FP64 copy against a 129 MB L2; the GPU arm also writes 256 MB "
+                  "between timed steps" % (K * Np * 4 * 8 / 1e9)}
 
 
 def input_params(N, final_time=1e9):
@@ -224,6 +237,7 @@ def cpu_baseline(wl, mesh, seconds, steps=None, warmup=0, max_steps=200):
     el = time.perf_counter() - t0
     dof = ora.K * ora.el.Np * 4 * 5
     return dict(value=dof * done / el, unit=UNIT, cores=threads, kind="port", steps=done, seconds=el,
+                K=ora.K, Np=ora.el.Np,
                 sample=f"{done} full SSP-RK steps of the same {ora.K}-element N={wl['N']} workload")
 
 
@@ -366,9 +380,11 @@ def run_ours(a, world, rank, local):
                 "ms_per_step": ms64 / a.fp64_steps, "steps": a.fp64_steps}
         s64.close()
 
-    # Adjoint cost: the reverse sweep of a recorded FP64 window (checkpoint every
-    # step: each reverse step recomputes its forward step once with the stage
-    # tape, then runs the stage adjoints) against the FP64 forward step.
+    # Adjoint cost: the reverse sweep of a recorded FP64 window against the
+    # FP64 forward step.  With a checkpoint every 10 steps (what the vortex1024
+    # adjoint runs) each segment is recomputed once with its per-step tape kept,
+    # then reversed; with a checkpoint every step each reverse step recomputes
+    # its forward step once with the tape.
     adjoint = None
     if a.adj_steps > 0:
         sa = Euler(ip, mesh, 1, precision="fp64", device=local, vortex_center=(0.0, 0.0))
@@ -383,23 +399,29 @@ def run_ours(a, world, rank, local):
         torch.cuda.synchronize()
         fwd_ms = f0.elapsed_time(f1) / a.adj_steps
         qbar = np.ones((4, Np, K))
-        sa.record(2, 1)
-        sa.step_vjp(qbar)  # warm-up (allocations, first launches)
+        legs = {}
+        for every in (10, 1):
+            sa.record(2 * every if every > 1 else 2, every)
+            sa.step_vjp(qbar)  # warm-up (allocations, first launches)
 
-        def sweep(n):
-            sa.record(n, 1)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            sa.step_vjp(qbar)
-            return (time.perf_counter() - t0) * 1e3
-        n1, n2 = max(1, a.adj_steps // 2), a.adj_steps + max(1, a.adj_steps // 2)
-        t1, t2 = sweep(n1), sweep(n2)
-        adj_ms = (t2 - t1) / (n2 - n1)  # per reverse step, without the window's fixed costs
-        adjoint = {"ms_per_step": adj_ms, "forward_ms_per_step": fwd_ms, "ratio": adj_ms / fwd_ms,
-                   "window_ms": {str(n1): t1, str(n2): t2}, "checkpoint_every": 1, "path": "fp64",
-                   "timing": "host clock around gcfd_step_vjp (synchronous) for two window lengths; per-step "
-                             "cost = difference / difference in steps (the adjoint's host transfer and set-up "
-                             "are per window); forward by CUDA events"}
+            def sweep(n):
+                sa.record(n, every)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                sa.step_vjp(qbar)
+                return (time.perf_counter() - t0) * 1e3
+            n1 = max(every, a.adj_steps // 2)
+            n2 = n1 + max(every, a.adj_steps)
+            n1, n2 = every * ((n1 + every - 1) // every), every * ((n2 + every - 1) // every)
+            t1, t2 = sweep(n1), sweep(n2)
+            adj_ms = (t2 - t1) / (n2 - n1)  # per reverse step, without the window's fixed costs
+            legs[every] = {"ms_per_step": adj_ms, "ratio": adj_ms / fwd_ms, "window_ms": {str(n1): t1, str(n2): t2}}
+        adjoint = {"ms_per_step": legs[10]["ms_per_step"], "forward_ms_per_step": fwd_ms,
+                   "ratio": legs[10]["ratio"], "checkpoint_every": 10, "path": "fp64",
+                   "window_ms": legs[10]["window_ms"], "checkpoint_every_1": legs[1],
+                   "timing": "host clock around gcfd_step_vjp (synchronous) for two window lengths; per-step cost = "
+                             "difference / difference in steps (the adjoint's host transfer and set-up are per "
+                             "window); forward by CUDA events"}
         sa.close()
 
     # End to end through the public API: pinned host state in, step, state out.
@@ -428,10 +450,29 @@ def run_ours(a, world, rank, local):
            "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes,
            "steps": a.e2e_steps, "api": "gcfd_set_state + gcfd_step + gcfd_get_state, pinned host shards"}
 
+    # Accuracy (the "at equal L2 error" half of the metric): the mixed paths
+    # against the FP64 path and both against the exact vortex, after the timed region.
+    accuracy = None
+    if rank == 0 and a.precision != "fp64":
+        solver.close()
+        solver = None
+        accuracy = {}
+        if a.acc_steps > 0:
+            accuracy["vortex256"] = accuracy_leg("vortex256", a.acc_steps, local, ("fp64", "fp32", "tf32x3"))
+        if a.acc_steps_large > 0 and a.workload != "vortex256":
+            accuracy[a.workload] = accuracy_leg(a.workload, a.acc_steps_large, local, ("fp64", a.precision))
+        m = accuracy.get("vortex256") or accuracy.get(a.workload)
+        if m:
+            accuracy["mixed_vs_fp64_rel_l2"] = m.get(f"{a.precision}_vs_fp64_rel_l2")
+            accuracy["mixed_vs_fp64_rel_linf"] = m.get(f"{a.precision}_vs_fp64_rel_linf")
+            accuracy["mixed_vs_fp64_steps"] = m["steps"]
+            accuracy["mixed_vs_fp64_workload"] = m["workload"]
+
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
         cpu = cpu_baseline(wl, mesh, a.cpu_seconds)
-    solver.close()
+    if solver is not None:
+        solver.close()
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
@@ -439,10 +480,10 @@ def run_ours(a, world, rank, local):
             "vs_baseline": None, "dtype": {"fp64": "fp64", "fp32": "fp32 (compensated fp32 state)",
                                                   "tf32x3": "3xtf32 tensor-core GEMM, fp32 elsewhere (compensated fp32 state)"}[a.precision],
             "data": "synthetic (analytic isentropic-vortex initial condition on a generated mesh)",
-            "config": {"workload": a.workload, "description": wl["desc"], "K": K, "N": wl["N"], "Np": Np,
-                       "dof_updates_per_step": dof_per_step, "flux": "roe", "cfl": 1.0,
-                       "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (256 MB write)",
-                       "timing": "CUDA events per graph-launched step on the solver stream"},
+            "config": workload_config(a.workload, K, Np),
+            "parallelism": f"replicas x{world}",
+            "timing": "CUDA events per graph-launched step on the solver stream",
+            "accuracy": accuracy,
             "e2e": e2e,
             "gpu_launches": launches_per_step * a.steps,
             "clocks": clk,
@@ -461,31 +502,40 @@ def run_ours(a, world, rank, local):
         dist.destroy_process_group()
 
 
-def run_accuracy(a, local):
-    import torch
+def accuracy_leg(workload, steps, local, precisions):
+    """Run `steps` steps of `workload` in each arithmetic and report the errors
+    against the exact vortex and the mixed paths' differences from FP64."""
     from gocfd_gb300.configs import exact_vortex_error
     from gocfd_gb300.euler2d import Euler
-    torch.cuda.set_device(local)
-    wl = WORKLOADS[a.workload]
+    wl = WORKLOADS[workload]
     mesh = make_mesh(wl)
     ip = input_params(wl["N"])
-    res = {"workload": a.workload, "steps": a.accuracy}
+    res = {"workload": workload, "steps": steps}
     states = {}
-    for prec in ("fp64", "fp32", "tf32x3"):
+    for prec in precisions:
         s = Euler(ip, mesh, 1, precision=prec, device=local, vortex_center=(0.0, 0.0))
-        info = s.step(a.accuracy)
+        info = s.step(steps)
         states[prec] = s.get_global_state()
         l2, linf = exact_vortex_error(s, info["time"])
-        res[prec] = {"time": info["time"], "rel_l2_vs_exact": l2, "rel_linf_vs_exact": linf,
-                     "resid_rms": info["resid_rms"]}
+        res[prec] = {"time": info["time"], "rel_l2_vs_exact": l2, "rel_linf_vs_exact": linf}
         s.close()
-    for prec in ("fp32", "tf32x3"):
-        d = states[prec] - states["fp64"]
-        res[f"{prec}_vs_fp64_rel_l2"] = float(np.linalg.norm(d) / np.linalg.norm(states["fp64"]))
-        res[f"{prec}_vs_fp64_rel_linf"] = float(np.abs(d).max() / np.abs(states["fp64"]).max())
-        res[f"{prec}_vs_fp64_rel_l2_per_var"] = [float(np.linalg.norm(d[n]) / np.linalg.norm(states["fp64"][n]))
+    ref = states["fp64"]
+    nref = np.linalg.norm(ref)
+    for prec in precisions:
+        if prec == "fp64":
+            continue
+        d = states[prec] - ref
+        res[f"{prec}_vs_fp64_rel_l2"] = float(np.linalg.norm(d) / nref)
+        res[f"{prec}_vs_fp64_rel_linf"] = float(np.abs(d).max() / np.abs(ref).max())
+        res[f"{prec}_vs_fp64_rel_l2_per_var"] = [float(np.linalg.norm(d[n]) / np.linalg.norm(ref[n]))
                                                 for n in range(4)]
-    print(json.dumps(res), flush=True)
+    return res
+
+
+def run_accuracy(a, local):
+    import torch
+    torch.cuda.set_device(local)
+    print(json.dumps(accuracy_leg(a.workload, a.accuracy, local, ("fp64", "fp32", "tf32x3"))), flush=True)
 
 
 def run_reference(a, world, rank):
@@ -502,8 +552,8 @@ def run_reference(a, world, rank):
            "steps": r["steps"], "warmup": min(a.warmup, 1), "ms_per_step": 1e3 * r["seconds"] / r["steps"],
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
            "data": "synthetic (analytic isentropic-vortex initial condition on a generated mesh)",
-           "config": {"workload": a.workload, "description": wl["desc"], "N": wl["N"], "flux": "roe",
-                      "cfl": 1.0, "parallelism": "OpenMP over host cores"},
+           "config": workload_config(a.workload, r["K"], r["Np"]),
+           "parallelism": "OpenMP over host cores",
            "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": "port",
                             "sample": r["sample"]},
            "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -32,7 +32,7 @@ EXPORTS = [
     "gcfd_get_time", "gcfd_rhs", "gcfd_step", "gcfd_enqueue_steps", "gcfd_get_stream", "gcfd_set_option",
     "gcfd_get_option", "gcfd_profile_step",
     "gcfd_host_operator", "gcfd_read_mesh", "gcfd_free_mesh", "gcfd_residual_norms_static", "gcfd_functional", "gcfd_rhs_vjp",
-    "gcfd_record_steps", "gcfd_step_vjp",
+    "gcfd_record_steps", "gcfd_step_vjp", "gcfd_sample_points", "gcfd_wall_points",
 ]
 
 
@@ -109,6 +109,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
                                      C.POINTER(PD), PD, PD]
         lib.gcfd_record_steps.argtypes = [C.c_void_p, C.c_int32, C.c_int32, PD, PD]
         lib.gcfd_step_vjp.argtypes = [C.c_void_p, C.c_int32, PI, C.POINTER(PD), C.c_double, C.POINTER(PD), PD, PD]
+        lib.gcfd_sample_points.argtypes = [C.c_void_p, C.c_int32, PD, PD, PD, PI]
+        lib.gcfd_wall_points.argtypes = [C.c_void_p, PI, PD, PD, PD, PD]
         _lib = lib
         return lib
 

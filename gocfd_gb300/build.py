@@ -2,7 +2,10 @@
 
 Each translation unit is compiled in parallel with nvcc, then linked into
 ``gocfd_gb300/libgcfd.so`` (CUDA runtime linked statically so the library
-loads without an rpath).  No cmake, no torch extension machinery.
+loads without an rpath).  The kernels of each polynomial order N = 0..4 sit in
+their own units (``gcfd_order.cu`` and ``gcfd_order_adj.cu`` compiled with
+-DGCFD_ORDER=N), so the build runs as wide as the host has cores.  No cmake,
+no torch extension machinery.
 """
 from __future__ import annotations
 
@@ -17,7 +20,11 @@ CSRC = os.path.join(PKG_DIR, "csrc")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libgcfd.so")
 
-SOURCES = ["gcfd.cu", "dfr_element.cpp", "mesh.cpp"]
+# (source, extra defines): the per-order units once per order, largest first.
+SOURCES = ([("gcfd_order.cu", [f"-DGCFD_ORDER={n}"]) for n in (4, 3, 2, 1, 0)] +
+           [("gcfd_order_adj.cu", [f"-DGCFD_ORDER={n}"]) for n in (4, 3, 2, 1, 0)] +
+           [("gcfd.cu", []), ("gcfd_adjoint_api.cu", []), ("gcfd_static.cu", []), ("gcfd_post.cu", []),
+            ("dfr_element.cpp", []), ("mesh.cpp", [])])
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "--expt-relaxed-constexpr"]
@@ -30,9 +37,11 @@ def nvcc_path() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libgcfd")
 
 
-def _compile(src: str, verbose: bool, extra: list[str]) -> str:
-    obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
-    cmd = [nvcc_path(), *ARCH, *NVCC_FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
+def _compile(unit, verbose: bool, extra: list[str]) -> str:
+    src, defs = unit
+    tag = "".join("_" + d.split("=")[-1] for d in defs)
+    obj = os.path.join(BUILD_DIR, os.path.basename(src) + tag + ".o")
+    cmd = [nvcc_path(), *ARCH, *NVCC_FLAGS, *defs, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
     if verbose:
         print(" ".join(cmd), flush=True)
     res = subprocess.run(cmd, capture_output=True, text=True)
@@ -60,7 +69,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         return LIB_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
     extra = ["-Xptxas", "-v"] if ptxas_info else []
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+    workers = max(1, min(len(SOURCES), os.cpu_count() or 1))
+    with cf.ThreadPoolExecutor(max_workers=workers) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose or ptxas_info, extra), SOURCES))
     tmp = LIB_PATH + ".tmp"
     cmd = [nvcc_path(), *ARCH, "-shared", "-o", tmp, *objs]

@@ -178,7 +178,7 @@ __device__ __forceinline__ void roe_vjp(const Gas<double>& g, const double QL[4]
 }
 
 // Any interior flux by forward-mode duals (8 tangents: QL then QR).
-__device__ __noinline__ void riemann_vjp_dual(int kind, const Gas<double>& g, const double QL[4], const double QR[4],
+static __device__ __noinline__ void riemann_vjp_dual(int kind, const Gas<double>& g, const double QL[4], const double QR[4],
                                               double nx, double ny, const double fb[4], double QLb[4],
                                               double QRb[4]) {
   using D = Dual<8>;
@@ -259,7 +259,7 @@ __device__ __forceinline__ void bc_point(const EdgeArgs<double>& a, int flag, in
 }
 
 // Reverse of bc_point: qib += J^T (fb, wsb); qinfb (4) and tb get the far-field and time parts.
-__device__ __noinline__ void bc_point_vjp(const EdgeArgs<double>& a, int flag, int bp, const double qi[4],
+static __device__ __noinline__ void bc_point_vjp(const EdgeArgs<double>& a, int flag, int bp, const double qi[4],
                                           double nx, double ny, double t, double oohK, const double fb[4], double wsb,
                                           double qib[4], double qinfb[4], double* tb) {
   using D = Dual<9>;
@@ -504,7 +504,7 @@ __global__ void __launch_bounds__(128) k_adj_edge_bc(EdgeArgs<double> a, AdjEdge
 }
 
 // Global dt: the edge that set this stage's max wave speed.
-__global__ void k_adj_argmax(const double* edgeSpeed, const double* gmaxS, int stage, int nEdges, int* argEdge) {
+static __global__ void k_adj_argmax(const double* edgeSpeed, const double* gmaxS, int stage, int nEdges, int* argEdge) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g < nEdges && edgeSpeed[g] == gmaxS[stage]) atomicMin(argEdge, g);
 }
@@ -537,7 +537,7 @@ struct AdjDtArgs {
 };
 
 // Global: dt = min-clip(CFL / gmax) (calculateGlobalDT, euler.go:945-971).
-__global__ void k_adj_gsel(AdjDtArgs a) {
+static __global__ void k_adj_gsel(AdjDtArgs a) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int s = a.stage;
   double dtb = a.dtbarG[s];
@@ -561,7 +561,7 @@ __global__ void k_adj_gsel(AdjDtArgs a) {
 
 // Local: DT_k = CFL / max(DT_k(prev stage) or -100 at stage 0, edge speeds)
 // (CalculateLocalDT, euler.go:973-1002).
-__global__ void k_adj_lts(AdjDtArgs a) {
+static __global__ void k_adj_lts(AdjDtArgs a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= a.K) return;
   const size_t sK = static_cast<size_t>(a.K);

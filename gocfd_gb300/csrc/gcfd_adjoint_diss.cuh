@@ -49,7 +49,7 @@ __device__ __forceinline__ double vert_sigma_mean(const DissArgs& d, int k, size
 }
 
 // Vertex argmax of the element sigma and eps of this stage (lowest element index).
-__global__ void k_diss_argmax(DissArgs d, const double* sigE, const double* epsE, int* sigArg, int* epsArg) {
+static __global__ void k_diss_argmax(DissArgs d, const double* sigE, const double* epsE, int* sigArg, int* epsArg) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= d.K) return;
   const size_t sK = static_cast<size_t>(d.K);
@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(128) k_adj_diss_limit(DissArgs d, AdjDissArgs 
 }
 
 // a = sin(pi sigma_bar / 2), sigma_bar = mean of the vertex sigV: to the vertices.
-__global__ void k_adj_diss_alpha(DissArgs d, AdjDissArgs x) {
+static __global__ void k_adj_diss_alpha(DissArgs d, AdjDissArgs x) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= d.K) return;
   const size_t sK = static_cast<size_t>(d.K);

@@ -37,6 +37,9 @@ struct Scalars {
   int steps;
   unsigned int errFlags;        // sticky device error bits (1: a tensor-core wait ran out, 2: misaligned
                                 //   dynamic shared memory, 4: a TMA copy wait ran out)
+  double* rpart;                // [unit][4] per-unit sums of R^2 of the final stage, and
+  double* rpart2;               // [kResidBlocks][4] their block sums: both reduced in a fixed order
+                                //   (k_resid_blocks, k_step_end), so the residual norms are deterministic
 };
 
 __device__ __forceinline__ unsigned long long order_key(double x) {
@@ -285,7 +288,7 @@ struct UpdateArgs {
   double* tapeRHSpre;        // k_diss_update: the RHS before the modal filter (adjoint tape)
 };
 
-__constant__ double kSSP[5][6] = {
+static __constant__ double kSSP[5][6] = {
     {0.391752226571890, 0, 0, 0, 0, 0},
     {0.444370493651235, 0.555629506348765, 0.368410593050371, 0, 0, 0},
     {0.620101851488403, 0.379898148511597, 0.251891774271694, 0, 0, 0},
@@ -323,9 +326,13 @@ __device__ __forceinline__ void ssp_stage_update(const UpdateArgs<T>& a, size_t 
   }
 }
 
-// Block-wide residual partials of the final stage -> Scalars (per warp atomics).
+// Block-wide residual partials of the final stage -> Scalars: the maxima by
+// (order-independent) atomics, the FP64 sums of squares of each warp into its
+// own slot of sc->rpart (unit = blockIdx.x * 4 + warp), summed by k_resid_blocks
+// and k_step_end.
 __device__ __forceinline__ void residual_reduce(Scalars* sc, const double rmax[4], const double rabs[4],
                                                 const double rs2[4]) {
+  const size_t unit = static_cast<size_t>(blockIdx.x) * 4 + (threadIdx.x >> 5);
 #pragma unroll
   for (int n = 0; n < 4; ++n) {
     const unsigned long long km = warp_max_u64(order_key(rmax[n]));
@@ -334,7 +341,7 @@ __device__ __forceinline__ void residual_reduce(Scalars* sc, const double rmax[4
     if ((threadIdx.x & 31) == 0) {
       atomicMax(&sc->rmax[n], km);
       atomicMax(&sc->rabs[n], static_cast<unsigned long long>(__double_as_longlong(am)));
-      atomicAdd(&sc->rsum2[n], s2);
+      sc->rpart[unit * 4 + n] = s2;
     }
   }
 }
@@ -430,7 +437,7 @@ __global__ void __launch_bounds__(128) k_div_update(UpdateArgs<T> a) {
 
 // Step bookkeeping: reset the per-stage reductions before a step, advance the
 // time by the last stage's dt after it (Solve, euler.go:176-181).
-__global__ void k_step_begin(Scalars* sc) {
+static __global__ void k_step_begin(Scalars* sc) {
   const int t = threadIdx.x;
   if (t < 5) {
     sc->gmax[t] = 0ULL;
@@ -439,11 +446,65 @@ __global__ void k_step_begin(Scalars* sc) {
   if (t < 4) {
     sc->rmax[t] = 0ULL;
     sc->rabs[t] = 0ULL;
-    sc->rsum2[t] = 0.0;
   }
 }
-__global__ void k_step_end(Scalars* sc, int localDT) {
+// The residual sums of squares of a step: the final stage wrote one FP64 sum
+// per unit into sc->rpart; k_resid_blocks sums fixed contiguous runs of units
+// (block b takes units [b*per, (b+1)*per), thread t every 256th of them, then a
+// fixed tree) into sc->rpart2, and k_step_end sums those kResidBlocks values
+// the same way.  The order never depends on scheduling, so the norms are the
+// same bits run to run.
+constexpr int kResidBlocks = 128;
+constexpr int kResidBlockThreads = 256;
+
+// Fixed-order block sum of 4 per-thread values; thread 0 returns the totals.
+template <int T>
+__device__ __forceinline__ void block_sum4(double s[4], double (*red)[T / 32]) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int n = 0; n < 4; ++n) {
+    s[n] = warp_sum(s[n]);
+    if (lane == 0) red[n][w] = s[n];
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      double v = 0.0;
+      for (int i = 0; i < T / 32; ++i) v += red[n][i];
+      s[n] = v;
+    }
+  }
+}
+
+static __global__ void __launch_bounds__(kResidBlockThreads) k_resid_blocks(Scalars* sc, int nunits) {
+  __shared__ double red[4][kResidBlockThreads / 32];
+  const int per = (nunits + kResidBlocks - 1) / kResidBlocks;
+  const int u0 = blockIdx.x * per, u1 = min(u0 + per, nunits);
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  const double2* p = reinterpret_cast<const double2*>(sc->rpart);
+  for (int u = u0 + threadIdx.x; u < u1; u += kResidBlockThreads) {
+    const double2 a = p[2 * u], b = p[2 * u + 1];
+    s[0] += a.x;
+    s[1] += a.y;
+    s[2] += b.x;
+    s[3] += b.y;
+  }
+  block_sum4<kResidBlockThreads>(s, red);
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int n = 0; n < 4; ++n) sc->rpart2[blockIdx.x * 4 + n] = s[n];
+}
+
+static __global__ void __launch_bounds__(kResidBlocks) k_step_end(Scalars* sc, int localDT) {
+  __shared__ double red[4][kResidBlocks / 32];
+  double s[4];
+#pragma unroll
+  for (int n = 0; n < 4; ++n) s[n] = sc->rpart2[threadIdx.x * 4 + n];
+  block_sum4<kResidBlocks>(s, red);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int n = 0; n < 4; ++n) sc->rsum2[n] = s[n];
     if (!localDT) sc->time += sc->dt[4];
     sc->steps += 1;
   }

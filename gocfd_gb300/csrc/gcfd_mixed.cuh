@@ -338,9 +338,9 @@ struct MixedDims {
 // [NPP][NE3P].  Every warp reads the same entry at the same time, so with the
 // loops unrolled each entry is an immediate constant-bank operand of its FMA
 // and the element kernels issue no shared-memory loads for them.
-__constant__ float cDivT0[MixedDims<0>::DSZ], cDivT1[MixedDims<1>::DSZ], cDivT2[MixedDims<2>::DSZ],
+static __constant__ float cDivT0[MixedDims<0>::DSZ], cDivT1[MixedDims<1>::DSZ], cDivT2[MixedDims<2>::DSZ],
     cDivT3[MixedDims<3>::DSZ], cDivT4[MixedDims<4>::DSZ];
-__constant__ float cIopT0[MixedDims<0>::ISZ], cIopT1[MixedDims<1>::ISZ], cIopT2[MixedDims<2>::ISZ],
+static __constant__ float cIopT0[MixedDims<0>::ISZ], cIopT1[MixedDims<1>::ISZ], cIopT2[MixedDims<2>::ISZ],
     cIopT3[MixedDims<3>::ISZ], cIopT4[MixedDims<4>::ISZ];
 
 // DivInt[r][j] = div_op<N>(j * NPP + r).
@@ -362,29 +362,72 @@ __device__ __forceinline__ float iop_op(int idx) {
   else return cIopT4[idx];
 }
 
+// Packed FP32 pairs: fma.rn.f32x2 (sm_100 and later) performs two independent
+// round-to-nearest FMAs in one instruction, so an operator applied to one
+// input value updates two outputs per instruction.  Each lane is an ordinary
+// fmaf, so a product accumulated through ffma2 rounds exactly like the same
+// chain of fmaf calls.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+// (DivInt[2h][j], DivInt[2h+1][j]) = div_pair<N>(j * NPP / 2 + h).
+template <int N>
+__device__ __forceinline__ float2 div_pair(int idx) {
+  if constexpr (N == 0) return reinterpret_cast<const float2*>(cDivT0)[idx];
+  else if constexpr (N == 1) return reinterpret_cast<const float2*>(cDivT1)[idx];
+  else if constexpr (N == 2) return reinterpret_cast<const float2*>(cDivT2)[idx];
+  else if constexpr (N == 3) return reinterpret_cast<const float2*>(cDivT3)[idx];
+  else return reinterpret_cast<const float2*>(cDivT4)[idx];
+}
+// (FluxEdgeInterp[2h][i], FluxEdgeInterp[2h+1][i]) = iop_pair<N>(i * NE3P / 2 + h).
+template <int N>
+__device__ __forceinline__ float2 iop_pair(int idx) {
+  if constexpr (N == 0) return reinterpret_cast<const float2*>(cIopT0)[idx];
+  else if constexpr (N == 1) return reinterpret_cast<const float2*>(cIopT1)[idx];
+  else if constexpr (N == 2) return reinterpret_cast<const float2*>(cIopT2)[idx];
+  else if constexpr (N == 3) return reinterpret_cast<const float2*>(cIopT3)[idx];
+  else return reinterpret_cast<const float2*>(cIopT4)[idx];
+}
+// acc[h] += (DivInt[2h][j], DivInt[2h+1][j]) * v for every output pair h.
+template <int N>
+__device__ __forceinline__ void div_column(int j, float v, float2 acc[]) {
+  constexpr int NH = MixedDims<N>::NPP / 2;
+  const float2 vv = make_float2(v, v);
+#pragma unroll
+  for (int h = 0; h < NH; ++h) acc[h] = ffma2(div_pair<N>(j * NH + h), vv, acc[h]);
+}
+
 // Writes the element's 3 edges of face deltas for variable n (face point
 // q = e*NE + p): out_q = sum_i FluxEdgeInterp[q][i] dq[i], accumulated over i
 // in order.
 template <int N>
 __device__ __forceinline__ void write_faces(const MixedArgs& a, const int eslot[3], int n, const float dq[]) {
   constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NEP = MixedDims<N>::NEP;
-  constexpr int NE3 = MixedDims<N>::NE3, NE3P = MixedDims<N>::NE3P;
-  float out[NE3];
+  constexpr int NE3P = MixedDims<N>::NE3P, NQ = NE3P / 2;
+  float2 out[NQ];
 #pragma unroll
-  for (int q = 0; q < NE3; ++q) out[q] = 0.0f;
+  for (int q = 0; q < NQ; ++q) out[q] = make_float2(0.0f, 0.0f);
 #pragma unroll
   for (int i = 0; i < NP; ++i) {
+    const float2 v = make_float2(dq[i], dq[i]);
 #pragma unroll
-    for (int q = 0; q < NE3; ++q) out[q] = fmaf(iop_op<N>(i * NE3P + q), dq[i], out[q]);
+    for (int q = 0; q < NQ; ++q) out[q] = ffma2(iop_pair<N>(i * NQ + q), v, out[q]);
   }
+  auto face = [&](int q) { return (q & 1) ? out[q >> 1].y : out[q >> 1].x; };
 #pragma unroll
   for (int e = 0; e < 3; ++e) {
     float* dst = a.faces + (static_cast<size_t>(eslot[e]) * 4 + n) * NEP;
     // (slot*4 + n) * NEP floats with NEP even: 8-byte aligned, pairs go out as float2.
 #pragma unroll
     for (int p = 0; p + 1 < NE; p += 2)
-      reinterpret_cast<float2*>(dst)[p / 2] = make_float2(out[e * NE + p], out[e * NE + p + 1]);
-    if (NE & 1) dst[NE - 1] = out[e * NE + NE - 1];
+      reinterpret_cast<float2*>(dst)[p / 2] = make_float2(face(e * NE + p), face(e * NE + p + 1));
+    if (NE & 1) dst[NE - 1] = face(e * NE + NE - 1);
   }
 }
 
@@ -421,7 +464,7 @@ __global__ void __launch_bounds__(128) k_mixed_prepare(MixedArgs a, int k0, int 
 
 // FP64 copy of the compensated state, for gcfd_get_state.
 // FP64 state = hi + lo for elements [k0, k1) of every [n][i] row (rows x K).
-__global__ void k_mixed_to_fp64(const float* __restrict__ hi, const float* __restrict__ lo,
+static __global__ void k_mixed_to_fp64(const float* __restrict__ hi, const float* __restrict__ lo,
                                 double* __restrict__ q, int K, int rows, int k0, int k1) {
   const int w = k1 - k0;
   const size_t n = static_cast<size_t>(rows) * w;
@@ -704,17 +747,40 @@ __device__ __forceinline__ void stage_tail_prefetch(const MixedArgs& a, int blk,
   }
 }
 
-// One warp's residual partials of the final stage (FP32 warp reductions; the
-// FP64 pipe is narrow), folded into the per-variable scalars by lane 0.
-__device__ __forceinline__ void residual_commit(Scalars* sc, int n, int lane, float rmax, float rabs, float rs2) {
+// One warp's residual partials of the final stage: the maxima by atomics
+// (order independent); the lanes' compensated FP32 sums of squares are summed
+// over the warp by a fixed shuffle tree of compensated additions (no FP64
+// arithmetic: GB300's FP64 pipe is narrow), and lane 0 stores hi + lo in FP64
+// in the warp's slot of sc->rpart (unit = CTA, variable n), which k_resid_blocks
+// and k_step_end sum in FP64 in a fixed order.
+__device__ __forceinline__ void residual_commit(Scalars* sc, int n, int lane, float rmax, float rabs, float2 rs2) {
   rmax = warp_max(rmax);
   rabs = warp_max(rabs);
-  rs2 = warp_sum_f(rs2);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, rs2.x, o);
+    const float ol = __shfl_xor_sync(0xffffffffu, rs2.y, o);
+    float s, e;
+    two_sum(rs2.x, oh, s, e);
+    rs2.x = s;
+    rs2.y = (rs2.y + ol) + e;
+  }
   if (lane == 0) {
     atomicMax(&sc->rmax[n], order_key(static_cast<double>(rmax)));
     atomicMax(&sc->rabs[n], static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(rabs))));
-    atomicAdd(&sc->rsum2[n], static_cast<double>(rs2));
+    sc->rpart[static_cast<size_t>(blockIdx.x) * 4 + n] = static_cast<double>(rs2.x) + static_cast<double>(rs2.y);
   }
+}
+
+// rs2 += x * x in compensated FP32: the product's rounding error from an FMA,
+// the sum's from a two-sum (about 48 significant bits).
+__device__ __forceinline__ void sumsq_add(float2& rs2, float x) {
+  const float p = x * x;
+  const float pe = fmaf(x, x, -p);
+  float s, e;
+  two_sum(rs2.x, p, s, e);
+  rs2.x = s;
+  rs2.y += e + pe;
 }
 
 // The stage's global time step (calculateGlobalDT, euler.go:945-971, with the
@@ -741,7 +807,7 @@ template <int N>
 __device__ __forceinline__ void stage_tail(const MixedArgs& a, const int eslot[3], int n, int k,
                                            size_t off, size_t sK, int s, const float rhs[], const float dq0[],
                                            const float ds[], double dtk, float& rmax, float& rabs,
-                                           float& rs2) {
+                                           float2& rs2) {
   constexpr int NP = MixedDims<N>::NP, NPP = MixedDims<N>::NPP;
   if (s < 0 || a.rhsOnly) {
 #pragma unroll
@@ -795,7 +861,7 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const int eslot[3
         a.Qlo[off + r * sK] = ql[r];
         rmax = fmaxf(rmax, inc);
         rabs = fmaxf(rabs, fabsf(inc));
-        rs2 = fmaf(inc, inc, rs2);
+        sumsq_add(rs2, inc);
         if (inc != inc) rabs = inc;
       }
       // Prepare the next step's stage 0 from the new state.
@@ -813,14 +879,65 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const int eslot[3
   }
 }
 
+// Interior transformed delta fluxes of variable V at every solution point and
+// their divergence columns (DivInt columns 0..2NP-1), accumulated into the
+// output pairs acc.  The stage delta at point i is d = dQ0 + (D_s - D_s(0))
+// (from shared memory); its velocity and pressure deltas come precomputed from
+// shared memory (spr), so the element's four variable warps share them.
+template <int N, int V>
+__device__ __forceinline__ void interior_columns(const BasePrim& b, const float (*sq0)[MixedDims<N>::NP][32],
+                                                 const float (*sds)[MixedDims<N>::NP][32],
+                                                 const float (*spr)[MixedDims<N>::NP][32], int lane, int s,
+                                                 float Jd, float J0, float J1, float J2, float J3, float2 acc[]) {
+  constexpr int NP = MixedDims<N>::NP;
+  // the variables flux V reads: rho-u and rho-v momentum deltas, or the energy delta
+  constexpr int C0 = (V == 3) ? 3 : 1, C1 = 2;
+  const float o0 = (s >= 1) ? sds[C0][0][lane] : 0.0f;
+  const float o1 = (s >= 1) ? sds[C1][0][lane] : 0.0f;
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    const float da = sq0[C0][i][lane] + ((s >= 1) ? sds[C0][i][lane] - o0 : 0.0f);
+    float fx, fy;
+    if constexpr (V == 0) {
+      const float db = sq0[C1][i][lane] + ((s >= 1) ? sds[C1][i][lane] - o1 : 0.0f);
+      fx = da;
+      fy = db;
+    } else if constexpr (V == 1) {
+      const float db = sq0[C1][i][lane] + ((s >= 1) ? sds[C1][i][lane] - o1 : 0.0f);
+      const float du = spr[0][i][lane], dp = spr[2][i][lane];
+      fx = b.m * du + da * b.u + da * du + dp;
+      fy = b.n * du + db * b.u + db * du;
+    } else if constexpr (V == 2) {
+      const float db = sq0[C1][i][lane] + ((s >= 1) ? sds[C1][i][lane] - o1 : 0.0f);
+      const float dv = spr[1][i][lane], dp = spr[2][i][lane];
+      fx = b.m * dv + da * b.v + da * dv;
+      fy = b.n * dv + db * b.v + db * dv + dp;
+    } else {
+      const float du = spr[0][i][lane], dv = spr[1][i][lane], dp = spr[2][i][lane];
+      const float dH = da + dp;
+      fx = b.u * dH + du * (b.H + dH);
+      fy = b.v * dH + dv * (b.H + dH);
+    }
+    const float Fr = Jd * (J0 * fx + J1 * fy);
+    const float Fs = Jd * (J2 * fx + J3 * fy);
+    div_column<N>(NP + i, Fs, acc);
+    div_column<N>(i, Fr, acc);
+  }
+}
+
 // (b)+(e): delta-form divergence, SSP stage update on the FP32 increments, and
 // the next stage's faces / reference states.  stage -1 writes the RHS only.
 //
-// One CTA = 32 elements x 4 variables.  The element's stage inputs (dQ0, D_s)
-// are staged in shared memory by coalesced row loads; its three edge records
-// (fhat, 4 x NEP floats, and corr, 4 floats, per edge) are gathered as 16-byte
-// cp.async chunks shared out over the element's four threads, waited for after
-// the interior flux work.
+// One CTA = 32 elements x 4 variables (warp n owns variable n, lane = element).
+// The element's stage inputs (dQ0, D_s) are staged in shared memory by
+// coalesced row loads; its three edge records (fhat, 4 x NEP floats, and
+// corr, 4 floats, per edge) are gathered as 16-byte cp.async chunks shared
+// out over the element's four threads and waited for after the interior flux
+// work.  The velocity and pressure deltas of the NP points are computed once
+// per element (warp n takes points n, n+4, ...) and shared through shared
+// memory.  Both GEMMs (DivInt against the flux DOFs, FluxEdgeInterp against
+// the next stage's deltas) run on packed FP32 pairs (two outputs per FMA
+// instruction, constant-bank operator pairs).
 template <int N>
 struct StageDims {
   static constexpr int NEP = MixedDims<N>::NEP;
@@ -830,6 +947,156 @@ struct StageDims {
 
 template <int N>
 __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
+  constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NPP = MixedDims<N>::NPP;
+  constexpr int NEP = MixedDims<N>::NEP, CH = StageDims<N>::CH, RW = StageDims<N>::RW;
+  constexpr int NH = NPP / 2;
+  // Rows are indexed by lane, so a 32-float stride is free of bank conflicts.
+  __shared__ float sq0[4][NP][32];
+  __shared__ float sds[4][NP][32];
+  __shared__ float spr[3][NP][32];
+  __shared__ __align__(16) float srec[32 * RW];
+  __shared__ double sdt;
+  const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = blockIdx.x * 32 + lane;
+  const bool active = k < a.K;
+  const size_t sK = static_cast<size_t>(a.K);
+  const size_t off = static_cast<size_t>(n) * NP * sK + k;
+  const int s = a.stage;
+  int eslot[3] = {0, 0, 0};
+  float eII[3] = {0.f, 0.f, 0.f};
+  if (active) {
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      eslot[e] = a.eslot[e * sK + k];
+      eII[e] = a.II[e * sK + k];
+    }
+    // Chunks c = n, n+4, ... of the element's 3 x CH record chunks.
+#pragma unroll
+    for (int t = 0; t < (3 * CH + 3) / 4; ++t) {
+      const int c = n + 4 * t;
+      if (c < 3 * CH) {
+        const int e = c / CH, j = c - e * CH;
+        const size_t g = static_cast<size_t>((e == 0 ? eslot[0] : (e == 1 ? eslot[1] : eslot[2])) >> 1);
+        const float* src = (j < NEP) ? a.fhat + g * 4 * NEP + 4 * j : a.corr + g * 4;
+        const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(&srec[lane * RW + 4 * c]));
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src));
+      }
+    }
+  }
+  asm volatile("cp.async.commit_group;\n" ::);
+  stage_tail_prefetch<N>(a, blockIdx.x, n, lane, sK, s);
+  float Jd = 0.f, J0 = 0.f, J1 = 0.f, J2 = 0.f, J3 = 0.f, ooJ = 0.f;
+  if (active) {
+#pragma unroll
+    for (int i = 0; i < NP; ++i) sq0[n][i][lane] = a.dQ0[off + i * sK];
+    if (s >= 1) {
+#pragma unroll
+      for (int i = 0; i < NP; ++i) sds[n][i][lane] = a.D[s][off + i * sK];
+    }
+    Jd = a.geo[k];
+    J0 = a.geo[sK + k];
+    J1 = a.geo[2 * sK + k];
+    J2 = a.geo[3 * sK + k];
+    J3 = a.geo[4 * sK + k];
+    ooJ = a.geo[5 * sK + k];
+  } else {
+    // lanes past K: zero deltas for the shared work
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+      sq0[n][i][lane] = 0.0f;
+      sds[n][i][lane] = 0.0f;
+    }
+  }
+  // Local time step of this stage: DT persists across stages, so every thread
+  // of the element reads it before the barrier and one writes it after.
+  double dtk = 0.0;
+  if (active && a.localDT && s >= 0 && !a.rhsOnly) {
+    double v = (s == 0) ? -100.0 : a.DT[k];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) v = fmax(v, a.edgeSpeed[eslot[e] >> 1]);
+    dtk = a.cfl / v;
+  }
+  if (threadIdx.x == 0 && needs_global_dt(a, s)) sdt = global_stage_dt(a, s);
+  __syncthreads();
+  if (needs_global_dt(a, s)) dtk = sdt;
+  const float gm1 = a.gamma - 1.0f;
+  float bq[4] = {1.0f, 0.0f, 0.0f, 2.5f};  // lanes past K: a harmless reference state
+  if (active) {
+    const float4* pb = reinterpret_cast<const float4*>(a.base + static_cast<size_t>(k) * 4);
+    const float4 b01 = pb[0], b23 = pb[1];
+    bq[0] = b01.x;
+    bq[1] = b01.z;
+    bq[2] = b23.x;
+    bq[3] = b23.z;
+  }
+  const BasePrim b = base_prim(bq, gm1);
+  // Velocity and pressure deltas of points n, n+4, ... for the whole element.
+#pragma unroll
+  for (int t = 0; t < (NP + 3) / 4; ++t) {
+    const int i = n + 4 * t;
+    if (i < NP) {
+      float d[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) d[c] = sq0[c][i][lane] + ((s >= 1) ? sds[c][i][lane] - sds[c][0][lane] : 0.0f);
+      const DeltaPrim q = delta_prim(b, d, gm1);
+      spr[0][i][lane] = q.du;
+      spr[1][i][lane] = q.dv;
+      spr[2][i][lane] = q.dp;
+    }
+  }
+  __syncthreads();
+  float2 acc[NH];
+#pragma unroll
+  for (int h = 0; h < NH; ++h) acc[h] = make_float2(0.0f, 0.0f);
+  switch (n) {
+    case 0: interior_columns<N, 0>(b, sq0, sds, spr, lane, s, Jd, J0, J1, J2, J3, acc); break;
+    case 1: interior_columns<N, 1>(b, sq0, sds, spr, lane, s, Jd, J0, J1, J2, J3, acc); break;
+    case 2: interior_columns<N, 2>(b, sq0, sds, spr, lane, s, Jd, J0, J1, J2, J3, acc); break;
+    default: interior_columns<N, 3>(b, sq0, sds, spr, lane, s, Jd, J0, J1, J2, J3, acc); break;
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncthreads();  // every thread's record chunks
+  float rmax = -3.4028235e38f, rabs = 0.0f;
+  float2 rs2 = make_float2(0.0f, 0.0f);
+  if (active) {
+    // Edge DOFs: IInII * (s fhat - n_e.F(Qb)), owner order / reversed for the right side.
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      const float* rec = &srec[lane * RW + e * CH * 4];
+      const bool right = eslot[e] & 1;
+      const float ii = eII[e];
+      const float cc = right ? rec[4 * NEP + n] : 0.0f;
+      float v[NEP];
+      const float2* rp = reinterpret_cast<const float2*>(rec + n * NEP);
+#pragma unroll
+      for (int q = 0; q < NEP / 2; ++q) {
+        const float2 t = rp[q];
+        v[2 * q] = t.x;
+        v[2 * q + 1] = t.y;
+      }
+#pragma unroll
+      for (int p = 0; p < NE; ++p) {
+        const float dof = right ? -(v[NE - 1 - p] - cc) * ii : v[p] * ii;
+        div_column<N>(2 * NP + e * NE + p, dof, acc);
+      }
+    }
+    float rhs[NP], dq0[NP], ds[NP];
+#pragma unroll
+    for (int r = 0; r < NP; ++r) {
+      rhs[r] = -((r & 1) ? acc[r >> 1].y : acc[r >> 1].x) * ooJ;
+      dq0[r] = sq0[n][r][lane];
+      ds[r] = (s >= 1) ? sds[n][r][lane] : 0.0f;
+    }
+    stage_tail<N>(a, eslot, n, k, off, sK, s, rhs, dq0, ds, dtk, rmax, rabs, rs2);
+  }
+  if (s == 4 && !a.rhsOnly) {
+    residual_commit(a.sc, n, lane, rmax, rabs, rs2);
+  }
+}
+
+// TEMP A/B: the previous one-block stage kernel
+template <int N>
+__global__ void __launch_bounds__(128, 7) k_mixed_stage_old(MixedArgs a) {
   constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NPP = MixedDims<N>::NPP;
   constexpr int NEP = MixedDims<N>::NEP, CH = StageDims<N>::CH, RW = StageDims<N>::RW;
   __shared__ float sq0[4][NP][33];
@@ -923,7 +1190,8 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
   }
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();  // every thread's record chunks
-  float rmax = -3.4028235e38f, rabs = 0.0f, rs2 = 0.0f;
+  float rmax = -3.4028235e38f, rabs = 0.0f;
+  float2 rs2 = make_float2(0.0f, 0.0f);
   if (active) {
     // Edge DOFs: IInII * (s fhat - n_e.F(Qb)), owner order / reversed for the right side.
 #pragma unroll

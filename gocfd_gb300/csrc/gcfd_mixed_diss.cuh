@@ -15,11 +15,11 @@ namespace gcfd {
 
 // The modal filter's operators (V, V^-1, the mode filter) in constant memory,
 // one copy per order N, for the same reason as the divergence operator.
-__constant__ float cV0[Dims<0>::NP * Dims<0>::NP], cV1[Dims<1>::NP * Dims<1>::NP],
+static __constant__ float cV0[Dims<0>::NP * Dims<0>::NP], cV1[Dims<1>::NP * Dims<1>::NP],
     cV2[Dims<2>::NP * Dims<2>::NP], cV3[Dims<3>::NP * Dims<3>::NP], cV4[Dims<4>::NP * Dims<4>::NP];
-__constant__ float cVi0[Dims<0>::NP * Dims<0>::NP], cVi1[Dims<1>::NP * Dims<1>::NP],
+static __constant__ float cVi0[Dims<0>::NP * Dims<0>::NP], cVi1[Dims<1>::NP * Dims<1>::NP],
     cVi2[Dims<2>::NP * Dims<2>::NP], cVi3[Dims<3>::NP * Dims<3>::NP], cVi4[Dims<4>::NP * Dims<4>::NP];
-__constant__ float cMf0[Dims<0>::NP], cMf1[Dims<1>::NP], cMf2[Dims<2>::NP], cMf3[Dims<3>::NP],
+static __constant__ float cMf0[Dims<0>::NP], cMf1[Dims<1>::NP], cMf2[Dims<2>::NP], cMf3[Dims<3>::NP],
     cMf4[Dims<4>::NP];
 template <int N>
 __device__ __forceinline__ float v_op(int i) {
@@ -352,7 +352,8 @@ __global__ void __launch_bounds__(128, N >= 4 ? 3 : 5) k_mixed_diss_update(Mixed
   if (threadIdx.x == 0 && needs_global_dt(a, s)) sdt = global_stage_dt(a, s);
   __syncthreads();
   if (needs_global_dt(a, s)) dtLocal = sdt;
-  float rmax = -3.4028235e38f, rabs = 0.0f, rs2 = 0.0f;
+  float rmax = -3.4028235e38f, rabs = 0.0f;
+  float2 rs2 = make_float2(0.0f, 0.0f);
   if (active) {
     const double Jdd = u.Jdet[k];
     const float Jd = static_cast<float>(Jdd), oojd = static_cast<float>(1.0 / Jdd);

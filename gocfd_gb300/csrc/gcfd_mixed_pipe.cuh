@@ -170,7 +170,8 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_pipe(const __grid_consta
     issue(blk, 0);
     prefetch_tail(blk);
   }
-  float rmax = -3.4028235e38f, rabs = 0.0f, rs2 = 0.0f;
+  float rmax = -3.4028235e38f, rabs = 0.0f;
+  float2 rs2 = make_float2(0.0f, 0.0f);
   for (int j = 0; blk < nblk; ++j, blk += gridDim.x) {
     const int buf = j & 1;
     const uint32_t par = (j >> 1) & 1;

@@ -206,7 +206,8 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
   uint32_t dv[16];
   tc::ld16(trow + TcDims<N>::COL_D, dv);
   tc::wait_ld();
-  float rmax = -3.4028235e38f, rabs = 0.0f, rs2 = 0.0f;
+  float rmax = -3.4028235e38f, rabs = 0.0f;
+  float2 rs2 = make_float2(0.0f, 0.0f);
   if (active) {
     float rhs[NP];
 #pragma unroll

@@ -1,0 +1,329 @@
+// Adjoint launchers of one polynomial order: compiled once per order with
+// -DGCFD_ORDER=N (0..4), exporting adj_ops_N.
+#include "gcfd_adjoint.cuh"
+#include "gcfd_adjoint_diss.cuh"
+#include "gcfd_launch.cuh"
+
+#ifndef GCFD_ORDER
+#error "compile with -DGCFD_ORDER=<0..4>"
+#endif
+#define GCFD_CAT2(a, b) a##b
+#define GCFD_CAT(a, b) GCFD_CAT2(a, b)
+
+namespace gcfd_host {
+namespace {
+
+constexpr int kN = GCFD_ORDER;
+
+// Adjoint launchers (FP64 path).
+template <int N>
+struct AdjLaunch {
+  using L = Launch<N, double>;
+  static int grid(int n) { return (n + 127) / 128; }
+  static EdgeArgs<double> edge_args(gcfd_ctx* c, const double* time) {
+    EdgeArgs<double> e = L::edge_args(c, time);
+    e.QF = static_cast<const double*>(c->QF);
+    return e;
+  }
+  static AdjEdgeArgs adj_edge_args(gcfd_ctx* c) {
+    AdjEdgeArgs x;
+    x.FEb = c->FEb;
+    x.QFb = c->QFb;
+    x.qinfb = c->adjS + 5;
+    x.tb = c->adjS + 9;
+    x.esBar = c->esBar;
+    x.useManualRoe = 1;
+    return x;
+  }
+  static AdjArgs adj_args(gcfd_ctx* c, int s, const double* Qs, const double* Qbn, double* Qbs) {
+    AdjArgs a;
+    a.K = c->K;
+    a.stage = s;
+    a.localDT = c->prm.local_time_stepping;
+    a.Qs = Qs;
+    a.Qbn = Qbn;
+    a.rhs = s >= 0 ? c->tapeRHS[s] : nullptr;
+    a.rhs3 = c->tapeRHS[3];
+    a.Qb0 = c->Qb[0];
+    a.Qbs = Qbs;
+    a.Qb2 = c->Qb[2];
+    a.Qb3 = c->Qb[3];
+    a.Rb3 = c->Rb3;
+    a.dtS = c->tapeSc->dt;
+    a.dtK = s >= 0 ? c->tapeDT[s] : nullptr;
+    a.dtbarG = c->adjS;
+    a.dtOwnK = c->dtOwnK;
+    a.DivInt = c->Div;
+    a.Jdet = c->Jdet;
+    a.Jinv = c->Jinv;
+    a.FEb = c->FEb;
+    const double g = c->fsFar.gamma;
+    a.gas = Gas<double>{g, g - 1.0, 1.0 / (g - 1.0)};
+    return a;
+  }
+  // Forward step with the tape: the same launches as L::step (so the states
+  // are bit-identical to the recorded trajectory), plus per-stage copies of
+  // the edge speeds, local dt and faces, the stage RHS written by the update
+  // kernel, and with the dissipation the rkStep-2 state before the limiter,
+  // DTVisc before each stage, the viscous speeds and the pre-filter RHS.
+  static void tape_step(gcfd_ctx* c) {
+    cudaMemcpyAsync(c->tapeSc0, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream);
+    k_step_begin<<<1, 32, 0, c->stream>>>(c->sc);
+    void* faces = c->QF;
+    const size_t SB = sizeof(double) * 4 * c->Np * static_cast<size_t>(c->K);
+    for (int s = 0; s < 5; ++s) {
+      c->QF = c->tapeQF[s];  // the stage's faces stay on the tape
+      if (c->diss) {
+        if (s == 2) cudaMemcpyAsync(c->tapeQ2pre, c->Q[2], SB, cudaMemcpyDeviceToDevice, c->stream);
+        cudaMemcpyAsync(c->tapeDTV[s], c->DTVisc, sizeof(double) * c->K, cudaMemcpyDeviceToDevice, c->stream);
+        L::diss_front(c, s, c->Q[s]);
+      } else {
+        L::interp(c, c->Q[s]);
+      }
+      L::edge(c, &c->sc->time, &c->sc->gmax[s]);
+      if (c->diss) {
+        L::diss_middle(c, s, c->Q[s]);
+        cudaMemcpyAsync(c->tapeVS[s], c->viscSpeed, sizeof(double) * c->nEdges, cudaMemcpyDeviceToDevice,
+                        c->stream);
+      }
+      c->QF = faces;
+      cudaMemcpyAsync(c->tapeES[s], c->edgeSpeed, sizeof(double) * c->nEdges, cudaMemcpyDeviceToDevice,
+                      c->stream);
+      if (c->diss) {
+        k_div_update<N, double><<<grid(c->K), 128, 0, c->stream>>>(L::update_args(c, -1, c->Q[s]));
+        UpdateArgs<double> u = L::update_args(c, s, c->Q[s]);
+        u.tapeRHS = c->tapeRHS[s];
+        u.tapeRHSpre = c->tapeRHSpre[s];
+        k_diss_update<N><<<grid(c->K), 128, 0, c->stream>>>(u);
+      } else {
+        UpdateArgs<double> u = L::update_args(c, s, c->Q[s]);
+        u.tapeRHS = c->tapeRHS[s];
+        k_div_update<N, double><<<grid(c->K), 128, 0, c->stream>>>(u);
+      }
+      if (c->prm.local_time_stepping)
+        cudaMemcpyAsync(c->tapeDT[s], c->DT, sizeof(double) * c->K, cudaMemcpyDeviceToDevice, c->stream);
+    }
+    k_resid_blocks<<<kResidBlocks, kResidBlockThreads, 0, c->stream>>>(c->sc, resid_units(c));
+    k_step_end<<<1, kResidBlocks, 0, c->stream>>>(c->sc, c->prm.local_time_stepping);
+    cudaMemcpyAsync(c->tapeSc, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream);
+  }
+  static void edges(gcfd_ctx* c, const EdgeArgs<double>& e, const AdjEdgeArgs& x) {
+    if (c->nInt > 0) {
+      if (e.flux == kFluxRoe && x.useManualRoe)
+        k_adj_edge<N, true><<<grid(c->nInt), 128, 0, c->stream>>>(e, x);
+      else
+        k_adj_edge<N, false><<<grid(c->nInt), 128, 0, c->stream>>>(e, x);
+    }
+    if (c->nBC > 0) k_adj_edge_bc<N><<<grid(c->nBC * Dims<N>::NE), 128, 0, c->stream>>>(e, x);
+  }
+  static AdjDissArgs adj_diss_args(gcfd_ctx* c, const double* Qsens, int s) {
+    AdjDissArgs x;
+    x.nverts = c->nverts;
+    x.Qsens = Qsens;
+    x.rhsPre = c->tapeRHSpre[s < 0 ? 0 : s];
+    x.RbE = c->RbE;
+    x.alphaBar = c->alphaBar;
+    x.sigVbar = c->sigVbar;
+    x.epsVbar = c->epsVbar;
+    x.VFbar = c->VFbar;
+    x.DissXbar = c->DissXbar;
+    x.DissYbar = c->DissYbar;
+    x.QFb = c->QFb;
+    x.vsBar = c->vsBar;
+    x.sigArg = c->sigArg;
+    x.epsArg = c->epsArg;
+    x.sigE = c->sigE;
+    x.SeE = c->SeE;
+    x.Q2pre = c->tapeQ2pre;
+    x.Qlim = c->Qb[2];
+    return x;
+  }
+  // Dissipation, reverse, part 1 (before the Euler part): recompute the
+  // stage's sensor and vertex maxima, then the update / filter / AddDissipation
+  // adjoint; the Euler RHS adjoint is left in RbE.
+  static void diss_reverse_update(gcfd_ctx* c, int s, const double* Qs, const double* Qsens, const double* Qbn,
+                                  double* Qbs, const double* faces) {
+    cudaMemsetAsync(c->sigV, 0, sizeof(unsigned long long) * c->nverts, c->stream);
+    cudaMemsetAsync(c->epsV, 0, sizeof(unsigned long long) * c->nverts, c->stream);
+    DissArgs d = L::diss_args(c, s, const_cast<double*>(Qsens));
+    d.sigE = c->sigE;
+    d.epsE = c->epsE;
+    d.SeE = c->SeE;
+    k_diss_sensor<N><<<grid(c->K), 128, 0, c->stream>>>(d);
+    cudaMemsetAsync(c->sigArg, 0x7f, sizeof(int) * c->nverts, c->stream);
+    cudaMemsetAsync(c->epsArg, 0x7f, sizeof(int) * c->nverts, c->stream);
+    k_diss_argmax<<<grid(c->K), 128, 0, c->stream>>>(d, c->sigE, c->epsE, c->sigArg, c->epsArg);
+    cudaMemsetAsync(c->sigVbar, 0, sizeof(double) * c->nverts, c->stream);
+    cudaMemsetAsync(c->epsVbar, 0, sizeof(double) * c->nverts, c->stream);
+    cudaMemsetAsync(c->VFbar, 0, sizeof(double) * (c->nInt + c->nBC) * 4 * c->NE, c->stream);
+    d.Qs = Qs;
+    d.QF = const_cast<double*>(faces);
+    k_adj_diss_update<N><<<grid(c->K), 128, 0, c->stream>>>(d, adj_args(c, s, Qs, Qbn, Qbs),
+                                                             adj_diss_args(c, Qsens, s));
+  }
+  // Dissipation, reverse, part 2 (after the Euler edge and speed adjoints):
+  // viscous edges, gradient, face transpose, limiter (rkStep 2), sensor.
+  static void diss_reverse_rest(gcfd_ctx* c, int s, const double* Qs, const double* Qsens, double* Qbs,
+                                const double* faces) {
+    DissArgs d = L::diss_args(c, s, const_cast<double*>(Qs));
+    d.QF = const_cast<double*>(faces);
+    const AdjDissArgs x = adj_diss_args(c, Qsens, s);
+    k_adj_diss_edge<N><<<grid(c->nInt + c->nBC), 128, 0, c->stream>>>(d, x);
+    constexpr int NF = Dims<N>::NF;
+    k_adj_diss_grad<N><<<grid(c->K), 128, sizeof(double) * (NF * NF + NF * 3), c->stream>>>(d, x, Qbs);
+    k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, Qbs, c->K);
+    if (s == 2) k_adj_diss_limit<N><<<grid(4 * c->K), 128, 0, c->stream>>>(d, x);
+    k_adj_diss_alpha<<<grid(c->K), 128, 0, c->stream>>>(d, x);
+    k_adj_diss_sensor<N><<<grid(c->K), 128, 0, c->stream>>>(d, x, Qbs);
+  }
+  // The reverse of stage s.  Q0 is the step's initial state.  With a segment
+  // tape the stage faces are not taped (they are FluxEdgeInterp of the stage
+  // state, after the rkStep-2 limiter where it applies) and are rebuilt here.
+  static void reverse_stage(gcfd_ctx* c, int s, const double* Q0) {
+    const double* Qs = (s == 0) ? Q0 : c->Q[s];
+    if (c->facesFromState) {
+      void* f = c->QF;
+      c->QF = c->tapeQF[s];
+      L::interp(c, Qs);
+      c->QF = f;
+    }
+    const double* Qbn = (s == 4) ? c->Qbf : c->Qb[s + 1];
+    const double* Qsens = (s == 2) ? c->tapeQ2pre : Qs;
+    if (c->diss) {
+      diss_reverse_update(c, s, Qs, Qsens, Qbn, c->Qb[s], c->tapeQF[s]);
+      k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, -1, Qs, c->RbE, c->Qb[s]));
+    } else {
+      k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, s, Qs, Qbn, c->Qb[s]));
+    }
+    EdgeArgs<double> e = edge_args(c, &c->tapeSc0->time);
+    e.QF = c->tapeQF[s];
+    const AdjEdgeArgs x = adj_edge_args(c);
+    const int nE = c->nInt + c->nBC;
+    edges(c, e, x);
+    cudaMemsetAsync(c->esBar, 0, sizeof(double) * nE, c->stream);
+    if (c->diss) cudaMemsetAsync(c->vsBar, 0, sizeof(double) * nE, c->stream);
+    AdjDtArgs d;
+    d.K = c->K;
+    d.stage = s;
+    d.nEdges = nE;
+    d.cfl = c->prm.cfl;
+    d.finalTime = c->prm.final_time;
+    d.gmaxS = reinterpret_cast<const double*>(c->tapeSc->gmax);
+    d.tn = &c->tapeSc0->time;
+    d.dtbarG = c->adjS;
+    d.tbarNext = c->adjS + 10;
+    d.tbarCur = c->adjS + 9;
+    d.argEdge = c->argEdge + s;
+    d.esBar = c->esBar;
+    d.dtPrev = s > 0 ? c->tapeDT[s - 1] : nullptr;
+    d.edgeSpeed = c->tapeES[s];
+    d.elemEdge = c->elemEdge;
+    d.dtOwnK = c->dtOwnK;
+    d.carry = c->carry;
+    d.diss = c->diss ? 1 : 0;
+    d.cdiff = 1.0 / (double(c->N + 1) * double(c->N + 1));
+    d.gviscS = reinterpret_cast<const double*>(c->tapeSc->gvisc);
+    d.argVisc = c->argVisc + s;
+    d.vsBar = c->vsBar;
+    d.dtvPrev = c->diss ? c->tapeDTV[s] : nullptr;
+    d.viscSpeed = c->diss ? c->tapeVS[s] : nullptr;
+    d.carryV = c->carryV;
+    if (c->prm.local_time_stepping) {
+      k_adj_lts<<<grid(c->K), 128, 0, c->stream>>>(d);
+    } else {
+      cudaMemsetAsync(c->argEdge + s, 0x7f, sizeof(int), c->stream);
+      k_adj_argmax<<<grid(nE), 128, 0, c->stream>>>(c->tapeES[s], d.gmaxS, s, nE, c->argEdge + s);
+      if (c->diss) {
+        cudaMemsetAsync(c->argVisc + s, 0x7f, sizeof(int), c->stream);
+        k_adj_argmax<<<grid(nE), 128, 0, c->stream>>>(c->tapeVS[s], d.gviscS, s, nE, c->argVisc + s);
+      }
+      k_adj_gsel<<<1, 32, 0, c->stream>>>(d);
+    }
+    k_adj_speed<N><<<grid(nE), 128, 0, c->stream>>>(e, x);
+    if (c->diss)
+      diss_reverse_rest(c, s, Qs, Qsens, c->Qb[s], c->tapeQF[s]);
+    else
+      k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[s], c->K);
+  }
+  // Adjoint of one step whose initial state is Q0 (already in c->Q[0]) and
+  // time is in c->sc.  In: Qbf, adjS[10] (t-bar of the step's end).  Out:
+  // Qbf <- adjoint of Q0, adjS[10] <- t-bar of the step's start.  carryV (the
+  // DTVisc adjoint) runs on across steps.
+  static void reverse_step(gcfd_ctx* c, const double* Q0) {
+    tape_step(c);
+    reverse_taped(c, Q0);
+  }
+  // The adjoint of a step whose tape is already bound (tape_step ran earlier
+  // into the context's current tape slot).
+  static void reverse_taped(gcfd_ctx* c, const double* Q0) {
+    // no zeroing of the stage adjoints: the first write to each is a store
+    cudaMemsetAsync(c->adjS, 0, sizeof(double) * 5, c->stream);
+    cudaMemcpyAsync(c->adjS + 9, c->adjS + 10, sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemsetAsync(c->carry, 0, sizeof(double) * c->K, c->stream);
+    for (int s = 4; s >= 0; --s) reverse_stage(c, s, Q0);
+    std::swap(c->Qbf, c->Qb[0]);
+    cudaMemcpyAsync(c->adjS + 10, c->adjS + 9, sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  }
+  // RHS adjoint at c->Qtmp and sc->rhs_time: Qb[0] <- J^T Qbf.
+  static void rhs_vjp(gcfd_ctx* c) {
+    const size_t S = sizeof(double) * 4 * c->Np * static_cast<size_t>(c->K);
+    void* faces = c->QF;
+    if (c->diss) {  // the forward RHS once more, keeping the pre-filter RHS
+      c->QF = c->tapeQF[0];
+      L::diss_front(c, -1, c->Qtmp);
+      L::edge(c, &c->sc->rhs_time, &c->sc->gmax[0]);
+      L::diss_middle(c, -1, c->Qtmp);
+      k_div_update<N, double><<<grid(c->K), 128, 0, c->stream>>>(L::update_args(c, -1, c->Qtmp));
+      UpdateArgs<double> u = L::update_args(c, -1, c->Qtmp);
+      u.tapeRHSpre = c->tapeRHSpre[0];
+      k_diss_update<N><<<grid(c->K), 128, 0, c->stream>>>(u);
+    } else {
+      L::interp(c, c->Qtmp);
+    }
+    cudaMemsetAsync(c->Qb[0], 0, S, c->stream);
+    const EdgeArgs<double> e = edge_args(c, &c->sc->rhs_time);
+    if (c->diss) {
+      diss_reverse_update(c, -1, c->Qtmp, c->Qtmp, c->Qbf, c->Qb[0], static_cast<const double*>(c->QF));
+      k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, -1, c->Qtmp, c->RbE, c->Qb[0]));
+    } else {
+      k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, -1, c->Qtmp, c->Qbf, c->Qb[0]));
+    }
+    edges(c, e, adj_edge_args(c));
+    if (c->diss) {
+      cudaMemsetAsync(c->vsBar, 0, sizeof(double) * (c->nInt + c->nBC), c->stream);
+      diss_reverse_rest(c, -1, c->Qtmp, c->Qtmp, c->Qb[0], static_cast<const double*>(c->QF));
+      c->QF = faces;
+    } else {
+      k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[0], c->K);
+    }
+  }
+  // Functionals of the current state Q[0]: J into adjS[11], dJ/dQ into Qb[0],
+  // dJ/dt into adjS[9].
+  static void functional(gcfd_ctx* c, int kind) {
+    const size_t S = sizeof(double) * 4 * c->Np * static_cast<size_t>(c->K);
+    cudaMemsetAsync(c->Qb[0], 0, S, c->stream);
+    if (kind == GCFD_FUNC_VORTEX_ERROR) {
+      k_func_vortex<N><<<grid(c->K), 128, 0, c->stream>>>(c->Q[0], c->dXs, c->dYs, c->K, c->vbeta, c->vx0, c->vy0,
+                                                          c->vgamma, &c->sc->time, c->Qb[0], c->adjS + 11,
+                                                          c->adjS + 9);
+      return;
+    }
+    L::interp(c, c->Q[0]);
+    cudaMemsetAsync(c->QFb, 0, sizeof(double) * 4 * 3 * c->NE * static_cast<size_t>(c->K), c->stream);
+    const EdgeArgs<double> e = edge_args(c, &c->sc->time);
+    if (c->nBC > 0)
+      k_func_wall<N><<<grid(c->nBC), 128, 0, c->stream>>>(e, c->edgeW, kind == GCFD_FUNC_WALL_FORCE_Y, c->QFb,
+                                                          c->adjS + 11);
+    k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[0], c->K);
+  }
+};
+
+}  // namespace
+
+const AdjOps* GCFD_CAT(adj_ops_, GCFD_ORDER)() {
+  static const AdjOps o{&AdjLaunch<kN>::tape_step, &AdjLaunch<kN>::reverse_step, &AdjLaunch<kN>::reverse_taped,
+                        &AdjLaunch<kN>::rhs_vjp, &AdjLaunch<kN>::functional};
+  return &o;
+}
+
+}  // namespace gcfd_host

@@ -18,6 +18,115 @@ static inline uint64_t edge_key(int a, int b) {
   return lo | (hi << 32);
 }
 
+namespace {
+
+// The edges of one periodic half as a connected curve, as Curve.ReOrder does
+// (types/elemental.go:141-199, AssembleCurve :201-240): start from the half's
+// first edge (its last with `reverse`), which must sit at an open end of the
+// curve, and walk the shared vertices.  Where the listed start is not an end
+// edge, ReOrder starts at the end that Go's map iteration yields first; this
+// restatement takes the end with the smaller vertex index instead.
+std::string order_curve(const Topology& t, const std::vector<int>& edges, bool reverse, std::vector<int>* out) {
+  std::unordered_map<int, std::vector<int>> at;  // vertex -> incident edges of the curve
+  for (int en : edges) {
+    at[static_cast<int>(t.key[en] & 0xffffffffULL)].push_back(en);
+    at[static_cast<int>(t.key[en] >> 32)].push_back(en);
+  }
+  int nends = 0, endv = -1;
+  for (const auto& kv : at) {
+    if (kv.second.size() > 2) return "periodic boundary curve branches at a vertex";
+    if (kv.second.size() == 1) {
+      ++nends;
+      if (endv < 0 || kv.first < endv) endv = kv.first;
+    }
+  }
+  if (nends != 2) return "periodic boundary edges do not form one open curve";
+  auto deg = [&](int v) { return static_cast<int>(at[v].size()); };
+  int start = reverse ? edges.back() : edges.front();
+  const int s0 = static_cast<int>(t.key[start] & 0xffffffffULL), s1 = static_cast<int>(t.key[start] >> 32);
+  if (deg(s0) != 1 && deg(s1) != 1) start = at[endv][0];
+  out->clear();
+  out->push_back(start);
+  const int a = static_cast<int>(t.key[start] & 0xffffffffULL), b = static_cast<int>(t.key[start] >> 32);
+  int end = (deg(a) == 2) ? a : b;  // the open end to continue from
+  int prev = start;
+  while (deg(end) == 2) {
+    const std::vector<int>& inc = at[end];
+    const int next = (inc[0] == prev) ? inc[1] : inc[0];
+    out->push_back(next);
+    const int na = static_cast<int>(t.key[next] & 0xffffffffULL), nb = static_cast<int>(t.key[next] >> 32);
+    end = (na == end) ? nb : na;
+    prev = next;
+    if (out->size() > edges.size()) return "periodic boundary curve is closed";
+  }
+  if (out->size() != edges.size()) return "periodic boundary edges do not form one open curve";
+  return "";
+}
+
+}  // namespace
+
+// Periodic pairs, as NewTriangulation does (triangulation.go:63-99): each
+// tag's edge list is split into halves, each half is ordered as a connected
+// curve (the second starting from its last edge for PeriodicReversed), and the
+// i-th edges of the two curves become one shared edge: the first curve's
+// element is the left side, the second curve's element the right side (its
+// face points reversed like any shared edge's).  The reference keeps the
+// second edge as a one-sided edge whose flux is a no-op (edges.go:436-437) and
+// lets the order of Go's map iteration decide which of the two records the
+// second element's edge uses (dfr_startup.go:289-310); here the second edge is
+// removed and the element's edge is the shared one.  Each side keeps its own
+// geometry (normal, ||n||) from its own edge (keyR).
+std::string pair_periodic(const std::vector<std::pair<int, std::vector<int>>>& groups, Topology* t) {
+  if (groups.empty()) return "";
+  std::vector<char> dead(t->nEdges, 0);
+  for (const auto& g : groups) {
+    const std::vector<int>& L = g.second;
+    const bool reversed = (g.first & 0xff) == BC_PeriodicReversed;
+    if (L.size() % 2 != 0)
+      return "periodic boundaries must be present in pairs, have dimension " + std::to_string(L.size()) +
+             ", not even";
+    const size_t l2 = L.size() / 2;
+    std::vector<int> c0, c1;
+    std::string msg = order_curve(*t, std::vector<int>(L.begin(), L.begin() + l2), false, &c0);
+    if (msg.empty()) msg = order_curve(*t, std::vector<int>(L.begin() + l2, L.end()), reversed, &c1);
+    if (!msg.empty()) return msg;
+    for (size_t i = 0; i < l2; ++i) {
+      const int e1 = c0[i], e2 = c1[i];
+      if (t->kR[e1] >= 0 || t->kR[e2] >= 0 || dead[e1] || dead[e2] || e1 == e2)
+        return "periodic boundary edge is not a free boundary edge";
+      t->kR[e1] = t->kL[e2];
+      t->eR[e1] = t->eL[e2];
+      t->revR[e1] = t->revL[e2];
+      t->keyR[e1] = t->key[e2];
+      t->bc[e1] = BC_None;
+      t->elemEdge[3 * t->kL[e2] + t->eL[e2]] = e1;
+      dead[e2] = 1;
+    }
+  }
+  // Drop the absorbed edges and renumber.
+  std::vector<int> newIndex(t->nEdges, -1);
+  int n = 0;
+  for (int en = 0; en < t->nEdges; ++en)
+    if (!dead[en]) newIndex[en] = n++;
+  auto compact = [&](auto& v) {
+    for (int en = 0; en < t->nEdges; ++en)
+      if (!dead[en]) v[newIndex[en]] = v[en];
+    v.resize(n);
+  };
+  compact(t->key);
+  compact(t->keyR);
+  compact(t->kL);
+  compact(t->eL);
+  compact(t->kR);
+  compact(t->eR);
+  compact(t->revL);
+  compact(t->revR);
+  compact(t->bc);
+  for (int& e : t->elemEdge) e = newIndex[e];
+  t->nEdges = n;
+  return "";
+}
+
 std::string build_topology(int Nv, int K, const int32_t* etov, int nbc, const int32_t* bc_v1,
                            const int32_t* bc_v2, const int32_t* bc_flag, Topology* t) {
   t->K = K;
@@ -56,19 +165,33 @@ std::string build_topology(int Nv, int K, const int32_t* etov, int nbc, const in
     }
   }
   t->nEdges = static_cast<int>(t->key.size());
+  t->keyR = t->key;
+  // Periodic tags: the edges of each (group, flag) in input order.
+  std::vector<std::pair<int, std::vector<int>>> periodic;
   for (int i = 0; i < nbc; ++i) {
-    const int flag = bc_flag[i];
+    const int flag = bc_flag[i] & 0xff, group = bc_flag[i] >> 8;
     auto it = index.find(edge_key(bc_v1[i], bc_v2[i]));
     if (it == index.end()) return "boundary condition names an edge that is not in the mesh";
     switch (flag) {
       case BC_Far: case BC_IVortex: case BC_Wall: case BC_In: case BC_Out: case BC_Cyl:
+        if (group != 0) return "boundary flag " + std::to_string(bc_flag[i]) + ": group bits on a non-periodic BC";
         t->bc[it->second] = flag;
         break;
+      case BC_Periodic: case BC_PeriodicReversed: {
+        const int gk = (group << 8) | flag;
+        auto g = std::find_if(periodic.begin(), periodic.end(), [&](const auto& x) { return x.first == gk; });
+        if (g == periodic.end()) {
+          periodic.emplace_back(gk, std::vector<int>());
+          g = periodic.end() - 1;
+        }
+        g->second.push_back(it->second);
+        break;
+      }
       default:
         return "boundary condition type not implemented: " + std::to_string(flag);
     }
   }
-  return "";
+  return pair_periodic(periodic, t);
 }
 
 void build_geometry(const DFRElement& el, const Topology& t, const double* vx, const double* vy,
@@ -92,11 +215,13 @@ void build_geometry(const DFRElement& el, const Topology& t, const double* vx, c
   g->ny.assign(3 * static_cast<size_t>(K), 0.0);
   g->IInII.assign(3 * static_cast<size_t>(K), 0.0);
   for (int en = 0; en < t.nEdges; ++en) {
-    const int lo = static_cast<int>(t.key[en] & 0xffffffffULL);
-    const int hi = static_cast<int>(t.key[en] >> 32);
     for (int c = 0; c < 2; ++c) {
       const int k = c == 0 ? t.kL[en] : t.kR[en];
       if (k < 0) continue;
+      // each side's own edge (a periodic pair's right side has its own key)
+      const uint64_t key = (c == 0) ? t.key[en] : t.keyR[en];
+      const int lo = static_cast<int>(key & 0xffffffffULL);
+      const int hi = static_cast<int>(key >> 32);
       const int ed = c == 0 ? t.eL[en] : t.eR[en];
       const bool rev = (c == 0 ? t.revL[en] : t.revR[en]) != 0;
       // Vertices ordered opposite to the element's traversal: (-dy, dx) points out.
@@ -171,8 +296,17 @@ struct Lines {
 };
 
 void add_bc(MeshFile* m, const std::string& tag, int a, int b) {
-  const int f = bc_flag_of_tag(tag);
+  int f = bc_flag_of_tag(tag);
   if (f < 0) throw std::runtime_error("unable to find BC with base name, full tag: [" + tag + "]");
+  if (f == BC_Periodic || f == BC_PeriodicReversed) {
+    // one group per periodic tag (BCMAP keys it by the full tag, types/cfd.go:43)
+    std::string low;
+    for (char ch : tag) low.push_back(static_cast<char>(std::tolower(static_cast<unsigned char>(ch))));
+    auto it = std::find(m->periodicTags.begin(), m->periodicTags.end(), low);
+    const int g = static_cast<int>(it - m->periodicTags.begin());
+    if (it == m->periodicTags.end()) m->periodicTags.push_back(low);
+    f |= g << 8;
+  }
   m->bc_v1.push_back(a);
   m->bc_v2.push_back(b);
   m->bc_flag.push_back(f);

@@ -12,6 +12,7 @@
 #pragma once
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "dfr_element.hpp"
@@ -36,6 +37,7 @@ enum BCFlag : int {
 struct Topology {
   int K = 0, Nv = 0, nEdges = 0;
   std::vector<uint64_t> key;            // packed vertex pair
+  std::vector<uint64_t> keyR;           // the right side's own edge (differs from key on periodic pairs)
   std::vector<int> kL, eL, kR, eR;      // kR = eR = -1 on boundary edges
   std::vector<uint8_t> revL, revR;      // traversal direction flag per connection
   std::vector<int> bc;                  // BCFlag per edge
@@ -50,8 +52,13 @@ struct Geometry {
 };
 
 // Builds the edge table.  Returns an empty string on success, else a message.
+// Boundary flags are BCFLAGs; periodic ones (10, 11) carry a group number in
+// bits 8 and up (one group per periodic tag), and each group's edges are
+// paired into shared edges (pair_periodic).
 std::string build_topology(int Nv, int K, const int32_t* etov, int nbc, const int32_t* bc_v1,
                            const int32_t* bc_v2, const int32_t* bc_flag, Topology* topo);
+
+std::string pair_periodic(const std::vector<std::pair<int, std::vector<int>>>& groups, Topology* t);
 
 void build_geometry(const DFRElement& el, const Topology& topo, const double* vx,
                     const double* vy, const int32_t* etov, Geometry* geo);
@@ -71,7 +78,8 @@ inline void element_point(const int32_t* etov, const double* vx, const double* v
 struct MeshFile {
   std::vector<double> vx, vy;
   std::vector<int32_t> etov;  // K x 3
-  std::vector<int32_t> bc_v1, bc_v2, bc_flag;
+  std::vector<int32_t> bc_v1, bc_v2, bc_flag;  // periodic flags carry their tag's group in bits 8..
+  std::vector<std::string> periodicTags;       // group -> tag
 };
 
 // BC tag -> BCFLAG as types.BCNameMap (types/cfd.go:28-73): the part of the tag

@@ -329,6 +329,42 @@ class Euler:
             self._ptrs(out), qinf, C.byref(tb)))
         return self.unshard(out), np.array(qinf[:]), tb.value
 
+    # -- post-processing -----------------------------------------------------------
+    def sample_points(self, x, y):
+        """The state interpolated at points (x, y) (gcfd_sample_points; the Sod line
+        samples of shock_tube.go:27-142): (4 x npts array, containing elements)."""
+        x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+        y = np.ascontiguousarray(y, dtype=np.float64).ravel()
+        q = np.zeros((4, x.size))
+        el = np.zeros(x.size, np.int32)
+        _lib.check(self.lib, self.ctx, self.lib.gcfd_sample_points(
+            self.ctx, x.size, x.ctypes.data_as(_lib.PD), y.ctypes.data_as(_lib.PD), q.ctypes.data_as(_lib.PD),
+            el.ctypes.data_as(_lib.PI)))
+        return q, el
+
+    def sod_line(self, npts: int):
+        """NewSODShockTube's samples (shock_tube.go:27-49): npts x locations equally spaced
+        on [0, 1] (the ends moved 1e-5 inward) along the mesh's mid-height line; returns
+        (x, 4 x npts state)."""
+        x = np.arange(npts) / (npts - 1.0)
+        x[0] += 1e-5
+        x[-1] -= 1e-5
+        ymid = 0.5 * (self.mesh.VY.max() - self.mesh.VY.min()) + self.mesh.VY.min()
+        q, _ = self.sample_points(x, np.full(npts, ymid))
+        return x, q
+
+    def wall_points(self):
+        """Wall data of OutputFinal (euler.go:251-316; gcfd_wall_points): x, y, state
+        (4 x npts) and pressure at every Wall/Cyl edge flux point."""
+        n = C.c_int32(0)
+        _lib.check(self.lib, self.ctx, self.lib.gcfd_wall_points(self.ctx, C.byref(n), None, None, None, None))
+        x, y, p = np.zeros(n.value), np.zeros(n.value), np.zeros(n.value)
+        q = np.zeros((4, n.value))
+        _lib.check(self.lib, self.ctx, self.lib.gcfd_wall_points(
+            self.ctx, C.byref(n), x.ctypes.data_as(_lib.PD), y.ctypes.data_as(_lib.PD), q.ctypes.data_as(_lib.PD),
+            p.ctypes.data_as(_lib.PD)))
+        return x, y, q, p
+
     def step(self, nsteps: int = 1):
         """Advance nsteps; returns dict(time, dt, resid_max, resid_absmax, resid_rms)."""
         t, dt = C.c_double(), C.c_double()

@@ -29,13 +29,17 @@ def bc_flag(tag: str) -> int:
     return BC_FLAGS[base]
 
 
+PERIODIC_FLAGS = (10, 11)
+
+
 @dataclass
 class Mesh:
     VX: np.ndarray                 # Nv
     VY: np.ndarray
     EToV: np.ndarray               # K x 3, int32, 0-based
-    bc_edges: list = field(default_factory=list)   # (v1, v2, flag)
+    bc_edges: list = field(default_factory=list)   # (v1, v2, flag); periodic flags | group << 8
     bc_tags: dict = field(default_factory=dict)    # tag -> list of (v1, v2)
+    periodic_tags: list = field(default_factory=list)  # group -> periodic tag
 
     @property
     def K(self) -> int:
@@ -52,7 +56,13 @@ class Mesh:
 
 def _add_bc(mesh: Mesh, tag: str, pairs):
     flag = bc_flag(tag)
-    mesh.bc_tags.setdefault(tag.lower(), []).extend(pairs)
+    low = tag.strip().lower()
+    if flag in PERIODIC_FLAGS:
+        # one group per periodic tag (the reference's BCMAP is keyed by the full tag, types/cfd.go:43)
+        if low not in mesh.periodic_tags:
+            mesh.periodic_tags.append(low)
+        flag |= mesh.periodic_tags.index(low) << 8
+    mesh.bc_tags.setdefault(low, []).extend(pairs)
     mesh.bc_edges.extend((int(a), int(b), flag) for a, b in pairs)
 
 
@@ -207,6 +217,15 @@ def vortex_box(n: int, *, jitter: float = 0.0, seed: int = 0) -> Mesh:
     return structured_triangles(n, n, -5.0, 5.0, -5.0, 5.0, jitter=jitter, seed=seed)
 
 
+def periodic_box(n: int, *, L: float = 10.0, jitter: float = 0.0, seed: int = 0) -> Mesh:
+    """[-L/2, L/2]^2 with n x n quads, periodic in x (tag periodic-1: the right
+    side's edges, then the left side's, both listed bottom to top) and in y
+    (periodic-2: bottom, then top, both left to right), so NewTriangulation's
+    pairing matches edges at the same y (x).  Boundary nodes are not jittered."""
+    return structured_triangles(n, n, -0.5 * L, 0.5 * L, -0.5 * L, 0.5 * L, jitter=jitter, seed=seed,
+                                tags=("periodic-2", "periodic-1", "periodic-2", "periodic-1"))
+
+
 def sod_channel(nx: int = 2000, ny: int = 100) -> Mesh:
     """[0,1] x [0,0.05]: inflow left, outflow right, walls top and bottom."""
     return structured_triangles(nx, ny, 0.0, 1.0, 0.0, 0.05, tags=("wall", "out", "wall", "in"))
@@ -236,6 +255,8 @@ def write_gambit(mesh: Mesh, path: str):
         for fidx, (p, q) in enumerate(((v[0], v[1]), (v[1], v[2]), (v[2], v[0]))):
             face_of[(min(p, q), max(p, q))] = (k, fidx)
     names = {v: k for k, v in BC_FLAGS.items() if k not in ("inflow", "outflow")}
+    for g, tag in enumerate(mesh.periodic_tags):
+        names[bc_flag(tag) | (g << 8)] = tag
     with open(path, "w") as f:
         f.write("CONTROL INFO 2.0.0\n** GAMBIT NEUTRAL FILE\ngcfd\nPROGRAM: gcfd\nDATE\n")
         f.write("     NUMNP     NELEM     NGRPS    NBSETS     NDFCD     NDFVL\n")

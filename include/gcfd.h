@@ -47,10 +47,16 @@ enum { GCFD_LIMITER_NONE = 0, GCFD_LIMITER_PERSSON_C0 = 1 };
  * residual scalars); TF32X3 is the same path with the divergence GEMM on the
  * tensor cores as three TF32 products (hi*hi + hi*lo + lo*hi). */
 enum { GCFD_PREC_FP64 = 0, GCFD_PREC_FP32 = 1, GCFD_PREC_TF32X3 = 2 };
-/* BC flags, numbered as types.BCFLAG (types/cfd.go:11-26). */
+/* BC flags, numbered as types.BCFLAG (types/cfd.go:11-26).  A periodic flag
+ * carries its tag's group in bits 8 and up (flag | group << 8: one group per
+ * periodic tag, e.g. "periodic-1", "periodic-2"); the edges of a group are
+ * paired as NewTriangulation pairs them (DG2D/triangulation.go:63-99): the
+ * first half and the second half of the group's list, each ordered as a
+ * connected curve from its first edge (the second half from its last edge for
+ * PERIODIC_REVERSED), edge i with edge i, each pair becoming one shared edge. */
 enum {
   GCFD_BC_NONE = 0, GCFD_BC_IN = 1, GCFD_BC_FAR = 4, GCFD_BC_WALL = 5, GCFD_BC_CYL = 6,
-  GCFD_BC_OUT = 8, GCFD_BC_IVORTEX = 9
+  GCFD_BC_OUT = 8, GCFD_BC_IVORTEX = 9, GCFD_BC_PERIODIC = 10, GCFD_BC_PERIODIC_REVERSED = 11
 };
 
 /* Triangle mesh as readfiles.ReadGambit2d / ReadSU2 return it
@@ -152,9 +158,9 @@ int gcfd_enqueue_steps(gcfd_ctx* ctx, int32_t nsteps);
 int gcfd_get_stream(gcfd_ctx* ctx, void** stream);
 
 /* Implementation choices of a context; no counterpart in the reference.
- * GCFD_OPT_STAGE_PIPELINE: 1 (the default) runs the mixed path's stage update
- * as the persistent kernel whose element inputs are double-buffered by TMA
- * copies (used when K % 4 == 0); 0 selects the one-block-per-CTA kernel.
+ * GCFD_OPT_STAGE_PIPELINE: 1 runs the mixed path's stage update as the
+ * persistent kernel whose element inputs are double-buffered by TMA copies
+ * (used when K % 4 == 0); 0 (the default) keeps the one-block-per-CTA kernel.
  * Setting an option records the per-step CUDA graph again.  Reading
  * GCFD_OPT_STAGE_PIPELINE gives 1 only while the pipelined kernel runs. */
 #define GCFD_OPT_STAGE_PIPELINE 1
@@ -219,6 +225,32 @@ int gcfd_record_steps(gcfd_ctx* ctx, int32_t nsteps, int32_t checkpoint_every, d
 int gcfd_step_vjp(gcfd_ctx* ctx, int32_t nshards, const int32_t* Kmax, const double* const* Qfinal_bar,
                   double tfinal_bar, double* const* Q0_bar, double* qinf_bar4, double* t0_bar);
 
+/* ---- Post-processing of the current state ---- */
+
+/* The solution interpolated at npts points (x[p], y[p]) by the element's own
+ * polynomial (the Lagrange basis of its solution points at the point's
+ * reference coordinates), replacing the sampled lines of the Sod validation
+ * (NewSODShockTube / InterpolateFields,
+ * model_problems/Euler2D/sod_shock_tube/shock_tube.go:27-142).  q4 receives
+ * 4 x npts values (variable-major: rho, rhoU, rhoV, E); elem (may be NULL)
+ * the containing element of each point, or -1.  A point on a shared edge or
+ * vertex takes the element with the lowest index.  GCFD_ERR_ARG when a point
+ * lies in no element.  The reference maps the barycentric coordinates of the
+ * point straight to the element's (r, s) (getUVCoords, shock_tube.go:81-128),
+ * which samples a different point of the element; this call samples the
+ * point itself. */
+int gcfd_sample_points(gcfd_ctx* ctx, int32_t npts, const double* x, const double* y, double* q4,
+                       int32_t* elem);
+
+/* The wall data of OutputFinal (model_problems/Euler2D/euler.go:251-316): for
+ * every Wall or Cyl boundary edge (in the mesh's order) and each of its NpEdge
+ * edge flux points (one point per edge at N = 0), the point's coordinates, the
+ * state interpolated there from the wall element's solution points (4 x npts,
+ * variable-major) and the pressure.  With x, y, q4 and p all NULL only *npts
+ * is set (the count); otherwise *npts gives the room in each array on entry
+ * and the count on return.  Any of x, y, q4, p may be NULL. */
+int gcfd_wall_points(gcfd_ctx* ctx, int32_t* npts, double* x, double* y, double* q4, double* p);
+
 /* Residual norms of an increment array that the caller owns, computed without
  * allocating anything.  This entry point has no counterpart in the reference.
  *
@@ -243,10 +275,14 @@ int gcfd_step_vjp(gcfd_ctx* ctx, int32_t nshards, const int32_t* Kmax, const dou
  * reads is written earlier in the same call, so nothing carries over from one
  * call to the next.  All calls on a device share the array: calls that can
  * overlap on the GPU (other streams, other host threads) race and must be
- * serialised by the caller.  The first call on each device looks up the
- * array's device address (cudaGetSymbolAddress, which can load the module);
- * make that first call before any stream capture.  GCFD_ERR_NAN when an
- * increment is not finite (the outputs are still written). */
+ * serialised by the caller.  The call blocks on the stream (it copies the 12
+ * results to the host and synchronises), so it must not be called on a
+ * stream that is being captured into a CUDA graph.  The first call on each
+ * device, and the first after that device's context was destroyed and
+ * recreated (cudaDeviceReset), looks up the array's device address
+ * (cudaGetSymbolAddress, which can load the module) and so costs more than
+ * the later ones.  GCFD_ERR_NAN when an increment is not finite (the outputs
+ * are still written). */
 #define GCFD_RESID_STATIC_MAX_POINTS 33554432 /* 16384 blocks x 2048 points */
 int gcfd_residual_norms_static(const double* dR, int32_t Np, int32_t K, void* stream, double* resid_max4,
                                double* resid_absmax4, double* resid_rms4);

@@ -323,6 +323,51 @@ class Geometry:
     EtoEdge: np.ndarray   # K x 3
 
 
+def _curve(ekeys, edges, reverse):
+    """Curve.ReOrder + AssembleCurve (types/elemental.go:141-240): the edges
+    as one open chain, starting from the first edge (the last with reverse)."""
+    ends_of = {}
+    for e in edges:
+        for v in (int(ekeys[e]) & 0xFFFFFFFF, int(ekeys[e]) >> 32):
+            ends_of.setdefault(v, []).append(e)
+    dangling = sorted(v for v, es in ends_of.items() if len(es) == 1)
+    if len(dangling) != 2 or any(len(es) > 2 for es in ends_of.values()):
+        raise ValueError("periodic edges do not form one open curve")
+    start = edges[-1] if reverse else edges[0]
+    if all(len(ends_of[v]) == 2 for v in (int(ekeys[start]) & 0xFFFFFFFF, int(ekeys[start]) >> 32)):
+        start = ends_of[dangling[0]][0]
+    chain = [start]
+    verts = (int(ekeys[start]) & 0xFFFFFFFF, int(ekeys[start]) >> 32)
+    tip = verts[0] if len(ends_of[verts[0]]) == 2 else verts[1]
+    while len(ends_of[tip]) == 2:
+        nxt = [e for e in ends_of[tip] if e != chain[-1]][0]
+        chain.append(nxt)
+        a, b = int(ekeys[nxt]) & 0xFFFFFFFF, int(ekeys[nxt]) >> 32
+        tip = b if a == tip else a
+    if len(chain) != len(edges):
+        raise ValueError("periodic edges do not form one open curve")
+    return chain
+
+
+def _pair_periodic(groups, ekeys, kL, eL, kR, eR, edge_of):
+    """Periodic pairing of NewTriangulation (triangulation.go:63-99): per tag,
+    the first and second halves of its edge list as curves, edge i of one
+    shared with edge i of the other (second element = right side; its edge
+    slot points at the shared edge).  Returns the edges that remain."""
+    gone = np.zeros(len(ekeys), bool)
+    for flag, lst in groups.items():
+        if len(lst) % 2:
+            raise ValueError("periodic boundaries must be present in pairs")
+        h = len(lst) // 2
+        c1 = _curve(ekeys, lst[:h], False)
+        c2 = _curve(ekeys, lst[h:], (flag & 0xFF) == 11)
+        for e1, e2 in zip(c1, c2):
+            kR[e1], eR[e1] = kL[e2], eL[e2]
+            edge_of[kL[e2] * 3 + eL[e2]] = e1
+            gone[e2] = True
+    return np.flatnonzero(~gone)
+
+
 def build_geometry(el: Element, VX, VY, EToV, bc_edges) -> Geometry:
     """NewTriangulation + ProcessGeometry + GetEdgeLengths
     (triangulation.go:19-171, dfr_startup.go:125-175,256-314).
@@ -361,11 +406,23 @@ def build_geometry(el: Element, VX, VY, EToV, bc_edges) -> Geometry:
     eR[edge_of[sec]] = sec % 3
     ekeys = uniq[order]
     bcf = np.zeros(nE, np.int64)
+    edge_of = edge_of.copy()
     if bc_edges is not None and len(bc_edges):
         lookup = {int(k): i for i, k in enumerate(ekeys)}
+        groups = {}
         for (v1, v2, flag) in bc_edges:
             kk = min(v1, v2) + (max(v1, v2) << 32)
-            bcf[lookup[kk]] = flag
+            if (flag & 0xFF) in (10, 11):      # BC_Periodic, BC_PeriodicReversed: group in bits 8..
+                groups.setdefault(flag, []).append(lookup[kk])
+            else:
+                bcf[lookup[kk]] = flag
+        if groups:
+            keep = _pair_periodic(groups, ekeys, kL, eL, kR, eR, edge_of)
+            ekeys, kL, eL, kR, eR, bcf = (x[keep] for x in (ekeys, kL, eL, kR, eR, bcf))
+            renum = -np.ones(nE, np.int64)
+            renum[keep] = np.arange(len(keep))
+            edge_of = renum[edge_of]
+            nE = len(keep)
     # Jacobian (dfr_startup.go:256-287)
     v1, v2, v3 = EToV[:, 0], EToV[:, 1], EToV[:, 2]
     xr, yr = 0.5 * (VX[v2] - VX[v1]), 0.5 * (VY[v2] - VY[v1])

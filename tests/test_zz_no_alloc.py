@@ -56,6 +56,37 @@ def test_static_norms_match_step_norms_twice():
             assert np.all(ab > 0.0)
 
 
+@pytest.mark.parametrize("Np,K", [(16, 40000), (16, 33554432 // 16 - 3)])
+def test_static_norms_of_random_increments(Np, K):
+    """Sizes with more than 256 first-pass blocks (the second pass loops) and
+    just under the fixed limit, against torch's own FP64 reductions; after one
+    warm-up call (module loading), repeated calls leave the device's free
+    memory unchanged, i.e. they allocate nothing."""
+    torch = pytest.importorskip("torch")
+    lib = _lib.load()
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(11)
+    dR = torch.randn((4, Np, K), dtype=torch.float64, device="cuda", generator=gen)
+    dR[1] *= 1e-3
+    dR[3] += 0.5
+    stream = torch.cuda.current_stream().cuda_stream
+    static_norms(lib, dR, Np, K, stream)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    outs = [static_norms(lib, dR, Np, K, stream) for _ in range(3)]
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    flat = dR.reshape(4, -1)
+    ref_mx = flat.amax(dim=1).cpu().numpy()
+    ref_ab = flat.abs().amax(dim=1).cpu().numpy()
+    ref_rms = torch.sqrt((flat * flat).sum(dim=1) / flat.shape[1]).cpu().numpy()
+    for mx, ab, rms in outs:
+        assert np.array_equal(mx, ref_mx)
+        assert np.array_equal(ab, ref_ab)
+        assert np.allclose(rms, ref_rms, rtol=1e-12, atol=0), (rms, ref_rms)
+        assert np.array_equal(rms, outs[0][2])  # fixed reduction order: same bits every call
+
+
 def test_static_norms_reject_sizes_beyond_the_limit():
     torch = pytest.importorskip("torch")
     lib = _lib.load()
