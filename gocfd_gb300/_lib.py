@@ -32,7 +32,7 @@ EXPORTS = [
     "gcfd_get_time", "gcfd_rhs", "gcfd_step", "gcfd_enqueue_steps", "gcfd_get_stream", "gcfd_set_option",
     "gcfd_get_option", "gcfd_profile_step",
     "gcfd_host_operator", "gcfd_read_mesh", "gcfd_free_mesh", "gcfd_residual_norms_static", "gcfd_functional", "gcfd_rhs_vjp",
-    "gcfd_record_steps", "gcfd_step_vjp", "gcfd_sample_points", "gcfd_wall_points",
+    "gcfd_record_steps", "gcfd_step_vjp", "gcfd_sample_points", "gcfd_wall_points", "gcfd_device_fma_peaks",
 ]
 
 
@@ -111,6 +111,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         lib.gcfd_step_vjp.argtypes = [C.c_void_p, C.c_int32, PI, C.POINTER(PD), C.c_double, C.POINTER(PD), PD, PD]
         lib.gcfd_sample_points.argtypes = [C.c_void_p, C.c_int32, PD, PD, PD, PI]
         lib.gcfd_wall_points.argtypes = [C.c_void_p, PI, PD, PD, PD, PD]
+        lib.gcfd_device_fma_peaks.argtypes = [C.c_int32, PD, PD]
         _lib = lib
         return lib
 
@@ -145,3 +146,11 @@ def host_operator(N: int, which: int) -> np.ndarray:
     out = np.zeros((rows.value, cols.value), dtype=np.float64)
     check(lib, None, lib.gcfd_host_operator(N, which, out.ctypes.data_as(PD), C.byref(rows), C.byref(cols)))
     return out
+
+
+def device_fma_peaks(device: int = 0):
+    """(FP64, FP32) SIMT FMA rates of the device in TFLOP/s (gcfd_device_fma_peaks)."""
+    lib = load()
+    f64, f32 = C.c_double(), C.c_double()
+    check(lib, None, lib.gcfd_device_fma_peaks(int(device), C.byref(f64), C.byref(f32)))
+    return f64.value, f32.value

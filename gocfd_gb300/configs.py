@@ -185,7 +185,11 @@ def run(name: str, precision: str = "fp64", scale: float = 1.0, device: int = 0,
                 steps += 50
                 rel = float(np.max(np.array(info["resid_rms"]) / qn))
                 if report_every and steps % report_every == 0:
-                    hist.append((steps, rel))
+                    # absolute increment RMS per variable, and relative to the current state's RMS
+                    qc = np.sqrt(np.mean(s.get_global_state() ** 2, axis=(1, 2)))
+                    hist.append({"step": steps, "rel_initial_floored": rel,
+                                 "abs_rms": [float(v) for v in info["resid_rms"]],
+                                 "rel_current": [float(v) for v in np.array(info["resid_rms"]) / qc]})
                 if rel < cfg.residual_tol:
                     break
             out.update(steps=steps, residual_rel_rms=rel, converged=bool(rel < cfg.residual_tol), history=hist)

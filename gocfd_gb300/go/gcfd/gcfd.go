@@ -274,3 +274,53 @@ func (c *Context) RHSBackward(t float64, Q, RHSbar, Qbar [][4][]float64, Kmax []
 	}
 	return qinfBar, float64(tt), err
 }
+
+// Periodic boundary flags: a periodic tag's edges carry BCPeriodic (or
+// BCPeriodicReversed) with the tag's group in bits 8 and up, e.g.
+// PeriodicFlag(BCPeriodic, 1) for the second periodic tag of the mesh.
+const (
+	BCPeriodic         = int32(C.GCFD_BC_PERIODIC)
+	BCPeriodicReversed = int32(C.GCFD_BC_PERIODIC_REVERSED)
+)
+
+// PeriodicFlag returns the BC flag of group g of a periodic kind.
+func PeriodicFlag(kind int32, g int) int32 { return kind | int32(g)<<8 }
+
+// SamplePoints interpolates the current state at the points (x[p], y[p]):
+// q[n][p] for the four variables, and each point's element (the Sod line
+// samples of sod_shock_tube.NewSODShockTube / InterpolateFields).
+func (c *Context) SamplePoints(x, y []float64) (q [4][]float64, elem []int32, err error) {
+	n := len(x)
+	if len(y) != n {
+		return q, nil, fmt.Errorf("gcfd: SamplePoints: %d x and %d y values", n, len(y))
+	}
+	flat := make([]float64, 4*n)
+	elem = make([]int32, n)
+	if n > 0 {
+		err = status(c.ctx, C.gcfd_sample_points(c.ctx, C.int32_t(n), (*C.double)(unsafe.Pointer(&x[0])),
+			(*C.double)(unsafe.Pointer(&y[0])), (*C.double)(unsafe.Pointer(&flat[0])),
+			(*C.int32_t)(unsafe.Pointer(&elem[0]))))
+	}
+	for v := 0; v < 4; v++ {
+		q[v] = flat[v*n : (v+1)*n]
+	}
+	return q, elem, err
+}
+
+// WallPoints returns the wall data OutputFinal writes: coordinates, state and
+// pressure at every Wall/Cyl edge point.
+func (c *Context) WallPoints() (x, y []float64, q [4][]float64, p []float64, err error) {
+	var n C.int32_t
+	if err = status(c.ctx, C.gcfd_wall_points(c.ctx, &n, nil, nil, nil, nil)); err != nil || n == 0 {
+		return
+	}
+	m := int(n)
+	x, y, p = make([]float64, m), make([]float64, m), make([]float64, m)
+	flat := make([]float64, 4*m)
+	err = status(c.ctx, C.gcfd_wall_points(c.ctx, &n, (*C.double)(unsafe.Pointer(&x[0])),
+		(*C.double)(unsafe.Pointer(&y[0])), (*C.double)(unsafe.Pointer(&flat[0])), (*C.double)(unsafe.Pointer(&p[0]))))
+	for v := 0; v < 4; v++ {
+		q[v] = flat[v*m : (v+1)*m]
+	}
+	return
+}

@@ -173,6 +173,12 @@ int gcfd_get_option(const gcfd_ctx* ctx, int32_t option, int32_t* value);
  * bookkeeping.  Used to attribute time for the roofline. */
 int gcfd_profile_step(gcfd_ctx* ctx, double* kernel_ms4, int32_t* launches4);
 
+/* SIMT FMA rates of the device (TFLOP/s, FMA = 2 flops), measured by
+ * independent FMA chains on every SM: the compute roofline of the FP64 path's
+ * kernels and of the mixed path's FP32 arithmetic.  No counterpart in the
+ * reference.  Either output may be NULL. */
+int gcfd_device_fma_peaks(int32_t device, double* fp64_tflops, double* fp32_tflops);
+
 /* Host-only (no GPU needed): the FP64 operator matrices built for order N.
  * which: 0 FluxEdgeInterp (3NpEdge x Np), 1 DivInt (Np x NpFlux),
  * 2 Div (NpFlux x NpFlux), 3 V (Np x Np), 4 solution r,s (Np x 2),
