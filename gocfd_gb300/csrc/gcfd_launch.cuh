@@ -2,7 +2,6 @@
 // and arithmetic: Launch<N, double> (FP64 path) and MixedLaunch<N> (mixed
 // path).  Included by the per-order translation units only.
 #pragma once
-#include <cstdlib>
 #include "gcfd_ctx.hpp"
 #include "gcfd_diss.cuh"
 #include "gcfd_kernels.cuh"
@@ -299,11 +298,8 @@ struct MixedLaunch {
         k_mixed_stage_pipe<N, false><<<g, 128, c->pipeSmem, c->stream>>>(c->pipeMaps, a);
       return;
     }
-    static const bool useOld = getenv("GCFD_TMP_OLD_STAGE") != nullptr;  // TEMP A/B
     if (c->tc)
       k_mixed_stage_tc<N><<<gridE(c), 128, c->tcDynSmem, c->stream>>>(a);
-    else if (useOld)
-      k_mixed_stage_old<N><<<gridE(c), 128, 0, c->stream>>>(a);
     else
       k_mixed_stage<N><<<gridE(c), 128, 0, c->stream>>>(a);
   }

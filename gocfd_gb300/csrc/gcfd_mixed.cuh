@@ -879,45 +879,43 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const int eslot[3
   }
 }
 
-// Interior transformed delta fluxes of variable V at every solution point and
+// Interior transformed delta fluxes of variable n at every solution point and
 // their divergence columns (DivInt columns 0..2NP-1), accumulated into the
 // output pairs acc.  The stage delta at point i is d = dQ0 + (D_s - D_s(0))
-// (from shared memory); its velocity and pressure deltas come precomputed from
-// shared memory (spr), so the element's four variable warps share them.
-template <int N, int V>
-__device__ __forceinline__ void interior_columns(const BasePrim& b, const float (*sq0)[MixedDims<N>::NP][32],
+// (from shared memory); its velocity and pressure deltas du, dv, dp come from
+// shared memory (spr), computed once per element.  The four variables' delta
+// fluxes share one form,
+//     dFx = Px wx + sx (Bx + wx) + cx,   dFy = Py wy + sy (By + wy) + cy,
+// with per-variable choices (n = 0: sx, sy = d1, d2 and w = P = 0, B = 1;
+// n = 1: w = du, s = d1, d2, P = m_b, n_b, B = u_b, cx = dp; n = 2: w = dv,
+// B = v_b, cy = dp; n = 3: s = d3 + dp, wx, wy = du, dv, P = H_b, B = u_b, v_b),
+// so all four warps of a CTA run the same instructions on different operands
+// (the exact algebra of delta_flux_c, regrouped).
+template <int N>
+__device__ __forceinline__ void interior_columns(int n, const BasePrim& b, const float (*sq0)[MixedDims<N>::NP][32],
                                                  const float (*sds)[MixedDims<N>::NP][32],
                                                  const float (*spr)[MixedDims<N>::NP][32], int lane, int s,
                                                  float Jd, float J0, float J1, float J2, float J3, float2 acc[]) {
   constexpr int NP = MixedDims<N>::NP;
-  // the variables flux V reads: rho-u and rho-v momentum deltas, or the energy delta
-  constexpr int C0 = (V == 3) ? 3 : 1, C1 = 2;
-  const float o0 = (s >= 1) ? sds[C0][0][lane] : 0.0f;
-  const float o1 = (s >= 1) ? sds[C1][0][lane] : 0.0f;
+  const int ra = (n == 3) ? 3 : 1, rb = (n == 3) ? 3 : 2;  // rows of sx and sy
+  const int wxr = (n == 2) ? 1 : 0, wyr = (n == 1) ? 0 : 1;  // du or dv
+  const float mw = (n == 0) ? 0.0f : 1.0f;                   // variable 0 has no velocity term
+  const float ms = (n == 3) ? 1.0f : 0.0f;                   // energy: s = d3 + dp
+  const float mcx = (n == 1) ? 1.0f : 0.0f, mcy = (n == 2) ? 1.0f : 0.0f;
+  const float Px = (n == 3) ? b.H : ((n == 0) ? 0.0f : b.m);
+  const float Py = (n == 3) ? b.H : ((n == 0) ? 0.0f : b.n);
+  const float Bx = (n == 0) ? 1.0f : ((n == 2) ? b.v : b.u);
+  const float By = (n == 0) ? 1.0f : ((n == 1) ? b.u : b.v);
+  const float oa = (s >= 1) ? sds[ra][0][lane] : 0.0f;
+  const float ob = (s >= 1) ? sds[rb][0][lane] : 0.0f;
 #pragma unroll
   for (int i = 0; i < NP; ++i) {
-    const float da = sq0[C0][i][lane] + ((s >= 1) ? sds[C0][i][lane] - o0 : 0.0f);
-    float fx, fy;
-    if constexpr (V == 0) {
-      const float db = sq0[C1][i][lane] + ((s >= 1) ? sds[C1][i][lane] - o1 : 0.0f);
-      fx = da;
-      fy = db;
-    } else if constexpr (V == 1) {
-      const float db = sq0[C1][i][lane] + ((s >= 1) ? sds[C1][i][lane] - o1 : 0.0f);
-      const float du = spr[0][i][lane], dp = spr[2][i][lane];
-      fx = b.m * du + da * b.u + da * du + dp;
-      fy = b.n * du + db * b.u + db * du;
-    } else if constexpr (V == 2) {
-      const float db = sq0[C1][i][lane] + ((s >= 1) ? sds[C1][i][lane] - o1 : 0.0f);
-      const float dv = spr[1][i][lane], dp = spr[2][i][lane];
-      fx = b.m * dv + da * b.v + da * dv;
-      fy = b.n * dv + db * b.v + db * dv + dp;
-    } else {
-      const float du = spr[0][i][lane], dv = spr[1][i][lane], dp = spr[2][i][lane];
-      const float dH = da + dp;
-      fx = b.u * dH + du * (b.H + dH);
-      fy = b.v * dH + dv * (b.H + dH);
-    }
+    const float dp = spr[2][i][lane];
+    const float sx = fmaf(ms, dp, sq0[ra][i][lane] + ((s >= 1) ? sds[ra][i][lane] - oa : 0.0f));
+    const float sy = fmaf(ms, dp, sq0[rb][i][lane] + ((s >= 1) ? sds[rb][i][lane] - ob : 0.0f));
+    const float wx = mw * spr[wxr][i][lane], wy = mw * spr[wyr][i][lane];
+    const float fx = fmaf(Px, wx, fmaf(sx, Bx + wx, mcx * dp));
+    const float fy = fmaf(Py, wy, fmaf(sy, By + wy, mcy * dp));
     const float Fr = Jd * (J0 * fx + J1 * fy);
     const float Fs = Jd * (J2 * fx + J3 * fy);
     div_column<N>(NP + i, Fs, acc);
@@ -1048,12 +1046,7 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
   float2 acc[NH];
 #pragma unroll
   for (int h = 0; h < NH; ++h) acc[h] = make_float2(0.0f, 0.0f);
-  switch (n) {
-    case 0: interior_columns<N, 0>(b, sq0, sds, spr, lane, s, Jd, J0, J1, J2, J3, acc); break;
-    case 1: interior_columns<N, 1>(b, sq0, sds, spr, lane, s, Jd, J0, J1, J2, J3, acc); break;
-    case 2: interior_columns<N, 2>(b, sq0, sds, spr, lane, s, Jd, J0, J1, J2, J3, acc); break;
-    default: interior_columns<N, 3>(b, sq0, sds, spr, lane, s, Jd, J0, J1, J2, J3, acc); break;
-  }
+  interior_columns<N>(n, b, sq0, sds, spr, lane, s, Jd, J0, J1, J2, J3, acc);
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();  // every thread's record chunks
   float rmax = -3.4028235e38f, rabs = 0.0f;
@@ -1084,141 +1077,6 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
 #pragma unroll
     for (int r = 0; r < NP; ++r) {
       rhs[r] = -((r & 1) ? acc[r >> 1].y : acc[r >> 1].x) * ooJ;
-      dq0[r] = sq0[n][r][lane];
-      ds[r] = (s >= 1) ? sds[n][r][lane] : 0.0f;
-    }
-    stage_tail<N>(a, eslot, n, k, off, sK, s, rhs, dq0, ds, dtk, rmax, rabs, rs2);
-  }
-  if (s == 4 && !a.rhsOnly) {
-    residual_commit(a.sc, n, lane, rmax, rabs, rs2);
-  }
-}
-
-// TEMP A/B: the previous one-block stage kernel
-template <int N>
-__global__ void __launch_bounds__(128, 7) k_mixed_stage_old(MixedArgs a) {
-  constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NPP = MixedDims<N>::NPP;
-  constexpr int NEP = MixedDims<N>::NEP, CH = StageDims<N>::CH, RW = StageDims<N>::RW;
-  __shared__ float sq0[4][NP][33];
-  __shared__ float sds[4][NP][33];
-  __shared__ float sbase[4][32];
-  __shared__ __align__(16) float srec[32 * RW];
-  __shared__ double sdt;
-  const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int k = blockIdx.x * 32 + lane;
-  const bool active = k < a.K;
-  const size_t sK = static_cast<size_t>(a.K);
-  const size_t off = static_cast<size_t>(n) * NP * sK + k;
-  const int s = a.stage;
-  int eslot[3] = {0, 0, 0};
-  float eII[3] = {0.f, 0.f, 0.f};
-  if (active) {
-#pragma unroll
-    for (int e = 0; e < 3; ++e) {
-      eslot[e] = a.eslot[e * sK + k];
-      eII[e] = a.II[e * sK + k];
-    }
-    // Chunks c = n, n+4, ... of the element's 3 x CH record chunks.
-#pragma unroll
-    for (int t = 0; t < (3 * CH + 3) / 4; ++t) {
-      const int c = n + 4 * t;
-      if (c < 3 * CH) {
-        const int e = c / CH, j = c - e * CH;
-        const size_t g = static_cast<size_t>((e == 0 ? eslot[0] : (e == 1 ? eslot[1] : eslot[2])) >> 1);
-        const float* src = (j < NEP) ? a.fhat + g * 4 * NEP + 4 * j : a.corr + g * 4;
-        const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(&srec[lane * RW + 4 * c]));
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src));
-      }
-    }
-  }
-  asm volatile("cp.async.commit_group;\n" ::);
-  stage_tail_prefetch<N>(a, blockIdx.x, n, lane, sK, s);
-  float Jd = 0.f, J0 = 0.f, J1 = 0.f, J2 = 0.f, J3 = 0.f, ooJ = 0.f;
-  if (active) {
-#pragma unroll
-    for (int i = 0; i < NP; ++i) sq0[n][i][lane] = a.dQ0[off + i * sK];
-    if (s >= 1) {
-#pragma unroll
-      for (int i = 0; i < NP; ++i) sds[n][i][lane] = a.D[s][off + i * sK];
-    }
-    sbase[n][lane] = a.base[static_cast<size_t>(k) * 4 + n].x;
-    Jd = a.geo[k];
-    J0 = a.geo[sK + k];
-    J1 = a.geo[2 * sK + k];
-    J2 = a.geo[3 * sK + k];
-    J3 = a.geo[4 * sK + k];
-    ooJ = a.geo[5 * sK + k];
-  }
-  // Local time step of this stage: DT persists across stages, so every thread
-  // of the element reads it before the barrier and one writes it after.
-  double dtk = 0.0;
-  if (active && a.localDT && s >= 0 && !a.rhsOnly) {
-    double v = (s == 0) ? -100.0 : a.DT[k];
-#pragma unroll
-    for (int e = 0; e < 3; ++e) v = fmax(v, a.edgeSpeed[eslot[e] >> 1]);
-    dtk = a.cfl / v;
-  }
-  if (threadIdx.x == 0 && needs_global_dt(a, s)) sdt = global_stage_dt(a, s);
-  __syncthreads();
-  if (needs_global_dt(a, s)) dtk = sdt;
-  float acc[NP];
-#pragma unroll
-  for (int r = 0; r < NP; ++r) acc[r] = 0.0f;
-  if (active) {
-    const float bq[4] = {sbase[0][lane], sbase[1][lane], sbase[2][lane], sbase[3][lane]};
-    const float gm1 = a.gamma - 1.0f;
-    const BasePrim b = base_prim(bq, gm1);
-    float d0[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) d0[c] = (s >= 1) ? sds[c][0][lane] : 0.0f;
-    // Interior transformed delta fluxes, DivInt columns 0..2NP-1; the stage
-    // delta relative to point 0 is dQ0 + (D_s - D_s(point 0)).
-#pragma unroll
-    for (int i = 0; i < NP; ++i) {
-      float d[4];
-#pragma unroll
-      for (int c = 0; c < 4; ++c) d[c] = sq0[c][i][lane] + ((s >= 1) ? sds[c][i][lane] - d0[c] : 0.0f);
-      const DeltaPrim q = delta_prim(b, d, gm1);
-      float fx, fy;
-      delta_flux_c(n, b, d, q, &fx, &fy);
-      const float Fr = Jd * (J0 * fx + J1 * fy);
-      const float Fs = Jd * (J2 * fx + J3 * fy);
-#pragma unroll
-      for (int r = 0; r < NP; ++r)
-        acc[r] = fmaf(div_op<N>(i * NPP + r), Fr, fmaf(div_op<N>((NP + i) * NPP + r), Fs, acc[r]));
-    }
-  }
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-  __syncthreads();  // every thread's record chunks
-  float rmax = -3.4028235e38f, rabs = 0.0f;
-  float2 rs2 = make_float2(0.0f, 0.0f);
-  if (active) {
-    // Edge DOFs: IInII * (s fhat - n_e.F(Qb)), owner order / reversed for the right side.
-#pragma unroll
-    for (int e = 0; e < 3; ++e) {
-      const float* rec = &srec[lane * RW + e * CH * 4];
-      const bool right = eslot[e] & 1;
-      const float ii = eII[e];
-      const float cc = right ? rec[4 * NEP + n] : 0.0f;
-      float v[NEP];
-      const float2* rp = reinterpret_cast<const float2*>(rec + n * NEP);
-#pragma unroll
-      for (int q = 0; q < NEP / 2; ++q) {
-        const float2 t = rp[q];
-        v[2 * q] = t.x;
-        v[2 * q + 1] = t.y;
-      }
-#pragma unroll
-      for (int p = 0; p < NE; ++p) {
-        const float dof = right ? -(v[NE - 1 - p] - cc) * ii : v[p] * ii;
-#pragma unroll
-        for (int r = 0; r < NP; ++r) acc[r] = fmaf(div_op<N>((2 * NP + e * NE + p) * NPP + r), dof, acc[r]);
-      }
-    }
-    float rhs[NP], dq0[NP], ds[NP];
-#pragma unroll
-    for (int r = 0; r < NP; ++r) {
-      rhs[r] = -acc[r] * ooJ;
       dq0[r] = sq0[n][r][lane];
       ds[r] = (s >= 1) ? sds[n][r][lane] : 0.0f;
     }

@@ -424,7 +424,10 @@ def test_segment_tape_matches_per_step_recompute(limiter, local_dt):
     """A window with several steps per checkpoint segment keeps each recomputed
     step's tape (one slot per step, faces rebuilt from the stage states); one
     step per segment tapes each step as it is reversed.  Both run the same
-    kernels on the same states, so the adjoints agree bit for bit."""
+    kernels on the same states; they differ only where the adjoint sums over
+    the mesh with atomics (the global time step's adjoint), in the order of
+    those FP64 additions, so they agree to round-off (1e-12 of the largest
+    entry), as two sweeps of one window do."""
     if limiter:
         mesh = meshes.sod_channel(24, 3)
         init, minf = "shocktube", 0.0
@@ -446,8 +449,9 @@ def test_segment_tape_matches_per_step_recompute(limiter, local_dt):
             out.append(gpu.step_vjp(Qbf, 0.3))
             # a second reverse sweep of the same window gives the same adjoint
             again = gpu.step_vjp(Qbf, 0.3)
-            assert np.array_equal(again[0], out[-1][0])
+            assert np.abs(again[0] - out[-1][0]).max() <= 1e-12 * np.abs(out[-1][0]).max()
+    scale = np.abs(out[0][0]).max()
     for qb, qinf, tb in out[1:]:
-        assert np.array_equal(qb, out[0][0])
-        assert np.array_equal(qinf, out[0][1])
-        assert tb == out[0][2]
+        assert np.abs(qb - out[0][0]).max() <= 1e-12 * scale
+        assert np.allclose(qinf, out[0][1], rtol=1e-11, atol=1e-12 * scale)
+        assert abs(tb - out[0][2]) <= 1e-11 * max(abs(tb), 1e-300) + 1e-12 * scale

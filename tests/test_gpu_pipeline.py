@@ -93,7 +93,10 @@ def test_pipeline_matches_one_block_partial_block(precision, N):
     mesh = meshes.vortex_box(10, jitter=0.1, seed=4)  # K = 200 = 6 x 32 + 8
     (qa, ia), (qb, ib) = run_both(mesh, N, precision, 20)
     assert_as_accurate(qa, qb, oracle_run(mesh, N, 20), f"K={mesh.K} N={N} {precision}")
-    assert ia["time"] == pytest.approx(ib["time"], rel=1e-6)
+    # dt comes from FP32 wave speeds and the two kernels group the interior delta-flux
+    # algebra differently; at N = 1 (DivInt entries ~1.8e3) their times drift apart
+    # by ~1e-7 per step
+    assert ia["time"] == pytest.approx(ib["time"], rel=5e-6)
     assert np.allclose(ia["resid_rms"], ib["resid_rms"], rtol=1e-3, atol=0)
 
 

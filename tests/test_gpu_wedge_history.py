@@ -5,12 +5,12 @@ side by side for 2,000 steps and their per-step residual histories (RMS of
 the final RK increment per variable, the residual Solve prints,
 euler.go:814-849) are compared.
 
-Both histories flatten out at the same level instead of decaying: the
-reference's scheme itself stops converging there (the shock sensor keeps
-switching the artificial viscosity on elements near the shock).  The test
-checks that the two histories agree step by step to a relative 1e-6 while
-the trajectories stay together, that the plateau is the same, and where the
-residual sits: mostly on elements whose sensor is active.
+Both histories flatten out at the same level (the increment RMS stops
+decaying after ~500 steps) and agree step by step to round-off, with the two
+states still equal to ~1e-12 after 2,000 steps: the plateau belongs to the
+scheme the oracle restates, not to the GPU implementation.  At the end, the
+largest increments sit on a few elements at the top wall downstream of the
+reflected shock, where the shock sensor is off.
 """
 import os
 
@@ -63,9 +63,10 @@ def test_wedge_residual_history_matches_oracle():
     print(f"state rel L2 GPU vs oracle after {STEPS} steps: {state_diff:.3e}")
     print(f"top 1% elements by |R_E| carry {share:.2f} of ||R_E||^2; sensor active on {active_top:.2f} of them;"
           f" centroids x in [{cx.min():.2f}, {cx.max():.2f}], y in [{cy.min():.2f}, {cy.max():.2f}]")
-    # the histories agree while the trajectories agree; the plateau is the oracle's too
-    together = rel.max(axis=1) < 1e-6
-    assert together[: min(200, STEPS)].all(), rel[:200].max()
+    # the histories agree step by step; the states stay together; the plateau is the oracle's too
+    assert rel.max() <= 1e-9, rel.max()
+    assert state_diff <= 1e-10
     late = slice(STEPS // 2, STEPS)
-    assert np.allclose(np.median(hg[late], axis=0), np.median(ho[late], axis=0), rtol=0.2)
-    assert hg[-1, 3] > 1e-3 * hg[0, 3]  # no decay to the steady state: the plateau
+    assert np.allclose(np.median(hg[late], axis=0), np.median(ho[late], axis=0), rtol=1e-6)
+    if STEPS >= 1000:  # no decay towards a steady state after the first few hundred steps
+        assert hg[-1, 3] > 0.5 * hg[STEPS // 4, 3]

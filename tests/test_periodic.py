@@ -92,13 +92,14 @@ def test_periodic_freestream_preserved(precision):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32", 1e-7)])
-def test_periodic_step_parity(precision, tol):
+@pytest.mark.parametrize("precision,tol,ttol", [("fp64", 1e-10, 1e-12), ("fp32", 1e-7, 1e-7)])
+def test_periodic_step_parity(precision, tol, ttol):
+    """FP64: the oracle's trajectory; mixed: its FP32 wave speeds set dt to ~1e-8 relative."""
     mesh = meshes.periodic_box(12, jitter=0.1, seed=6)
     gpu, ora = _pair(mesh, 3, precision=precision)
     info = gpu.step(20)
     t_ora, _, _ = ora.step(20)
-    assert abs(info["time"] - t_ora) <= 1e-9 * t_ora
+    assert abs(info["time"] - t_ora) <= ttol * t_ora
     q = gpu.get_global_state()
     assert np.linalg.norm(q - ora.Q) / np.linalg.norm(ora.Q) <= tol
     gpu.close()
