@@ -77,6 +77,7 @@ struct gcfd_ctx {
   bool dirty = true;  // Q0 changed outside a step: the stage-0 data must be rebuilt
   bool tc = false;     // mixed path with the divergence GEMM on the tensor cores (3xTF32)
   float* mBtc = nullptr;
+  float* mBtcF = nullptr;  // tensor-core path: FluxEdgeInterp split hi / lo (face GEMM operand)
   int tcDynSmem = 0;   // dynamic shared memory that caps the stage kernel's CTAs per SM to its TMEM share
   // persistent TMA-pipelined stage kernel (needs K % 4 == 0 for 16-byte row strides)
   bool pipe = false;   // built and usable

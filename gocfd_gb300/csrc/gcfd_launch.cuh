@@ -279,6 +279,7 @@ struct MixedLaunch {
     a.vgamma = c->vgamma;
     a.rhsOut = c->rhsOut;
     a.Btc = c->mBtc;
+    a.BtcF = c->mBtcF;
     a.DissX32 = reinterpret_cast<const float*>(c->DissX);
     a.DissY32 = reinterpret_cast<const float*>(c->DissY);
     a.VF32 = reinterpret_cast<const float*>(c->VF);

@@ -304,6 +304,7 @@ struct MixedArgs {
   const unsigned long long* gviscS;  // per-stage max viscous speed when the dissipation limits dt
   double cdiff;
   const float* Btc;           // tensor-core path: DivInt split hi / lo in the shared-memory operand layout
+  const float* BtcF;          // tensor-core path: FluxEdgeInterp split hi / lo, the same layout
   const float* DissX32;       // PerssonC0: FP32 eps-gradient rows [4][NR][K] and viscous fluxes [edge][4][NE]
   const float* DissY32;
   const float* VF32;
@@ -406,9 +407,25 @@ __device__ __forceinline__ void div_column(int j, float v, float2 acc[]) {
 // Writes the element's 3 edges of face deltas for variable n (face point
 // q = e*NE + p): out_q = sum_i FluxEdgeInterp[q][i] dq[i], accumulated over i
 // in order.
+// Stores the element's 3 edges of face deltas for variable n from the face
+// values out[q], q = e*NE + p.
+template <int N>
+__device__ __forceinline__ void store_faces(const MixedArgs& a, const int eslot[3], int n, const float out[]) {
+  constexpr int NE = MixedDims<N>::NE, NEP = MixedDims<N>::NEP;
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    float* dst = a.faces + (static_cast<size_t>(eslot[e]) * 4 + n) * NEP;
+    // (slot*4 + n) * NEP floats with NEP even: 8-byte aligned, pairs go out as float2.
+#pragma unroll
+    for (int p = 0; p + 1 < NE; p += 2)
+      reinterpret_cast<float2*>(dst)[p / 2] = make_float2(out[e * NE + p], out[e * NE + p + 1]);
+    if (NE & 1) dst[NE - 1] = out[e * NE + NE - 1];
+  }
+}
+
 template <int N>
 __device__ __forceinline__ void write_faces(const MixedArgs& a, const int eslot[3], int n, const float dq[]) {
-  constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NEP = MixedDims<N>::NEP;
+  constexpr int NP = MixedDims<N>::NP, NE3 = MixedDims<N>::NE3;
   constexpr int NE3P = MixedDims<N>::NE3P, NQ = NE3P / 2;
   float2 out[NQ];
 #pragma unroll
@@ -419,16 +436,10 @@ __device__ __forceinline__ void write_faces(const MixedArgs& a, const int eslot[
 #pragma unroll
     for (int q = 0; q < NQ; ++q) out[q] = ffma2(iop_pair<N>(i * NQ + q), v, out[q]);
   }
-  auto face = [&](int q) { return (q & 1) ? out[q >> 1].y : out[q >> 1].x; };
+  float f[NE3];
 #pragma unroll
-  for (int e = 0; e < 3; ++e) {
-    float* dst = a.faces + (static_cast<size_t>(eslot[e]) * 4 + n) * NEP;
-    // (slot*4 + n) * NEP floats with NEP even: 8-byte aligned, pairs go out as float2.
-#pragma unroll
-    for (int p = 0; p + 1 < NE; p += 2)
-      reinterpret_cast<float2*>(dst)[p / 2] = make_float2(face(e * NE + p), face(e * NE + p + 1));
-    if (NE & 1) dst[NE - 1] = face(e * NE + NE - 1);
-  }
+  for (int q = 0; q < NE3; ++q) f[q] = (q & 1) ? out[q >> 1].y : out[q >> 1].x;
+  store_faces<N>(a, eslot, n, f);
 }
 
 // Stage-0 preparation from the FP64 state: hi/lo split, dQ0, faces, reference states.
@@ -803,11 +814,15 @@ __device__ __forceinline__ bool needs_global_dt(const MixedArgs& a, int s) {
 // the next stage's faces and reference state, and at stage 4 the compensated
 // state and the residual partials.  dtk is the element's time step: its local
 // one with local time stepping, else the stage's global one.
-template <int N>
+//
+// With DeferFaces the next stage's deltas are left in dqnOut instead of being
+// interpolated to the faces here (the tensor-core kernel runs that GEMM on
+// tcgen05 for the whole CTA afterwards).
+template <int N, bool DeferFaces = false>
 __device__ __forceinline__ void stage_tail(const MixedArgs& a, const int eslot[3], int n, int k,
                                            size_t off, size_t sK, int s, const float rhs[], const float dq0[],
                                            const float ds[], double dtk, float& rmax, float& rabs,
-                                           float2& rs2) {
+                                           float2& rs2, float* dqnOut = nullptr) {
   constexpr int NP = MixedDims<N>::NP, NPP = MixedDims<N>::NPP;
   if (s < 0 || a.rhsOnly) {
 #pragma unroll
@@ -843,7 +858,12 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const int eslot[3
       float dqn[NPP];
 #pragma unroll
       for (int r = 0; r < NPP; ++r) dqn[r] = (r < NP) ? dq0[r] + (dn[r] - dn[0]) : 0.0f;
-      write_faces<N>(a, eslot, n, dqn);
+      if constexpr (DeferFaces) {
+#pragma unroll
+        for (int r = 0; r < NPP; ++r) dqnOut[r] = dqn[r];
+      } else {
+        write_faces<N>(a, eslot, n, dqn);
+      }
       float h = a.Qhi[off], l = a.Qlo[off];
       df_add(h, l, dn[0]);
       a.base[static_cast<size_t>(k) * 4 + n] = make_float2(h, l);
@@ -873,7 +893,12 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const int eslot[3
         dqn[r] = df_diff(qh[r], ql[r], qh[0], ql[0]);
         a.dQ0[off + r * sK] = dqn[r];
       }
-      write_faces<N>(a, eslot, n, dqn);
+      if constexpr (DeferFaces) {
+#pragma unroll
+        for (int r = 0; r < NPP; ++r) dqnOut[r] = dqn[r];
+      } else {
+        write_faces<N>(a, eslot, n, dqn);
+      }
       a.base[static_cast<size_t>(k) * 4 + n] = make_float2(qh[0], ql[0]);
     }
   }

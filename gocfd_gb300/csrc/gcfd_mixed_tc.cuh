@@ -11,7 +11,14 @@
 // One thread issues 3 x NFP/8 tcgen05.mma.kind::tf32 (M = 128, N = 16, K = 8):
 // hi*hi + hi*lo + lo*hi ("3xTF32"), about FP32 accuracy, accumulated in FP32
 // in Tensor Memory, then every thread reads its row back with tcgen05.ld and
-// applies the same stage update as the FMA kernel (stage_tail).
+// applies the same stage update as the FMA kernel (stage_tail).  The next
+// stage's face deltas (InterpolateSolutionToEdges, edges.go:485-488) are a
+// second GEMM on the tensor cores:
+//     F[m][q] = sum_i dq_m[i] * FluxEdgeInterp[q][i],   q < 3 NpEdge,
+// each thread's updated deltas (16 K columns, TF32 hi and lo) stored into the
+// columns the divergence's A used, FluxEdgeInterp split the same way in shared
+// memory, 3 x 2 MMAs (M = 128, N = 16 or 32, K = 8) into the divergence's D
+// columns, read back and stored as the edge-major faces.
 #pragma once
 #include "gcfd_mixed.cuh"
 #include "gcfd_tc.cuh"
@@ -29,6 +36,14 @@ struct TcDims {
   static constexpr int NCOLS = NEED <= 32 ? 32 : (NEED <= 64 ? 64 : (NEED <= 128 ? 128 : 256));
   static constexpr int BSZ = NOUT * NFP;       // floats per B split
   static_assert(MixedDims<N>::NP <= NOUT, "output points must fit the N = 16 tile");
+  // Face GEMM (FluxEdgeInterp): K = 16 solution points (padded), N = the 3 NpEdge
+  // face points rounded up to 16; A (hi, lo) reuses columns [0, 32), D the
+  // columns of the divergence result from COL_D.
+  static constexpr int KF = 16;
+  static constexpr int NFACE = ((MixedDims<N>::NE3 + 15) / 16) * 16;
+  static constexpr int BFSZ = NFACE * KF;      // floats per face-operand split
+  static_assert(COL_D >= 2 * KF && COL_D + NFACE <= NCOLS, "face GEMM must fit the allocated columns");
+  static_assert(NFACE <= 32 && MixedDims<N>::NPP <= KF, "face GEMM tile");
 };
 
 // Host-side layout of one B split: element (r, j) of the 16 x NFP operand at
@@ -41,7 +56,9 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
   constexpr int NP = MixedDims<N>::NP, NE = MixedDims<N>::NE, NE3 = MixedDims<N>::NE3;
   constexpr int NEP = MixedDims<N>::NEP;
   constexpr int NFP = TcDims<N>::NFP, NCOLS = TcDims<N>::NCOLS, BSZ = TcDims<N>::BSZ;
+  constexpr int BFSZ = TcDims<N>::BFSZ, NFACE = TcDims<N>::NFACE, NPP = MixedDims<N>::NPP;
   __shared__ __align__(128) float sB[2 * BSZ];
+  __shared__ __align__(128) float sBF[2 * BFSZ];
   __shared__ float sdq[4][NP][33];
   __shared__ float sbase[4][32];
   __shared__ float sfh[4][NE3][32];
@@ -50,7 +67,8 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
   __shared__ uint32_t tmem_base;
   __shared__ double sdt;
   for (int i = threadIdx.x; i < 2 * BSZ; i += blockDim.x) sB[i] = a.Btc[i];
-  tc::fence_proxy_async();  // sB is read by the tensor core
+  for (int i = threadIdx.x; i < 2 * BFSZ; i += blockDim.x) sBF[i] = a.BtcF[i];
+  tc::fence_proxy_async();  // sB and sBF are read by the tensor core
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) tc::mbar_init(&mbar, 1);
   if (n == 0) {
@@ -200,7 +218,7 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
   bool ok = tc::mbar_wait(&mbar, 0, 1 << 20);
   if (!ok) {
     if (lane == 0) atomicOr(a.err, 1u);
-    ok = tc::mbar_wait(&mbar, 0, 1 << 20);  // let the MMAs drain before the TMEM is freed
+    ok = tc::mbar_wait(&mbar, 0, 1 << 20);  // let the MMAs drain before the TMEM is reused or freed
   }
   tc::fence_after();
   uint32_t dv[16];
@@ -208,11 +226,66 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
   tc::wait_ld();
   float rmax = -3.4028235e38f, rabs = 0.0f;
   float2 rs2 = make_float2(0.0f, 0.0f);
+  // the next stage's faces: on the tensor cores unless the divergence's wait gave up
+  const bool faces = s >= 0 && !a.rhsOnly;
+  const bool tcFaces = __syncthreads_and(ok) && faces;
+  float dqn[NPP];
+#pragma unroll
+  for (int r = 0; r < NPP; ++r) dqn[r] = 0.0f;
   if (active) {
     float rhs[NP];
 #pragma unroll
     for (int r = 0; r < NP; ++r) rhs[r] = -__uint_as_float(dv[r]) * ooJ;
-    stage_tail<N>(a, eslot, n, k, off, sK, s, rhs, dq0, ds, dtk, rmax, rabs, rs2);
+    if (tcFaces)
+      stage_tail<N, true>(a, eslot, n, k, off, sK, s, rhs, dq0, ds, dtk, rmax, rabs, rs2, dqn);
+    else
+      stage_tail<N>(a, eslot, n, k, off, sK, s, rhs, dq0, ds, dtk, rmax, rabs, rs2);
+  }
+  if (tcFaces) {
+    uint32_t hi[16], lo[16];
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      const float x = (t < NPP) ? dqn[t < NPP ? t : 0] : 0.0f;
+      hi[t] = tc::to_tf32(x);
+      lo[t] = tc::to_tf32(x - __uint_as_float(hi[t]));
+    }
+    tc::st16(trow, hi);
+    tc::st16(trow + 16, lo);
+    tc::wait_st();
+    tc::fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tc::fence_after();
+      constexpr uint32_t idescF = tc::idesc_tf32(128, NFACE);
+      constexpr uint32_t lbo = 128, sbo = (TcDims<N>::KF / 4) * 128;
+      const uint32_t bhi = tc::smem_u32(sBF), blo = tc::smem_u32(sBF + BFSZ);
+      const uint32_t dcol = tbase + TcDims<N>::COL_D;
+#pragma unroll
+      for (int kk = 0; kk < TcDims<N>::KF / 8; ++kk) {
+        const uint64_t dh = tc::smem_desc(bhi + 256 * kk, lbo, sbo);
+        const uint64_t dl = tc::smem_desc(blo + 256 * kk, lbo, sbo);
+        tc::mma_tf32_ts(dcol, tbase + 8 * kk, dh, idescF, kk > 0 ? 1u : 0u);
+        tc::mma_tf32_ts(dcol, tbase + 8 * kk, dl, idescF, 1u);
+        tc::mma_tf32_ts(dcol, tbase + 16 + 8 * kk, dh, idescF, 1u);
+      }
+      tc::commit(&mbar);
+    }
+    bool okF = tc::mbar_wait(&mbar, 1, 1 << 20);
+    if (!okF) {
+      if (lane == 0) atomicOr(a.err, 1u);
+      tc::mbar_wait(&mbar, 1, 1 << 20);
+    }
+    tc::fence_after();
+    uint32_t fv[NFACE];
+    tc::ld16(trow + TcDims<N>::COL_D, fv);
+    if constexpr (NFACE > 16) tc::ld16(trow + TcDims<N>::COL_D + 16, fv + 16);
+    tc::wait_ld();
+    if (active) {
+      float f[MixedDims<N>::NE3];
+#pragma unroll
+      for (int q = 0; q < MixedDims<N>::NE3; ++q) f[q] = __uint_as_float(fv[q]);
+      store_faces<N>(a, eslot, n, f);
+    }
   }
   tc::fence_before();
   __syncthreads();

@@ -49,6 +49,18 @@ int build_tc_n(gcfd_ctx* c) {
     }
   int rc = upload(c, &c->mBtc, b);
   if (rc) return rc;
+  // FluxEdgeInterp (3 NpEdge x Np) as the face GEMM's B: N = face point q, K = solution point i.
+  constexpr int KF = TcDims<N>::KF, BFSZ = TcDims<N>::BFSZ;
+  std::vector<float> bf(2 * static_cast<size_t>(BFSZ), 0.f);
+  for (int q = 0; q < 3 * c->NE; ++q)
+    for (int i = 0; i < Np; ++i) {
+      const double v = c->el.FluxEdgeInterp(q, i);
+      const float hi = tf32_round(static_cast<float>(v));
+      const float lo = tf32_round(static_cast<float>(v - static_cast<double>(hi)));
+      bf[tc_b_index(q, i, KF)] = hi;
+      bf[BFSZ + tc_b_index(q, i, KF)] = lo;
+    }
+  if ((rc = upload(c, &c->mBtcF, bf))) return rc;
   cudaFuncAttributes attr{};
   GCFD_CUDA(c, cudaFuncGetAttributes(&attr, k_mixed_stage_tc<N>));
   const int perSM = 512 / NCOLS;  // CTAs whose TMEM fits at once
