@@ -55,7 +55,7 @@ def args_parse():
     p.add_argument("--precision", choices=["fp32", "tf32x3", "fp64"], default="fp32")
     p.add_argument("--workload", choices=sorted(WORKLOADS), default="vortex1024")
     p.add_argument("--fp64-steps", type=int, default=100)
-    p.add_argument("--adj-steps", type=int, default=20, help="steps of the FP64 adjoint timing (0: skip)")
+    p.add_argument("--adj-steps", type=int, default=20, help="steps of the adjoint timings, FP64 and mixed (0: skip)")
     p.add_argument("--e2e-steps", type=int, default=50)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu", action="store_true")
@@ -400,14 +400,14 @@ def run_ours(a, world, rank, local):
                                                                     "k_step"])}}
         s64.close()
 
-    # Adjoint cost: the reverse sweep of a recorded FP64 window against the
-    # FP64 forward step.  With a checkpoint every 10 steps (what the vortex1024
-    # adjoint runs) each segment is recomputed once with its per-step tape kept,
-    # then reversed; with a checkpoint every step each reverse step recomputes
-    # its forward step once with the tape.
-    adjoint = None
-    if a.adj_steps > 0:
-        sa = Euler(ip, mesh, 1, precision="fp64", device=local, vortex_center=(0.0, 0.0))
+    # Adjoint cost: the reverse sweep of a recorded window against the forward
+    # step of the same path (FP64, and the mixed path's FP32 adjoint).  With a
+    # checkpoint every 10 steps (what the vortex1024 adjoint runs) each segment
+    # is recomputed once with its per-step tape kept, then reversed; with a
+    # checkpoint every step each reverse step recomputes its forward step once
+    # with the tape.
+    def adjoint_cost(precision):
+        sa = Euler(ip, mesh, 1, precision=precision, device=local, vortex_center=(0.0, 0.0))
         sta = torch.cuda.ExternalStream(sa.stream_handle(), device=torch.device("cuda", local))
         sa.enqueue_steps(2)
         torch.cuda.synchronize()
@@ -436,13 +436,18 @@ def run_ours(a, world, rank, local):
             t1, t2 = sweep(n1), sweep(n2)
             adj_ms = (t2 - t1) / (n2 - n1)  # per reverse step, without the window's fixed costs
             legs[every] = {"ms_per_step": adj_ms, "ratio": adj_ms / fwd_ms, "window_ms": {str(n1): t1, str(n2): t2}}
-        adjoint = {"ms_per_step": legs[10]["ms_per_step"], "forward_ms_per_step": fwd_ms,
-                   "ratio": legs[10]["ratio"], "checkpoint_every": 10, "path": "fp64",
-                   "window_ms": legs[10]["window_ms"], "checkpoint_every_1": legs[1],
-                   "timing": "host clock around gcfd_step_vjp (synchronous) for two window lengths; per-step cost = "
-                             "difference / difference in steps (the adjoint's host transfer and set-up are per "
-                             "window); forward by CUDA events"}
         sa.close()
+        return {"ms_per_step": legs[10]["ms_per_step"], "forward_ms_per_step": fwd_ms,
+                "ratio": legs[10]["ratio"], "checkpoint_every": 10, "path": precision,
+                "window_ms": legs[10]["window_ms"], "checkpoint_every_1": legs[1],
+                "timing": "host clock around gcfd_step_vjp (synchronous) for two window lengths; per-step cost = "
+                          "difference / difference in steps (the adjoint's host transfer and set-up are per "
+                          "window); forward by CUDA events"}
+
+    adjoint = adjoint_cost("fp64") if a.adj_steps > 0 else None
+    adjoint_mixed = adjoint_cost("fp32") if a.adj_steps > 0 else None
+    if adjoint_mixed is not None:
+        adjoint_mixed["vs_fp64_adjoint"] = adjoint["ms_per_step"] / adjoint_mixed["ms_per_step"]
 
     # End to end through the public API: pinned host state in, step, state out.
     import torch as _t
@@ -512,6 +517,7 @@ def run_ours(a, world, rank, local):
             "fp64_path": fp64,
             "other_mixed_path": other,
             "adjoint": adjoint,
+            "adjoint_mixed": adjoint_mixed,
             "final_time": info["time"],
         }
         if cpu:

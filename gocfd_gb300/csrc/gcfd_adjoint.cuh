@@ -24,20 +24,21 @@
 namespace gcfd {
 
 // Euler flux (FluxCalcBase, fluxes.go:76-87) in reverse: qb += (dFx/dq)^T Fxb + (dFy/dq)^T Fyb.
-__device__ __forceinline__ void euler_flux_vjp(const Gas<double>& g, const double q[4], const double Fxb[4],
-                                               const double Fyb[4], double qb[4]) {
-  const double rho = q[0], m = q[1], n = q[2], E = q[3];
-  const double oorho = 1.0 / rho;
-  const double u = m * oorho, v = n * oorho;
-  const double p = g.gm1 * (E - 0.5 * rho * (u * u + v * v));
-  double mb = Fxb[0] + u * Fxb[1] + v * Fxb[2];
-  double nb = Fyb[0] + u * Fyb[1] + v * Fyb[2];
-  double ub = m * Fxb[1] + (E + p) * Fxb[3] + n * Fyb[1];
-  double vb = m * Fxb[2] + n * Fyb[2] + (E + p) * Fyb[3];
-  double Eb = u * Fxb[3] + v * Fyb[3];
-  const double pb = Fxb[1] + u * Fxb[3] + Fyb[2] + v * Fyb[3];
+template <typename T>
+__device__ __forceinline__ void euler_flux_vjp(const Gas<T>& g, const T q[4], const T Fxb[4], const T Fyb[4],
+                                               T qb[4]) {
+  const T rho = q[0], m = q[1], n = q[2], E = q[3];
+  const T oorho = T(1) / rho;
+  const T u = m * oorho, v = n * oorho;
+  const T p = g.gm1 * (E - T(0.5) * rho * (u * u + v * v));
+  T mb = Fxb[0] + u * Fxb[1] + v * Fxb[2];
+  T nb = Fyb[0] + u * Fyb[1] + v * Fyb[2];
+  T ub = m * Fxb[1] + (E + p) * Fxb[3] + n * Fyb[1];
+  T vb = m * Fxb[2] + n * Fyb[2] + (E + p) * Fyb[3];
+  T Eb = u * Fxb[3] + v * Fyb[3];
+  const T pb = Fxb[1] + u * Fxb[3] + Fyb[2] + v * Fyb[3];
   // p = gm1 (E - (m^2 + n^2) / (2 rho))
-  double rhob = g.gm1 * 0.5 * (u * u + v * v) * pb;
+  T rhob = g.gm1 * T(0.5) * (u * u + v * v) * pb;
   mb -= g.gm1 * u * pb;
   nb -= g.gm1 * v * pb;
   Eb += g.gm1 * pb;
@@ -61,74 +62,77 @@ __device__ __forceinline__ void pressure_vjp(const Gas<double>& g, const double 
   qb[3] += g.gm1 * pb;
 }
 
-__device__ __forceinline__ double sgn(double x) { return x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : 0.0); }
+template <typename T>
+__device__ __forceinline__ T sgn(T x) { return x > T(0) ? T(1) : (x < T(0) ? T(-1) : T(0)); }
 
 // RoeFlux (fluxes.go:284-413) in reverse: QLb, QRb += (df/dQL)^T fb, (df/dQR)^T fb.
-// Divisions are taken once as reciprocals (FP64 division is a multi-instruction
-// sequence); the forward intermediates are recomputed from QL, QR.
-__device__ __forceinline__ void roe_vjp(const Gas<double>& g, const double QL[4], const double QR[4], double nx,
-                                        double ny, const double fbo[4], double QLb[4], double QRb[4]) {
+// Divisions are taken once as reciprocals (division is a multi-instruction
+// sequence); the forward intermediates are recomputed from QL, QR.  T = double
+// on the FP64 path, float on the mixed one.
+template <typename T>
+__device__ __forceinline__ void roe_vjp(const Gas<T>& g, const T QL[4], const T QR[4], T nx, T ny, const T fbo[4],
+                                        T QLb[4], T QRb[4]) {
   // forward
-  const double iL = 1.0 / QL[0], iR = 1.0 / QR[0];
-  const double rhoULr = QL[1] * nx + QL[2] * ny, rhoVLr = -QL[1] * ny + QL[2] * nx;
-  const double rhoURr = QR[1] * nx + QR[2] * ny, rhoVRr = -QR[1] * ny + QR[2] * nx;
-  const double rhoL = QL[0], uL = rhoULr * iL, vL = rhoVLr * iL;
-  const double rhoR = QR[0], uR = rhoURr * iR, vR = rhoVRr * iR;
-  const double uxL = QL[1] * iL, uyL = QL[2] * iL, uxR = QR[1] * iR, uyR = QR[2] * iR;
-  const double pL = g.gm1 * (QL[3] - 0.5 * rhoL * (uxL * uxL + uyL * uyL));
-  const double pR = g.gm1 * (QR[3] - 0.5 * rhoR * (uxR * uxR + uyR * uyR));
-  const double hL = (QL[3] + pL) * iL, hR = (QR[3] + pR) * iR;
-  const double rhoLs = sqrt(rhoL), rhoRs = sqrt(rhoR);
-  const double S = rhoLs + rhoRs, oS = 1.0 / S;
-  const double rho = rhoLs * rhoRs;
-  const double u = (rhoLs * uL + rhoRs * uR) * oS;
-  const double v = (rhoLs * vL + rhoRs * vR) * oS;
-  const double h = (rhoLs * hL + rhoRs * hR) * oS;
-  const double c2 = g.gm1 * (h - 0.5 * (u * u + v * v));
-  const double C = sqrt(c2), oC = 1.0 / C, oc2 = oC * oC;
-  const double du = uR - uL, dp = pR - pL;
-  const double a1 = -0.5 * (rho * du) * oC + 0.5 * dp * oc2;
-  const double a2 = (rhoR - rhoL) - dp * oc2;
-  const double a3 = rho * (vR - vL);
-  const double a4 = 0.5 * (rho * du) * oC + 0.5 * dp * oc2;
-  const double l1 = fabs(u - C), l2 = fabs(u), l4 = fabs(u + C);
-  const double W1 = l1 * a1, W2 = l2 * a2, W3 = l2 * a3, W4 = l4 * a4;
+  const T iL = T(1.0) / QL[0], iR = T(1.0) / QR[0];
+  const T rhoULr = QL[1] * nx + QL[2] * ny, rhoVLr = -QL[1] * ny + QL[2] * nx;
+  const T rhoURr = QR[1] * nx + QR[2] * ny, rhoVRr = -QR[1] * ny + QR[2] * nx;
+  const T rhoL = QL[0], uL = rhoULr * iL, vL = rhoVLr * iL;
+  const T rhoR = QR[0], uR = rhoURr * iR, vR = rhoVRr * iR;
+  const T uxL = QL[1] * iL, uyL = QL[2] * iL, uxR = QR[1] * iR, uyR = QR[2] * iR;
+  const T pL = g.gm1 * (QL[3] - T(0.5) * rhoL * (uxL * uxL + uyL * uyL));
+  const T pR = g.gm1 * (QR[3] - T(0.5) * rhoR * (uxR * uxR + uyR * uyR));
+  const T hL = (QL[3] + pL) * iL, hR = (QR[3] + pR) * iR;
+  const T rhoLs = sqrt(rhoL), rhoRs = sqrt(rhoR);
+  const T S = rhoLs + rhoRs, oS = T(1.0) / S;
+  const T rho = rhoLs * rhoRs;
+  const T u = (rhoLs * uL + rhoRs * uR) * oS;
+  const T v = (rhoLs * vL + rhoRs * vR) * oS;
+  const T h = (rhoLs * hL + rhoRs * hR) * oS;
+  const T c2 = g.gm1 * (h - T(0.5) * (u * u + v * v));
+  const T C = sqrt(c2), oC = T(1.0) / C, oc2 = oC * oC;
+  const T du = uR - uL, dp = pR - pL;
+  const T a1 = -T(0.5) * (rho * du) * oC + T(0.5) * dp * oc2;
+  const T a2 = (rhoR - rhoL) - dp * oc2;
+  const T a3 = rho * (vR - vL);
+  const T a4 = T(0.5) * (rho * du) * oC + T(0.5) * dp * oc2;
+  const T l1 = fabs(u - C), l2 = fabs(u), l4 = fabs(u + C);
+  const T W1 = l1 * a1, W2 = l2 * a2, W3 = l2 * a3, W4 = l4 * a4;
   // output rotation: out0 = f0, out1 = nx f1 - ny f2, out2 = ny f1 + nx f2, out3 = f3
-  const double f0b = fbo[0], f1b = nx * fbo[1] + ny * fbo[2], f2b = -ny * fbo[1] + nx * fbo[2], f3b = fbo[3];
-  double rhoULrb = 0.5 * f0b + 0.5 * uL * f1b;
-  double rhoURrb = 0.5 * f0b + 0.5 * uR * f1b;
-  double rhoVLrb = 0.5 * uL * f2b;
-  double rhoVRrb = 0.5 * uR * f2b;
-  double uLb = 0.5 * rhoULr * f1b + 0.5 * rhoVLr * f2b + 0.5 * (pL + QL[3]) * f3b;
-  double uRb = 0.5 * rhoURr * f1b + 0.5 * rhoVRr * f2b + 0.5 * (pR + QR[3]) * f3b;
-  double vLb = 0.0, vRb = 0.0;
-  double pLb = 0.5 * f1b + 0.5 * uL * f3b;
-  double pRb = 0.5 * f1b + 0.5 * uR * f3b;
-  double QL3b = 0.5 * uL * f3b, QR3b = 0.5 * uR * f3b;
+  const T f0b = fbo[0], f1b = nx * fbo[1] + ny * fbo[2], f2b = -ny * fbo[1] + nx * fbo[2], f3b = fbo[3];
+  T rhoULrb = T(0.5) * f0b + T(0.5) * uL * f1b;
+  T rhoURrb = T(0.5) * f0b + T(0.5) * uR * f1b;
+  T rhoVLrb = T(0.5) * uL * f2b;
+  T rhoVRrb = T(0.5) * uR * f2b;
+  T uLb = T(0.5) * rhoULr * f1b + T(0.5) * rhoVLr * f2b + T(0.5) * (pL + QL[3]) * f3b;
+  T uRb = T(0.5) * rhoURr * f1b + T(0.5) * rhoVRr * f2b + T(0.5) * (pR + QR[3]) * f3b;
+  T vLb = T(0.0), vRb = T(0.0);
+  T pLb = T(0.5) * f1b + T(0.5) * uL * f3b;
+  T pRb = T(0.5) * f1b + T(0.5) * uR * f3b;
+  T QL3b = T(0.5) * uL * f3b, QR3b = T(0.5) * uR * f3b;
   // dissipation terms: f0 -= T0/2, f1 -= T1/2, f2 -= T2/2, f3 -= T3/2
-  const double T0b = -0.5 * f0b, T1b = -0.5 * f1b, T2b = -0.5 * f2b, T3b = -0.5 * f3b;
-  const double W1b = T0b + (u - C) * T1b + v * T2b + (h - u * C) * T3b;
-  const double W2b = T0b + u * T1b + v * T2b + 0.5 * (u * u + v * v) * T3b;
-  const double W3b = T2b + v * T3b;
-  const double W4b = T0b + (u + C) * T1b + v * T2b + (h + u * C) * T3b;
-  double ub = (W1 + W2 + W4) * T1b + (-W1 * C + W2 * u + W4 * C) * T3b;
-  double vb = (W1 + W2 + W4) * T2b + (W2 * v + W3) * T3b;
-  double hb = (W1 + W4) * T3b;
-  double Cb = (-W1 + W4) * T1b + (-W1 * u + W4 * u) * T3b;
+  const T T0b = -T(0.5) * f0b, T1b = -T(0.5) * f1b, T2b = -T(0.5) * f2b, T3b = -T(0.5) * f3b;
+  const T W1b = T0b + (u - C) * T1b + v * T2b + (h - u * C) * T3b;
+  const T W2b = T0b + u * T1b + v * T2b + T(0.5) * (u * u + v * v) * T3b;
+  const T W3b = T2b + v * T3b;
+  const T W4b = T0b + (u + C) * T1b + v * T2b + (h + u * C) * T3b;
+  T ub = (W1 + W2 + W4) * T1b + (-W1 * C + W2 * u + W4 * C) * T3b;
+  T vb = (W1 + W2 + W4) * T2b + (W2 * v + W3) * T3b;
+  T hb = (W1 + W4) * T3b;
+  T Cb = (-W1 + W4) * T1b + (-W1 * u + W4 * u) * T3b;
   // W = l * a
-  const double a1b = l1 * W1b, a2b = l2 * W2b, a3b = l2 * W3b, a4b = l4 * W4b;
-  const double l1b = a1 * W1b, l2b = a2 * W2b + a3 * W3b, l4b = a4 * W4b;
-  const double s1 = sgn(u - C), s2 = sgn(u), s4 = sgn(u + C);
+  const T a1b = l1 * W1b, a2b = l2 * W2b, a3b = l2 * W3b, a4b = l4 * W4b;
+  const T l1b = a1 * W1b, l2b = a2 * W2b + a3 * W3b, l4b = a4 * W4b;
+  const T s1 = sgn(u - C), s2 = sgn(u), s4 = sgn(u + C);
   ub += s1 * l1b + s2 * l2b + s4 * l4b;
   Cb += -s1 * l1b + s4 * l4b;
   // a1..a4
-  const double a14 = a4b - a1b;
-  double rhob = 0.5 * du * oC * a14 + (vR - vL) * a3b;
-  const double dub = 0.5 * rho * oC * a14;
-  Cb -= 0.5 * rho * du * oc2 * a14;
-  const double dpb = oc2 * (0.5 * (a1b + a4b) - a2b);
-  double c2b = dp * oc2 * oc2 * (a2b - 0.5 * (a1b + a4b));
-  double rhoRb = a2b, rhoLb = -a2b;
+  const T a14 = a4b - a1b;
+  T rhob = T(0.5) * du * oC * a14 + (vR - vL) * a3b;
+  const T dub = T(0.5) * rho * oC * a14;
+  Cb -= T(0.5) * rho * du * oc2 * a14;
+  const T dpb = oc2 * (T(0.5) * (a1b + a4b) - a2b);
+  T c2b = dp * oc2 * oc2 * (a2b - T(0.5) * (a1b + a4b));
+  T rhoRb = a2b, rhoLb = -a2b;
   vRb += rho * a3b;
   vLb -= rho * a3b;
   uRb += dub;
@@ -136,7 +140,7 @@ __device__ __forceinline__ void roe_vjp(const Gas<double>& g, const double QL[4]
   pRb += dpb;
   pLb -= dpb;
   // C = sqrt(c2); c2 = gm1 (h - (u^2 + v^2) / 2)
-  c2b += 0.5 * Cb * oC;
+  c2b += T(0.5) * Cb * oC;
   hb += g.gm1 * c2b;
   ub -= g.gm1 * u * c2b;
   vb -= g.gm1 * v * c2b;
@@ -145,11 +149,11 @@ __device__ __forceinline__ void roe_vjp(const Gas<double>& g, const double QL[4]
   uRb += rhoRs * oS * ub;
   vLb += rhoLs * oS * vb;
   vRb += rhoRs * oS * vb;
-  const double hLb = rhoLs * oS * hb, hRb = rhoRs * oS * hb;
-  const double rhoLsb = ((uL - u) * ub + (vL - v) * vb + (hL - h) * hb) * oS + rhoRs * rhob;
-  const double rhoRsb = ((uR - u) * ub + (vR - v) * vb + (hR - h) * hb) * oS + rhoLs * rhob;
-  rhoLb += 0.5 * rhoLsb / rhoLs;
-  rhoRb += 0.5 * rhoRsb / rhoRs;
+  const T hLb = rhoLs * oS * hb, hRb = rhoRs * oS * hb;
+  const T rhoLsb = ((uL - u) * ub + (vL - v) * vb + (hL - h) * hb) * oS + rhoRs * rhob;
+  const T rhoRsb = ((uR - u) * ub + (vR - v) * vb + (hR - h) * hb) * oS + rhoLs * rhob;
+  rhoLb += T(0.5) * rhoLsb / rhoLs;
+  rhoRb += T(0.5) * rhoRsb / rhoRs;
   // h = (E + p) / rho
   QL3b += hLb * iL;
   pLb += hLb * iL;
@@ -165,8 +169,8 @@ __device__ __forceinline__ void roe_vjp(const Gas<double>& g, const double QL[4]
   rhoVRrb += vRb * iR;
   rhoRb -= (uR * uRb + vR * vRb) * iR;
   // p = gm1 (E - (m^2 + n^2) / (2 rho))
-  rhoLb += g.gm1 * 0.5 * (uxL * uxL + uyL * uyL) * pLb;
-  rhoRb += g.gm1 * 0.5 * (uxR * uxR + uyR * uyR) * pRb;
+  rhoLb += g.gm1 * T(0.5) * (uxL * uxL + uyL * uyL) * pLb;
+  rhoRb += g.gm1 * T(0.5) * (uxR * uxR + uyR * uyR) * pRb;
   QLb[0] += rhoLb;
   QRb[0] += rhoRb;
   QLb[3] += QL3b + g.gm1 * pLb;
@@ -296,17 +300,21 @@ static __device__ __noinline__ void bc_point_vjp(const EdgeArgs<double>& a, int 
   }
 }
 
+// T: the arithmetic and array type of the adjoint (double: FP64 path; float:
+// mixed path, whose stage states are Q0 + D_s with the FP32 increments D_s).
+template <typename T>
 struct AdjArgs {
   int K, stage, localDT;
-  const double* Qs;     // stage state
-  const double* Qbn;    // adjoint of the stage output (stage -1: the RHS adjoint)
-  const double* rhs;    // taped RHS of this stage
-  const double* rhs3;   // taped RHS of stage 3 (stage 4)
-  double* Qb0;          // adjoint of the step's initial state (accumulated)
-  double* Qbs;          // adjoint of this stage's state (accumulated)
-  double* Qb2;          // stage 4 feeds the stage-2 and stage-3 states directly
-  double* Qb3;
-  double* Rb3;          // W3 dt4 Qbar_final, stage 4 -> stage 3
+  const double* Qs;     // stage state (mixed path: the step's initial state Q0)
+  const float* Ds;      // mixed path, stage > 0: the stage increment (state = Q0 + Ds)
+  const T* Qbn;         // adjoint of the stage output (stage -1: the RHS adjoint)
+  const T* rhs;         // taped RHS of this stage
+  const T* rhs3;        // taped RHS of stage 3 (stage 4)
+  T* Qb0;               // adjoint of the step's initial state (accumulated)
+  T* Qbs;               // adjoint of this stage's state (accumulated)
+  T* Qb2;               // stage 4 feeds the stage-2 and stage-3 states directly
+  T* Qb3;
+  T* Rb3;               // W3 dt4 Qbar_final, stage 4 -> stage 3
   const double* dtS;    // taped global dt per stage [5]
   const double* dtK;    // taped local dt of this stage [K]
   double* dtbarG;       // [5] global dt adjoints
@@ -314,8 +322,8 @@ struct AdjArgs {
   const double* DivInt;
   const double* Jdet;
   const double* Jinv;
-  double* FEb;          // [n][3NE][K]
-  Gas<double> gas;
+  T* FEb;               // [n][3NE][K]
+  Gas<T> gas;
 };
 
 // Forward stage coefficients (rkAdvance, euler.go:460-566): stage s < 4 forms
@@ -330,33 +338,40 @@ __device__ __forceinline__ void stage_coeffs(int s, double& alpha, double& beta,
   }
 }
 
-template <int N>
-__global__ void __launch_bounds__(128) k_adj_div(AdjArgs a) {
+// Stage state value at flat index ind.
+template <typename T>
+__device__ __forceinline__ T stage_value(const AdjArgs<T>& a, size_t ind) {
+  if (a.Ds) return static_cast<T>(a.Qs[ind]) + static_cast<T>(a.Ds[ind]);
+  return static_cast<T>(a.Qs[ind]);
+}
+
+template <int N, typename T>
+__global__ void __launch_bounds__(128) k_adj_div(AdjArgs<T> a) {
   constexpr int NP = Dims<N>::NP, NE3 = Dims<N>::NE3, NF = Dims<N>::NF;
-  __shared__ double sD[NP * NF];
+  __shared__ T sD[NP * NF];
   stage_operator(sD, a.DivInt, NP * NF);
   __syncthreads();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = k < a.K;
   const size_t sK = static_cast<size_t>(a.K);
   const int s = a.stage;
-  double dtb = 0.0;
+  T dtb = T(0);
   if (active) {
-    double Rb[4][NP];
+    T Rb[4][NP];
     if (s < 0) {
 #pragma unroll
       for (int n = 0; n < 4; ++n)
 #pragma unroll
         for (int r = 0; r < NP; ++r) Rb[n][r] = a.Qbn[(n * NP + r) * sK + k];
     } else if (s == 4) {
-      const double dt4 = a.localDT ? a.dtK[k] : a.dtS[4];
-      const double A2 = kSSP[4][0], A3 = kSSP[4][1], A4 = kSSP[4][2], W3 = kSSP[4][3], C4 = kSSP[4][4];
+      const T dt4 = static_cast<T>(a.localDT ? a.dtK[k] : a.dtS[4]);
+      const T A2 = kSSP[4][0], A3 = kSSP[4][1], A4 = kSSP[4][2], W3 = kSSP[4][3], C4 = kSSP[4][4];
 #pragma unroll
       for (int n = 0; n < 4; ++n)
 #pragma unroll
         for (int r = 0; r < NP; ++r) {
           const size_t ind = (n * NP + r) * sK + k;
-          const double qb = a.Qbn[ind];
+          const T qb = a.Qbn[ind];
           Rb[n][r] = C4 * dt4 * qb;
           a.Rb3[ind] = W3 * dt4 * qb;
           dtb += qb * (W3 * a.rhs3[ind] + C4 * a.rhs[ind]);
@@ -365,33 +380,35 @@ __global__ void __launch_bounds__(128) k_adj_div(AdjArgs a) {
           a.Qbs[ind] = A4 * qb;
         }
     } else {
-      double al, be, ga;
-      stage_coeffs(s, al, be, ga);
-      const double dt = a.localDT ? a.dtK[k] : a.dtS[s];
+      double ald, bed, gad;
+      stage_coeffs(s, ald, bed, gad);
+      const T al = static_cast<T>(ald), be = static_cast<T>(bed), ga = static_cast<T>(gad);
+      const T dt = static_cast<T>(a.localDT ? a.dtK[k] : a.dtS[s]);
 #pragma unroll
       for (int n = 0; n < 4; ++n)
 #pragma unroll
         for (int r = 0; r < NP; ++r) {
           const size_t ind = (n * NP + r) * sK + k;
-          const double qb = a.Qbn[ind];
-          Rb[n][r] = ga * dt * qb + (s == 3 ? a.Rb3[ind] : 0.0);
+          const T qb = a.Qbn[ind];
+          Rb[n][r] = ga * dt * qb + (s == 3 ? a.Rb3[ind] : T(0));
           dtb += ga * qb * a.rhs[ind];
           // first writers: stage 3 of the step's Q0 adjoint, stage 1 of its own
           if (s == 3) a.Qb0[ind] = al * qb;
           else a.Qb0[ind] += al * qb;
           if (s == 1) a.Qbs[ind] = be * qb;
-          else if (be != 0.0) a.Qbs[ind] += be * qb;
+          else if (be != T(0)) a.Qbs[ind] += be * qb;
         }
     }
     // RHS = -(1/J) DivInt . DOF  =>  DOFb = -(1/J) DivInt^T Rb
-    const double Jd = a.Jdet[k], mooj = -(1.0 / Jd);
-    const double J0 = a.Jinv[k], J1 = a.Jinv[sK + k], J2 = a.Jinv[2 * sK + k], J3 = a.Jinv[3 * sK + k];
+    const T Jd = static_cast<T>(a.Jdet[k]), mooj = -(T(1) / Jd);
+    const T J0 = static_cast<T>(a.Jinv[k]), J1 = static_cast<T>(a.Jinv[sK + k]);
+    const T J2 = static_cast<T>(a.Jinv[2 * sK + k]), J3 = static_cast<T>(a.Jinv[3 * sK + k]);
 #pragma unroll 1
     for (int i = 0; i < NP; ++i) {
-      double Fxb[4], Fyb[4], q[4], qb[4] = {0.0, 0.0, 0.0, 0.0};
+      T Fxb[4], Fyb[4], q[4], qb[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
       for (int n = 0; n < 4; ++n) {
-        double fr = 0.0, fs = 0.0;
+        T fr = T(0), fs = T(0);
 #pragma unroll
         for (int r = 0; r < NP; ++r) {
           fr += sD[r * NF + i] * Rb[n][r];
@@ -401,7 +418,7 @@ __global__ void __launch_bounds__(128) k_adj_div(AdjArgs a) {
         fs *= mooj;
         Fxb[n] = Jd * (J0 * fr + J2 * fs);
         Fyb[n] = Jd * (J1 * fr + J3 * fs);
-        q[n] = a.Qs[(n * NP + i) * sK + k];
+        q[n] = stage_value(a, (n * NP + i) * sK + k);
       }
       euler_flux_vjp(a.gas, q, Fxb, Fyb, qb);
 #pragma unroll
@@ -411,55 +428,76 @@ __global__ void __launch_bounds__(128) k_adj_div(AdjArgs a) {
     for (int j = 0; j < NE3; ++j) {
 #pragma unroll
       for (int n = 0; n < 4; ++n) {
-        double d = 0.0;
+        T d = T(0);
 #pragma unroll
         for (int r = 0; r < NP; ++r) d += sD[r * NF + 2 * NP + j] * Rb[n][r];
         a.FEb[(n * NE3 + j) * sK + k] = mooj * d;
       }
     }
-    if (s >= 0 && a.localDT) a.dtOwnK[k] = dtb;
+    if (s >= 0 && a.localDT) a.dtOwnK[k] = static_cast<double>(dtb);
   }
   if (s >= 0 && !a.localDT) {
-    const double t = warp_sum(active ? dtb : 0.0);
+    const double t = warp_sum(active ? static_cast<double>(dtb) : 0.0);
     if ((threadIdx.x & 31) == 0) atomicAdd(&a.dtbarG[s], t);
   }
 }
 
+template <typename T>
 struct AdjEdgeArgs {
-  double* FEb;     // [n][3NE][K] edge DOF adjoints (from k_adj_div)
-  double* QFb;     // [n][3NE][K] face adjoints (written here)
+  const T* QF;     // [n][3NE][K] face states of the stage
+  T* FEb;          // [n][3NE][K] edge DOF adjoints (from k_adj_div)
+  T* QFb;          // [n][3NE][K] face adjoints (written here)
   double* qinfb;   // [4] far-field Qinf adjoint
   double* tb;      // solver-time adjoint
   double* esBar;   // per edge: adjoint of the edge's max wave speed
   int useManualRoe;
 };
 
+template <typename T>
+__device__ __forceinline__ Gas<T> gas_as(const Gas<double>& g) {
+  return Gas<T>{static_cast<T>(g.gamma), static_cast<T>(g.gm1), static_cast<T>(g.oogm1)};
+}
+
 // Interior edges [0, nInt): Riemann flux Jacobian^T at each edge point
-// (ROE: the reverse-mode Roe adjoint; otherwise the dual-number one).
-template <int N, bool ROE>
-__global__ void __launch_bounds__(128) k_adj_edge(EdgeArgs<double> a, AdjEdgeArgs x) {
+// (ROE: the reverse-mode Roe adjoint in T; otherwise the dual-number one in FP64).
+template <int N, bool ROE, typename T>
+__global__ void __launch_bounds__(128) k_adj_edge(EdgeArgs<double> a, AdjEdgeArgs<T> x) {
   constexpr int NE = Dims<N>::NE, NE3 = Dims<N>::NE3;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= a.nInt) return;
   const size_t sK = static_cast<size_t>(a.K);
   const int kL = a.kL[e], kR = a.kR[e];
   const int eL = a.eLR[e] & 3, eR = a.eLR[e] >> 2;
-  const double nx = a.nx[e], ny = a.ny[e];
-  const double IIL = a.IIL[e], IIR = a.IIR[e];
+  const T nx = static_cast<T>(a.nx[e]), ny = static_cast<T>(a.ny[e]);
+  const T IIL = static_cast<T>(a.IIL[e]), IIR = static_cast<T>(a.IIR[e]);
+  const Gas<T> g = gas_as<T>(a.gas);
 #pragma unroll 1
   for (int p = 0; p < NE; ++p) {
     const int jL = eL * NE + p, jR = eR * NE + (NE - 1 - p);
-    double qL[4], qR[4], fb[4], qLb[4] = {0.0, 0.0, 0.0, 0.0}, qRb[4] = {0.0, 0.0, 0.0, 0.0};
+    T qL[4], qR[4], fb[4], qLb[4] = {T(0), T(0), T(0), T(0)}, qRb[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
     for (int n = 0; n < 4; ++n) {
-      qL[n] = a.QF[(n * NE3 + jL) * sK + kL];
-      qR[n] = a.QF[(n * NE3 + jR) * sK + kR];
+      qL[n] = x.QF[(n * NE3 + jL) * sK + kL];
+      qR[n] = x.QF[(n * NE3 + jR) * sK + kR];
       fb[n] = IIL * x.FEb[(n * NE3 + jL) * sK + kL] - IIR * x.FEb[(n * NE3 + jR) * sK + kR];
     }
-    if (ROE)
-      roe_vjp(a.gas, qL, qR, nx, ny, fb, qLb, qRb);
-    else
-      riemann_vjp_dual(a.flux, a.gas, qL, qR, nx, ny, fb, qLb, qRb);
+    if (ROE) {
+      roe_vjp<T>(g, qL, qR, nx, ny, fb, qLb, qRb);
+    } else {
+      double dL[4], dR[4], dfb[4], dLb[4] = {0.0, 0.0, 0.0, 0.0}, dRb[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+        dL[n] = qL[n];
+        dR[n] = qR[n];
+        dfb[n] = fb[n];
+      }
+      riemann_vjp_dual(a.flux, a.gas, dL, dR, a.nx[e], a.ny[e], dfb, dLb, dRb);
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+        qLb[n] = static_cast<T>(dLb[n]);
+        qRb[n] = static_cast<T>(dRb[n]);
+      }
+    }
 #pragma unroll
     for (int n = 0; n < 4; ++n) {
       x.QFb[(n * NE3 + jL) * sK + kL] = qLb[n];
@@ -468,10 +506,10 @@ __global__ void __launch_bounds__(128) k_adj_edge(EdgeArgs<double> a, AdjEdgeArg
   }
 }
 
-// Boundary edges [nInt, nInt + nBC): boundary state and flux by duals, one
-// thread per (boundary edge, edge point).
-template <int N>
-__global__ void __launch_bounds__(128) k_adj_edge_bc(EdgeArgs<double> a, AdjEdgeArgs x) {
+// Boundary edges [nInt, nInt + nBC): boundary state and flux by duals in FP64,
+// one thread per (boundary edge, edge point).
+template <int N, typename T>
+__global__ void __launch_bounds__(128) k_adj_edge_bc(EdgeArgs<double> a, AdjEdgeArgs<T> x) {
   constexpr int NE = Dims<N>::NE, NE3 = Dims<N>::NE3;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   double qinfb[4] = {0.0, 0.0, 0.0, 0.0}, tb = 0.0;
@@ -485,12 +523,12 @@ __global__ void __launch_bounds__(128) k_adj_edge_bc(EdgeArgs<double> a, AdjEdge
     double qi[4], fb[4], qib[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
     for (int n = 0; n < 4; ++n) {
-      qi[n] = a.QF[(n * NE3 + jL) * sK + kL];
-      fb[n] = IIL * x.FEb[(n * NE3 + jL) * sK + kL];
+      qi[n] = static_cast<double>(x.QF[(n * NE3 + jL) * sK + kL]);
+      fb[n] = IIL * static_cast<double>(x.FEb[(n * NE3 + jL) * sK + kL]);
     }
     bc_point_vjp(a, a.bcFlag[b], tid, qi, a.nx[e], a.ny[e], *a.time, a.oohK[e], fb, 0.0, qib, qinfb, &tb);
 #pragma unroll
-    for (int n = 0; n < 4; ++n) x.QFb[(n * NE3 + jL) * sK + kL] = qib[n];
+    for (int n = 0; n < 4; ++n) x.QFb[(n * NE3 + jL) * sK + kL] = static_cast<T>(qib[n]);
   }
 #pragma unroll
   for (int n = 0; n < 4; ++n) qinfb[n] = warp_sum(qinfb[n]);
@@ -611,9 +649,9 @@ static __global__ void k_adj_lts(AdjDtArgs a) {
   }
 }
 
-// esBar[g] onto the face state at the edge's max wave-speed point.
-template <int N>
-__global__ void __launch_bounds__(128) k_adj_speed(EdgeArgs<double> a, AdjEdgeArgs x) {
+// esBar[g] onto the face state at the edge's max wave-speed point (in FP64).
+template <int N, typename T>
+__global__ void __launch_bounds__(128) k_adj_speed(EdgeArgs<double> a, AdjEdgeArgs<T> x) {
   constexpr int NE = Dims<N>::NE, NE3 = Dims<N>::NE3;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= a.nInt + a.nBC) return;
@@ -635,7 +673,7 @@ __global__ void __launch_bounds__(128) k_adj_speed(EdgeArgs<double> a, AdjEdgeAr
     const int jL = eL * NE + p;
     double qi[4];
 #pragma unroll
-    for (int n = 0; n < 4; ++n) qi[n] = a.QF[(n * NE3 + jL) * sK + kL];
+    for (int n = 0; n < 4; ++n) qi[n] = static_cast<double>(x.QF[(n * NE3 + jL) * sK + kL]);
     double ws;
     if (bc) {
       double f[4];
@@ -648,7 +686,7 @@ __global__ void __launch_bounds__(128) k_adj_speed(EdgeArgs<double> a, AdjEdgeAr
   const int jL = eL * NE + pb;
   double qi[4], qib[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
-  for (int n = 0; n < 4; ++n) qi[n] = a.QF[(n * NE3 + jL) * sK + kL];
+  for (int n = 0; n < 4; ++n) qi[n] = static_cast<double>(x.QF[(n * NE3 + jL) * sK + kL]);
   if (bc) {
     double qinfb[4] = {0.0, 0.0, 0.0, 0.0}, tb = 0.0;
     const double fb[4] = {0.0, 0.0, 0.0, 0.0};
@@ -661,7 +699,67 @@ __global__ void __launch_bounds__(128) k_adj_speed(EdgeArgs<double> a, AdjEdgeAr
     wave_speed_vjp(a.gas, oohK, qi, wbar, qib);
   }
 #pragma unroll
-  for (int n = 0; n < 4; ++n) x.QFb[(n * NE3 + jL) * sK + kL] += qib[n];
+  for (int n = 0; n < 4; ++n) x.QFb[(n * NE3 + jL) * sK + kL] += static_cast<T>(qib[n]);
+}
+
+// Qbs += FluxEdgeInterp^T QFb, one thread per (variable, element).
+template <int N, typename T>
+__global__ void __launch_bounds__(128) k_adj_interp(const T* QFb, const double* Iop, T* Qbs, int K) {
+  constexpr int NP = Dims<N>::NP, NE3 = Dims<N>::NE3;
+  __shared__ T sI[NE3 * NP];
+  stage_operator(sI, Iop, NE3 * NP);
+  __syncthreads();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 4 * K) return;
+  const int n = t / K, k = t - n * K;
+  const size_t sK = static_cast<size_t>(K);
+  T f[NE3];
+#pragma unroll
+  for (int j = 0; j < NE3; ++j) f[j] = QFb[(n * NE3 + j) * sK + k];
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    T acc = T(0);
+#pragma unroll
+    for (int j = 0; j < NE3; ++j) acc += sI[j * NP + i] * f[j];
+    Qbs[(n * NP + i) * sK + k] += acc;
+  }
+}
+
+// Mixed path: the faces of the stage state Q0 + D (D = nullptr: Q0) in FP32,
+// FluxEdgeInterp applied per variable (the reverse sweep's linearisation point
+// at the edges).
+template <int N>
+__global__ void __launch_bounds__(128) k_adj_faces(const double* __restrict__ Q0, const float* __restrict__ D,
+                                                   const double* __restrict__ Iop, float* __restrict__ QF, int K) {
+  constexpr int NP = Dims<N>::NP, NE3 = Dims<N>::NE3;
+  __shared__ float sI[NE3 * NP];
+  stage_operator(sI, Iop, NE3 * NP);
+  __syncthreads();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 4 * K) return;
+  const int n = t / K, k = t - n * K;
+  const size_t sK = static_cast<size_t>(K);
+  float q[NP];
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    const size_t ind = (n * NP + i) * sK + k;
+    q[i] = static_cast<float>(Q0[ind]) + (D ? D[ind] : 0.0f);
+  }
+#pragma unroll
+  for (int j = 0; j < NE3; ++j) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int i = 0; i < NP; ++i) acc += sI[j * NP + i] * q[i];
+    QF[(n * NE3 + j) * sK + k] = acc;
+  }
+}
+
+// Element-wise conversion between the FP64 interface arrays and the FP32 adjoint.
+template <typename A, typename B>
+__global__ void k_convert(const A* __restrict__ src, B* __restrict__ dst, size_t n) {
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x)
+    dst[i] = static_cast<B>(src[i]);
 }
 
 // Qbs += FluxEdgeInterp^T QFb, one thread per (variable, element).

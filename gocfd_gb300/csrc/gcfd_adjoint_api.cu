@@ -11,8 +11,14 @@
 namespace gcfd_host {
 namespace {
 
+// The mixed path's adjoint (FP32 reverse of the mixed forward) covers the
+// Euler RHS and step without the artificial dissipation, with the FMA or
+// tensor-core stage kernel.
 int adj_check(gcfd_ctx* c) {
-  if (c->fp32) return fail(c, GCFD_ERR_UNSUPPORTED, "the adjoint runs on the FP64 path only");
+  if (c->fp32 && c->diss)
+    return fail(c, GCFD_ERR_UNSUPPORTED, "the adjoint of the mixed path runs without the PerssonC0 dissipation");
+  if (c->fp32 && c->pipe && c->pipeOn)
+    return fail(c, GCFD_ERR_UNSUPPORTED, "the adjoint of the mixed path does not run with the pipelined stage kernel");
   return GCFD_OK;
 }
 
@@ -79,6 +85,27 @@ int adj_init(gcfd_ctx* c) {
   const size_t S = static_cast<size_t>(4) * c->Np * c->K;
   const size_t F = static_cast<size_t>(4) * 3 * c->NE * c->K;
   const int nE = c->nInt + c->nBC;
+  if (c->fp32) {  // FP32 adjoint arrays; the stage increments are the forward's own
+    for (int s = 0; s < 5; ++s) {
+      if ((rc = dalloc(c, &c->tapeRHS32[s], S))) return rc;
+      if ((rc = dalloc(c, &c->tapeES[s], static_cast<size_t>(nE)))) return rc;
+      if ((rc = dalloc(c, &c->tapeDT[s], static_cast<size_t>(c->K)))) return rc;
+      if ((rc = dalloc(c, &c->Qb32[s], S))) return rc;
+    }
+    for (float** p : {&c->Qbf32, &c->Rb3_32})
+      if ((rc = dalloc(c, p, S))) return rc;
+    for (float** p : {&c->QF32, &c->QFb32, &c->FEb32})
+      if ((rc = dalloc(c, p, F))) return rc;
+    if ((rc = dalloc(c, &c->tapeSc0, 1))) return rc;
+    if ((rc = dalloc(c, &c->tapeSc, 1))) return rc;
+    if ((rc = dalloc(c, &c->Qbf, S))) return rc;  // FP64 staging of the caller's adjoints
+    if ((rc = dalloc(c, &c->carry, static_cast<size_t>(c->K)))) return rc;
+    if ((rc = dalloc(c, &c->dtOwnK, static_cast<size_t>(c->K)))) return rc;
+    if ((rc = dalloc(c, &c->esBar, static_cast<size_t>(nE)))) return rc;
+    if ((rc = dalloc(c, &c->argEdge, 8))) return rc;
+    c->adjReady = true;
+    return GCFD_OK;
+  }
   for (int s = 0; s < 5; ++s) {
     if ((rc = dalloc(c, &c->tapeRHS[s], S))) return rc;
     if ((rc = dalloc(c, &c->tapeES[s], static_cast<size_t>(nE)))) return rc;
@@ -134,6 +161,17 @@ int win_alloc(gcfd_ctx* c, double** p, size_t count) {
 // Point the context's stage arrays and tape at segment-tape slot i.
 void bind_slot(gcfd_ctx* c, int i) {
   const gcfd_ctx::TapeSlot& t = c->slots[i];
+  if (c->fp32) {
+    for (int s = 0; s < 5; ++s) {
+      if (s > 0) c->Dk[s] = t.D[s];
+      c->tapeRHS32[s] = t.rhs32[s];
+      c->tapeES[s] = t.es[s];
+      c->tapeDT[s] = t.dt[s];
+    }
+    c->tapeSc0 = t.sc0;
+    c->tapeSc = t.sc;
+    return;
+  }
   for (int s = 0; s < 5; ++s) {
     if (s > 0) c->Q[s] = t.Q[s];
     c->tapeRHS[s] = t.rhs[s];
@@ -151,7 +189,10 @@ void bind_slot(gcfd_ctx* c, int i) {
 // Slot 0 is the context's own stage arrays and tape; slots 1.. are allocated
 // per window (they go with the window's allocations).  Returns false, with
 // nothing kept, when they do not fit in device memory.
+bool alloc_slots_mixed(gcfd_ctx* c, int nslots);
+
 bool alloc_slots(gcfd_ctx* c, int nslots) {
+  if (c->fp32) return alloc_slots_mixed(c, nslots);
   c->slots.clear();
   gcfd_ctx::TapeSlot base{};
   for (int s = 0; s < 5; ++s) {
@@ -209,6 +250,140 @@ bool alloc_slots(gcfd_ctx* c, int nslots) {
   return true;
 }
 
+// The mixed path's slots: the stage increments D1..D4 and stage RHS in FP32,
+// edge speeds, local dt and scalars as on the FP64 path.
+bool alloc_slots_mixed(gcfd_ctx* c, int nslots) {
+  c->slots.clear();
+  gcfd_ctx::TapeSlot base{};
+  for (int s = 0; s < 5; ++s) {
+    base.D[s] = c->Dk[s];
+    base.rhs32[s] = c->tapeRHS32[s];
+    base.es[s] = c->tapeES[s];
+    base.dt[s] = c->tapeDT[s];
+  }
+  base.sc0 = c->tapeSc0;
+  base.sc = c->tapeSc;
+  c->slots.push_back(base);
+  const size_t S = static_cast<size_t>(4) * c->Np * c->K, K = c->K, nE = c->nInt + c->nBC;
+  auto rup = [](size_t b) { return (b + 255) & ~static_cast<size_t>(255); };
+  const size_t bS = rup(S * sizeof(float)), bE = rup(nE * sizeof(double)), bK = rup(K * sizeof(double));
+  const size_t bSc = rup(sizeof(Scalars));
+  const size_t per = 9 * bS + 5 * (bE + bK) + 2 * bSc;
+  std::vector<void*> got;
+  for (int i = 1; i < nslots; ++i) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, per) != cudaSuccess) {
+      cudaGetLastError();
+      for (void* q : got) cudaFree(q);
+      c->slots.resize(1);
+      return false;
+    }
+    got.push_back(p);
+    char* d = static_cast<char*>(p);
+    auto take = [&](size_t n) {
+      char* r = d;
+      d += n;
+      return r;
+    };
+    gcfd_ctx::TapeSlot t{};
+    for (int s = 1; s < 5; ++s) t.D[s] = reinterpret_cast<float*>(take(bS));
+    for (int s = 0; s < 5; ++s) {
+      t.rhs32[s] = reinterpret_cast<float*>(take(bS));
+      t.es[s] = reinterpret_cast<double*>(take(bE));
+      t.dt[s] = reinterpret_cast<double*>(take(bK));
+    }
+    t.sc0 = reinterpret_cast<Scalars*>(take(bSc));
+    t.sc = reinterpret_cast<Scalars*>(take(bSc));
+    c->slots.push_back(t);
+  }
+  for (void* q : got) c->winAllocs.push_back(q);
+  return true;
+}
+
+// gcfd_step_vjp on the mixed path: the recorded window's segments are
+// recomputed by the mixed forward from their FP64 checkpoints (hi + lo of the
+// compensated state), each step taped (stage RHS, edge speeds, dt; the stage
+// increments stay in the slot's D arrays), and reversed in FP32.
+int step_vjp_mixed(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const double* const* Qfinal_bar,
+                   double tfinal_bar, double* const* Q0_bar, double* qinf_bar4, double* t0_bar) {
+  const AdjOps& o = *adj_ops(c->N);
+  const OrderOps& fo = *order_ops(c->N);
+  const Ops fwd = fo.mixed;
+  const size_t S = static_cast<size_t>(4) * c->Np * c->K;
+  const size_t SB = S * sizeof(double);
+  int rc;
+  if ((rc = copy_shards(c, c->Qbf, nshards, Kmax, Qfinal_bar, true, nullptr))) return rc;
+  o.mixed_bar_convert(c, true);
+  GCFD_CUDA(c, cudaMemsetAsync(c->adjS, 0, sizeof(double) * 12, c->stream));
+  GCFD_CUDA(c, cudaMemcpyAsync(c->adjS + 10, &tfinal_bar, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  const int every = c->winEvery, nsteps = c->winSteps;
+  const int nseg = (nsteps + every - 1) / every;
+  // a step from the FP64 state in Q[0] and the time in sc: the stage-0 data
+  // rebuilt from Q[0], then one taped step into the bound slot
+  auto taped_step = [&]() {
+    fwd.prep(c);
+    fo.mixed_tape(c);
+    c->fp64Stale = true;
+  };
+  for (int seg = nseg - 1; seg >= 0; --seg) {
+    const int n0 = seg * every, m = std::min(every, nsteps - n0);
+    GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], c->ckpt + S * seg, SB, cudaMemcpyDeviceToDevice, c->stream));
+    GCFD_CUDA(c, cudaMemcpyAsync(&c->sc->time, c->ckptT + seg, sizeof(double), cudaMemcpyDeviceToDevice,
+                                 c->stream));
+    c->fp64Stale = false;
+    const bool taped = m > 1 && static_cast<int>(c->slots.size()) >= m;
+    fwd.prep(c);
+    for (int i = 0; i < m; ++i) {
+      if ((rc = sync_fp64_state(c))) return rc;
+      GCFD_CUDA(c, cudaMemcpyAsync(c->segQ + S * i, c->Q[0], SB, cudaMemcpyDeviceToDevice, c->stream));
+      GCFD_CUDA(c, cudaMemcpyAsync(c->segT + i, &c->sc->time, sizeof(double), cudaMemcpyDeviceToDevice,
+                                   c->stream));
+      if (taped) {  // the recompute keeps each step's tape in its own slot
+        bind_slot(c, i);
+        fo.mixed_tape(c);
+        c->fp64Stale = true;
+        GCFD_CUDA(c, cudaGetLastError());
+      } else if (i + 1 < m) {
+        GCFD_CUDA(c, cudaGraphLaunch(c->graphExec, c->stream));
+        c->fp64Stale = true;
+      }
+    }
+    if (taped) {
+      for (int i = m - 1; i >= 0; --i) {
+        bind_slot(c, i);
+        o.mixed_reverse_taped(c, c->segQ + S * i);
+        GCFD_CUDA(c, cudaGetLastError());
+      }
+      bind_slot(c, 0);
+      continue;
+    }
+    for (int i = m - 1; i >= 0; --i) {
+      GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], c->segQ + S * i, SB, cudaMemcpyDeviceToDevice, c->stream));
+      GCFD_CUDA(c, cudaMemcpyAsync(&c->sc->time, c->segT + i, sizeof(double), cudaMemcpyDeviceToDevice,
+                                   c->stream));
+      c->fp64Stale = false;
+      taped_step();
+      o.mixed_reverse_taped(c, c->segQ + S * i);
+      GCFD_CUDA(c, cudaGetLastError());
+    }
+  }
+  o.mixed_bar_convert(c, false);
+  double h[6];
+  GCFD_CUDA(c, cudaMemcpyAsync(h, c->adjS + 5, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  if ((rc = copy_shards(c, c->Qbf, nshards, Kmax, nullptr, false, Q0_bar))) return rc;
+  // back to the window's end: the FP64 state, rebuilt into the mixed state by
+  // the next step
+  GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], c->endQ, SB, cudaMemcpyDeviceToDevice, c->stream));
+  GCFD_CUDA(c, cudaMemcpyAsync(c->sc, c->endSc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream));
+  c->dirty = true;
+  c->fp64Stale = false;
+  GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (qinf_bar4)
+    for (int i = 0; i < 4; ++i) qinf_bar4[i] = h[i];
+  if (t0_bar) *t0_bar = h[5];
+  return GCFD_OK;
+}
+
 }  // namespace
 }  // namespace gcfd_host
 
@@ -248,6 +423,15 @@ int gcfd_rhs_vjp(gcfd_ctx* c, double time, int32_t nshards, const int32_t* Kmax,
   if ((rc = copy_shards(c, c->Qbf, nshards, Kmax, RHSbar, true, nullptr))) return rc;
   GCFD_CUDA(c, cudaMemcpyAsync(&c->sc->rhs_time, &time, sizeof(double), cudaMemcpyHostToDevice, c->stream));
   GCFD_CUDA(c, cudaMemsetAsync(c->adjS + 5, 0, sizeof(double) * 5, c->stream));
+  // One RHS adjoint costs about one RHS: it runs the FP64 kernels on every
+  // context (the mixed path's FP32 transpose of a single RHS loses up to ~5e-5
+  // relative at N = 1 and 4 to DivInt's cancellation; over a step dt scales
+  // that away, which is where the FP32 reverse sweep runs).
+  if (c->fp32 && !c->FEb) {
+    double* fe = nullptr;
+    if ((rc = dalloc(c, &fe, static_cast<size_t>(4) * 3 * c->NE * c->K))) return rc;
+    c->FEb = fe;
+  }
   const AdjOps& o = *adj_ops(c->N);
   o.rhs_vjp(c);
   GCFD_CUDA(c, cudaGetLastError());
@@ -291,9 +475,11 @@ int gcfd_record_steps(gcfd_ctx* c, int32_t nsteps, int32_t every, double* time, 
   // The segment tape (one slot per step of a segment) when it fits; without
   // it every step of a segment is recomputed twice in the reverse sweep.
   if (every > 1) alloc_slots(c, std::min(every, nsteps));
+  if ((rc = prepare_if_dirty(c))) return rc;
   for (int n = 0; n < nsteps; ++n) {
     if (n % every == 0) {
       const int j = n / every;
+      if ((rc = sync_fp64_state(c))) return rc;  // mixed path: the checkpoint is hi + lo in FP64
       GCFD_CUDA(c, cudaMemcpyAsync(c->ckpt + S * j, c->Q[0], S * sizeof(double), cudaMemcpyDeviceToDevice,
                                    c->stream));
       GCFD_CUDA(c, cudaMemcpyAsync(c->ckptT + j, &c->sc->time, sizeof(double), cudaMemcpyDeviceToDevice,
@@ -303,7 +489,9 @@ int gcfd_record_steps(gcfd_ctx* c, int32_t nsteps, int32_t every, double* time, 
                                      c->stream));
     }
     GCFD_CUDA(c, cudaGraphLaunch(c->graphExec, c->stream));
+    if (c->fp32) c->fp64Stale = true;
   }
+  if ((rc = sync_fp64_state(c))) return rc;
   GCFD_CUDA(c, cudaMemcpyAsync(c->endQ, c->Q[0], S * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
   if (c->diss)
     GCFD_CUDA(c, cudaMemcpyAsync(c->endV, c->DTVisc, KV * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
@@ -325,6 +513,7 @@ int gcfd_step_vjp(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doubl
   if (rc) return rc;
   if (c->winSteps < 1) return fail(c, GCFD_ERR_ARG, "no recorded window: call gcfd_record_steps first");
   if ((rc = check_shards(c, nshards, Kmax))) return rc;
+  if (c->fp32) return step_vjp_mixed(c, nshards, Kmax, Qfinal_bar, tfinal_bar, Q0_bar, qinf_bar4, t0_bar);
   const AdjOps& o = *adj_ops(c->N);
   const size_t S = static_cast<size_t>(4) * c->Np * c->K;
   const size_t SB = S * sizeof(double);

@@ -65,7 +65,7 @@ static __global__ void k_diss_argmax(DissArgs d, const double* sigE, const doubl
 // The SSP part is the same as k_adj_div's; the Euler RHS adjoint goes to RbE
 // for k_adj_div (stage -1 form) to transpose.
 template <int N>
-__global__ void __launch_bounds__(128) k_adj_diss_update(DissArgs d, AdjArgs a, AdjDissArgs x) {
+__global__ void __launch_bounds__(128) k_adj_diss_update(DissArgs d, AdjArgs<double> a, AdjDissArgs x) {
   constexpr int NP = DissDims<N>::NP, NE = DissDims<N>::NE, NF = DissDims<N>::NF, NR = DissDims<N>::NR;
   __shared__ double sD[NP * NF], sV[NP * NP], sVi[NP * NP], smf[NP];
   stage_operator(sD, a.DivInt, NP * NF);

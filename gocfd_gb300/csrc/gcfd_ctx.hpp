@@ -107,6 +107,11 @@ struct gcfd_ctx {
   double *carry = nullptr, *dtOwnK = nullptr, *esBar = nullptr;
   double* adjS = nullptr;      // [0,5) dt adjoints, [5,9) Qinf adjoint, [9] t-bar current, [10] t-bar next, [11] J
   int* argEdge = nullptr;      // [5]
+  // adjoint of the mixed path (FP32 arrays, same layouts; the stage states are
+  // Q0 + D_s with the forward's own increments Dk)
+  float* tapeRHS32[5] = {};
+  float* Qb32[5] = {};
+  float *Qbf32 = nullptr, *Rb3_32 = nullptr, *QF32 = nullptr, *QFb32 = nullptr, *FEb32 = nullptr;
   double *dXs = nullptr, *dYs = nullptr, *edgeW = nullptr;
   // adjoint of the dissipation
   double* tapeQ2pre = nullptr;
@@ -127,6 +132,8 @@ struct gcfd_ctx {
     double *rhs[5], *es[5], *dt[5], *dtv[5], *vs[5], *rhspre[5];
     double* q2pre;
     Scalars *sc0, *sc;
+    float* D[5];       // mixed path: D[1..4] stage increments
+    float* rhs32[5];   // mixed path: stage RHS
   };
   std::vector<TapeSlot> slots;
   bool facesFromState = false;  // reverse stages rebuild their faces (the segment tape keeps none)
@@ -208,6 +215,7 @@ struct OrderOps {
   Ops fp64, mixed;
   int (*mixed_consts)(gcfd_ctx*);  // FP32 operators into constant memory, tensor-core operand and launch shape
   int (*mixed_pipe)(gcfd_ctx*);    // tensor maps and grid of the persistent stage kernel
+  void (*mixed_tape)(gcfd_ctx*);   // one mixed step with the adjoint tape (stage RHS, edge speeds, dt)
 };
 
 // Adjoint launchers of one order (gcfd_order_adj.cu).
@@ -217,6 +225,8 @@ struct AdjOps {
   void (*reverse_taped)(gcfd_ctx*, const double*);
   void (*rhs_vjp)(gcfd_ctx*);
   void (*functional)(gcfd_ctx*, int);
+  void (*mixed_reverse_taped)(gcfd_ctx*, const double*);  // FP32 adjoint of a step taped by mixed_tape
+  void (*mixed_bar_convert)(gcfd_ctx*, bool);  // Qbf (FP64) -> Qbf32 (true) or back (false)
 };
 
 const OrderOps* order_ops_0();
@@ -251,6 +261,7 @@ inline int resid_units(const gcfd_ctx* c) {
 
 // Shared host helpers (gcfd.cu).
 int sync_fp64_state(gcfd_ctx* c);
+int prepare_if_dirty(gcfd_ctx* c);
 int check_shards(gcfd_ctx* c, int nshards, const int32_t* Kmax);
 int copy_shards(gcfd_ctx* c, double* dst, int nshards, const int32_t* Kmax, const double* const* Q,
                 bool toDevice, double* const* Qout);

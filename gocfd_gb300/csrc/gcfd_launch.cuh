@@ -285,6 +285,7 @@ struct MixedLaunch {
     a.VF32 = reinterpret_cast<const float*>(c->VF);
     a.err = reinterpret_cast<unsigned int*>(&c->sc->errFlags);
     a.rhsOnly = 0;
+    a.tapeRHS = nullptr;
     a.gviscS = nullptr;
     a.cdiff = 0.0;
     return a;
@@ -422,6 +423,27 @@ struct MixedLaunch {
     m2.gviscS = c->sc->gvisc;
     m2.cdiff = 1.0 / (double(c->N + 1) * double(c->N + 1));
     k_mixed_diss_update<N><<<gridE(c), 128, 0, c->stream>>>(m2, L::update_args(c, s, Qs64));
+  }
+  // One step with the adjoint tape: the launches of step() (so the stage
+  // increments Dk are those of the recorded trajectory), plus the stage RHS
+  // written by the stage kernel, per-stage copies of the edge speeds and local
+  // dt, and the scalars before (BC time) and after (per-stage gmax and dt).
+  static void tape_step(gcfd_ctx* c) {
+    cudaMemcpyAsync(c->tapeSc0, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream);
+    k_step_begin<<<1, 32, 0, c->stream>>>(c->sc);
+    for (int s = 0; s < 5; ++s) {
+      edges(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s], true);
+      cudaMemcpyAsync(c->tapeES[s], c->edgeSpeed, sizeof(double) * c->nEdges, cudaMemcpyDeviceToDevice,
+                      c->stream);
+      MixedArgs a = args(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]);
+      a.tapeRHS = c->tapeRHS32[s];
+      stage_kernel(c, a);
+      if (c->prm.local_time_stepping)
+        cudaMemcpyAsync(c->tapeDT[s], c->DT, sizeof(double) * c->K, cudaMemcpyDeviceToDevice, c->stream);
+    }
+    k_resid_blocks<<<kResidBlocks, kResidBlockThreads, 0, c->stream>>>(c->sc, resid_units(c));
+    k_step_end<<<1, kResidBlocks, 0, c->stream>>>(c->sc, c->prm.local_time_stepping);
+    cudaMemcpyAsync(c->tapeSc, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream);
   }
   static void prep_state(gcfd_ctx* c) { prepare(c, c->Q[0]); }
   static void prep_state_range(gcfd_ctx* c, int k0, int k1) { prepare_range(c, c->Q[0], k0, k1); }

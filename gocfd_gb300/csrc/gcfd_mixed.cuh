@@ -309,6 +309,7 @@ struct MixedArgs {
   const float* DissY32;
   const float* VF32;
   unsigned int* err;          // error flags (bit 0: a tensor-core wait ran out)
+  float* tapeRHS;             // adjoint tape: the stage's RHS [n][i][k] (nullptr: not taped)
 };
 
 // SSP(5,4) weights of rkAdvance (euler.go:511-564) in increment form:
@@ -834,6 +835,10 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const int eslot[3
       if (k == 0 && n == 0) a.sc->dt[s] = dtk;
     }
     const float dt = static_cast<float>(dtk);
+    if (a.tapeRHS) {
+#pragma unroll
+      for (int r = 0; r < NP; ++r) a.tapeRHS[off + r * sK] = rhs[r];
+    }
     float dn[NP];
     if (s == 0) {
 #pragma unroll

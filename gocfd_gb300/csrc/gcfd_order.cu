@@ -190,7 +190,7 @@ const OrderOps* GCFD_CAT(order_ops_, GCFD_ORDER)() {
       Ops{&Launch<kN, double>::step, &Launch<kN, double>::rhs, nullptr, nullptr},
       Ops{&MixedLaunch<kN>::step, &MixedLaunch<kN>::rhs, &MixedLaunch<kN>::prep_state,
           &MixedLaunch<kN>::prep_state_range},
-      &mixed_consts, &mixed_pipe};
+      &mixed_consts, &mixed_pipe, &MixedLaunch<kN>::tape_step};
   return &o;
 }
 

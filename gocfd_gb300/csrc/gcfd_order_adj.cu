@@ -15,7 +15,7 @@ namespace {
 
 constexpr int kN = GCFD_ORDER;
 
-// Adjoint launchers (FP64 path).
+// Adjoint launchers (FP64 path, and the FP32 reverse of the mixed path).
 template <int N>
 struct AdjLaunch {
   using L = Launch<N, double>;
@@ -25,8 +25,9 @@ struct AdjLaunch {
     e.QF = static_cast<const double*>(c->QF);
     return e;
   }
-  static AdjEdgeArgs adj_edge_args(gcfd_ctx* c) {
-    AdjEdgeArgs x;
+  static AdjEdgeArgs<double> adj_edge_args(gcfd_ctx* c, const double* faces) {
+    AdjEdgeArgs<double> x;
+    x.QF = faces;
     x.FEb = c->FEb;
     x.QFb = c->QFb;
     x.qinfb = c->adjS + 5;
@@ -35,12 +36,13 @@ struct AdjLaunch {
     x.useManualRoe = 1;
     return x;
   }
-  static AdjArgs adj_args(gcfd_ctx* c, int s, const double* Qs, const double* Qbn, double* Qbs) {
-    AdjArgs a;
+  static AdjArgs<double> adj_args(gcfd_ctx* c, int s, const double* Qs, const double* Qbn, double* Qbs) {
+    AdjArgs<double> a;
     a.K = c->K;
     a.stage = s;
     a.localDT = c->prm.local_time_stepping;
     a.Qs = Qs;
+    a.Ds = nullptr;
     a.Qbn = Qbn;
     a.rhs = s >= 0 ? c->tapeRHS[s] : nullptr;
     a.rhs3 = c->tapeRHS[3];
@@ -107,14 +109,15 @@ struct AdjLaunch {
     k_step_end<<<1, kResidBlocks, 0, c->stream>>>(c->sc, c->prm.local_time_stepping);
     cudaMemcpyAsync(c->tapeSc, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream);
   }
-  static void edges(gcfd_ctx* c, const EdgeArgs<double>& e, const AdjEdgeArgs& x) {
+  template <typename T>
+  static void edges(gcfd_ctx* c, const EdgeArgs<double>& e, const AdjEdgeArgs<T>& x) {
     if (c->nInt > 0) {
       if (e.flux == kFluxRoe && x.useManualRoe)
-        k_adj_edge<N, true><<<grid(c->nInt), 128, 0, c->stream>>>(e, x);
+        k_adj_edge<N, true, T><<<grid(c->nInt), 128, 0, c->stream>>>(e, x);
       else
-        k_adj_edge<N, false><<<grid(c->nInt), 128, 0, c->stream>>>(e, x);
+        k_adj_edge<N, false, T><<<grid(c->nInt), 128, 0, c->stream>>>(e, x);
     }
-    if (c->nBC > 0) k_adj_edge_bc<N><<<grid(c->nBC * Dims<N>::NE), 128, 0, c->stream>>>(e, x);
+    if (c->nBC > 0) k_adj_edge_bc<N, T><<<grid(c->nBC * Dims<N>::NE), 128, 0, c->stream>>>(e, x);
   }
   static AdjDissArgs adj_diss_args(gcfd_ctx* c, const double* Qsens, int s) {
     AdjDissArgs x;
@@ -171,35 +174,17 @@ struct AdjLaunch {
     k_adj_diss_edge<N><<<grid(c->nInt + c->nBC), 128, 0, c->stream>>>(d, x);
     constexpr int NF = Dims<N>::NF;
     k_adj_diss_grad<N><<<grid(c->K), 128, sizeof(double) * (NF * NF + NF * 3), c->stream>>>(d, x, Qbs);
-    k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, Qbs, c->K);
+    k_adj_interp<N, double><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, Qbs, c->K);
     if (s == 2) k_adj_diss_limit<N><<<grid(4 * c->K), 128, 0, c->stream>>>(d, x);
     k_adj_diss_alpha<<<grid(c->K), 128, 0, c->stream>>>(d, x);
     k_adj_diss_sensor<N><<<grid(c->K), 128, 0, c->stream>>>(d, x, Qbs);
   }
-  // The reverse of stage s.  Q0 is the step's initial state.  With a segment
-  // tape the stage faces are not taped (they are FluxEdgeInterp of the stage
-  // state, after the rkStep-2 limiter where it applies) and are rebuilt here.
-  static void reverse_stage(gcfd_ctx* c, int s, const double* Q0) {
-    const double* Qs = (s == 0) ? Q0 : c->Q[s];
-    if (c->facesFromState) {
-      void* f = c->QF;
-      c->QF = c->tapeQF[s];
-      L::interp(c, Qs);
-      c->QF = f;
-    }
-    const double* Qbn = (s == 4) ? c->Qbf : c->Qb[s + 1];
-    const double* Qsens = (s == 2) ? c->tapeQ2pre : Qs;
-    if (c->diss) {
-      diss_reverse_update(c, s, Qs, Qsens, Qbn, c->Qb[s], c->tapeQF[s]);
-      k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, -1, Qs, c->RbE, c->Qb[s]));
-    } else {
-      k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, s, Qs, Qbn, c->Qb[s]));
-    }
-    EdgeArgs<double> e = edge_args(c, &c->tapeSc0->time);
-    e.QF = c->tapeQF[s];
-    const AdjEdgeArgs x = adj_edge_args(c);
+  // The time-step adjoints of stage s (after the edge adjoints): the dt
+  // adjoint onto the wave speed that set it (global: the argmax edge; local:
+  // per element), with the viscous limit of the dissipation.  esBar is left
+  // for k_adj_speed.
+  static void dt_reverse(gcfd_ctx* c, int s) {
     const int nE = c->nInt + c->nBC;
-    edges(c, e, x);
     cudaMemsetAsync(c->esBar, 0, sizeof(double) * nE, c->stream);
     if (c->diss) cudaMemsetAsync(c->vsBar, 0, sizeof(double) * nE, c->stream);
     AdjDtArgs d;
@@ -239,11 +224,36 @@ struct AdjLaunch {
       }
       k_adj_gsel<<<1, 32, 0, c->stream>>>(d);
     }
-    k_adj_speed<N><<<grid(nE), 128, 0, c->stream>>>(e, x);
+  }
+  // The reverse of stage s.  Q0 is the step's initial state.  With a segment
+  // tape the stage faces are not taped (they are FluxEdgeInterp of the stage
+  // state, after the rkStep-2 limiter where it applies) and are rebuilt here.
+  static void reverse_stage(gcfd_ctx* c, int s, const double* Q0) {
+    const double* Qs = (s == 0) ? Q0 : c->Q[s];
+    if (c->facesFromState) {
+      void* f = c->QF;
+      c->QF = c->tapeQF[s];
+      L::interp(c, Qs);
+      c->QF = f;
+    }
+    const double* Qbn = (s == 4) ? c->Qbf : c->Qb[s + 1];
+    const double* Qsens = (s == 2) ? c->tapeQ2pre : Qs;
+    if (c->diss) {
+      diss_reverse_update(c, s, Qs, Qsens, Qbn, c->Qb[s], c->tapeQF[s]);
+      k_adj_div<N, double><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, -1, Qs, c->RbE, c->Qb[s]));
+    } else {
+      k_adj_div<N, double><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, s, Qs, Qbn, c->Qb[s]));
+    }
+    EdgeArgs<double> e = edge_args(c, &c->tapeSc0->time);
+    e.QF = c->tapeQF[s];
+    const AdjEdgeArgs<double> x = adj_edge_args(c, c->tapeQF[s]);
+    edges(c, e, x);
+    dt_reverse(c, s);
+    k_adj_speed<N, double><<<grid(c->nInt + c->nBC), 128, 0, c->stream>>>(e, x);
     if (c->diss)
       diss_reverse_rest(c, s, Qs, Qsens, c->Qb[s], c->tapeQF[s]);
     else
-      k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[s], c->K);
+      k_adj_interp<N, double><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[s], c->K);
   }
   // Adjoint of one step whose initial state is Q0 (already in c->Q[0]) and
   // time is in c->sc.  In: Qbf, adjS[10] (t-bar of the step's end).  Out:
@@ -284,17 +294,17 @@ struct AdjLaunch {
     const EdgeArgs<double> e = edge_args(c, &c->sc->rhs_time);
     if (c->diss) {
       diss_reverse_update(c, -1, c->Qtmp, c->Qtmp, c->Qbf, c->Qb[0], static_cast<const double*>(c->QF));
-      k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, -1, c->Qtmp, c->RbE, c->Qb[0]));
+      k_adj_div<N, double><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, -1, c->Qtmp, c->RbE, c->Qb[0]));
     } else {
-      k_adj_div<N><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, -1, c->Qtmp, c->Qbf, c->Qb[0]));
+      k_adj_div<N, double><<<grid(c->K), 128, 0, c->stream>>>(adj_args(c, -1, c->Qtmp, c->Qbf, c->Qb[0]));
     }
-    edges(c, e, adj_edge_args(c));
+    edges(c, e, adj_edge_args(c, static_cast<const double*>(c->QF)));
     if (c->diss) {
       cudaMemsetAsync(c->vsBar, 0, sizeof(double) * (c->nInt + c->nBC), c->stream);
       diss_reverse_rest(c, -1, c->Qtmp, c->Qtmp, c->Qb[0], static_cast<const double*>(c->QF));
       c->QF = faces;
     } else {
-      k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[0], c->K);
+      k_adj_interp<N, double><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[0], c->K);
     }
   }
   // Functionals of the current state Q[0]: J into adjS[11], dJ/dQ into Qb[0],
@@ -314,15 +324,89 @@ struct AdjLaunch {
     if (c->nBC > 0)
       k_func_wall<N><<<grid(c->nBC), 128, 0, c->stream>>>(e, c->edgeW, kind == GCFD_FUNC_WALL_FORCE_Y, c->QFb,
                                                           c->adjS + 11);
-    k_adj_interp<N><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[0], c->K);
+    k_adj_interp<N, double><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb, c->Iop, c->Qb[0], c->K);
+  }
+
+  // ---- mixed path: the FP32 adjoint of a step taped by the mixed forward ----
+  static AdjArgs<float> adj_args32(gcfd_ctx* c, int s, const double* Q0, const float* Qbn, float* Qbs) {
+    AdjArgs<float> a;
+    a.K = c->K;
+    a.stage = s;
+    a.localDT = c->prm.local_time_stepping;
+    a.Qs = Q0;
+    a.Ds = s > 0 ? c->Dk[s] : nullptr;
+    a.Qbn = Qbn;
+    a.rhs = s >= 0 ? c->tapeRHS32[s] : nullptr;
+    a.rhs3 = c->tapeRHS32[3];
+    a.Qb0 = c->Qb32[0];
+    a.Qbs = Qbs;
+    a.Qb2 = c->Qb32[2];
+    a.Qb3 = c->Qb32[3];
+    a.Rb3 = c->Rb3_32;
+    a.dtS = c->tapeSc->dt;
+    a.dtK = s >= 0 ? c->tapeDT[s] : nullptr;
+    a.dtbarG = c->adjS;
+    a.dtOwnK = c->dtOwnK;
+    a.DivInt = c->Div;
+    a.Jdet = c->Jdet;
+    a.Jinv = c->Jinv;
+    a.FEb = c->FEb32;
+    const float g = static_cast<float>(c->fsFar.gamma);
+    a.gas = Gas<float>{g, g - 1.0f, 1.0f / (g - 1.0f)};
+    return a;
+  }
+  static AdjEdgeArgs<float> adj_edge_args32(gcfd_ctx* c) {
+    AdjEdgeArgs<float> x;
+    x.QF = c->QF32;
+    x.FEb = c->FEb32;
+    x.QFb = c->QFb32;
+    x.qinfb = c->adjS + 5;
+    x.tb = c->adjS + 9;
+    x.esBar = c->esBar;
+    x.useManualRoe = 1;
+    return x;
+  }
+  // Stage s in reverse: the stage state is Q0 + D_s (the taped increments), its
+  // faces are interpolated once more in FP32, then the kernels of the FP64
+  // sweep in FP32 (the boundary points and wave-speed maxima in FP64).
+  static void mixed_reverse_stage(gcfd_ctx* c, int s, const double* Q0) {
+    k_adj_faces<N><<<grid(4 * c->K), 128, 0, c->stream>>>(Q0, s > 0 ? c->Dk[s] : nullptr, c->Iop, c->QF32, c->K);
+    const float* Qbn = (s == 4) ? c->Qbf32 : c->Qb32[s + 1];
+    k_adj_div<N, float><<<grid(c->K), 128, 0, c->stream>>>(adj_args32(c, s, Q0, Qbn, c->Qb32[s]));
+    const EdgeArgs<double> e = edge_args(c, &c->tapeSc0->time);
+    const AdjEdgeArgs<float> x = adj_edge_args32(c);
+    edges(c, e, x);
+    dt_reverse(c, s);
+    k_adj_speed<N, float><<<grid(c->nInt + c->nBC), 128, 0, c->stream>>>(e, x);
+    k_adj_interp<N, float><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb32, c->Iop, c->Qb32[s], c->K);
+  }
+  // The adjoint of a mixed step whose tape is bound; Q0 is the step's initial
+  // state (FP64).  In: Qbf32, adjS[10]; out: Qbf32 <- adjoint of Q0, adjS[10]
+  // <- t-bar of the step's start.
+  static void mixed_reverse_taped(gcfd_ctx* c, const double* Q0) {
+    cudaMemsetAsync(c->adjS, 0, sizeof(double) * 5, c->stream);
+    cudaMemcpyAsync(c->adjS + 9, c->adjS + 10, sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemsetAsync(c->carry, 0, sizeof(double) * c->K, c->stream);
+    for (int s = 4; s >= 0; --s) mixed_reverse_stage(c, s, Q0);
+    std::swap(c->Qbf32, c->Qb32[0]);
+    cudaMemcpyAsync(c->adjS + 10, c->adjS + 9, sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  }
+  static void mixed_bar_convert(gcfd_ctx* c, bool toFP32) {
+    const size_t S = static_cast<size_t>(4) * c->Np * c->K;
+    if (toFP32)
+      k_convert<double, float><<<1024, 256, 0, c->stream>>>(c->Qbf, c->Qbf32, S);
+    else
+      k_convert<float, double><<<1024, 256, 0, c->stream>>>(c->Qbf32, c->Qbf, S);
   }
 };
 
 }  // namespace
 
 const AdjOps* GCFD_CAT(adj_ops_, GCFD_ORDER)() {
-  static const AdjOps o{&AdjLaunch<kN>::tape_step, &AdjLaunch<kN>::reverse_step, &AdjLaunch<kN>::reverse_taped,
-                        &AdjLaunch<kN>::rhs_vjp, &AdjLaunch<kN>::functional};
+  static const AdjOps o{&AdjLaunch<kN>::tape_step,       &AdjLaunch<kN>::reverse_step,
+                        &AdjLaunch<kN>::reverse_taped,   &AdjLaunch<kN>::rhs_vjp,
+                        &AdjLaunch<kN>::functional,      &AdjLaunch<kN>::mixed_reverse_taped,
+                        &AdjLaunch<kN>::mixed_bar_convert};
   return &o;
 }
 

@@ -185,15 +185,22 @@ int gcfd_device_fma_peaks(int32_t device, double* fp64_tflops, double* fp32_tflo
  * 5 flux-point r,s (NpFlux x 2).  With out == NULL only rows/cols are set. */
 int gcfd_host_operator(int32_t N, int32_t which, double* out, int32_t* rows, int32_t* cols);
 
-/* ---- Adjoint (vector-Jacobian products), FP64 path ----
+/* ---- Adjoint (vector-Jacobian products) ----
  * The reference has no adjoint; these transpose its discrete RHS and step
  * exactly, including the time step's dependence on the state (the global max
  * wave speed of calculateGlobalDT, euler.go:945-971, with the FinalTime clip;
  * the running max of CalculateLocalDT, euler.go:973-1002), the IVortex
  * boundary state's dependence on the solver time and, with the PerssonC0
  * limiter, the sensor, vertex maxima, limiter, RT gradient, viscous fluxes and
- * viscous time-step limit.  A mixed-precision context returns
- * GCFD_ERR_UNSUPPORTED (its state is handed to an FP64 context instead). */
+ * viscous time-step limit.
+ * On a mixed-precision context (GCFD_PREC_FP32 / GCFD_PREC_TF32X3) the
+ * window's steps are recomputed and taped by the mixed forward itself and the
+ * reverse sweep of gcfd_step_vjp runs in FP32 (boundary points and wave-speed
+ * maxima in FP64); the state adjoints agree with the FP64 path's to ~1e-6
+ * relative.  gcfd_rhs_vjp runs the FP64 kernels on every context.  The mixed
+ * path's adjoint covers the Euler RHS and step without the PerssonC0
+ * dissipation and without GCFD_OPT_STAGE_PIPELINE; those return
+ * GCFD_ERR_UNSUPPORTED. */
 
 /* Functionals of the current state: the wall pressure force, summed over Wall
  * and Cyl boundary edges as |edge| sum_p w_p p n_x (or n_y), with the
@@ -219,7 +226,9 @@ int gcfd_rhs_vjp(gcfd_ctx* ctx, double time, int32_t nshards, const int32_t* Kma
 
 /* Advance nsteps like gcfd_step, keeping a checkpoint of the state every
  * checkpoint_every steps for a following gcfd_step_vjp (memory: the
- * checkpoints plus checkpoint_every states). */
+ * checkpoints plus checkpoint_every states, FP64; plus, when it fits, a tape
+ * slot per step of a segment).  A mixed-precision context checkpoints its
+ * compensated state as hi + lo in FP64, which restores it exactly. */
 int gcfd_record_steps(gcfd_ctx* ctx, int32_t nsteps, int32_t checkpoint_every, double* time, double* dt_last);
 
 /* Adjoint of the recorded window (RungeKutta5SSP.Step x nsteps, euler.go:408-418):

@@ -293,20 +293,9 @@ def test_vortex_error_functional():
     gpu.close()
 
 
-def test_adjoint_rejects_mixed_path():
-    from gocfd_gb300 import _lib
-    mesh = far_box(2, 2)
-    ip = InputParameters2D(CFL=0.5, FluxType="roe", InitType="freestream", PolynomialOrder=2, FinalTime=1e9,
-                           Minf=0.5, Gamma=1.4)
-    with Euler(ip, mesh, 1, precision="fp32") as gpu:
-        with pytest.raises(_lib.GcfdError) as e:
-            gpu.record(1)
-        assert e.value.code == -7
-
-
 @pytest.mark.parametrize("precision,limiter", [("fp32", ""), ("fp64", "PerssonC0")])
-def test_functional_on_paths_without_adjoint(precision, limiter):
-    """The functionals need no adjoint: the mixed path and the PerssonC0 path evaluate them too."""
+def test_functional_on_mixed_and_dissipation_paths(precision, limiter):
+    """The functionals on the mixed path and the PerssonC0 path, against the FP64 one."""
     mesh = meshes.wedge_channel(8, 4)
     ip = InputParameters2D(CFL=0.5, FluxType="roe", InitType="freestream", PolynomialOrder=2, FinalTime=1e9,
                            Minf=2.0, Gamma=1.4, Limiter=limiter, Kappa=6.0)

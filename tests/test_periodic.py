@@ -103,3 +103,61 @@ def test_periodic_step_parity(precision, tol, ttol):
     q = gpu.get_global_state()
     assert np.linalg.norm(q - ora.Q) / np.linalg.norm(ora.Q) <= tol
     gpu.close()
+
+
+@pytest.mark.gpu
+def test_periodic_step_vjp_against_oracle_fd():
+    """The adjoint runs through the paired periodic edges like any shared edge:
+    a 6-step window (checkpoint every 3) against the oracle's central differences."""
+    mesh = meshes.periodic_box(6, jitter=0.1, seed=8)
+    gpu, ora = _pair(mesh, 2)
+    rng = np.random.default_rng(21)
+    Q0 = np.ascontiguousarray(ora.Q * (1.0 + 0.01 * rng.uniform(-1, 1, ora.Q.shape)))
+    nsteps = 6
+    gpu.set_global_state(Q0)
+    gpu.time = 0.0
+    gpu.record(nsteps, 3)
+    Qbf = rng.standard_normal(Q0.shape)
+    Qb0, _, _ = gpu.step_vjp(Qbf)
+    d = rng.standard_normal(Q0.shape) * np.abs(Q0)
+    h = 1e-6
+
+    def J(sign):
+        ora.Q = np.ascontiguousarray(Q0 + sign * h * d)
+        ora.time = 0.0
+        ora.step(nsteps)
+        return float(np.sum(Qbf * ora.Q))
+    fd = (J(1.0) - J(-1.0)) / (2 * h)
+    ad = float(np.sum(Qb0 * d))
+    assert abs(ad - fd) <= 1e-6 * max(abs(ad), abs(fd)), (ad, fd)
+    gpu.close()
+
+
+@pytest.mark.gpu
+def test_periodic_with_shock_capturing_matches_oracle():
+    """PerssonC0 on a periodic box ([-1, 1]^2) holding Sod states joined by a tanh
+    front inside the elements at x = 0.5 (the sensor is on there) and by a jump
+    across the periodic seam at x = -1 / 1: the sensor, vertex maxima, viscous edge
+    fluxes and limiter run on the paired edges; 10 FP64 steps against the oracle."""
+    mesh = meshes.periodic_box(16, L=2.0, jitter=0.1, seed=9)
+    ip = InputParameters2D(CFL=0.3, FluxType="roe", InitType="shocktube", PolynomialOrder=2, FinalTime=1e9,
+                           Gamma=1.4, MaxIterations=10 ** 9, Limiter="PerssonC0", Kappa=5.0)
+    gpu = Euler(ip, mesh, 1, precision="fp64")
+    ora = oracle.OracleSolver(2, mesh.VX, mesh.VY, mesh.EToV, mesh.bc_edges, flux="roe", init="shocktube", cfl=0.3,
+                              gamma=1.4, limiter="PerssonC0", kappa=5.0)
+    X = ora.geo.SolX
+    front = 0.5 * (1.0 + np.tanh((X - 0.5) / 0.03))
+    h = np.clip(front * 0.5 * (1.0 - np.tanh((X + 0.6) / 0.03)) + front, 0.0, 1.0)
+    Q = np.zeros((4,) + X.shape)
+    Q[0], Q[3] = 1.0 + (0.125 - 1.0) * h, (1.0 + (0.1 - 1.0) * h) / 0.4
+    Q = np.ascontiguousarray(Q)
+    ora.Q = Q.copy()
+    gpu.set_global_state(Q)
+    _, sigma, _, _, _ = ora.sensor(ora.Q)
+    assert (sigma > 0).any()  # the shock capturing is active
+    gpu.step(10)
+    ora.step(10)
+    q = gpu.get_global_state()
+    assert np.isfinite(q).all()
+    assert np.linalg.norm(q - ora.Q) / np.linalg.norm(ora.Q) <= 1e-10
+    gpu.close()
