@@ -266,7 +266,8 @@ def exact_vortex_param_derivative(X, Y, t, param: str, vortex=(5.0, 0.0, 0.0, 1.
 
 
 def adjoint_smooth(name: str, steps: int, every: int, warm_steps: int = 0, warm_precision: str = "fp32",
-                   params=("x0", "beta"), hs=(2e-4, 1e-4, 5e-5, 2.5e-5), device: int = 0):
+                   params=("x0", "beta"), hs=(2e-4, 1e-4, 5e-5, 2.5e-5), device: int = 0,
+                   adjoint_precision: str = "fp64"):
     """The field-error adjoint of a vortex configuration checked along smooth
     one-parameter directions of the window's initial state: d = dQ/d(param) of
     the exact vortex at the window's start (a shift of the vortex centre, or a
@@ -279,7 +280,15 @@ def adjoint_smooth(name: str, steps: int, every: int, warm_steps: int = 0, warm_
     different maximiser the map has a kink.  Each run records its per-step dt,
     and dt_fd(h) = (dt+ - dt-) / 2h is compared with dt_fd(h/2): a step where
     they disagree by more than 1% straddles such a switch.  These counts go
-    into the output beside the gradients."""
+    into the output beside the gradients.
+
+    adjoint_precision "fp32" (or "tf32x3") takes the gradient from the mixed
+    path's FP32 adjoint instead, over its own recorded window, with the FP64
+    path's field-error weight dJ/dQ_final: the differences stay FP64, and both
+    sides then differentiate the same weighted sum.  (The mixed path's own
+    weight 2 (Q_final - Q_exact) is not the FP64 one: after 1000+ steps the
+    discretisation error is ~3e-7 per value and the mixed path's rounding
+    differs from the FP64 path's by a tenth of that.)"""
     cfg = CONFIGS[name]
     assert cfg.mesh == "vortex"
     mesh = build_mesh(cfg)
@@ -294,12 +303,26 @@ def adjoint_smooth(name: str, steps: int, every: int, warm_steps: int = 0, warm_
                 s.time = info["time"]
         Q0, t0 = s.get_global_state(), s.time
         out["K"], out["t0"] = s.K, t0
-        t1 = time.perf_counter()
-        s.record(steps, every)
-        t2 = time.perf_counter()
-        J, Qbf, tbf = s.functional("vortex_error")
-        Qb0, _, _ = s.step_vjp(Qbf, tbf)
-        t3 = time.perf_counter()
+        out["adjoint_precision"] = adjoint_precision
+        if adjoint_precision == "fp64":
+            t1 = time.perf_counter()
+            s.record(steps, every)
+            t2 = time.perf_counter()
+            J, Qbf, tbf = s.functional("vortex_error")
+            Qb0, _, _ = s.step_vjp(Qbf, tbf)
+            t3 = time.perf_counter()
+        else:
+            s.step(steps)
+            J, Qbf, tbf = s.functional("vortex_error")
+            with Euler(ip, mesh, 1, precision=adjoint_precision, device=device, vortex_center=(0.0, 0.0)) as g:
+                g.set_global_state(Q0)
+                g.time = t0
+                t1 = time.perf_counter()
+                g.record(steps, every)
+                t2 = time.perf_counter()
+                out["J_adjoint_path"] = g.functional("vortex_error")[0]
+                Qb0, _, _ = g.step_vjp(Qbf, tbf)
+                t3 = time.perf_counter()
         out.update(J=J, record_s=t2 - t1, vjp_s=t3 - t2)
         X, Y = solution_points_xy(s)
 
@@ -394,12 +417,15 @@ def main(argv=None):
     p.add_argument("--smooth", action="store_true",
                    help="vortex adjoint: check along the smooth directions d/dx0 and d/dbeta of the exact vortex "
                         "with an h sweep and Richardson extrapolation instead of a random direction")
+    p.add_argument("--adjoint-precision", choices=["fp64", "fp32", "tf32x3"], default="fp64",
+                   help="with --smooth: the path whose adjoint gives the gradient (fp32: the mixed path)")
     a = p.parse_args(argv)
     if a.adjoint_steps and a.config.startswith("wedge"):
         res = wedge_sensitivity(a.adjoint_steps, a.checkpoint_every, a.scale, fd_h=a.fd_h)
     elif a.adjoint_steps and a.smooth:
         res = adjoint_smooth(a.config, a.adjoint_steps, a.checkpoint_every, a.warm_steps,
-                             a.precision if a.precision != "fp64" else "fp32")
+                             a.precision if a.precision != "fp64" else "fp32",
+                             adjoint_precision=a.adjoint_precision)
     elif a.adjoint_steps:
         res = adjoint(a.config, a.adjoint_steps, a.checkpoint_every, a.warm_steps,
                       a.precision if a.precision != "fp64" else "fp32", fd_h=a.fd_h)

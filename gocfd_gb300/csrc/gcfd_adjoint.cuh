@@ -18,6 +18,8 @@
 //   k_adj_speed   wave speed Jacobian^T at each edge's max point
 //   k_adj_interp  FluxEdgeInterp^T of the face adjoints
 #pragma once
+#include <type_traits>
+
 #include "gcfd_dual.cuh"
 #include "gcfd_kernels.cuh"
 
@@ -206,17 +208,19 @@ static __device__ __noinline__ void riemann_vjp_dual(int kind, const Gas<double>
   }
 }
 
-// Edge-point wave speed oohK (|u| + c) (StoreEdgeAggregates, edges.go:274-286) in reverse.
+// Edge-point wave speed oohK (|u| + c) (StoreEdgeAggregates, edges.go:274-286)
+// in reverse, tangents in S.
+template <typename S>
 __device__ __forceinline__ void wave_speed_vjp(const Gas<double>& g, double oohK, const double q[4], double wb,
                                                double qb[4]) {
-  using D = Dual<4>;
+  using D = Dual<4, S>;
   D d[4];
 #pragma unroll
-  for (int i = 0; i < 4; ++i) d[i] = seed<4>(q[i], i);
-  const Gas<D> gd = dual_gas<4>(g);
+  for (int i = 0; i < 4; ++i) d[i] = seed<4, S>(q[i], i);
+  const Gas<D> gd = dual_gas<4, S>(g);
   const D ws = D(oohK) * (speed(d[0], d[1], d[2]) + sound_speed(gd, d[0], d[1], d[2], d[3]));
 #pragma unroll
-  for (int i = 0; i < 4; ++i) qb[i] += wb * ws.d[i];
+  for (int i = 0; i < 4; ++i) qb[i] += wb * static_cast<double>(ws.d[i]);
 }
 
 // One boundary edge point by duals (tangents: interior face state 0..3, the
@@ -263,37 +267,45 @@ __device__ __forceinline__ void bc_point(const EdgeArgs<double>& a, int flag, in
 }
 
 // Reverse of bc_point: qib += J^T (fb, wsb); qinfb (4) and tb get the far-field and time parts.
+// The inputs are numbered j = 0..8 (interior face state 0..3, Qinf 4..7, time
+// 8); this evaluates the M of them from j0 on as dual tangents (all nine: one
+// thread per point; three groups of three: three threads per point).  The
+// tangents run in S: double on the FP64 path, float for the mixed path's
+// reverse sweep (whose boundary Jacobians then cost FP32 rather than FP64 work).
+template <typename S, int M = 9>
 static __device__ __noinline__ void bc_point_vjp(const EdgeArgs<double>& a, int flag, int bp, const double qi[4],
                                           double nx, double ny, double t, double oohK, const double fb[4], double wsb,
-                                          double qib[4], double qinfb[4], double* tb) {
-  using D = Dual<9>;
+                                          double qib[4], double qinfb[4], double* tb, int j0 = 0) {
+  using D = Dual<M, S>;
+  auto arg = [&](double v, int j) { return (j >= j0 && j < j0 + M) ? seed<M, S>(v, j - j0) : D(v); };
   D q[4];
 #pragma unroll
-  for (int i = 0; i < 4; ++i) q[i] = seed<9>(qi[i], i);
+  for (int i = 0; i < 4; ++i) q[i] = arg(qi[i], i);
   FreeStreamT<D> far, in, out;
-  const Gas<D> gd = dual_gas<9>(a.gas);
+  const Gas<D> gd = dual_gas<M, S>(a.gas);
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    far.qinf[i] = seed<9>(a.fsFar.qinf[i], 4 + i);
+    far.qinf[i] = arg(a.fsFar.qinf[i], 4 + i);
     in.qinf[i] = D(a.fsIn.qinf[i]);
     out.qinf[i] = D(a.fsOut.qinf[i]);
   }
   // pinf, cinf follow Qinf (FreeStream, fluids.go:370-406); values kept bit-equal to the forward's
   far.pinf = pressure(gd, far.qinf[0], far.qinf[1], far.qinf[2], far.qinf[3]);
   far.cinf = sound_speed(gd, far.qinf[0], far.qinf[1], far.qinf[2], far.qinf[3]);
-  far.pinf.v = a.fsFar.pinf;
-  far.cinf.v = a.fsFar.cinf;
+  far.pinf.v = static_cast<S>(a.fsFar.pinf);
+  far.cinf.v = static_cast<S>(a.fsFar.cinf);
   far.gamma = D(a.fsFar.gamma);
   far.minf = D(a.fsFar.minf);
   in.pinf = D(a.fsIn.pinf); in.cinf = D(a.fsIn.cinf); in.gamma = D(a.fsIn.gamma); in.minf = D(a.fsIn.minf);
   out.pinf = D(a.fsOut.pinf); out.cinf = D(a.fsOut.cinf); out.gamma = D(a.fsOut.gamma); out.minf = D(a.fsOut.minf);
   D f[4], ws;
-  bc_point<D>(a, flag, bp, q, D(nx), D(ny), far, in, out, seed<9>(t, 8), D(oohK), f, ws);
+  bc_point<D>(a, flag, bp, q, D(nx), D(ny), far, in, out, arg(t, 8), D(oohK), f, ws);
 #pragma unroll
-  for (int j = 0; j < 9; ++j) {
-    double s = wsb * ws.d[j];
+  for (int jj = 0; jj < M; ++jj) {
+    const int j = j0 + jj;
+    double s = wsb * static_cast<double>(ws.d[jj]);
 #pragma unroll
-    for (int n = 0; n < 4; ++n) s += fb[n] * f[n].d[j];
+    for (int n = 0; n < 4; ++n) s += fb[n] * static_cast<double>(f[n].d[jj]);
     if (j < 4) qib[j] += s;
     else if (j < 8) qinfb[j - 4] += s;
     else *tb += s;
@@ -305,7 +317,8 @@ static __device__ __noinline__ void bc_point_vjp(const EdgeArgs<double>& a, int 
 template <typename T>
 struct AdjArgs {
   int K, stage, localDT;
-  const double* Qs;     // stage state (mixed path: the step's initial state Q0)
+  const double* Qs;     // stage state (FP64 path)
+  const float* Qs32;    // mixed path: the hi part of the step's initial state Q0
   const float* Ds;      // mixed path, stage > 0: the stage increment (state = Q0 + Ds)
   const T* Qbn;         // adjoint of the stage output (stage -1: the RHS adjoint)
   const T* rhs;         // taped RHS of this stage
@@ -341,7 +354,7 @@ __device__ __forceinline__ void stage_coeffs(int s, double& alpha, double& beta,
 // Stage state value at flat index ind.
 template <typename T>
 __device__ __forceinline__ T stage_value(const AdjArgs<T>& a, size_t ind) {
-  if (a.Ds) return static_cast<T>(a.Qs[ind]) + static_cast<T>(a.Ds[ind]);
+  if (a.Qs32) return static_cast<T>(a.Qs32[ind]) + (a.Ds ? static_cast<T>(a.Ds[ind]) : T(0));
   return static_cast<T>(a.Qs[ind]);
 }
 
@@ -506,15 +519,19 @@ __global__ void __launch_bounds__(128) k_adj_edge(EdgeArgs<double> a, AdjEdgeArg
   }
 }
 
-// Boundary edges [nInt, nInt + nBC): boundary state and flux by duals in FP64,
-// one thread per (boundary edge, edge point).
+// Boundary edges [nInt, nInt + nBC): boundary state and flux by dual numbers
+// (the point values in FP64).  FP64 path: one thread per (boundary edge, edge
+// point) with all nine tangents in FP64; mixed path (T = float): three threads
+// per point, three FP32 tangents each.
 template <int N, typename T>
 __global__ void __launch_bounds__(128) k_adj_edge_bc(EdgeArgs<double> a, AdjEdgeArgs<T> x) {
   constexpr int NE = Dims<N>::NE, NE3 = Dims<N>::NE3;
+  constexpr int G = std::is_same<T, float>::value ? 3 : 1;  // threads per point
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   double qinfb[4] = {0.0, 0.0, 0.0, 0.0}, tb = 0.0;
-  if (tid < a.nBC * NE) {
-    const int b = tid / NE, p = tid - b * NE;
+  if (tid < a.nBC * NE * G) {
+    const int pt = tid / G, g = tid - pt * G;
+    const int b = pt / NE, p = pt - b * NE;
     const int e = a.nInt + b;
     const size_t sK = static_cast<size_t>(a.K);
     const int kL = a.kL[e];
@@ -526,9 +543,18 @@ __global__ void __launch_bounds__(128) k_adj_edge_bc(EdgeArgs<double> a, AdjEdge
       qi[n] = static_cast<double>(x.QF[(n * NE3 + jL) * sK + kL]);
       fb[n] = IIL * static_cast<double>(x.FEb[(n * NE3 + jL) * sK + kL]);
     }
-    bc_point_vjp(a, a.bcFlag[b], tid, qi, a.nx[e], a.ny[e], *a.time, a.oohK[e], fb, 0.0, qib, qinfb, &tb);
+    if (G == 1) {
+      bc_point_vjp<T>(a, a.bcFlag[b], pt, qi, a.nx[e], a.ny[e], *a.time, a.oohK[e], fb, 0.0, qib, qinfb, &tb);
 #pragma unroll
-    for (int n = 0; n < 4; ++n) x.QFb[(n * NE3 + jL) * sK + kL] = static_cast<T>(qib[n]);
+      for (int n = 0; n < 4; ++n) x.QFb[(n * NE3 + jL) * sK + kL] = static_cast<T>(qib[n]);
+    } else {
+      bc_point_vjp<T, 3>(a, a.bcFlag[b], pt, qi, a.nx[e], a.ny[e], *a.time, a.oohK[e], fb, 0.0, qib, qinfb, &tb,
+                         3 * g);
+      // group 0 owns face components 0..2, group 1 component 3
+#pragma unroll
+      for (int n = 0; n < 4; ++n)
+        if (n / 3 == g) x.QFb[(n * NE3 + jL) * sK + kL] = static_cast<T>(qib[n]);
+    }
   }
 #pragma unroll
   for (int n = 0; n < 4; ++n) qinfb[n] = warp_sum(qinfb[n]);
@@ -649,7 +675,8 @@ static __global__ void k_adj_lts(AdjDtArgs a) {
   }
 }
 
-// esBar[g] onto the face state at the edge's max wave-speed point (in FP64).
+// esBar[g] onto the face state at the edge's max wave-speed point (the point
+// chosen in FP64, the tangents in T).
 template <int N, typename T>
 __global__ void __launch_bounds__(128) k_adj_speed(EdgeArgs<double> a, AdjEdgeArgs<T> x) {
   constexpr int NE = Dims<N>::NE, NE3 = Dims<N>::NE3;
@@ -690,13 +717,70 @@ __global__ void __launch_bounds__(128) k_adj_speed(EdgeArgs<double> a, AdjEdgeAr
   if (bc) {
     double qinfb[4] = {0.0, 0.0, 0.0, 0.0}, tb = 0.0;
     const double fb[4] = {0.0, 0.0, 0.0, 0.0};
-    bc_point_vjp(a, flag, b * NE + pb, qi, nx, ny, t, oohK, fb, wbar, qib, qinfb, &tb);
+    bc_point_vjp<T>(a, flag, b * NE + pb, qi, nx, ny, t, oohK, fb, wbar, qib, qinfb, &tb);
 #pragma unroll
     for (int n = 0; n < 4; ++n)
       if (qinfb[n] != 0.0) atomicAdd(&x.qinfb[n], qinfb[n]);
     if (tb != 0.0) atomicAdd(x.tb, tb);
   } else {
-    wave_speed_vjp(a.gas, oohK, qi, wbar, qib);
+    wave_speed_vjp<T>(a.gas, oohK, qi, wbar, qib);
+  }
+#pragma unroll
+  for (int n = 0; n < 4; ++n) x.QFb[(n * NE3 + jL) * sK + kL] += static_cast<T>(qib[n]);
+}
+
+// Global dt: the one edge that set the stage's dt (argEdge), one warp, lane p
+// evaluating edge point p (k_adj_speed's work for that edge without a thread
+// per edge of the mesh).
+template <int N, typename T>
+__global__ void __launch_bounds__(32) k_adj_speed_one(EdgeArgs<double> a, AdjEdgeArgs<T> x, const int* argEdge) {
+  constexpr int NE = Dims<N>::NE, NE3 = Dims<N>::NE3;
+  const int e = *argEdge;
+  if (e < 0 || e >= a.nInt + a.nBC) return;
+  const double wbar = x.esBar[e];
+  if (wbar == 0.0) return;
+  const int p = threadIdx.x;
+  const size_t sK = static_cast<size_t>(a.K);
+  const int kL = a.kL[e];
+  const int eL = a.eLR[e] & 3;
+  const double nx = a.nx[e], ny = a.ny[e];
+  const double oohK = a.oohK[e];
+  const bool bc = e >= a.nInt;
+  const int b = e - a.nInt;
+  const int flag = bc ? a.bcFlag[b] : 0;
+  const double t = *a.time;
+  double ws = -1.0;
+  double qi[4];
+  if (p < NE) {
+    const int jL = eL * NE + p;
+#pragma unroll
+    for (int n = 0; n < 4; ++n) qi[n] = static_cast<double>(x.QF[(n * NE3 + jL) * sK + kL]);
+    if (bc) {
+      double f[4];
+      bc_point<double>(a, flag, b * NE + p, qi, nx, ny, a.fsFar, a.fsIn, a.fsOut, t, oohK, f, ws);
+    } else {
+      ws = oohK * (speed(qi[0], qi[1], qi[2]) + sound_speed(a.gas, qi[0], qi[1], qi[2], qi[3]));
+    }
+  }
+  // the forward's max is the first strict increase: the lowest point holding the max
+  double m = ws;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  const unsigned hit = __ballot_sync(0xffffffffu, p < NE && ws == m && ws > -1.0);
+  const int pb = hit ? __ffs(hit) - 1 : 0;
+  if (p != pb) return;
+  const int jL = eL * NE + pb;
+  double qib[4] = {0.0, 0.0, 0.0, 0.0};
+  if (bc) {
+    double qinfb[4] = {0.0, 0.0, 0.0, 0.0}, tb = 0.0;
+    const double fb[4] = {0.0, 0.0, 0.0, 0.0};
+    bc_point_vjp<T>(a, flag, b * NE + pb, qi, nx, ny, t, oohK, fb, wbar, qib, qinfb, &tb);
+#pragma unroll
+    for (int n = 0; n < 4; ++n)
+      if (qinfb[n] != 0.0) atomicAdd(&x.qinfb[n], qinfb[n]);
+    if (tb != 0.0) atomicAdd(x.tb, tb);
+  } else {
+    wave_speed_vjp<T>(a.gas, oohK, qi, wbar, qib);
   }
 #pragma unroll
   for (int n = 0; n < 4; ++n) x.QFb[(n * NE3 + jL) * sK + kL] += static_cast<T>(qib[n]);
@@ -725,35 +809,6 @@ __global__ void __launch_bounds__(128) k_adj_interp(const T* QFb, const double* 
   }
 }
 
-// Mixed path: the faces of the stage state Q0 + D (D = nullptr: Q0) in FP32,
-// FluxEdgeInterp applied per variable (the reverse sweep's linearisation point
-// at the edges).
-template <int N>
-__global__ void __launch_bounds__(128) k_adj_faces(const double* __restrict__ Q0, const float* __restrict__ D,
-                                                   const double* __restrict__ Iop, float* __restrict__ QF, int K) {
-  constexpr int NP = Dims<N>::NP, NE3 = Dims<N>::NE3;
-  __shared__ float sI[NE3 * NP];
-  stage_operator(sI, Iop, NE3 * NP);
-  __syncthreads();
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 4 * K) return;
-  const int n = t / K, k = t - n * K;
-  const size_t sK = static_cast<size_t>(K);
-  float q[NP];
-#pragma unroll
-  for (int i = 0; i < NP; ++i) {
-    const size_t ind = (n * NP + i) * sK + k;
-    q[i] = static_cast<float>(Q0[ind]) + (D ? D[ind] : 0.0f);
-  }
-#pragma unroll
-  for (int j = 0; j < NE3; ++j) {
-    float acc = 0.0f;
-#pragma unroll
-    for (int i = 0; i < NP; ++i) acc += sI[j * NP + i] * q[i];
-    QF[(n * NE3 + j) * sK + k] = acc;
-  }
-}
-
 // Element-wise conversion between the FP64 interface arrays and the FP32 adjoint.
 template <typename A, typename B>
 __global__ void k_convert(const A* __restrict__ src, B* __restrict__ dst, size_t n) {
@@ -762,28 +817,6 @@ __global__ void k_convert(const A* __restrict__ src, B* __restrict__ dst, size_t
     dst[i] = static_cast<B>(src[i]);
 }
 
-// Qbs += FluxEdgeInterp^T QFb, one thread per (variable, element).
-template <int N>
-__global__ void __launch_bounds__(128) k_adj_interp(const double* QFb, const double* Iop, double* Qbs, int K) {
-  constexpr int NP = Dims<N>::NP, NE3 = Dims<N>::NE3;
-  __shared__ double sI[NE3 * NP];
-  stage_operator(sI, Iop, NE3 * NP);
-  __syncthreads();
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 4 * K) return;
-  const int n = t / K, k = t - n * K;
-  const size_t sK = static_cast<size_t>(K);
-  double f[NE3];
-#pragma unroll
-  for (int j = 0; j < NE3; ++j) f[j] = QFb[(n * NE3 + j) * sK + k];
-#pragma unroll
-  for (int i = 0; i < NP; ++i) {
-    double acc = 0.0;
-#pragma unroll
-    for (int j = 0; j < NE3; ++j) acc += sI[j * NP + i] * f[j];
-    Qbs[(n * NP + i) * sK + k] += acc;
-  }
-}
 
 // ---------------------------------------------------------------------------
 // Functionals of the state, with their gradients.

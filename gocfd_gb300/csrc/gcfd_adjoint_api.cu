@@ -103,6 +103,7 @@ int adj_init(gcfd_ctx* c) {
     if ((rc = dalloc(c, &c->dtOwnK, static_cast<size_t>(c->K)))) return rc;
     if ((rc = dalloc(c, &c->esBar, static_cast<size_t>(nE)))) return rc;
     if ((rc = dalloc(c, &c->argEdge, 8))) return rc;
+    if ((rc = adj_ops(c->N)->mixed_consts(c))) return rc;
     c->adjReady = true;
     return GCFD_OK;
   }
@@ -314,59 +315,75 @@ int step_vjp_mixed(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doub
   int rc;
   if ((rc = copy_shards(c, c->Qbf, nshards, Kmax, Qfinal_bar, true, nullptr))) return rc;
   o.mixed_bar_convert(c, true);
+  c->adjFacesPending = false;
   GCFD_CUDA(c, cudaMemsetAsync(c->adjS, 0, sizeof(double) * 12, c->stream));
   GCFD_CUDA(c, cudaMemcpyAsync(c->adjS + 10, &tfinal_bar, sizeof(double), cudaMemcpyHostToDevice, c->stream));
   const int every = c->winEvery, nsteps = c->winSteps;
   const int nseg = (nsteps + every - 1) / every;
-  // a step from the FP64 state in Q[0] and the time in sc: the stage-0 data
-  // rebuilt from Q[0], then one taped step into the bound slot
-  auto taped_step = [&]() {
-    fwd.prep(c);
-    fo.mixed_tape(c);
-    c->fp64Stale = true;
+  // The compensated state (hi, lo) at the start of step i of a segment: the
+  // reverse sweep evaluates the stage states as hi + D_s in FP32.
+  auto save_pair = [&](float* dst) -> int {
+    GCFD_CUDA(c, cudaMemcpyAsync(dst, c->Qhi, S * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+    GCFD_CUDA(c, cudaMemcpyAsync(dst + S, c->Qlo, S * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+    return GCFD_OK;
   };
+  float* pairTmp = reinterpret_cast<float*>(c->Qtmp);  // S doubles of room = one (hi, lo) pair
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int n0 = seg * every, m = std::min(every, nsteps - n0);
     GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], c->ckpt + S * seg, SB, cudaMemcpyDeviceToDevice, c->stream));
     GCFD_CUDA(c, cudaMemcpyAsync(&c->sc->time, c->ckptT + seg, sizeof(double), cudaMemcpyDeviceToDevice,
                                  c->stream));
     c->fp64Stale = false;
-    const bool taped = m > 1 && static_cast<int>(c->slots.size()) >= m;
     fwd.prep(c);
+    if (m > 1 && static_cast<int>(c->slots.size()) >= m) {
+      // segment tape: each step recomputed once with its tape in its own slot,
+      // segQ entry i holding the step's starting (hi, lo)
+      for (int i = 0; i < m; ++i) {
+        float* pr = reinterpret_cast<float*>(c->segQ + S * i);
+        if ((rc = save_pair(pr))) return rc;
+        bind_slot(c, i);
+        fo.mixed_tape(c);
+        GCFD_CUDA(c, cudaGetLastError());
+      }
+      for (int i = m - 1; i >= 0; --i) {
+        bind_slot(c, i);
+        o.mixed_reverse_taped(c, reinterpret_cast<const float*>(c->segQ + S * i));
+        GCFD_CUDA(c, cudaGetLastError());
+      }
+      bind_slot(c, 0);
+      c->fp64Stale = true;
+      continue;
+    }
+    // without it: the segment's steps once through the graph, keeping each
+    // step's starting state in FP64 (segQ), then per step in reverse order the
+    // state restored and prepared (the last step's is current already), its
+    // (hi, lo) kept, one taped step and its reverse
     for (int i = 0; i < m; ++i) {
       if ((rc = sync_fp64_state(c))) return rc;
       GCFD_CUDA(c, cudaMemcpyAsync(c->segQ + S * i, c->Q[0], SB, cudaMemcpyDeviceToDevice, c->stream));
       GCFD_CUDA(c, cudaMemcpyAsync(c->segT + i, &c->sc->time, sizeof(double), cudaMemcpyDeviceToDevice,
                                    c->stream));
-      if (taped) {  // the recompute keeps each step's tape in its own slot
-        bind_slot(c, i);
-        fo.mixed_tape(c);
-        c->fp64Stale = true;
-        GCFD_CUDA(c, cudaGetLastError());
-      } else if (i + 1 < m) {
+      if (i + 1 < m) {
         GCFD_CUDA(c, cudaGraphLaunch(c->graphExec, c->stream));
         c->fp64Stale = true;
       }
     }
-    if (taped) {
-      for (int i = m - 1; i >= 0; --i) {
-        bind_slot(c, i);
-        o.mixed_reverse_taped(c, c->segQ + S * i);
-        GCFD_CUDA(c, cudaGetLastError());
-      }
-      bind_slot(c, 0);
-      continue;
-    }
     for (int i = m - 1; i >= 0; --i) {
-      GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], c->segQ + S * i, SB, cudaMemcpyDeviceToDevice, c->stream));
-      GCFD_CUDA(c, cudaMemcpyAsync(&c->sc->time, c->segT + i, sizeof(double), cudaMemcpyDeviceToDevice,
-                                   c->stream));
-      c->fp64Stale = false;
-      taped_step();
-      o.mixed_reverse_taped(c, c->segQ + S * i);
+      if (i < m - 1) {
+        GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], c->segQ + S * i, SB, cudaMemcpyDeviceToDevice, c->stream));
+        GCFD_CUDA(c, cudaMemcpyAsync(&c->sc->time, c->segT + i, sizeof(double), cudaMemcpyDeviceToDevice,
+                                     c->stream));
+        c->fp64Stale = false;
+        fwd.prep(c);
+      }
+      if ((rc = save_pair(pairTmp))) return rc;
+      fo.mixed_tape(c);
+      c->fp64Stale = true;
+      o.mixed_reverse_taped(c, pairTmp);
       GCFD_CUDA(c, cudaGetLastError());
     }
   }
+  o.mixed_finish_faces(c);
   o.mixed_bar_convert(c, false);
   double h[6];
   GCFD_CUDA(c, cudaMemcpyAsync(h, c->adjS + 5, sizeof(h), cudaMemcpyDeviceToHost, c->stream));

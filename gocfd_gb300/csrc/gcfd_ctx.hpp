@@ -112,6 +112,7 @@ struct gcfd_ctx {
   float* tapeRHS32[5] = {};
   float* Qb32[5] = {};
   float *Qbf32 = nullptr, *Rb3_32 = nullptr, *QF32 = nullptr, *QFb32 = nullptr, *FEb32 = nullptr;
+  bool adjFacesPending = false;  // QFb32 holds stage-0 face adjoints not yet in Qbf32
   double *dXs = nullptr, *dYs = nullptr, *edgeW = nullptr;
   // adjoint of the dissipation
   double* tapeQ2pre = nullptr;
@@ -225,8 +226,11 @@ struct AdjOps {
   void (*reverse_taped)(gcfd_ctx*, const double*);
   void (*rhs_vjp)(gcfd_ctx*);
   void (*functional)(gcfd_ctx*, int);
-  void (*mixed_reverse_taped)(gcfd_ctx*, const double*);  // FP32 adjoint of a step taped by mixed_tape
+  void (*mixed_reverse_taped)(gcfd_ctx*, const float*);  // FP32 adjoint of a step taped by mixed_tape,
+                                                         // from the step's starting hi part
   void (*mixed_bar_convert)(gcfd_ctx*, bool);  // Qbf (FP64) -> Qbf32 (true) or back (false)
+  int (*mixed_consts)(gcfd_ctx*);              // FP32 operators of the mixed reverse sweep
+  void (*mixed_finish_faces)(gcfd_ctx*);       // the sweep's last deferred face transpose into Qbf32
 };
 
 const OrderOps* order_ops_0();

@@ -2,6 +2,7 @@
 // -DGCFD_ORDER=N (0..4), exporting adj_ops_N.
 #include "gcfd_adjoint.cuh"
 #include "gcfd_adjoint_diss.cuh"
+#include "gcfd_adjoint_mixed.cuh"
 #include "gcfd_launch.cuh"
 
 #ifndef GCFD_ORDER
@@ -42,6 +43,7 @@ struct AdjLaunch {
     a.stage = s;
     a.localDT = c->prm.local_time_stepping;
     a.Qs = Qs;
+    a.Qs32 = nullptr;
     a.Ds = nullptr;
     a.Qbn = Qbn;
     a.rhs = s >= 0 ? c->tapeRHS[s] : nullptr;
@@ -117,7 +119,11 @@ struct AdjLaunch {
       else
         k_adj_edge<N, false, T><<<grid(c->nInt), 128, 0, c->stream>>>(e, x);
     }
-    if (c->nBC > 0) k_adj_edge_bc<N, T><<<grid(c->nBC * Dims<N>::NE), 128, 0, c->stream>>>(e, x);
+    // boundary points: dual numbers, a long dependent chain per thread (on the
+    // narrow FP64 pipe for the FP64 path), so one warp per block spreads them
+    // over every SM
+    constexpr int G = std::is_same<T, float>::value ? 3 : 1;  // threads per point (k_adj_edge_bc)
+    if (c->nBC > 0) k_adj_edge_bc<N, T><<<(c->nBC * Dims<N>::NE * G + 31) / 32, 32, 0, c->stream>>>(e, x);
   }
   static AdjDissArgs adj_diss_args(gcfd_ctx* c, const double* Qsens, int s) {
     AdjDissArgs x;
@@ -225,6 +231,15 @@ struct AdjLaunch {
       k_adj_gsel<<<1, 32, 0, c->stream>>>(d);
     }
   }
+  // esBar onto the face states: with global dt one warp on the stage's argmax
+  // edge (every other edge has esBar = 0), with local dt a thread per edge.
+  template <typename T>
+  static void speed_reverse(gcfd_ctx* c, int s, const EdgeArgs<double>& e, const AdjEdgeArgs<T>& x) {
+    if (c->prm.local_time_stepping)
+      k_adj_speed<N, T><<<grid(c->nInt + c->nBC), 128, 0, c->stream>>>(e, x);
+    else
+      k_adj_speed_one<N, T><<<1, 32, 0, c->stream>>>(e, x, c->argEdge + s);
+  }
   // The reverse of stage s.  Q0 is the step's initial state.  With a segment
   // tape the stage faces are not taped (they are FluxEdgeInterp of the stage
   // state, after the rkStep-2 limiter where it applies) and are rebuilt here.
@@ -249,7 +264,7 @@ struct AdjLaunch {
     const AdjEdgeArgs<double> x = adj_edge_args(c, c->tapeQF[s]);
     edges(c, e, x);
     dt_reverse(c, s);
-    k_adj_speed<N, double><<<grid(c->nInt + c->nBC), 128, 0, c->stream>>>(e, x);
+    speed_reverse(c, s, e, x);
     if (c->diss)
       diss_reverse_rest(c, s, Qs, Qsens, c->Qb[s], c->tapeQF[s]);
     else
@@ -328,12 +343,13 @@ struct AdjLaunch {
   }
 
   // ---- mixed path: the FP32 adjoint of a step taped by the mixed forward ----
-  static AdjArgs<float> adj_args32(gcfd_ctx* c, int s, const double* Q0, const float* Qbn, float* Qbs) {
+  static AdjArgs<float> adj_args32(gcfd_ctx* c, int s, const float* Q0hi, const float* Qbn, float* Qbs) {
     AdjArgs<float> a;
     a.K = c->K;
     a.stage = s;
     a.localDT = c->prm.local_time_stepping;
-    a.Qs = Q0;
+    a.Qs = nullptr;
+    a.Qs32 = Q0hi;
     a.Ds = s > 0 ? c->Dk[s] : nullptr;
     a.Qbn = Qbn;
     a.rhs = s >= 0 ? c->tapeRHS32[s] : nullptr;
@@ -369,27 +385,54 @@ struct AdjLaunch {
   // Stage s in reverse: the stage state is Q0 + D_s (the taped increments), its
   // faces are interpolated once more in FP32, then the kernels of the FP64
   // sweep in FP32 (the boundary points and wave-speed maxima in FP64).
-  static void mixed_reverse_stage(gcfd_ctx* c, int s, const double* Q0) {
-    k_adj_faces<N><<<grid(4 * c->K), 128, 0, c->stream>>>(Q0, s > 0 ? c->Dk[s] : nullptr, c->Iop, c->QF32, c->K);
+  //
+  // The face transpose of stage s + 1 rides in stage s's divergence kernel
+  // (k_adj_div32), and stage 0's in the stage-4 kernel of the step reversed
+  // next (c->adjFacesPending until then; mixed_finish_faces ends a sweep).
+  static void mixed_reverse_stage(gcfd_ctx* c, int s, const float* Q0) {
     const float* Qbn = (s == 4) ? c->Qbf32 : c->Qb32[s + 1];
-    k_adj_div<N, float><<<grid(c->K), 128, 0, c->stream>>>(adj_args32(c, s, Q0, Qbn, c->Qb32[s]));
+    const bool pending = (s < 4) || c->adjFacesPending;
+    k_adj_div32<N><<<(c->K + 31) / 32, 128, 0, c->stream>>>(adj_args32(c, s, Q0, Qbn, c->Qb32[s]), c->mgeo,
+                                                           pending ? c->QFb32 : nullptr, c->QF32);
+    c->adjFacesPending = false;
     const EdgeArgs<double> e = edge_args(c, &c->tapeSc0->time);
     const AdjEdgeArgs<float> x = adj_edge_args32(c);
     edges(c, e, x);
     dt_reverse(c, s);
-    k_adj_speed<N, float><<<grid(c->nInt + c->nBC), 128, 0, c->stream>>>(e, x);
-    k_adj_interp<N, float><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb32, c->Iop, c->Qb32[s], c->K);
+    speed_reverse(c, s, e, x);
+    if (s == 0) c->adjFacesPending = true;
   }
-  // The adjoint of a mixed step whose tape is bound; Q0 is the step's initial
-  // state (FP64).  In: Qbf32, adjS[10]; out: Qbf32 <- adjoint of Q0, adjS[10]
-  // <- t-bar of the step's start.
-  static void mixed_reverse_taped(gcfd_ctx* c, const double* Q0) {
+  // The last stage-0 face transpose of a reverse sweep into its result Qbf32.
+  static void mixed_finish_faces(gcfd_ctx* c) {
+    if (!c->adjFacesPending) return;
+    k_adj_interp<N, float><<<grid(4 * c->K), 128, 0, c->stream>>>(c->QFb32, c->Iop, c->Qbf32, c->K);
+    c->adjFacesPending = false;
+  }
+  // The adjoint of a mixed step whose tape is bound; Q0 is the hi part of the
+  // step's initial state.  In: Qbf32, adjS[10]; out: Qbf32 <- adjoint of Q0,
+  // adjS[10] <- t-bar of the step's start.
+  static void mixed_reverse_taped(gcfd_ctx* c, const float* Q0) {
     cudaMemsetAsync(c->adjS, 0, sizeof(double) * 5, c->stream);
     cudaMemcpyAsync(c->adjS + 9, c->adjS + 10, sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
     cudaMemsetAsync(c->carry, 0, sizeof(double) * c->K, c->stream);
     for (int s = 4; s >= 0; --s) mixed_reverse_stage(c, s, Q0);
     std::swap(c->Qbf32, c->Qb32[0]);
     cudaMemcpyAsync(c->adjS + 10, c->adjS + 9, sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  }
+  // FP32 DivInt and FluxEdgeInterp into this unit's constant memory (k_adj_div32).
+  static int mixed_consts(gcfd_ctx* c) {
+    std::vector<float> d(c->el.DivInt.v.begin(), c->el.DivInt.v.end());
+    std::vector<float> f(c->el.FluxEdgeInterp.v.begin(), c->el.FluxEdgeInterp.v.end());
+    std::vector<float> cs(c->NF);
+    for (int j = 0; j < c->NF; ++j) {
+      double t = 0.0;
+      for (int r = 0; r < c->Np; ++r) t += c->el.DivInt(r, j);
+      cs[j] = static_cast<float>(t);
+    }
+    GCFD_CUDA(c, cudaMemcpyToSymbol(cAdjDiv, d.data(), d.size() * sizeof(float)));
+    GCFD_CUDA(c, cudaMemcpyToSymbol(cAdjDivCS, cs.data(), cs.size() * sizeof(float)));
+    GCFD_CUDA(c, cudaMemcpyToSymbol(cAdjIop, f.data(), f.size() * sizeof(float)));
+    return GCFD_OK;
   }
   static void mixed_bar_convert(gcfd_ctx* c, bool toFP32) {
     const size_t S = static_cast<size_t>(4) * c->Np * c->K;
@@ -406,7 +449,8 @@ const AdjOps* GCFD_CAT(adj_ops_, GCFD_ORDER)() {
   static const AdjOps o{&AdjLaunch<kN>::tape_step,       &AdjLaunch<kN>::reverse_step,
                         &AdjLaunch<kN>::reverse_taped,   &AdjLaunch<kN>::rhs_vjp,
                         &AdjLaunch<kN>::functional,      &AdjLaunch<kN>::mixed_reverse_taped,
-                        &AdjLaunch<kN>::mixed_bar_convert};
+                        &AdjLaunch<kN>::mixed_bar_convert, &AdjLaunch<kN>::mixed_consts,
+                        &AdjLaunch<kN>::mixed_finish_faces};
   return &o;
 }
 

@@ -87,8 +87,10 @@ def test_mixed_step_vjp_vortex(precision, every):
     and the window with and without the segment tape."""
     mesh = meshes.vortex_box(6, jitter=0.1)
     N, nsteps, t0 = 3, 10, 0.1
-    ip = params(N, init="ivortex", cfl=1.0)
-    ora = oracle_for(mesh, N, init="ivortex", cfl=1.0)
+    # CFL 0.5: the oracle's differences at h = 1e-6, 5e-7, 2e-7 agree to 5e-9 (at
+    # CFL 1 the h = 1e-6 pair straddles a switch of the dt-setting edge)
+    ip = params(N, init="ivortex", cfl=0.5)
+    ora = oracle_for(mesh, N, init="ivortex", cfl=0.5)
     rng = np.random.default_rng(7)
     Q0 = perturbed(ora.Q, 7, 0.01)
     Qbf = rng.standard_normal(Q0.shape)
