@@ -35,37 +35,6 @@ __device__ constexpr float kAdjAl[4] = {1.0f, 7455300.0f * kAdjQ, 10403583.0f * 
 __device__ constexpr float kAdjBe[4] = {0.0f, 9321916.0f * kAdjQ, 6373633.0f * kAdjQ, 13789530.0f * kAdjQ};
 constexpr float kAdjA2 = 8677707.0f * kAdjQ, kAdjA3 = 1611615.0f * kAdjQ, kAdjA4 = 6487894.0f * kAdjQ;
 
-// L2 prefetch of the 128 bytes at p (16-byte aligned).
-__device__ __forceinline__ void adj_prefetch_row(const float* p) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], 128;\n" ::"l"(p) : "memory");
-}
-
-// The block's 32-element slice of every row kernel k_adj_div32 reads for
-// variable n, prefetched to L2 by warp n at the start (lane j takes rows j,
-// j + 32, ...), so the loads of both phases find their lines on chip.  Needs K
-// a multiple of 4 (16-byte aligned rows) and a full block.
-template <int N>
-__device__ __forceinline__ void adj_div_prefetch(const AdjArgs<float>& a, const float* QFbNext, int n, int lane,
-                                                 size_t c0, bool rmwQb0, bool rmwQbs) {
-  constexpr int NP = Dims<N>::NP, NE3 = Dims<N>::NE3;
-  const size_t sK = static_cast<size_t>(a.K);
-  int t = lane;  // this lane's next row in the concatenated list
-  auto seg = [&](const float* p, int rows, int per) {
-    if (!p) return;
-    for (; t < rows; t += 32) adj_prefetch_row(p + (static_cast<size_t>(n) * per + t) * sK + c0);
-    t -= rows;
-  };
-  seg(a.Qbn, NP, NP);
-  seg(QFbNext, NE3, NE3);
-  seg(a.stage >= 0 ? a.rhs : nullptr, NP, NP);
-  seg(a.stage == 4 ? a.rhs3 : nullptr, NP, NP);
-  seg(a.stage == 3 ? a.Rb3 : nullptr, NP, NP);
-  seg(rmwQb0 ? a.Qb0 : nullptr, NP, NP);
-  seg(a.Qs32, NP, NP);
-  seg(a.Ds, NP, NP);
-  seg(rmwQbs ? a.Qbs : nullptr, NP, NP);
-}
-
 // faces (when not null) receives the stage state's FP32 faces, FluxEdgeInterp
 // applied to Q0 + Ds per variable: the linearisation point of the edge
 // adjoints that follow.
@@ -83,9 +52,6 @@ __global__ void __launch_bounds__(128) k_adj_div32(AdjArgs<float> a, const float
   const size_t off = static_cast<size_t>(n) * NP * sK + k;
   // Qbs is Qb0 at stage 0: its alpha term then joins the point update below
   const bool alias0 = (a.Qbs == a.Qb0);
-  if ((a.K & 3) == 0 && blockIdx.x * 32 + 32 <= a.K)
-    adj_div_prefetch<N>(a, QFbNext, n, lane, static_cast<size_t>(blockIdx.x) * 32, s >= 0 && s < 3 && !alias0,
-                        !(s == 1 || s == 4));
   float dtb = 0.0f;
   float Jd = 1.0f, J0 = 0.0f, J1 = 0.0f, J2 = 0.0f, J3 = 0.0f, mooj = 0.0f;
   if (active) {

@@ -200,3 +200,43 @@ def test_mixed_adjoint_rejects_dissipation():
         with pytest.raises(_lib.GcfdError) as e:
             gpu.record(1)
         assert e.value.code == -7
+
+
+def test_mixed_adjoint_smooth_directions_against_fp64_differences():
+    """The gradient check of the vortex configurations at a small size (N = 4,
+    vortex_box(48), 40 steps after 50, checkpoint every 10): the adjoint with the
+    FP64 path's field-error weight, along d/dx0 and d/dbeta of the exact vortex,
+    against Richardson-extrapolated FP64 central differences (GPU FP64 path): the
+    FP64 adjoint to 1e-8 (the differences are clean), the mixed one to 1e-5."""
+    from gocfd_gb300 import configs
+    mesh = meshes.vortex_box(48, jitter=0.1)
+    ip = InputParameters2D(CFL=1.0, FluxType="roe", InitType="ivortex", PolynomialOrder=4, FinalTime=1e9,
+                           Minf=0.5, Gamma=1.4, MaxIterations=10 ** 9)
+    steps = 40
+    with Euler(ip, mesh, 1, precision="fp64", vortex_center=(0.0, 0.0)) as s:
+        s.step(50)
+        Q0, t0 = s.get_global_state(), s.time
+        s.record(steps, 10)
+        J, Qbf, tbf = s.functional("vortex_error")
+        Qb64, _, _ = s.step_vjp(Qbf, tbf)
+        X, Y = configs.solution_points_xy(s)
+
+        def J_at(q):
+            s.set_global_state(q)
+            s.time = t0
+            s.step(steps)
+            return s.functional("vortex_error")[0]
+        with Euler(ip, mesh, 1, precision="fp32", vortex_center=(0.0, 0.0)) as g:
+            g.set_global_state(Q0)
+            g.time = t0
+            g.record(steps, 10)
+            Qb32, _, _ = g.step_vjp(Qbf, tbf)
+        for param in ("x0", "beta"):
+            d = configs.exact_vortex_param_derivative(X, Y, t0, param)
+            fd = {h: (J_at(Q0 + h * d) - J_at(Q0 - h * d)) / (2 * h) for h in (2e-4, 1e-4)}
+            rich = (4 * fd[1e-4] - fd[2e-4]) / 3
+            a64, a32 = float(np.sum(Qb64 * d)), float(np.sum(Qb32 * d))
+            print(f"smooth direction {param}: FD {rich:.10e}, FP64 adjoint rel {rel(a64, rich):.3e}, "
+                  f"mixed adjoint rel {rel(a32, rich):.3e}")
+            assert rel(a64, rich) <= 1e-8
+            assert rel(a32, rich) <= GRAD_RTOL
