@@ -33,6 +33,7 @@ EXPORTS = [
     "gcfd_get_option", "gcfd_profile_step",
     "gcfd_host_operator", "gcfd_read_mesh", "gcfd_free_mesh", "gcfd_residual_norms_static", "gcfd_functional", "gcfd_rhs_vjp",
     "gcfd_record_steps", "gcfd_step_vjp", "gcfd_sample_points", "gcfd_wall_points", "gcfd_device_fma_peaks",
+    "gcfd_host_graph_element", "gcfd_graph_mesh", "gcfd_graph_fields",
 ]
 
 
@@ -112,6 +113,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         lib.gcfd_sample_points.argtypes = [C.c_void_p, C.c_int32, PD, PD, PD, PI]
         lib.gcfd_wall_points.argtypes = [C.c_void_p, PI, PD, PD, PD, PD]
         lib.gcfd_device_fma_peaks.argtypes = [C.c_int32, PD, PD]
+        lib.gcfd_host_graph_element.argtypes = [C.c_int32, PI, PI, PD, PI]
+        lib.gcfd_graph_mesh.argtypes = [C.c_void_p, PI, PI, C.POINTER(C.c_float), C.POINTER(C.c_int64)]
+        lib.gcfd_graph_fields.argtypes = [C.c_void_p, C.c_int32, PI, C.POINTER(C.c_float)]
         _lib = lib
         return lib
 
@@ -120,6 +124,18 @@ def check(lib, ctx, rc: int):
     if rc != GCFD_OK:
         msg = lib.gcfd_last_error(ctx)
         raise GcfdError(rc, msg.decode() if msg else "")
+
+
+def graph_element(N: int):
+    """The reference element's graph points (len_element x 2 (r, s)) and
+    sub-triangles (ntri x 3, local indices) of the solution output (no GPU)."""
+    lib = load()
+    L, nt = C.c_int32(), C.c_int32()
+    check(lib, None, lib.gcfd_host_graph_element(int(N), C.byref(L), C.byref(nt), None, None))
+    rs = np.zeros((L.value, 2))
+    tris = np.zeros((nt.value, 3), dtype=np.int32)
+    check(lib, None, lib.gcfd_host_graph_element(int(N), None, None, rs.ctypes.data_as(PD), tris.ctypes.data_as(PI)))
+    return rs, tris
 
 
 def read_mesh(path: str):

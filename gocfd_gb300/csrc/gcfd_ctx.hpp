@@ -142,6 +142,7 @@ struct gcfd_ctx {
   std::vector<double> meshVX, meshVY;
   std::vector<int32_t> meshEToV;
   std::shared_ptr<void> post;  // post-processing state (gcfd_post.cu), built on first use
+  std::shared_ptr<void> graphOut;  // solution-output graph element and buffers (gcfd_graph.cu), on first use
   double *ckpt = nullptr, *ckptT = nullptr, *segQ = nullptr, *segT = nullptr, *endQ = nullptr;
   double *ckptV = nullptr, *segV = nullptr, *endV = nullptr;  // DTVisc (dissipation), K per entry
   Scalars* endSc = nullptr;

@@ -365,6 +365,34 @@ class Euler:
             p.ctypes.data_as(_lib.PD)))
         return x, y, q, p
 
+    # the reference's FlowFunction names and values (fluids.go:209-222)
+    FLOW_FUNCTIONS = {"Density": 0, "XMomentum": 1, "YMomentum": 2, "Energy": 3, "Mach": 4, "StaticPressure": 5,
+                      "DynamicPressure": 6, "PressureCoefficient": 7, "SoundSpeed": 8, "Velocity": 9,
+                      "XVelocity": 10, "YVelocity": 11, "Enthalpy": 12, "Entropy": 13}
+
+    def graph_mesh(self):
+        """The solution output's graph mesh (gcfd_graph_mesh; CreateAVSGraphMesh,
+        graphics_support.go:173-230): XY as (K * len_element) x 2 float32 and the
+        sub-triangles as (K * ntri) x 3 int64 global point indices."""
+        L, nt = C.c_int32(), C.c_int32()
+        _lib.check(self.lib, self.ctx, self.lib.gcfd_graph_mesh(self.ctx, C.byref(L), C.byref(nt), None, None))
+        xy = np.zeros((self.K * L.value, 2), dtype=np.float32)
+        tris = np.zeros((self.K * nt.value, 3), dtype=np.int64)
+        _lib.check(self.lib, self.ctx, self.lib.gcfd_graph_mesh(
+            self.ctx, None, None, xy.ctypes.data_as(C.POINTER(C.c_float)), tris.ctypes.data_as(C.POINTER(C.c_int64))))
+        return xy, tris
+
+    def graph_fields(self, names):
+        """Flow functions (names of FLOW_FUNCTIONS) at the graph points, a dict of
+        float32 arrays of K * len_element (gcfd_graph_fields; GetPlotField, plot.go:14-85)."""
+        kinds = np.array([self.FLOW_FUNCTIONS[n] for n in names], dtype=np.int32)
+        L = C.c_int32()
+        _lib.check(self.lib, self.ctx, self.lib.gcfd_graph_mesh(self.ctx, C.byref(L), None, None, None))
+        out = np.zeros((len(names), self.K * L.value), dtype=np.float32)
+        _lib.check(self.lib, self.ctx, self.lib.gcfd_graph_fields(self.ctx, len(names), kinds.ctypes.data_as(_lib.PI),
+                                                                 out.ctypes.data_as(C.POINTER(C.c_float))))
+        return {n: out[i] for i, n in enumerate(names)}
+
     def step(self, nsteps: int = 1):
         """Advance nsteps; returns dict(time, dt, resid_max, resid_absmax, resid_rms)."""
         t, dt = C.c_double(), C.c_double()

@@ -324,3 +324,45 @@ func (c *Context) WallPoints() (x, y []float64, q [4][]float64, p []float64, err
 	}
 	return
 }
+
+// GraphMesh returns the solution output's graph mesh (CreateAVSGraphMesh):
+// XY as interleaved float32 pairs, the sub-triangles as int64 point indices
+// (the avs TriMesh's XY and TriVerts), and the points per element.
+func (c *Context) GraphMesh() (xy []float32, tris [][3]int64, lenElement int, err error) {
+	var L, nt, k32 C.int32_t
+	if err = status(c.ctx, C.gcfd_graph_mesh(c.ctx, &L, &nt, nil, nil)); err != nil {
+		return
+	}
+	if err = status(c.ctx, C.gcfd_dims(c.ctx, &k32, nil, nil, nil, nil)); err != nil {
+		return
+	}
+	K := int(k32)
+	xy = make([]float32, 2*K*int(L))
+	tris = make([][3]int64, K*int(nt))
+	if K > 0 {
+		err = status(c.ctx, C.gcfd_graph_mesh(c.ctx, nil, nil, (*C.float)(unsafe.Pointer(&xy[0])),
+			(*C.int64_t)(unsafe.Pointer(&tris[0][0]))))
+	}
+	return xy, tris, int(L), err
+}
+
+// GraphFields evaluates flow functions (the reference's FlowFunction values
+// 0..13) at the graph points, K x lenElement float32 per field: the fields
+// map AVSFieldWriter.Save takes.
+func (c *Context) GraphFields(kinds []int32, lenElement int) (out [][]float32, err error) {
+	var k32 C.int32_t
+	if err = status(c.ctx, C.gcfd_dims(c.ctx, &k32, nil, nil, nil, nil)); err != nil {
+		return
+	}
+	n := int(k32) * lenElement
+	flat := make([]float32, len(kinds)*n)
+	if len(kinds) > 0 && n > 0 {
+		err = status(c.ctx, C.gcfd_graph_fields(c.ctx, C.int32_t(len(kinds)), (*C.int32_t)(unsafe.Pointer(&kinds[0])),
+			(*C.float)(unsafe.Pointer(&flat[0]))))
+	}
+	out = make([][]float32, len(kinds))
+	for f := range kinds {
+		out[f] = flat[f*n : (f+1)*n]
+	}
+	return out, err
+}

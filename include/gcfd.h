@@ -266,6 +266,39 @@ int gcfd_sample_points(gcfd_ctx* ctx, int32_t npts, const double* x, const doubl
  * and the count on return.  Any of x, y, q4, p may be NULL. */
 int gcfd_wall_points(gcfd_ctx* ctx, int32_t* npts, double* x, double* y, double* q4, double* p);
 
+/* ---- Solution output: the graph mesh and fields ----
+ * What the reference streams to meshfile.gobcfd and solutionfile.gobcfd
+ * (CreateAVSGraphMesh, AVSFieldWriter, DG2D/graphics_support.go:43-128,173-230;
+ * GetPlotField, model_problems/Euler2D/plot.go:14-85; Solve, euler.go:190-215),
+ * as arrays for the caller's writer (the Go caller keeps its gob encoder).
+ * Each element has len_element = 3 (NpEdge + 1) + Np graph points: per edge
+ * n = 0..2 its starting vertex then its NpEdge flux points counter-clockwise,
+ * then the Np solution points; element-major (point k * len_element + p). */
+
+/* The reference element's graph points (2 x len_element r, s pairs) and its
+ * sub-triangles (3 x ntri local point indices, counter-clockwise): the Delaunay
+ * triangulation of the graph points (the reference's constrained triangulation
+ * with Triangle, geometry2D/triangulate.go:34-93; its constraints lie on the
+ * hull).  Needs no context; NULL outputs are skipped. */
+int gcfd_host_graph_element(int32_t N, int32_t* len_element, int32_t* ntri, double* rs, int32_t* tris);
+
+/* The mesh's graph points as FP32 (x, y) pairs (2 x K x len_element; the
+ * vertices are the mesh's, the edge and solution points their affine images)
+ * and the sub-triangles as global point indices (3 x K x ntri_per_element,
+ * int64 like the reference's TriMesh).  NULL outputs are skipped. */
+int gcfd_graph_mesh(gcfd_ctx* ctx, int32_t* len_element, int32_t* ntri_per_element, float* xy, int64_t* tris);
+
+/* Flow functions of the current state at the graph points, FP32, K x
+ * len_element per field, fields one after another.  kinds are the reference's
+ * FlowFunction values 0..13 (fluids.go:209-222: Density, XMomentum, YMomentum,
+ * Energy, Mach, StaticPressure, DynamicPressure, PressureCoefficient,
+ * SoundSpeed, Velocity, XVelocity, YVelocity, Enthalpy, Entropy), evaluated at
+ * the solution points (GetFlowFunctionBase, fluids.go:289-336, with the far
+ * field's Pinf and dynamic pressure), taken to the graph points by the
+ * solution basis, each vertex value then the mean of the two edge points
+ * beside it (AverageGraphFieldVertices, DG2D/graphics_support2.go:184-199). */
+int gcfd_graph_fields(gcfd_ctx* ctx, int32_t nfields, const int32_t* kinds, float* out);
+
 /* Residual norms of an increment array that the caller owns, computed without
  * allocating anything.  This entry point has no counterpart in the reference.
  *
