@@ -200,13 +200,15 @@ def run(name: str, precision: str = "fp64", scale: float = 1.0, device: int = 0,
 
 
 def adjoint(name: str, steps: int, every: int, warm_steps: int = 0, warm_precision: str = "fp32",
-            fd_h: float = 1e-8, device: int = 0, seed: int = 0):
+            fd_h: float = 1e-8, device: int = 0, seed: int = 0, adjoint_precision: str = "fp64"):
     """The field-error adjoint of a vortex configuration: advance warm_steps in
     warm_precision, then record `steps` FP64 steps with a checkpoint every
     `every` steps, take J = sum (Q - Q_exact(t))^2 at the end and run the
     adjoint back to the window's start.  The gradient is checked along one
     random direction against central differences of the FP64 forward
-    (the GPU FP64 path, which tracks the oracle to 1e-10)."""
+    (the GPU FP64 path, which tracks the oracle to 1e-10).  adjoint_precision
+    "fp32" / "tf32x3" records and reverses the window on the mixed path instead
+    (its own J; no difference check)."""
     cfg = CONFIGS[name]
     assert cfg.mesh == "vortex"
     mesh = build_mesh(cfg)
@@ -220,16 +222,24 @@ def adjoint(name: str, steps: int, every: int, warm_steps: int = 0, warm_precisi
                 s.set_global_state(w.get_global_state())
                 s.time = info["time"]
         Q0, t0 = s.get_global_state(), s.time
+        g = s
+        if adjoint_precision != "fp64":
+            g = Euler(ip, mesh, 1, precision=adjoint_precision, device=device, vortex_center=(0.0, 0.0))
+            g.set_global_state(Q0)
+            g.time = t0
+        out["adjoint_precision"] = adjoint_precision
         t1 = time.perf_counter()
-        s.record(steps, every)
+        g.record(steps, every)
         t2 = time.perf_counter()
-        J, Qbf, tbf = s.functional("vortex_error")
+        J, Qbf, tbf = g.functional("vortex_error")
         t3 = time.perf_counter()
-        Qb0, qinfb, tb0 = s.step_vjp(Qbf, tbf)
+        Qb0, qinfb, tb0 = g.step_vjp(Qbf, tbf)
         t4 = time.perf_counter()
         out.update(J=J, grad_norm=float(np.linalg.norm(Qb0)), time_bar0=tb0,
                    record_s=t2 - t1, vjp_s=t4 - t3, vjp_over_record=(t4 - t3) / (t2 - t1))
-        if fd_h > 0:
+        if g is not s:
+            g.close()
+        if fd_h > 0 and g is s:
             rng = np.random.default_rng(seed)
             d = rng.standard_normal(Q0.shape) * np.abs(Q0)
 
@@ -418,7 +428,7 @@ def main(argv=None):
                    help="vortex adjoint: check along the smooth directions d/dx0 and d/dbeta of the exact vortex "
                         "with an h sweep and Richardson extrapolation instead of a random direction")
     p.add_argument("--adjoint-precision", choices=["fp64", "fp32", "tf32x3"], default="fp64",
-                   help="with --smooth: the path whose adjoint gives the gradient (fp32: the mixed path)")
+                   help="vortex adjoint: the path whose adjoint runs the window (fp32: the mixed path)")
     a = p.parse_args(argv)
     if a.adjoint_steps and a.config.startswith("wedge"):
         res = wedge_sensitivity(a.adjoint_steps, a.checkpoint_every, a.scale, fd_h=a.fd_h)
@@ -428,7 +438,8 @@ def main(argv=None):
                              adjoint_precision=a.adjoint_precision)
     elif a.adjoint_steps:
         res = adjoint(a.config, a.adjoint_steps, a.checkpoint_every, a.warm_steps,
-                      a.precision if a.precision != "fp64" else "fp32", fd_h=a.fd_h)
+                      a.precision if a.precision != "fp64" else "fp32", fd_h=a.fd_h,
+                      adjoint_precision=a.adjoint_precision)
     else:
         res = run(a.config, a.precision, a.scale, max_steps=a.max_steps, report_every=a.report_every,
                   stage_pipeline=a.stage_pipeline)

@@ -39,7 +39,7 @@ constexpr float kAdjA2 = 8677707.0f * kAdjQ, kAdjA3 = 1611615.0f * kAdjQ, kAdjA4
 // applied to Q0 + Ds per variable: the linearisation point of the edge
 // adjoints that follow.
 template <int N>
-__global__ void __launch_bounds__(128) k_adj_div32(AdjArgs<float> a, const float* __restrict__ geo,
+__global__ void __launch_bounds__(128, 8) k_adj_div32(AdjArgs<float> a, const float* __restrict__ geo,
                                                    const float* __restrict__ QFbNext, float* __restrict__ faces) {
   constexpr int NP = Dims<N>::NP, NE3 = Dims<N>::NE3, NF = Dims<N>::NF;
   __shared__ float sFx[4][NP][32], sFy[4][NP][32], sC[4][NP][32];
