@@ -160,10 +160,10 @@ def test_graph_fields_against_oracle(N, precision):
 
 @pytest.mark.gpu
 def test_solution_writer_on_a_solver(tmp_path):
-    mesh = meshes.vortex_box(6, jitter=0.1)
-    ip = InputParameters2D(CFL=1.0, FluxType="roe", InitType="ivortex", PolynomialOrder=2, FinalTime=1e9)
+    mesh = meshes.vortex_box(8, jitter=0.1)
+    ip = InputParameters2D(CFL=0.5, FluxType="roe", InitType="ivortex", PolynomialOrder=2, FinalTime=1e9)
     mp, sp = os.path.join(tmp_path, "m.gcfd"), os.path.join(tmp_path, "s.gcfd")
-    with Euler(ip, mesh, 1, precision="fp32") as g:
+    with Euler(ip, mesh, 1, precision="fp32", vortex_center=(0.0, 0.0)) as g:
         output.write_mesh(mp, g)
         with output.SolutionWriter(sp, g, ["Density", "Mach"], {"CFL": 1.0}) as w:
             for it in range(3):
