@@ -13,14 +13,30 @@
 // adjoints (FluxEdgeInterp of Q0 + D_s, from the rows the block reads anyway).
 #pragma once
 #include "gcfd_adjoint.cuh"
+#include "gcfd_mixed.cuh"
 
 namespace gcfd {
 
 // Operators of the order this translation unit is built for (one order per
-// unit), set by adj_mixed_consts.
-static __constant__ float cAdjDiv[Dims<4>::NP * Dims<4>::NF];   // DivInt [r][j]
-static __constant__ float cAdjDivCS[Dims<4>::NF];               // its column sums sum_r DivInt[r][j] (FP64, rounded)
-static __constant__ float cAdjIop[Dims<4>::NE3 * Dims<4>::NP];  // FluxEdgeInterp [j][i]
+// unit), set by AdjLaunch::mixed_consts, as packed pairs for fma.rn.f32x2
+// (ffma2): one instruction updates two outputs, each lane rounding like fmaf.
+//   cAdjDivFS[r][i]   (DivInt[r][i], DivInt[r][NP + i]): the r- and s-flux adjoints of point i
+//   cAdjDivE[r][q]    (DivInt[r][2NP + 2q], DivInt[r][2NP + 2q + 1]): edge DOFs 2q, 2q + 1
+//   cAdjCSFS, cAdjCSE the same pairs of DivInt's column sums (FP64, rounded)
+//   cAdjIopT[j][h]    (FluxEdgeInterp[j][2h], FluxEdgeInterp[j][2h + 1]): FluxEdgeInterp^T
+//   cAdjIop[i][q]     (FluxEdgeInterp[2q][i], FluxEdgeInterp[2q + 1][i]): the faces
+// (zero past the last row or column).
+template <int N>
+struct AdjDims {
+  static constexpr int NP = Dims<N>::NP, NE3 = Dims<N>::NE3, NF = Dims<N>::NF;
+  static constexpr int NEH = (NE3 + 1) / 2, NPH = (NP + 1) / 2;
+};
+static __constant__ float2 cAdjDivFS[AdjDims<4>::NP * AdjDims<4>::NP];
+static __constant__ float2 cAdjDivE[AdjDims<4>::NP * AdjDims<4>::NEH];
+static __constant__ float2 cAdjCSFS[AdjDims<4>::NP];
+static __constant__ float2 cAdjCSE[AdjDims<4>::NEH];
+static __constant__ float2 cAdjIopT[AdjDims<4>::NE3 * AdjDims<4>::NPH];
+static __constant__ float2 cAdjIop[AdjDims<4>::NP * AdjDims<4>::NEH];
 
 // SSP(5,4) weights on the stage states (rkAdvance, euler.go:511-564) for the
 // FP32 reverse sweep.  The transpose carries the step's final-state adjoint to
@@ -39,9 +55,10 @@ constexpr float kAdjA2 = 8677707.0f * kAdjQ, kAdjA3 = 1611615.0f * kAdjQ, kAdjA4
 // applied to Q0 + Ds per variable: the linearisation point of the edge
 // adjoints that follow.
 template <int N>
-__global__ void __launch_bounds__(128, 8) k_adj_div32(AdjArgs<float> a, const float* __restrict__ geo,
+__global__ void __launch_bounds__(128) k_adj_div32(AdjArgs<float> a, const float* __restrict__ geo,
                                                    const float* __restrict__ QFbNext, float* __restrict__ faces) {
-  constexpr int NP = Dims<N>::NP, NE3 = Dims<N>::NE3, NF = Dims<N>::NF;
+  constexpr int NP = Dims<N>::NP, NE3 = Dims<N>::NE3;
+  constexpr int NEH = AdjDims<N>::NEH, NPH = AdjDims<N>::NPH;
   __shared__ float sFx[4][NP][32], sFy[4][NP][32], sC[4][NP][32];
   __shared__ float sDt[4][32];
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -69,11 +86,12 @@ __global__ void __launch_bounds__(128, 8) k_adj_div32(AdjArgs<float> a, const fl
 #pragma unroll
       for (int j = 0; j < NE3; ++j) f[j] = QFbNext[(static_cast<size_t>(n) * NE3 + j) * sK + k];
 #pragma unroll
-      for (int r = 0; r < NP; ++r) {
-        float acc = qb[r];
+      for (int h = 0; h < NPH; ++h) {
+        float2 acc = make_float2(qb[2 * h], 2 * h + 1 < NP ? qb[2 * h + 1] : 0.0f);
 #pragma unroll
-        for (int j = 0; j < NE3; ++j) acc = fmaf(cAdjIop[j * NP + r], f[j], acc);
-        qb[r] = acc;
+        for (int j = 0; j < NE3; ++j) acc = ffma2(cAdjIopT[j * NPH + h], make_float2(f[j], f[j]), acc);
+        qb[2 * h] = acc.x;
+        if (2 * h + 1 < NP) qb[2 * h + 1] = acc.y;
       }
     }
     // the SSP stage combination in reverse (k_adj_div's first part)
@@ -126,22 +144,19 @@ __global__ void __launch_bounds__(128, 8) k_adj_div32(AdjArgs<float> a, const fl
     // the edge-DOF adjoints of this variable, and its interior transformed-flux
     // adjoints (to the point phase through shared memory)
 #pragma unroll
-    for (int j = 0; j < NE3; ++j) {
-      float d = b0 * cAdjDivCS[2 * NP + j];
+    for (int q = 0; q < NEH; ++q) {
+      float2 e = make_float2(b0 * cAdjCSE[q].x, b0 * cAdjCSE[q].y);
 #pragma unroll
-      for (int r = 1; r < NP; ++r) d = fmaf(cAdjDiv[r * NF + 2 * NP + j], Rb[r], d);
-      a.FEb[(static_cast<size_t>(n) * NE3 + j) * sK + k] = mooj * d;
+      for (int r = 1; r < NP; ++r) e = ffma2(cAdjDivE[r * NEH + q], make_float2(Rb[r], Rb[r]), e);
+      a.FEb[(static_cast<size_t>(n) * NE3 + 2 * q) * sK + k] = mooj * e.x;
+      if (2 * q + 1 < NE3) a.FEb[(static_cast<size_t>(n) * NE3 + 2 * q + 1) * sK + k] = mooj * e.y;
     }
 #pragma unroll
     for (int i = 0; i < NP; ++i) {
-      float fr = b0 * cAdjDivCS[i], fs = b0 * cAdjDivCS[NP + i];
+      float2 f = make_float2(b0 * cAdjCSFS[i].x, b0 * cAdjCSFS[i].y);
 #pragma unroll
-      for (int r = 1; r < NP; ++r) {
-        fr = fmaf(cAdjDiv[r * NF + i], Rb[r], fr);
-        fs = fmaf(cAdjDiv[r * NF + NP + i], Rb[r], fs);
-      }
-      fr *= mooj;
-      fs *= mooj;
+      for (int r = 1; r < NP; ++r) f = ffma2(cAdjDivFS[r * NP + i], make_float2(Rb[r], Rb[r]), f);
+      const float fr = f.x * mooj, fs = f.y * mooj;
       sFx[n][i][lane] = Jd * (J0 * fr + J2 * fs);
       sFy[n][i][lane] = Jd * (J1 * fr + J3 * fs);
     }
@@ -150,11 +165,12 @@ __global__ void __launch_bounds__(128, 8) k_adj_div32(AdjArgs<float> a, const fl
 #pragma unroll
       for (int i = 0; i < NP; ++i) q[i] = stage_value(a, off + i * sK);
 #pragma unroll
-      for (int j = 0; j < NE3; ++j) {
-        float f = 0.0f;
+      for (int h = 0; h < NEH; ++h) {
+        float2 fc = make_float2(0.0f, 0.0f);
 #pragma unroll
-        for (int i = 0; i < NP; ++i) f = fmaf(cAdjIop[j * NP + i], q[i], f);
-        faces[(static_cast<size_t>(n) * NE3 + j) * sK + k] = f;
+        for (int i = 0; i < NP; ++i) fc = ffma2(cAdjIop[i * NEH + h], make_float2(q[i], q[i]), fc);
+        faces[(static_cast<size_t>(n) * NE3 + 2 * h) * sK + k] = fc.x;
+        if (2 * h + 1 < NE3) faces[(static_cast<size_t>(n) * NE3 + 2 * h + 1) * sK + k] = fc.y;
       }
     }
   }

@@ -419,19 +419,34 @@ struct AdjLaunch {
     std::swap(c->Qbf32, c->Qb32[0]);
     cudaMemcpyAsync(c->adjS + 10, c->adjS + 9, sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   }
-  // FP32 DivInt and FluxEdgeInterp into this unit's constant memory (k_adj_div32).
+  // FP32 DivInt and FluxEdgeInterp into this unit's constant memory as the
+  // packed pairs of k_adj_div32 (AdjDims), with DivInt's column sums in FP64.
   static int mixed_consts(gcfd_ctx* c) {
-    std::vector<float> d(c->el.DivInt.v.begin(), c->el.DivInt.v.end());
-    std::vector<float> f(c->el.FluxEdgeInterp.v.begin(), c->el.FluxEdgeInterp.v.end());
-    std::vector<float> cs(c->NF);
-    for (int j = 0; j < c->NF; ++j) {
-      double t = 0.0;
-      for (int r = 0; r < c->Np; ++r) t += c->el.DivInt(r, j);
-      cs[j] = static_cast<float>(t);
+    constexpr int NP = AdjDims<N>::NP, NE3 = AdjDims<N>::NE3, NEH = AdjDims<N>::NEH, NPH = AdjDims<N>::NPH;
+    const DMat& D = c->el.DivInt;
+    const DMat& I = c->el.FluxEdgeInterp;
+    std::vector<double> cs(c->NF, 0.0);
+    for (int j = 0; j < c->NF; ++j)
+      for (int r = 0; r < NP; ++r) cs[j] += D(r, j);
+    auto f2 = [](double x, double y) { return make_float2(static_cast<float>(x), static_cast<float>(y)); };
+    std::vector<float2> fs(NP * NP), de(NP * NEH), csfs(NP), cse(NEH), iopT(NE3 * NPH), iop(NP * NEH);
+    for (int r = 0; r < NP; ++r) {
+      for (int i = 0; i < NP; ++i) fs[r * NP + i] = f2(D(r, i), D(r, NP + i));
+      for (int q = 0; q < NEH; ++q)
+        de[r * NEH + q] = f2(D(r, 2 * NP + 2 * q), 2 * q + 1 < NE3 ? D(r, 2 * NP + 2 * q + 1) : 0.0);
     }
-    GCFD_CUDA(c, cudaMemcpyToSymbol(cAdjDiv, d.data(), d.size() * sizeof(float)));
-    GCFD_CUDA(c, cudaMemcpyToSymbol(cAdjDivCS, cs.data(), cs.size() * sizeof(float)));
-    GCFD_CUDA(c, cudaMemcpyToSymbol(cAdjIop, f.data(), f.size() * sizeof(float)));
+    for (int i = 0; i < NP; ++i) csfs[i] = f2(cs[i], cs[NP + i]);
+    for (int q = 0; q < NEH; ++q) cse[q] = f2(cs[2 * NP + 2 * q], 2 * q + 1 < NE3 ? cs[2 * NP + 2 * q + 1] : 0.0);
+    for (int j = 0; j < NE3; ++j)
+      for (int h = 0; h < NPH; ++h) iopT[j * NPH + h] = f2(I(j, 2 * h), 2 * h + 1 < NP ? I(j, 2 * h + 1) : 0.0);
+    for (int i = 0; i < NP; ++i)
+      for (int q = 0; q < NEH; ++q) iop[i * NEH + q] = f2(I(2 * q, i), 2 * q + 1 < NE3 ? I(2 * q + 1, i) : 0.0);
+    GCFD_CUDA(c, cudaMemcpyToSymbol(cAdjDivFS, fs.data(), fs.size() * sizeof(float2)));
+    GCFD_CUDA(c, cudaMemcpyToSymbol(cAdjDivE, de.data(), de.size() * sizeof(float2)));
+    GCFD_CUDA(c, cudaMemcpyToSymbol(cAdjCSFS, csfs.data(), csfs.size() * sizeof(float2)));
+    GCFD_CUDA(c, cudaMemcpyToSymbol(cAdjCSE, cse.data(), cse.size() * sizeof(float2)));
+    GCFD_CUDA(c, cudaMemcpyToSymbol(cAdjIopT, iopT.data(), iopT.size() * sizeof(float2)));
+    GCFD_CUDA(c, cudaMemcpyToSymbol(cAdjIop, iop.data(), iop.size() * sizeof(float2)));
     return GCFD_OK;
   }
   static void mixed_bar_convert(gcfd_ctx* c, bool toFP32) {
