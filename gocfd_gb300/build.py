@@ -23,7 +23,7 @@ LIB_PATH = os.path.join(PKG_DIR, "libgcfd.so")
 # (source, extra defines): the per-order units once per order, largest first.
 SOURCES = ([("gcfd_order.cu", [f"-DGCFD_ORDER={n}"]) for n in (4, 3, 2, 1, 0)] +
            [("gcfd_order_adj.cu", [f"-DGCFD_ORDER={n}"]) for n in (4, 3, 2, 1, 0)] +
-           [("gcfd.cu", []), ("gcfd_adjoint_api.cu", []), ("gcfd_static.cu", []), ("gcfd_post.cu", []), ("gcfd_graph.cu", []),
+           [("gcfd.cu", []), ("gcfd_adjoint_api.cu", []), ("gcfd_static.cu", []), ("gcfd_post.cu", []), ("gcfd_graph.cu", []), ("gcfd_geometry.cu", []),
             ("gcfd_peaks.cu", []),
             ("dfr_element.cpp", []), ("mesh.cpp", [])])
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -235,37 +235,6 @@ int copy_shards(gcfd_ctx* c, double* dst, int nshards, const int32_t* Kmax, cons
 
 namespace {
 
-// Initial condition, InitializeSolution (euler.go:728-794).
-std::vector<double> initial_state(gcfd_ctx* c) {
-  const int K = c->K, Np = c->Np;
-  std::vector<double> q(static_cast<size_t>(4) * Np * K);
-  for (int i = 0; i < Np; ++i)
-    for (int k = 0; k < K; ++k) {
-      double s[4];
-      const size_t pt = static_cast<size_t>(i) * K + k;
-      if (c->prm.init_type == GCFD_INIT_IVORTEX) {
-        const double x = c->geo.xSol[pt], y = c->geo.ySol[pt];
-        const double pi = 3.14159265358979323846, g = c->vgamma, GM1 = g - 1.0;
-        double u = 1.0, v = 0.0;
-        const double r2 = (x - c->vx0) * (x - c->vx0) + (y - c->vy0) * (y - c->vy0);
-        const double ex1r = std::exp(1.0 - r2);
-        const double tv1 = 1.0 - (GM1 * c->vbeta * c->vbeta * std::exp(2.0 * (1.0 - r2)) / (16.0 * g * pi * pi));
-        u -= c->vbeta * ex1r * (y - c->vy0) * (0.5 / pi);
-        v += c->vbeta * ex1r * (x - c->vx0) * (0.5 / pi);
-        const double rho = std::pow(tv1, 1.0 / GM1), p = std::pow(rho, g);
-        s[0] = rho; s[1] = rho * u; s[2] = rho * v;
-        s[3] = p * (1.0 / GM1) + 0.5 * rho * (u * u + v * v);
-      } else if (c->prm.init_type == GCFD_INIT_SHOCKTUBE) {
-        const double* src = (c->geo.xSol[pt] < 0.5) ? c->fsIn.qinf : c->fsOut.qinf;
-        for (int n = 0; n < 4; ++n) s[n] = src[n];
-      } else {
-        for (int n = 0; n < 4; ++n) s[n] = c->fsFar.qinf[n];
-      }
-      for (int n = 0; n < 4; ++n) q[(static_cast<size_t>(n) * Np + i) * K + k] = s[n];
-    }
-  return q;
-}
-
 // Buffers and operators of the artificial dissipation (FP64 path).
 int build_diss(gcfd_ctx* c, const gcfd_mesh* m) {
   const int K = c->K, Np = c->Np, NE = c->NE;
@@ -288,10 +257,6 @@ int build_diss(gcfd_ctx* c, const gcfd_mesh* m) {
   if ((rc = upload(c, &c->dSensP, c->el.SensP.v))) return rc;
   if ((rc = upload(c, &c->dMass, c->el.MassMatrix.v))) return rc;
   if ((rc = upload(c, &c->dSensD, c->el.SensD.v))) return rc;
-  if ((rc = upload(c, &c->dhK, c->geo.hK))) return rc;
-  if ((rc = upload(c, &c->dnxE, c->geo.nx))) return rc;
-  if ((rc = upload(c, &c->dnyE, c->geo.ny))) return rc;
-  if ((rc = upload(c, &c->dIIE, c->geo.IInII))) return rc;
   std::vector<int> ev(static_cast<size_t>(3) * K);
   for (int k = 0; k < K; ++k)
     for (int v = 0; v < 3; ++v) ev[static_cast<size_t>(v) * K + k] = m->etov[3 * k + v];
@@ -324,16 +289,7 @@ int build_mixed(gcfd_ctx* c) {
   GCFD_CUDA(c, cudaMemset(c->mfhat, 0, sizeof(float) * c->nEdges * 4 * NEP));
   GCFD_CUDA(c, cudaMemset(c->mcorr, 0, sizeof(float) * c->nEdges * 4));
   if ((rc = order_ops(c->N)->mixed_consts(c))) return rc;
-  const Geometry& g = c->geo;
-  std::vector<float> geo(static_cast<size_t>(6) * K), ii(static_cast<size_t>(3) * K);
-  for (int k = 0; k < K; ++k) {
-    geo[k] = static_cast<float>(g.Jdet[k]);
-    for (int q = 0; q < 4; ++q) geo[static_cast<size_t>(q + 1) * K + k] = static_cast<float>(g.Jinv[4 * k + q]);
-    geo[static_cast<size_t>(5) * K + k] = static_cast<float>(1.0 / g.Jdet[k]);
-    for (int e = 0; e < 3; ++e) ii[static_cast<size_t>(e) * K + k] = static_cast<float>(g.IInII[static_cast<size_t>(e) * K + k]);
-  }
-  if ((rc = upload(c, &c->mgeo, geo))) return rc;
-  if ((rc = upload(c, &c->mII, ii))) return rc;
+  if ((rc = device_geometry_mixed(c))) return rc;
   std::vector<int> slot(static_cast<size_t>(3) * K);
   std::vector<int> pos(c->topo.nEdges);
   for (int i = 0; i < c->nEdges; ++i) pos[c->edgeOrder[i]] = i;
@@ -344,15 +300,6 @@ int build_mixed(gcfd_ctx* c) {
       slot[static_cast<size_t>(e) * K + k] = pos[en] * 2 + side;
     }
   if ((rc = upload(c, &c->meslot, slot))) return rc;
-  std::vector<float> nx(c->nEdges), ny(c->nEdges), oh(c->nEdges);
-  for (int i = 0; i < c->nEdges; ++i) {
-    nx[i] = static_cast<float>(c->hnx[i]);
-    ny[i] = static_cast<float>(c->hny[i]);
-    oh[i] = static_cast<float>(c->hoohK[i]);
-  }
-  if ((rc = upload(c, &c->mnx, nx))) return rc;
-  if ((rc = upload(c, &c->mny, ny))) return rc;
-  if ((rc = upload(c, &c->moohK, oh))) return rc;
   return order_ops(c->N)->mixed_pipe(c);
 }
 
@@ -377,14 +324,9 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
   std::string msg = build_topology(m->nverts, m->K, m->etov, m->nbc, m->bc_v1, m->bc_v2, m->bc_flag,
                                    &c->topo);
   if (!msg.empty()) return fail(c, GCFD_ERR_ARG, msg);
-  build_geometry(c->el, c->topo, m->vx, m->vy, m->etov, &c->geo);
   c->meshVX.assign(m->vx, m->vx + m->nverts);
   c->meshVY.assign(m->vy, m->vy + m->nverts);
   c->meshEToV.assign(m->etov, m->etov + 3 * static_cast<size_t>(m->K));
-  for (int k = 0; k < c->K; ++k)
-    if (!(c->geo.Jdet[k] > 0.0))
-      return fail(c, GCFD_ERR_ARG, "element " + std::to_string(k) +
-                                       " is not counter-clockwise (|J| <= 0)");
 
   // Free streams and BC relabelling of InitializeSolution (euler.go:728-794).
   c->fsFar = freestream_from_mach(p.minf, p.gamma, p.alpha);
@@ -406,7 +348,6 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
 
   // Edge tables: interior edges first, then boundary edges, each in mesh order.
   const Topology& t = c->topo;
-  const Geometry& g = c->geo;
   std::vector<int> order;
   for (int en = 0; en < t.nEdges; ++en)
     if (t.kR[en] >= 0) order.push_back(en);
@@ -417,7 +358,6 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
   c->nBC = c->nEdges - c->nInt;
   const int K = c->K, NE = c->NE, Np = c->Np;
   std::vector<int> kL(c->nEdges), kR(c->nEdges), eLR(c->nEdges), flag(std::max(c->nBC, 1));
-  std::vector<double> nx(c->nEdges), ny(c->nEdges), IIL(c->nEdges), IIR(c->nEdges), oohK(c->nEdges);
   std::vector<double> bx(static_cast<size_t>(std::max(c->nBC, 1)) * NE), by(bx.size());
   std::vector<int> elemEdge(static_cast<size_t>(3) * K);
   std::vector<int> pos(t.nEdges);
@@ -427,12 +367,6 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
     kL[i] = t.kL[en];
     kR[i] = t.kR[en] >= 0 ? t.kR[en] : 0;
     eLR[i] = t.eL[en] | ((t.eR[en] >= 0 ? t.eR[en] : 0) << 2);
-    const size_t fl = static_cast<size_t>(t.eL[en]) * K + t.kL[en];
-    nx[i] = g.nx[fl];
-    ny[i] = g.ny[fl];
-    IIL[i] = g.IInII[fl];
-    IIR[i] = t.kR[en] >= 0 ? g.IInII[static_cast<size_t>(t.eR[en]) * K + t.kR[en]] : 0.0;
-    oohK[i] = 1.0 / g.hK[t.kL[en]];
     if (i >= c->nInt) {
       const int b = i - c->nInt;
       flag[b] = t.bc[en];
@@ -447,9 +381,6 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
     for (int ed = 0; ed < 3; ++ed)
       elemEdge[static_cast<size_t>(ed) * K + k] = pos[t.elemEdge[3 * k + ed]];
   c->edgeOrder = order;
-  c->hnx = nx;
-  c->hny = ny;
-  c->hoohK = oohK;
 
   GCFD_CUDA(c, cudaSetDevice(p.device));
   GCFD_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
@@ -457,6 +388,8 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
   const size_t nFace = static_cast<size_t>(4) * 3 * NE * K;
   const size_t tsz = c->fp32 ? sizeof(float) : sizeof(double);
   int rc;
+  // geometry and per-edge tables on the device (gcfd_geometry.cu)
+  if ((rc = device_geometry(c, m, kL, kR, eLR))) return rc;
   for (int s = 0; s < 5; ++s)
     if ((rc = dalloc(c, &c->Q[s], nState))) return rc;
   if ((rc = dalloc(c, &c->R, nState))) return rc;
@@ -475,21 +408,8 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
   if (c->diss && (rc = build_diss(c, m))) return rc;
   if ((rc = upload(c, &c->Iop, c->el.FluxEdgeInterp.v))) return rc;
   if ((rc = upload(c, &c->Div, c->el.DivInt.v))) return rc;
-  if ((rc = upload(c, &c->Jdet, g.Jdet))) return rc;
-  std::vector<double> jinvT(static_cast<size_t>(4) * K);
-  for (int k = 0; k < K; ++k)
-    for (int q = 0; q < 4; ++q) jinvT[static_cast<size_t>(q) * K + k] = g.Jinv[4 * k + q];
-  if ((rc = upload(c, &c->Jinv, jinvT))) return rc;
-  if ((rc = upload(c, &c->ekL, kL))) return rc;
-  if ((rc = upload(c, &c->ekR, kR))) return rc;
-  if ((rc = upload(c, &c->eLR, eLR))) return rc;
   if ((rc = upload(c, &c->bcFlag, flag))) return rc;
   if ((rc = upload(c, &c->elemEdge, elemEdge))) return rc;
-  if ((rc = upload(c, &c->enx, nx))) return rc;
-  if ((rc = upload(c, &c->eny, ny))) return rc;
-  if ((rc = upload(c, &c->eIIL, IIL))) return rc;
-  if ((rc = upload(c, &c->eIIR, IIR))) return rc;
-  if ((rc = upload(c, &c->eoohK, oohK))) return rc;
   if ((rc = upload(c, &c->bx, bx))) return rc;
   if ((rc = upload(c, &c->by, by))) return rc;
   if ((rc = dalloc(c, &c->edgeSpeed, static_cast<size_t>(c->nEdges)))) return rc;
@@ -503,8 +423,7 @@ int build_context(gcfd_ctx* c, const gcfd_mesh* m) {
   GCFD_CUDA(c, cudaMemcpy(&c->sc->rpart, rp, sizeof(rp), cudaMemcpyHostToDevice));
   GCFD_CUDA(c, cudaMemset(c->DT, 0, sizeof(double) * K));
   GCFD_CUDA(c, cudaMemset(c->R, 0, sizeof(double) * nState));
-  std::vector<double> q0 = initial_state(c);
-  GCFD_CUDA(c, cudaMemcpy(c->Q[0], q0.data(), nState * sizeof(double), cudaMemcpyHostToDevice));
+  if ((rc = device_initial_state(c))) return rc;
   for (auto& e : c->ev) GCFD_CUDA(c, cudaEventCreate(&e));
   if ((rc = capture_graph(c))) return rc;
   GCFD_CUDA(c, cudaStreamSynchronize(c->stream));

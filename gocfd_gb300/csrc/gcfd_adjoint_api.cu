@@ -69,8 +69,7 @@ int func_init(gcfd_ctx* c) {
   }
   if ((rc = dalloc(c, &c->Qb[0], S))) return rc;
   if ((rc = dalloc(c, &c->QFb, F))) return rc;
-  if ((rc = upload(c, &c->dXs, c->geo.xSol))) return rc;
-  if ((rc = upload(c, &c->dYs, c->geo.ySol))) return rc;
+  if ((rc = device_solution_points(c, &c->dXs, &c->dYs))) return rc;
   if ((rc = upload(c, &c->edgeW, edge_weights(c)))) return rc;
   if ((rc = dalloc(c, &c->adjS, 16))) return rc;
   GCFD_CUDA(c, cudaMemsetAsync(c->adjS, 0, sizeof(double) * 16, c->stream));

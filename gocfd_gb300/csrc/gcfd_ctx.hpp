@@ -42,7 +42,6 @@ struct gcfd_ctx {
   bool fp32 = false;
   DFRElement el;
   Topology topo;
-  Geometry geo;
   HostFreeStream fsFar{}, fsIn{}, fsOut{};
   double vbeta = 5.0, vx0 = 5.0, vy0 = 0.0, vgamma = 1.4;
   cudaStream_t stream = nullptr;
@@ -147,7 +146,9 @@ struct gcfd_ctx {
   double *ckptV = nullptr, *segV = nullptr, *endV = nullptr;  // DTVisc (dissipation), K per entry
   Scalars* endSc = nullptr;
   std::vector<int> edgeOrder;             // device edge i -> topology edge
-  std::vector<double> hnx, hny, hoohK;    // per device edge
+  // mesh and solution points on the device (gcfd_geometry.cu)
+  double *dVX = nullptr, *dVY = nullptr, *dRS = nullptr;
+  int32_t* dEToV = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graphExec = nullptr;
   cudaEvent_t ev[10] = {};
@@ -267,6 +268,15 @@ inline int resid_units(const gcfd_ctx* c) {
 // Shared host helpers (gcfd.cu).
 int sync_fp64_state(gcfd_ctx* c);
 int prepare_if_dirty(gcfd_ctx* c);
+
+// Device geometry (gcfd_geometry.cu): per-element geometry and per-edge tables
+// from the mesh arrays and the device edge lists; the mixed path's FP32 copies;
+// solution-point coordinates; the initial state into Q[0].
+int device_geometry(gcfd_ctx* c, const gcfd_mesh* m, const std::vector<int>& kL, const std::vector<int>& kR,
+                    const std::vector<int>& eLR);
+int device_geometry_mixed(gcfd_ctx* c);
+int device_solution_points(gcfd_ctx* c, double** X, double** Y);
+int device_initial_state(gcfd_ctx* c);
 int check_shards(gcfd_ctx* c, int nshards, const int32_t* Kmax);
 int copy_shards(gcfd_ctx* c, double* dst, int nshards, const int32_t* Kmax, const double* const* Q,
                 bool toDevice, double* const* Qout);

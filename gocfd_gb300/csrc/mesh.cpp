@@ -1,5 +1,5 @@
-// Host mesh topology and geometry.  See mesh.hpp for the reference functions
-// each piece follows.
+// Host mesh topology and the mesh-file readers.  See mesh.hpp for the reference
+// functions each piece follows.
 #include "mesh.hpp"
 
 #include <algorithm>
@@ -192,66 +192,6 @@ std::string build_topology(int Nv, int K, const int32_t* etov, int nbc, const in
     }
   }
   return pair_periodic(periodic, t);
-}
-
-void build_geometry(const DFRElement& el, const Topology& t, const double* vx, const double* vy,
-                    const int32_t* etov, Geometry* g) {
-  const int K = t.K;
-  g->J.assign(4 * static_cast<size_t>(K), 0.0);
-  g->Jinv.assign(4 * static_cast<size_t>(K), 0.0);
-  g->Jdet.assign(K, 0.0);
-  for (int k = 0; k < K; ++k) {
-    const int v1 = etov[3 * k], v2 = etov[3 * k + 1], v3 = etov[3 * k + 2];
-    const double xr = 0.5 * (vx[v2] - vx[v1]), yr = 0.5 * (vy[v2] - vy[v1]);
-    const double xs = 0.5 * (vx[v3] - vx[v1]), ys = 0.5 * (vy[v3] - vy[v1]);
-    const double det = xr * ys - xs * yr;
-    double* J = &g->J[4 * k];
-    double* Ji = &g->Jinv[4 * k];
-    J[0] = xr; J[1] = xs; J[2] = yr; J[3] = ys;
-    g->Jdet[k] = det;
-    Ji[0] = ys / det; Ji[1] = -xs / det; Ji[2] = -yr / det; Ji[3] = xr / det;
-  }
-  g->nx.assign(3 * static_cast<size_t>(K), 0.0);
-  g->ny.assign(3 * static_cast<size_t>(K), 0.0);
-  g->IInII.assign(3 * static_cast<size_t>(K), 0.0);
-  for (int en = 0; en < t.nEdges; ++en) {
-    for (int c = 0; c < 2; ++c) {
-      const int k = c == 0 ? t.kL[en] : t.kR[en];
-      if (k < 0) continue;
-      // each side's own edge (a periodic pair's right side has its own key)
-      const uint64_t key = (c == 0) ? t.key[en] : t.keyR[en];
-      const int lo = static_cast<int>(key & 0xffffffffULL);
-      const int hi = static_cast<int>(key >> 32);
-      const int ed = c == 0 ? t.eL[en] : t.eR[en];
-      const bool rev = (c == 0 ? t.revL[en] : t.revR[en]) != 0;
-      // Vertices ordered opposite to the element's traversal: (-dy, dx) points out.
-      const int a = rev ? lo : hi, b = rev ? hi : lo;
-      const double dx = vx[b] - vx[a], dy = vy[b] - vy[a];
-      const double len = std::sqrt(dx * dx + dy * dy);
-      const size_t ind = static_cast<size_t>(ed) * K + k;
-      g->nx[ind] = -dy / len;
-      g->ny[ind] = dx / len;
-      g->IInII[ind] = (ed == 1) ? len / (2.0 * std::sqrt(2.0)) : len / 2.0;
-    }
-  }
-  g->edgeLenMax.assign(K, 0.0);
-  g->hK.assign(K, 0.0);
-  const double np12 = double(el.N + 1) * double(el.N + 1);
-  for (int k = 0; k < K; ++k) {
-    double mx = -1.0;
-    for (int ed = 0; ed < 3; ++ed) mx = std::max(mx, g->IInII[static_cast<size_t>(ed) * K + k]);
-    g->edgeLenMax[k] = g->Jdet[k] / mx;
-    g->hK[k] = g->edgeLenMax[k] / np12;
-  }
-  // Solution-point coordinates (the flux points' are computed where needed, at
-  // boundary edges: element_point).
-  const int n = static_cast<int>(el.r.size());
-  g->xSol.assign(static_cast<size_t>(n) * K, 0.0);
-  g->ySol.assign(static_cast<size_t>(n) * K, 0.0);
-  for (int i = 0; i < n; ++i)
-    for (int k = 0; k < K; ++k)
-      element_point(etov, vx, vy, k, el.r[i], el.s[i], &g->xSol[static_cast<size_t>(i) * K + k],
-                    &g->ySol[static_cast<size_t>(i) * K + k]);
 }
 
 // ---------------------------------------------------------------------------

@@ -1,12 +1,10 @@
-// Host-side mesh topology and FP64 geometry for the DFR solver (set-up time).
+// Host-side mesh topology for the DFR solver (set-up time); the geometry is
+// built on the device from it (gcfd_geometry.cu).
 //
 // Reference behaviour followed (gocfd):
 //   DG2D/triangulation.go:19-171   edge creation per element (edges v0v1, v1v2, v2v0),
-//                                  first connected triangle = "left", orientation flag,
-//                                  ||n|| scale factor IInII per connection
+//                                  first connected triangle = "left", orientation flag
 //   types/elemental.go:12-46       EdgeKey = min | max<<32, GetVertices(rev)
-//   DG2D/triangulation.go:230-235  GetEdgeCoordinates, oriented for outward normals
-//   DG2D/dfr_startup.go:89-98,125-147,256-314  hK, EdgeLenMax, Jacobian, face normals
 //   DG2D/element_utils.go:163-175  CalculateElementLocalGeometry (x,y of points)
 //   types/cfd.go:11-26             BCFLAG numbering
 #pragma once
@@ -44,13 +42,6 @@ struct Topology {
   std::vector<int> elemEdge;            // K*3: edge index of (k, local edge)
 };
 
-struct Geometry {
-  std::vector<double> J, Jinv, Jdet;    // K*4 [xr xs yr ys], K*4 [ys -xs -yr xr]/|J|, K
-  std::vector<double> nx, ny, IInII;    // 3*K, index e*K + k (outward unit normal, ||n||)
-  std::vector<double> edgeLenMax, hK;   // K
-  std::vector<double> xSol, ySol;       // Np*K
-};
-
 // Builds the edge table.  Returns an empty string on success, else a message.
 // Boundary flags are BCFLAGs; periodic ones (10, 11) carry a group number in
 // bits 8 and up (one group per periodic tag), and each group's edges are
@@ -59,9 +50,6 @@ std::string build_topology(int Nv, int K, const int32_t* etov, int nbc, const in
                            const int32_t* bc_v2, const int32_t* bc_flag, Topology* topo);
 
 std::string pair_periodic(const std::vector<std::pair<int, std::vector<int>>>& groups, Topology* t);
-
-void build_geometry(const DFRElement& el, const Topology& topo, const double* vx,
-                    const double* vy, const int32_t* etov, Geometry* geo);
 
 // Physical coordinates of the reference point (r, s) of element k
 // (CalculateElementLocalGeometry, element_utils.go:163-175).

@@ -64,7 +64,8 @@ def test_rhs_parity_fp64_bc_mesh(N, flux):
     mesh = meshes.read_mesh(fixture("fstepA001.neu"))
     gpu, ora = make_pair(mesh, N, flux=flux, minf=0.5, alpha=10.0)
     Q0 = gpu.get_global_state()
-    assert np.allclose(Q0, ora.Q, rtol=0, atol=1e-15)
+    # built on the device (CUDA's exp / pow against the host's: a few ulp)
+    assert np.allclose(Q0, ora.Q, rtol=2e-15, atol=1e-15)
     Q = perturbed(ora.Q, seed=N)
     r = gpu.rhs_global(Q)
     ref = ora.rhs(Q)
