@@ -109,9 +109,10 @@ int gcfd_read_mesh(const char* path, gcfd_mesh* out);
 void gcfd_free_mesh(gcfd_mesh* mesh);
 
 /* Replaces Euler2D.NewEuler (model_problems/Euler2D/euler.go:61-136): builds
- * the DFR operators and FP64 geometry on the host, uploads them, sets the
- * initial condition (InitializeSolution, euler.go:728-794) on the device and
- * records the per-step CUDA graph. */
+ * the DFR operators and the mesh topology on the host, the FP64 geometry and
+ * the initial condition (InitializeSolution, euler.go:728-794) on the device,
+ * and records the per-step CUDA graph.  An element with |J| <= 0 (not
+ * counter-clockwise) is GCFD_ERR_ARG. */
 int gcfd_create(const gcfd_mesh* mesh, const gcfd_params* params, gcfd_ctx** out);
 int gcfd_destroy(gcfd_ctx* ctx);
 const char* gcfd_last_error(const gcfd_ctx* ctx);
