@@ -66,6 +66,8 @@ def args_parse():
                    help="after the timed region: steps of the accuracy leg on vortex256 (0: skip)")
     p.add_argument("--acc-steps-large", type=int, default=100,
                    help="after the timed region: steps of the accuracy leg on the benchmarked workload (0: skip)")
+    p.add_argument("--adj-acc-steps", type=int, default=200,
+                   help="after the timed region: window of the adjoint gradient check on vortex256 (0: skip)")
     return p.parse_args()
 
 
@@ -436,10 +438,33 @@ def run_ours(a, world, rank, local):
             t1, t2 = sweep(n1), sweep(n2)
             adj_ms = (t2 - t1) / (n2 - n1)  # per reverse step, without the window's fixed costs
             legs[every] = {"ms_per_step": adj_ms, "ratio": adj_ms / fwd_ms, "window_ms": {str(n1): t1, str(n2): t2}}
+        if precision != "fp64":
+            # the whole window taped while recording (checkpoint_every >= nsteps,
+            # when a tape slot per step fits): the reverse sweep recomputes nothing;
+            # the cost is the reverse plus the taping's extra over the plain forward
+            def taped(n):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                sa.record(n, n)
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                sa.step_vjp(qbar)
+                return (t1 - t0) * 1e3, (time.perf_counter() - t1) * 1e3
+            taped(2)
+            n1 = max(10, a.adj_steps // 2)
+            n2 = n1 + max(10, a.adj_steps)
+            (r1, v1), (r2, v2) = taped(n1), taped(n2)
+            vjp_ms = (v2 - v1) / (n2 - n1)
+            rec_extra = (r2 - r1) / (n2 - n1) - fwd_ms
+            legs["taped"] = {"ms_per_step": vjp_ms, "record_extra_ms_per_step": rec_extra,
+                             "ratio": (vjp_ms + max(rec_extra, 0.0)) / fwd_ms,
+                             "window_ms": {str(n1): [r1, v1], str(n2): [r2, v2]},
+                             "note": "ratio = (reverse per step + taping's extra per recorded step) / forward"}
         sa.close()
         return {"ms_per_step": legs[10]["ms_per_step"], "forward_ms_per_step": fwd_ms,
                 "ratio": legs[10]["ratio"], "checkpoint_every": 10, "path": precision,
                 "window_ms": legs[10]["window_ms"], "checkpoint_every_1": legs[1],
+                "window_taped": legs.get("taped"),
                 "timing": "host clock around gcfd_step_vjp (synchronous) for two window lengths; per-step cost = "
                           "difference / difference in steps (the adjoint's host transfer and set-up are per "
                           "window); forward by CUDA events"}
@@ -486,6 +511,8 @@ def run_ours(a, world, rank, local):
             accuracy["vortex256"] = accuracy_leg("vortex256", a.acc_steps, local, ("fp64", "fp32", "tf32x3"))
         if a.acc_steps_large > 0 and a.workload != "vortex256":
             accuracy[a.workload] = accuracy_leg(a.workload, a.acc_steps_large, local, ("fp64", a.precision))
+        if a.adj_acc_steps > 0:
+            accuracy["adjoint_vortex256"] = adjoint_accuracy_leg("vortex256", a.adj_acc_steps, local)
         m = accuracy.get("vortex256") or accuracy.get(a.workload)
         if m:
             accuracy["mixed_vs_fp64_rel_l2"] = m.get(f"{a.precision}_vs_fp64_rel_l2")
@@ -556,6 +583,52 @@ def accuracy_leg(workload, steps, local, precisions):
         res[f"{prec}_vs_fp64_rel_l2_per_var"] = [float(np.linalg.norm(d[n]) / np.linalg.norm(ref[n]))
                                                 for n in range(4)]
     return res
+
+
+def adjoint_accuracy_leg(workload, steps, local, warm_steps=1000, every=10, hs=(1e-4, 5e-5)):
+    """The adjoints' gradients against FP64 central differences: after
+    warm_steps mixed steps, the field-error adjoint through `steps` steps
+    (checkpoint every `every`) on the FP64 path and on the mixed path (FP32
+    reverse sweep, the FP64 path's weight), dotted with the smooth directions
+    d/dx0 and d/dbeta of the exact vortex at the window's start, against the
+    Richardson extrapolation of FP64 central differences over hs."""
+    from gocfd_gb300 import configs
+    from gocfd_gb300.euler2d import Euler
+    wl = WORKLOADS[workload]
+    mesh = make_mesh(wl)
+    ip = input_params(wl["N"])
+    out = {"workload": workload, "warm_steps": warm_steps, "steps": steps, "checkpoint_every": every,
+           "hs": list(hs), "directions": "d Q_exact / d x0, d Q_exact / d beta at the window's start"}
+    with Euler(ip, mesh, 1, precision="fp64", device=local, vortex_center=(0.0, 0.0)) as s:
+        with Euler(ip, mesh, 1, precision="fp32", device=local, vortex_center=(0.0, 0.0)) as w:
+            info = w.step(warm_steps)
+            Q0 = w.get_global_state()
+        t0 = info["time"]
+        s.set_global_state(Q0)
+        s.time = t0
+        s.record(steps, every)
+        J, Qbf, tbf = s.functional("vortex_error")
+        Qb64, _, _ = s.step_vjp(Qbf, tbf)
+        with Euler(ip, mesh, 1, precision="fp32", device=local, vortex_center=(0.0, 0.0)) as g:
+            g.set_global_state(Q0)
+            g.time = t0
+            g.record(steps, every)
+            Qb32, _, _ = g.step_vjp(Qbf, tbf)
+        X, Y = configs.solution_points_xy(s)
+
+        def J_at(q):
+            s.set_global_state(q)
+            s.time = t0
+            s.step(steps)
+            return s.functional("vortex_error")[0]
+        for param in ("x0", "beta"):
+            d = configs.exact_vortex_param_derivative(X, Y, t0, param)
+            fd = {h: (J_at(Q0 + h * d) - J_at(Q0 - h * d)) / (2 * h) for h in hs}
+            rich = (4 * fd[hs[1]] - fd[hs[0]]) / 3
+            a64, a32 = float(np.sum(Qb64 * d)), float(np.sum(Qb32 * d))
+            out[param] = {"richardson_fd": rich, "fp64_adjoint": a64, "mixed_adjoint": a32,
+                          "fp64_rel_diff": abs(a64 - rich) / abs(rich), "mixed_rel_diff": abs(a32 - rich) / abs(rich)}
+    return out
 
 
 def run_accuracy(a, local):

@@ -318,7 +318,15 @@ int step_vjp_mixed(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doub
   GCFD_CUDA(c, cudaMemsetAsync(c->adjS, 0, sizeof(double) * 12, c->stream));
   GCFD_CUDA(c, cudaMemcpyAsync(c->adjS + 10, &tfinal_bar, sizeof(double), cudaMemcpyHostToDevice, c->stream));
   const int every = c->winEvery, nsteps = c->winSteps;
-  const int nseg = (nsteps + every - 1) / every;
+  const int nseg = c->winTaped ? 0 : (nsteps + every - 1) / every;
+  if (c->winTaped) {  // the recording kept every step's tape: reverse only
+    for (int i = nsteps - 1; i >= 0; --i) {
+      bind_slot(c, i + 1);
+      o.mixed_reverse_taped(c, reinterpret_cast<const float*>(c->segQ + S * i));
+      GCFD_CUDA(c, cudaGetLastError());
+    }
+    bind_slot(c, 0);
+  }
   // The compensated state (hi, lo) at the start of step i of a segment: the
   // reverse sweep evaluates the stage states as hi + D_s in FP32.
   auto save_pair = [&](float* dst) -> int {
@@ -488,11 +496,32 @@ int gcfd_record_steps(gcfd_ctx* c, int32_t nsteps, int32_t every, double* time, 
   double* sc = nullptr;
   if ((rc = win_alloc(c, &sc, (sizeof(Scalars) + 7) / 8))) return rc;
   c->endSc = reinterpret_cast<Scalars*>(sc);
-  // The segment tape (one slot per step of a segment) when it fits; without
-  // it every step of a segment is recomputed twice in the reverse sweep.
-  if (every > 1) alloc_slots(c, std::min(every, nsteps));
+  // Mixed path, one segment for the whole window (every >= nsteps): when a
+  // tape slot per step fits in device memory the recording itself keeps every
+  // step's tape (slots 1..nsteps; slot 0, the context's own arrays, stays free
+  // for gcfd_step) and the reverse sweep recomputes nothing.
+  c->winTaped = c->fp32 && every >= nsteps && alloc_slots(c, nsteps + 1);
+  // Otherwise the segment tape (one slot per step of a segment) when it fits;
+  // without it every step of a segment is recomputed twice in the reverse sweep.
+  if (!c->winTaped && every > 1) alloc_slots(c, std::min(every, nsteps));
   if ((rc = prepare_if_dirty(c))) return rc;
-  for (int n = 0; n < nsteps; ++n) {
+  if (c->winTaped) {
+    if ((rc = sync_fp64_state(c))) return rc;
+    GCFD_CUDA(c, cudaMemcpyAsync(c->ckpt, c->Q[0], S * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    GCFD_CUDA(c, cudaMemcpyAsync(c->ckptT, &c->sc->time, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    const OrderOps& fo = *order_ops(c->N);
+    for (int n = 0; n < nsteps; ++n) {
+      float* pr = reinterpret_cast<float*>(c->segQ + S * n);  // the step's starting (hi, lo)
+      GCFD_CUDA(c, cudaMemcpyAsync(pr, c->Qhi, S * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+      GCFD_CUDA(c, cudaMemcpyAsync(pr + S, c->Qlo, S * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+      bind_slot(c, n + 1);
+      fo.mixed_tape(c);
+      GCFD_CUDA(c, cudaGetLastError());
+    }
+    bind_slot(c, 0);
+    c->fp64Stale = true;
+  }
+  for (int n = 0; n < (c->winTaped ? 0 : nsteps); ++n) {
     if (n % every == 0) {
       const int j = n / every;
       if ((rc = sync_fp64_state(c))) return rc;  // mixed path: the checkpoint is hi + lo in FP64
