@@ -229,7 +229,10 @@ int gcfd_rhs_vjp(gcfd_ctx* ctx, double time, int32_t nshards, const int32_t* Kma
  * checkpoint_every steps for a following gcfd_step_vjp (memory: the
  * checkpoints plus checkpoint_every states, FP64; plus, when it fits, a tape
  * slot per step of a segment).  A mixed-precision context checkpoints its
- * compensated state as hi + lo in FP64, which restores it exactly. */
+ * compensated state as hi + lo in FP64, which restores it exactly; with
+ * checkpoint_every >= nsteps it keeps every step's tape while recording when a
+ * slot per step fits in device memory (9 FP32 state copies per step), and
+ * gcfd_step_vjp then recomputes nothing. */
 int gcfd_record_steps(gcfd_ctx* ctx, int32_t nsteps, int32_t checkpoint_every, double* time, double* dt_last);
 
 /* Adjoint of the recorded window (RungeKutta5SSP.Step x nsteps, euler.go:408-418):
