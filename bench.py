@@ -432,7 +432,9 @@ def run_ours(a, world, rank, local):
                 t0 = time.perf_counter()
                 sa.step_vjp(qbar)
                 return (time.perf_counter() - t0) * 1e3
-            n1 = max(every, a.adj_steps // 2)
+            # windows of two segments or more, so both are checkpointed (a window of one
+            # segment is taped while recording: the third leg below)
+            n1 = max(2 * every, a.adj_steps // 2)
             n2 = n1 + max(every, a.adj_steps)
             n1, n2 = every * ((n1 + every - 1) // every), every * ((n2 + every - 1) // every)
             t1, t2 = sweep(n1), sweep(n2)
@@ -448,8 +450,10 @@ def run_ours(a, world, rank, local):
                 sa.record(n, n)
                 torch.cuda.synchronize()
                 t1 = time.perf_counter()
+                tapedOK.append(sa.window_taped())
                 sa.step_vjp(qbar)
                 return (t1 - t0) * 1e3, (time.perf_counter() - t1) * 1e3
+            tapedOK = []
             taped(2)
             n1 = max(10, a.adj_steps // 2)
             n2 = n1 + max(10, a.adj_steps)
@@ -459,6 +463,7 @@ def run_ours(a, world, rank, local):
             legs["taped"] = {"ms_per_step": vjp_ms, "record_extra_ms_per_step": rec_extra,
                              "ratio": (vjp_ms + max(rec_extra, 0.0)) / fwd_ms,
                              "window_ms": {str(n1): [r1, v1], str(n2): [r2, v2]},
+                             "taped": all(tapedOK),
                              "note": "ratio = (reverse per step + taping's extra per recorded step) / forward"}
         sa.close()
         return {"ms_per_step": legs[10]["ms_per_step"], "forward_ms_per_step": fwd_ms,

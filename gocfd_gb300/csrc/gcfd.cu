@@ -684,6 +684,10 @@ int gcfd_set_option(gcfd_ctx* c, int32_t option, int32_t value) {
 
 int gcfd_get_option(const gcfd_ctx* c, int32_t option, int32_t* value) {
   if (!c || !value) return GCFD_ERR_ARG;
+  if (option == GCFD_OPT_WINDOW_TAPED) {
+    *value = (c->winSteps > 0 && c->winTaped) ? 1 : 0;
+    return GCFD_OK;
+  }
   if (option != GCFD_OPT_STAGE_PIPELINE) return GCFD_ERR_ARG;
   *value = (c->fp32 && c->pipe && c->pipeOn) ? 1 : 0;
   return GCFD_OK;

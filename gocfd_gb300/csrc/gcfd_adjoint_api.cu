@@ -496,16 +496,30 @@ int gcfd_record_steps(gcfd_ctx* c, int32_t nsteps, int32_t every, double* time, 
   double* sc = nullptr;
   if ((rc = win_alloc(c, &sc, (sizeof(Scalars) + 7) / 8))) return rc;
   c->endSc = reinterpret_cast<Scalars*>(sc);
-  // Mixed path, one segment for the whole window (every >= nsteps): when a
-  // tape slot per step fits in device memory the recording itself keeps every
-  // step's tape (slots 1..nsteps; slot 0, the context's own arrays, stays free
-  // for gcfd_step) and the reverse sweep recomputes nothing.
-  c->winTaped = c->fp32 && every >= nsteps && alloc_slots(c, nsteps + 1);
+  // One segment for the whole window (every >= nsteps): when a tape slot per
+  // step fits in device memory the recording itself keeps every step's tape
+  // (slots 1..nsteps; slot 0, the context's own arrays, stays free for
+  // gcfd_step) and the reverse sweep recomputes nothing.
+  c->winTaped = every >= nsteps && alloc_slots(c, nsteps + 1);
   // Otherwise the segment tape (one slot per step of a segment) when it fits;
   // without it every step of a segment is recomputed twice in the reverse sweep.
   if (!c->winTaped && every > 1) alloc_slots(c, std::min(every, nsteps));
   if ((rc = prepare_if_dirty(c))) return rc;
-  if (c->winTaped) {
+  if (c->winTaped && !c->fp32) {  // FP64: the step's starting state and time, then the taped step
+    GCFD_CUDA(c, cudaMemcpyAsync(c->ckpt, c->Q[0], S * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    GCFD_CUDA(c, cudaMemcpyAsync(c->ckptT, &c->sc->time, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    if (c->diss)
+      GCFD_CUDA(c, cudaMemcpyAsync(c->ckptV, c->DTVisc, KV * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    const AdjOps& ao = *adj_ops(c->N);
+    for (int n = 0; n < nsteps; ++n) {
+      GCFD_CUDA(c, cudaMemcpyAsync(c->segQ + S * n, c->Q[0], S * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   c->stream));
+      bind_slot(c, n + 1);
+      ao.tape_step(c);
+      GCFD_CUDA(c, cudaGetLastError());
+    }
+    bind_slot(c, 0);
+  } else if (c->winTaped) {
     if ((rc = sync_fp64_state(c))) return rc;
     GCFD_CUDA(c, cudaMemcpyAsync(c->ckpt, c->Q[0], S * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     GCFD_CUDA(c, cudaMemcpyAsync(c->ckptT, &c->sc->time, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
@@ -568,7 +582,17 @@ int gcfd_step_vjp(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doubl
   const size_t KV = c->diss ? static_cast<size_t>(c->K) : 0;
   if (c->diss) GCFD_CUDA(c, cudaMemsetAsync(c->carryV, 0, KV * sizeof(double), c->stream));
   const int every = c->winEvery, nsteps = c->winSteps;
-  const int nseg = (nsteps + every - 1) / every;
+  const int nseg = c->winTaped ? 0 : (nsteps + every - 1) / every;
+  if (c->winTaped) {  // the recording kept every step's tape: reverse only, faces rebuilt from the stage states
+    c->facesFromState = true;
+    for (int i = nsteps - 1; i >= 0; --i) {
+      bind_slot(c, i + 1);
+      o.reverse_taped(c, c->segQ + S * i);
+      GCFD_CUDA(c, cudaGetLastError());
+    }
+    c->facesFromState = false;
+    bind_slot(c, 0);
+  }
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int n0 = seg * every, m = std::min(every, nsteps - n0);
     GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], c->ckpt + S * seg, SB, cudaMemcpyDeviceToDevice, c->stream));

@@ -123,7 +123,7 @@ struct gcfd_ctx {
   double *RbE = nullptr, *vsBar = nullptr;
   int *sigArg = nullptr, *epsArg = nullptr, *argVisc = nullptr;
   int winSteps = 0, winEvery = 1;
-  bool winTaped = false;  // mixed path: the recording kept every step's tape (slots 1..winSteps)
+  bool winTaped = false;  // the recording kept every step's tape (slots 1..winSteps)
   std::vector<void*> winAllocs;
   // Segment tape: one slot per step of a checkpoint segment, so each step of
   // the segment is recomputed once with its tape kept (slot 0 is the

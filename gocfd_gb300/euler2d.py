@@ -458,6 +458,15 @@ class Euler:
         _lib.check(self.lib, self.ctx, self.lib.gcfd_get_option(self.ctx, self.OPT_STAGE_PIPELINE, C.byref(v)))
         return bool(v.value)
 
+    # GCFD_OPT_WINDOW_TAPED of gcfd.h (read only)
+    OPT_WINDOW_TAPED = 2
+
+    def window_taped(self) -> bool:
+        """True when the last record() kept every step's tape (checkpoint_every >= nsteps, and it fitted)."""
+        v = C.c_int32()
+        _lib.check(self.lib, self.ctx, self.lib.gcfd_get_option(self.ctx, self.OPT_WINDOW_TAPED, C.byref(v)))
+        return bool(v.value)
+
 
 def parse_yaml_file(path: str) -> InputParameters2D:
     """The reference's input-file reader (InputParameters2D.Parse of a YAML file)."""

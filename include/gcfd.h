@@ -163,8 +163,12 @@ int gcfd_get_stream(gcfd_ctx* ctx, void** stream);
  * persistent kernel whose element inputs are double-buffered by TMA copies
  * (used when K % 4 == 0); 0 (the default) keeps the one-block-per-CTA kernel.
  * Setting an option records the per-step CUDA graph again.  Reading
- * GCFD_OPT_STAGE_PIPELINE gives 1 only while the pipelined kernel runs. */
+ * GCFD_OPT_STAGE_PIPELINE gives 1 only while the pipelined kernel runs.
+ * GCFD_OPT_WINDOW_TAPED (read only): 1 when the last gcfd_record_steps kept
+ * every step's tape while recording (checkpoint_every >= nsteps and the tape
+ * fitted in device memory), so gcfd_step_vjp recomputes nothing. */
 #define GCFD_OPT_STAGE_PIPELINE 1
+#define GCFD_OPT_WINDOW_TAPED 2
 int gcfd_set_option(gcfd_ctx* ctx, int32_t option, int32_t value);
 int gcfd_get_option(const gcfd_ctx* ctx, int32_t option, int32_t* value);
 

@@ -434,6 +434,8 @@ def test_segment_tape_matches_per_step_recompute(limiter, local_dt):
             Q0 = np.ascontiguousarray(Q0 * (1.0 + 0.003 * np.random.default_rng(40).uniform(-1, 1, Q0.shape)))
             gpu.set_global_state(Q0)
             gpu.record(7, every)
+            # every = 7 covers the window: it is taped while recording, nothing recomputed
+            assert gpu.window_taped() == (every == 7)
             Qbf = np.random.default_rng(42).standard_normal(Q0.shape)
             out.append(gpu.step_vjp(Qbf, 0.3))
             # a second reverse sweep of the same window gives the same adjoint

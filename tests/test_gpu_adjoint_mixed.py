@@ -266,6 +266,7 @@ def test_mixed_window_taped_while_recording():
         g.set_global_state(Q0)
         g.time = t0
         g.record(nsteps, nsteps)
+        assert g.window_taped()
         a1 = g.step_vjp(Qbf)[0]
         g.step(3)
         a2 = g.step_vjp(Qbf)[0]
