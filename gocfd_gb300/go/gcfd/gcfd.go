@@ -184,6 +184,15 @@ func (c *Context) SetStagePipeline(on bool) error {
 	return status(c.ctx, C.gcfd_set_option(c.ctx, C.GCFD_OPT_STAGE_PIPELINE, v))
 }
 
+// WindowTaped reports whether the last Forward (gcfd_record_steps) kept every
+// step's tape while recording, so Backward recomputes nothing
+// (GCFD_OPT_WINDOW_TAPED of gcfd.h).
+func (c *Context) WindowTaped() (bool, error) {
+	var v C.int32_t
+	err := status(c.ctx, C.gcfd_get_option(c.ctx, C.GCFD_OPT_WINDOW_TAPED, &v))
+	return v != 0, err
+}
+
 // RHS evaluates the right-hand side of Q at BC time t into RHS (same shards).
 func (c *Context) RHS(t float64, Q, RHS [][4][]float64, Kmax []int) error {
 	var pin runtime.Pinner
