@@ -327,14 +327,10 @@ int step_vjp_mixed(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doub
     }
     bind_slot(c, 0);
   }
-  // The compensated state (hi, lo) at the start of step i of a segment: the
-  // reverse sweep evaluates the stage states as hi + D_s in FP32.
-  auto save_pair = [&](float* dst) -> int {
-    GCFD_CUDA(c, cudaMemcpyAsync(dst, c->Qhi, S * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
-    GCFD_CUDA(c, cudaMemcpyAsync(dst + S, c->Qlo, S * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
-    return GCFD_OK;
-  };
-  float* pairTmp = reinterpret_cast<float*>(c->Qtmp);  // S doubles of room = one (hi, lo) pair
+  // The hi part of the compensated state at the start of each taped step (the
+  // reverse sweep evaluates the stage states as hi + D_s in FP32) is written by
+  // the step's stage-4 kernel into c->tapeQ0hi.
+  float* hiTmp = reinterpret_cast<float*>(c->Qtmp);  // S doubles of room
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int n0 = seg * every, m = std::min(every, nsteps - n0);
     GCFD_CUDA(c, cudaMemcpyAsync(c->Q[0], c->ckpt + S * seg, SB, cudaMemcpyDeviceToDevice, c->stream));
@@ -346,12 +342,12 @@ int step_vjp_mixed(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doub
       // segment tape: each step recomputed once with its tape in its own slot,
       // segQ entry i holding the step's starting (hi, lo)
       for (int i = 0; i < m; ++i) {
-        float* pr = reinterpret_cast<float*>(c->segQ + S * i);
-        if ((rc = save_pair(pr))) return rc;
+        c->tapeQ0hi = reinterpret_cast<float*>(c->segQ + S * i);
         bind_slot(c, i);
         fo.mixed_tape(c);
         GCFD_CUDA(c, cudaGetLastError());
       }
+      c->tapeQ0hi = nullptr;
       for (int i = m - 1; i >= 0; --i) {
         bind_slot(c, i);
         o.mixed_reverse_taped(c, reinterpret_cast<const float*>(c->segQ + S * i));
@@ -383,10 +379,11 @@ int step_vjp_mixed(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doub
         c->fp64Stale = false;
         fwd.prep(c);
       }
-      if ((rc = save_pair(pairTmp))) return rc;
+      c->tapeQ0hi = hiTmp;
       fo.mixed_tape(c);
+      c->tapeQ0hi = nullptr;
       c->fp64Stale = true;
-      o.mixed_reverse_taped(c, pairTmp);
+      o.mixed_reverse_taped(c, hiTmp);
       GCFD_CUDA(c, cudaGetLastError());
     }
   }
@@ -525,13 +522,12 @@ int gcfd_record_steps(gcfd_ctx* c, int32_t nsteps, int32_t every, double* time, 
     GCFD_CUDA(c, cudaMemcpyAsync(c->ckptT, &c->sc->time, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     const OrderOps& fo = *order_ops(c->N);
     for (int n = 0; n < nsteps; ++n) {
-      float* pr = reinterpret_cast<float*>(c->segQ + S * n);  // the step's starting (hi, lo)
-      GCFD_CUDA(c, cudaMemcpyAsync(pr, c->Qhi, S * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
-      GCFD_CUDA(c, cudaMemcpyAsync(pr + S, c->Qlo, S * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+      c->tapeQ0hi = reinterpret_cast<float*>(c->segQ + S * n);  // the step's starting hi
       bind_slot(c, n + 1);
       fo.mixed_tape(c);
       GCFD_CUDA(c, cudaGetLastError());
     }
+    c->tapeQ0hi = nullptr;
     bind_slot(c, 0);
     c->fp64Stale = true;
   }

@@ -112,6 +112,7 @@ struct gcfd_ctx {
   float* Qb32[5] = {};
   float *Qbf32 = nullptr, *Rb3_32 = nullptr, *QF32 = nullptr, *QFb32 = nullptr, *FEb32 = nullptr;
   bool adjFacesPending = false;  // QFb32 holds stage-0 face adjoints not yet in Qbf32
+  float* tapeQ0hi = nullptr;     // where the next taped step writes its starting Qhi
   double *dXs = nullptr, *dYs = nullptr, *edgeW = nullptr;
   // adjoint of the dissipation
   double* tapeQ2pre = nullptr;

@@ -286,6 +286,7 @@ struct MixedLaunch {
     a.err = reinterpret_cast<unsigned int*>(&c->sc->errFlags);
     a.rhsOnly = 0;
     a.tapeRHS = nullptr;
+    a.tapeQ0 = nullptr;
     a.gviscS = nullptr;
     a.cdiff = 0.0;
     return a;
@@ -425,9 +426,10 @@ struct MixedLaunch {
     k_mixed_diss_update<N><<<gridE(c), 128, 0, c->stream>>>(m2, L::update_args(c, s, Qs64));
   }
   // One step with the adjoint tape: the launches of step() (so the stage
-  // increments Dk are those of the recorded trajectory), plus the stage RHS
-  // written by the stage kernel, per-stage copies of the edge speeds and local
-  // dt, and the scalars before (BC time) and after (per-stage gmax and dt).
+  // increments Dk are those of the recorded trajectory), plus the stage RHS and
+  // the step's starting Qhi (c->tapeQ0hi) written by the stage kernel, per-stage
+  // copies of the edge speeds and local dt, and the scalars before (BC time)
+  // and after (per-stage gmax and dt).
   static void tape_step(gcfd_ctx* c) {
     cudaMemcpyAsync(c->tapeSc0, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream);
     k_step_begin<<<1, 32, 0, c->stream>>>(c->sc);
@@ -437,6 +439,7 @@ struct MixedLaunch {
                       c->stream);
       MixedArgs a = args(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]);
       a.tapeRHS = c->tapeRHS32[s];
+      if (s == 4) a.tapeQ0 = c->tapeQ0hi;  // the step's starting hi, read by stage 4 anyway
       stage_kernel(c, a);
       if (c->prm.local_time_stepping)
         cudaMemcpyAsync(c->tapeDT[s], c->DT, sizeof(double) * c->K, cudaMemcpyDeviceToDevice, c->stream);

@@ -310,6 +310,7 @@ struct MixedArgs {
   const float* VF32;
   unsigned int* err;          // error flags (bit 0: a tensor-core wait ran out)
   float* tapeRHS;             // adjoint tape: the stage's RHS [n][i][k] (nullptr: not taped)
+  float* tapeQ0;              // adjoint tape, stage 4: the step's starting Qhi [n][i][k] (nullptr: not taped)
 };
 
 // SSP(5,4) weights of rkAdvance (euler.go:511-564) in increment form:
@@ -881,6 +882,7 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const int eslot[3
                           kSspR3 * (dt * a.R3[off + r * sK]) + kSspC4 * (dt * rhs[r]);
         qh[r] = a.Qhi[off + r * sK];
         ql[r] = a.Qlo[off + r * sK];
+        if (a.tapeQ0) a.tapeQ0[off + r * sK] = qh[r];
         df_add(qh[r], ql[r], inc);
         a.Qhi[off + r * sK] = qh[r];
         a.Qlo[off + r * sK] = ql[r];
