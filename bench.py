@@ -422,16 +422,23 @@ def run_ours(a, world, rank, local):
         fwd_ms = f0.elapsed_time(f1) / a.adj_steps
         qbar = np.ones((4, Np, K))
         legs = {}
+        # the window's fixed costs (host copies of the adjoint in and out) vary by a
+        # few ms from call to call: the mixed path's short reverse steps take the
+        # best of two calls per window length
+        reps = 1 if precision == "fp64" else 2
         for every in (10, 1):
             sa.record(2 * every if every > 1 else 2, every)
             sa.step_vjp(qbar)  # warm-up (allocations, first launches)
 
             def sweep(n):
-                sa.record(n, every)
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                sa.step_vjp(qbar)
-                return (time.perf_counter() - t0) * 1e3
+                best = float("inf")
+                for _ in range(reps):
+                    sa.record(n, every)
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    sa.step_vjp(qbar)
+                    best = min(best, (time.perf_counter() - t0) * 1e3)
+                return best
             # windows of two segments or more, so both are checkpointed (a window of one
             # segment is taped while recording: the third leg below)
             n1 = max(2 * every, a.adj_steps // 2)
@@ -444,27 +451,34 @@ def run_ours(a, world, rank, local):
             # the whole window taped while recording (checkpoint_every >= nsteps,
             # when a tape slot per step fits): the reverse sweep recomputes nothing;
             # the cost is the reverse plus the taping's extra over the plain forward
-            def taped(n):
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                sa.record(n, n)
-                torch.cuda.synchronize()
-                t1 = time.perf_counter()
-                tapedOK.append(sa.window_taped())
-                sa.step_vjp(qbar)
-                return (t1 - t0) * 1e3, (time.perf_counter() - t1) * 1e3
+            def taped(n, reps=1):
+                r = v = float("inf")
+                for _ in range(reps):
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    sa.record(n, n)
+                    torch.cuda.synchronize()
+                    t1 = time.perf_counter()
+                    tapedOK.append(sa.window_taped())
+                    sa.step_vjp(qbar)
+                    r, v = min(r, (t1 - t0) * 1e3), min(v, (time.perf_counter() - t1) * 1e3)
+                return r, v
             tapedOK = []
-            taped(2)
             n1 = max(10, a.adj_steps // 2)
             n2 = n1 + max(10, a.adj_steps)
-            (r1, v1), (r2, v2) = taped(n1), taped(n2)
+            # the first window of n2 steps allocates its tape slots (a window's device
+            # blocks are kept for the next window); the timed windows reuse them
+            r0, _ = taped(n2)
+            (r1, v1), (r2, v2) = taped(n1, reps), taped(n2, reps)
             vjp_ms = (v2 - v1) / (n2 - n1)
             rec_extra = (r2 - r1) / (n2 - n1) - fwd_ms
             legs["taped"] = {"ms_per_step": vjp_ms, "record_extra_ms_per_step": rec_extra,
                              "ratio": (vjp_ms + max(rec_extra, 0.0)) / fwd_ms,
                              "window_ms": {str(n1): [r1, v1], str(n2): [r2, v2]},
+                             "first_record_ms": {str(n2): r0},
                              "taped": all(tapedOK),
-                             "note": "ratio = (reverse per step + taping's extra per recorded step) / forward"}
+                             "note": "ratio = (reverse per step + taping's extra per recorded step) / forward; "
+                                     "first_record_ms: the first window's recording, which allocates its tape"}
         sa.close()
         return {"ms_per_step": legs[10]["ms_per_step"], "forward_ms_per_step": fwd_ms,
                 "ratio": legs[10]["ratio"], "checkpoint_every": 10, "path": precision,

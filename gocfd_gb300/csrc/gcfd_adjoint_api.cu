@@ -147,13 +147,48 @@ int adj_init(gcfd_ctx* c) {
   return GCFD_OK;
 }
 
+// Device blocks of adjoint windows.  gcfd_record_steps hands the previous
+// window's blocks to c->winPool, and each request of the new window takes a
+// pooled block of the same size first: repeated windows of one shape (an
+// optimisation loop) allocate nothing after the first.  A cudaMalloc that
+// fails frees the pool and is tried once more; gcfd_destroy frees everything.
+void release_pool(gcfd_ctx* c) {
+  for (auto& b : c->winPool) cudaFree(b.first);
+  c->winPool.clear();
+}
+
+void* win_block(gcfd_ctx* c, size_t bytes) {
+  for (size_t i = 0; i < c->winPool.size(); ++i)
+    if (c->winPool[i].second == bytes) {
+      void* p = c->winPool[i].first;
+      c->winPool.erase(c->winPool.begin() + static_cast<std::ptrdiff_t>(i));
+      c->winAllocs.emplace_back(p, bytes);
+      return p;
+    }
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    release_pool(c);
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+  }
+  c->winAllocs.emplace_back(p, bytes);
+  return p;
+}
+
+// Frees blocks of the current window taken since its first `keep` blocks.
+void drop_blocks(gcfd_ctx* c, size_t keep) {
+  while (c->winAllocs.size() > keep) {
+    cudaFree(c->winAllocs.back().first);
+    c->winAllocs.pop_back();
+  }
+}
+
 int win_alloc(gcfd_ctx* c, double** p, size_t count) {
-  void* q = nullptr;
-  cudaError_t e = cudaMalloc(&q, count * sizeof(double) > 0 ? count * sizeof(double) : 16);
-  if (e != cudaSuccess)
-    return fail(c, e == cudaErrorMemoryAllocation ? GCFD_ERR_OOM : GCFD_ERR_CUDA,
-                std::string("cudaMalloc (adjoint window): ") + cudaGetErrorString(e));
-  c->winAllocs.push_back(q);
+  void* q = win_block(c, count * sizeof(double) > 0 ? count * sizeof(double) : 16);
+  if (!q) return fail(c, GCFD_ERR_OOM, "cudaMalloc (adjoint window): out of memory");
   *p = static_cast<double*>(q);
   return GCFD_OK;
 }
@@ -187,12 +222,13 @@ void bind_slot(gcfd_ctx* c, int i) {
 }
 
 // Slot 0 is the context's own stage arrays and tape; slots 1.. are allocated
-// per window (they go with the window's allocations).  Returns false, with
-// nothing kept, when they do not fit in device memory.
-bool alloc_slots_mixed(gcfd_ctx* c, int nslots);
+// per window (they go with the window's allocations; withQ0: each also keeps
+// its step's starting state, for a window taped while recording).  Returns
+// false, with nothing kept, when they do not fit in device memory.
+bool alloc_slots_mixed(gcfd_ctx* c, int nslots, bool withQ0);
 
-bool alloc_slots(gcfd_ctx* c, int nslots) {
-  if (c->fp32) return alloc_slots_mixed(c, nslots);
+bool alloc_slots(gcfd_ctx* c, int nslots, bool withQ0) {
+  if (c->fp32) return alloc_slots_mixed(c, nslots, withQ0);
   c->slots.clear();
   gcfd_ctx::TapeSlot base{};
   for (int s = 0; s < 5; ++s) {
@@ -210,17 +246,15 @@ bool alloc_slots(gcfd_ctx* c, int nslots) {
   c->slots.push_back(base);
   const size_t S = static_cast<size_t>(4) * c->Np * c->K, K = c->K, nE = c->nInt + c->nBC;
   const size_t per = 9 * S + 5 * (nE + K) + 2 * ((sizeof(Scalars) + 7) / 8) +
-                     (c->diss ? S + 5 * (K + nE + S) : 0);
-  std::vector<void*> got;
+                     (c->diss ? S + 5 * (K + nE + S) : 0) + (withQ0 ? S : 0);
+  const size_t keep = c->winAllocs.size();
   for (int i = 1; i < nslots; ++i) {
-    void* p = nullptr;
-    if (cudaMalloc(&p, per * sizeof(double)) != cudaSuccess) {
-      cudaGetLastError();
-      for (void* q : got) cudaFree(q);
+    void* p = win_block(c, per * sizeof(double));
+    if (!p) {
+      drop_blocks(c, keep);
       c->slots.resize(1);
       return false;
     }
-    got.push_back(p);
     double* d = static_cast<double*>(p);
     gcfd_ctx::TapeSlot t{};
     auto take = [&](size_t n) {
@@ -236,6 +270,7 @@ bool alloc_slots(gcfd_ctx* c, int nslots) {
     }
     t.sc0 = reinterpret_cast<Scalars*>(take((sizeof(Scalars) + 7) / 8));
     t.sc = reinterpret_cast<Scalars*>(take((sizeof(Scalars) + 7) / 8));
+    if (withQ0) t.q0 = take(S);
     if (c->diss) {
       t.q2pre = take(S);
       for (int s = 0; s < 5; ++s) {
@@ -246,13 +281,12 @@ bool alloc_slots(gcfd_ctx* c, int nslots) {
     }
     c->slots.push_back(t);
   }
-  for (void* q : got) c->winAllocs.push_back(q);
   return true;
 }
 
 // The mixed path's slots: the stage increments D1..D4 and stage RHS in FP32,
 // edge speeds, local dt and scalars as on the FP64 path.
-bool alloc_slots_mixed(gcfd_ctx* c, int nslots) {
+bool alloc_slots_mixed(gcfd_ctx* c, int nslots, bool withQ0) {
   c->slots.clear();
   gcfd_ctx::TapeSlot base{};
   for (int s = 0; s < 5; ++s) {
@@ -268,17 +302,15 @@ bool alloc_slots_mixed(gcfd_ctx* c, int nslots) {
   auto rup = [](size_t b) { return (b + 255) & ~static_cast<size_t>(255); };
   const size_t bS = rup(S * sizeof(float)), bE = rup(nE * sizeof(double)), bK = rup(K * sizeof(double));
   const size_t bSc = rup(sizeof(Scalars));
-  const size_t per = 9 * bS + 5 * (bE + bK) + 2 * bSc;
-  std::vector<void*> got;
+  const size_t per = 9 * bS + 5 * (bE + bK) + 2 * bSc + (withQ0 ? bS : 0);
+  const size_t keep = c->winAllocs.size();
   for (int i = 1; i < nslots; ++i) {
-    void* p = nullptr;
-    if (cudaMalloc(&p, per) != cudaSuccess) {
-      cudaGetLastError();
-      for (void* q : got) cudaFree(q);
+    void* p = win_block(c, per);
+    if (!p) {
+      drop_blocks(c, keep);
       c->slots.resize(1);
       return false;
     }
-    got.push_back(p);
     char* d = static_cast<char*>(p);
     auto take = [&](size_t n) {
       char* r = d;
@@ -294,9 +326,9 @@ bool alloc_slots_mixed(gcfd_ctx* c, int nslots) {
     }
     t.sc0 = reinterpret_cast<Scalars*>(take(bSc));
     t.sc = reinterpret_cast<Scalars*>(take(bSc));
+    if (withQ0) t.q0hi = reinterpret_cast<float*>(take(bS));
     c->slots.push_back(t);
   }
-  for (void* q : got) c->winAllocs.push_back(q);
   return true;
 }
 
@@ -322,7 +354,7 @@ int step_vjp_mixed(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doub
   if (c->winTaped) {  // the recording kept every step's tape: reverse only
     for (int i = nsteps - 1; i >= 0; --i) {
       bind_slot(c, i + 1);
-      o.mixed_reverse_taped(c, reinterpret_cast<const float*>(c->segQ + S * i));
+      o.mixed_reverse_taped(c, c->slots[i + 1].q0hi);
       GCFD_CUDA(c, cudaGetLastError());
     }
     bind_slot(c, 0);
@@ -340,7 +372,7 @@ int step_vjp_mixed(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doub
     fwd.prep(c);
     if (m > 1 && static_cast<int>(c->slots.size()) >= m) {
       // segment tape: each step recomputed once with its tape in its own slot,
-      // segQ entry i holding the step's starting (hi, lo)
+      // segQ entry i receiving the step's starting hi from its stage-4 kernel
       for (int i = 0; i < m; ++i) {
         c->tapeQ0hi = reinterpret_cast<float*>(c->segQ + S * i);
         bind_slot(c, i);
@@ -359,8 +391,8 @@ int step_vjp_mixed(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doub
     }
     // without it: the segment's steps once through the graph, keeping each
     // step's starting state in FP64 (segQ), then per step in reverse order the
-    // state restored and prepared (the last step's is current already), its
-    // (hi, lo) kept, one taped step and its reverse
+    // state restored and prepared (the last step's is current already), one
+    // taped step (its starting hi into hiTmp) and its reverse
     for (int i = 0; i < m; ++i) {
       if ((rc = sync_fp64_state(c))) return rc;
       GCFD_CUDA(c, cudaMemcpyAsync(c->segQ + S * i, c->Q[0], SB, cudaMemcpyDeviceToDevice, c->stream));
@@ -474,15 +506,14 @@ int gcfd_record_steps(gcfd_ctx* c, int32_t nsteps, int32_t every, double* time, 
   GCFD_CUDA(c, cudaStreamSynchronize(c->stream));
   if (!c->slots.empty()) bind_slot(c, 0);
   c->slots.clear();
-  for (void* p : c->winAllocs) cudaFree(p);
+  c->winPool.insert(c->winPool.end(), c->winAllocs.begin(), c->winAllocs.end());
   c->winAllocs.clear();
+  c->segQ = c->segT = nullptr;
   c->winSteps = 0;
   const size_t S = static_cast<size_t>(4) * c->Np * c->K;
   const int nck = (nsteps + every - 1) / every;
   if ((rc = win_alloc(c, &c->ckpt, S * nck))) return rc;
   if ((rc = win_alloc(c, &c->ckptT, static_cast<size_t>(nck)))) return rc;
-  if ((rc = win_alloc(c, &c->segQ, S * std::min(every, nsteps)))) return rc;
-  if ((rc = win_alloc(c, &c->segT, static_cast<size_t>(std::min(every, nsteps))))) return rc;
   if ((rc = win_alloc(c, &c->endQ, S))) return rc;
   const size_t KV = c->diss ? static_cast<size_t>(c->K) : 0;  // DTVisc persists across steps
   if (c->diss) {
@@ -497,10 +528,14 @@ int gcfd_record_steps(gcfd_ctx* c, int32_t nsteps, int32_t every, double* time, 
   // step fits in device memory the recording itself keeps every step's tape
   // (slots 1..nsteps; slot 0, the context's own arrays, stays free for
   // gcfd_step) and the reverse sweep recomputes nothing.
-  c->winTaped = every >= nsteps && alloc_slots(c, nsteps + 1);
+  c->winTaped = every >= nsteps && alloc_slots(c, nsteps + 1, true);
+  if (!c->winTaped) {  // the segment's starting states, for the reverse sweep
+    if ((rc = win_alloc(c, &c->segQ, S * std::min(every, nsteps)))) return rc;
+    if ((rc = win_alloc(c, &c->segT, static_cast<size_t>(std::min(every, nsteps))))) return rc;
+  }
   // Otherwise the segment tape (one slot per step of a segment) when it fits;
   // without it every step of a segment is recomputed twice in the reverse sweep.
-  if (!c->winTaped && every > 1) alloc_slots(c, std::min(every, nsteps));
+  if (!c->winTaped && every > 1) alloc_slots(c, std::min(every, nsteps), false);
   if ((rc = prepare_if_dirty(c))) return rc;
   if (c->winTaped && !c->fp32) {  // FP64: the step's starting state and time, then the taped step
     GCFD_CUDA(c, cudaMemcpyAsync(c->ckpt, c->Q[0], S * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
@@ -509,7 +544,7 @@ int gcfd_record_steps(gcfd_ctx* c, int32_t nsteps, int32_t every, double* time, 
       GCFD_CUDA(c, cudaMemcpyAsync(c->ckptV, c->DTVisc, KV * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     const AdjOps& ao = *adj_ops(c->N);
     for (int n = 0; n < nsteps; ++n) {
-      GCFD_CUDA(c, cudaMemcpyAsync(c->segQ + S * n, c->Q[0], S * sizeof(double), cudaMemcpyDeviceToDevice,
+      GCFD_CUDA(c, cudaMemcpyAsync(c->slots[n + 1].q0, c->Q[0], S * sizeof(double), cudaMemcpyDeviceToDevice,
                                    c->stream));
       bind_slot(c, n + 1);
       ao.tape_step(c);
@@ -522,7 +557,7 @@ int gcfd_record_steps(gcfd_ctx* c, int32_t nsteps, int32_t every, double* time, 
     GCFD_CUDA(c, cudaMemcpyAsync(c->ckptT, &c->sc->time, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     const OrderOps& fo = *order_ops(c->N);
     for (int n = 0; n < nsteps; ++n) {
-      c->tapeQ0hi = reinterpret_cast<float*>(c->segQ + S * n);  // the step's starting hi
+      c->tapeQ0hi = c->slots[n + 1].q0hi;  // the step's starting hi, from its stage-4 kernel
       bind_slot(c, n + 1);
       fo.mixed_tape(c);
       GCFD_CUDA(c, cudaGetLastError());
@@ -583,7 +618,7 @@ int gcfd_step_vjp(gcfd_ctx* c, int32_t nshards, const int32_t* Kmax, const doubl
     c->facesFromState = true;
     for (int i = nsteps - 1; i >= 0; --i) {
       bind_slot(c, i + 1);
-      o.reverse_taped(c, c->segQ + S * i);
+      o.reverse_taped(c, c->slots[i + 1].q0);
       GCFD_CUDA(c, cudaGetLastError());
     }
     c->facesFromState = false;

@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/gcfd.h"
@@ -125,7 +126,9 @@ struct gcfd_ctx {
   int *sigArg = nullptr, *epsArg = nullptr, *argVisc = nullptr;
   int winSteps = 0, winEvery = 1;
   bool winTaped = false;  // the recording kept every step's tape (slots 1..winSteps)
-  std::vector<void*> winAllocs;
+  // device blocks of the current adjoint window, and those of earlier windows
+  // kept for reuse (pointer, bytes)
+  std::vector<std::pair<void*, size_t>> winAllocs, winPool;
   // Segment tape: one slot per step of a checkpoint segment, so each step of
   // the segment is recomputed once with its tape kept (slot 0 is the
   // context's own stage arrays and tape); empty when it did not fit.
@@ -136,6 +139,8 @@ struct gcfd_ctx {
     Scalars *sc0, *sc;
     float* D[5];       // mixed path: D[1..4] stage increments
     float* rhs32[5];   // mixed path: stage RHS
+    double* q0;        // window-taped slots, FP64 path: the step's starting state
+    float* q0hi;       // window-taped slots, mixed path: the step's starting hi
   };
   std::vector<TapeSlot> slots;
   bool facesFromState = false;  // reverse stages rebuild their faces (the segment tape keeps none)
@@ -162,7 +167,8 @@ struct gcfd_ctx {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
-    for (void* p : winAllocs) cudaFree(p);
+    for (auto& b : winAllocs) cudaFree(b.first);
+    for (auto& b : winPool) cudaFree(b.first);
     for (auto& e : evChunk)
       if (e) cudaEventDestroy(e);
     if (evFork) cudaEventDestroy(evFork);

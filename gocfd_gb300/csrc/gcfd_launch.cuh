@@ -427,16 +427,18 @@ struct MixedLaunch {
   }
   // One step with the adjoint tape: the launches of step() (so the stage
   // increments Dk are those of the recorded trajectory), plus the stage RHS and
-  // the step's starting Qhi (c->tapeQ0hi) written by the stage kernel, per-stage
-  // copies of the edge speeds and local dt, and the scalars before (BC time)
-  // and after (per-stage gmax and dt).
+  // the step's starting Qhi (c->tapeQ0hi) written by the stage kernel, the edge
+  // speeds written by the edge kernels straight into the tape (every edge's
+  // speed is written at every stage and read only within it), per-stage copies
+  // of the local dt, and the scalars before (BC time) and after (per-stage gmax
+  // and dt).
   static void tape_step(gcfd_ctx* c) {
+    double* const edgeSpeed = c->edgeSpeed;
     cudaMemcpyAsync(c->tapeSc0, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream);
     k_step_begin<<<1, 32, 0, c->stream>>>(c->sc);
     for (int s = 0; s < 5; ++s) {
+      c->edgeSpeed = c->tapeES[s];
       edges(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s], true);
-      cudaMemcpyAsync(c->tapeES[s], c->edgeSpeed, sizeof(double) * c->nEdges, cudaMemcpyDeviceToDevice,
-                      c->stream);
       MixedArgs a = args(c, s, c->Q[0], &c->sc->time, &c->sc->gmax[s]);
       a.tapeRHS = c->tapeRHS32[s];
       if (s == 4) a.tapeQ0 = c->tapeQ0hi;  // the step's starting hi, read by stage 4 anyway
@@ -444,6 +446,7 @@ struct MixedLaunch {
       if (c->prm.local_time_stepping)
         cudaMemcpyAsync(c->tapeDT[s], c->DT, sizeof(double) * c->K, cudaMemcpyDeviceToDevice, c->stream);
     }
+    c->edgeSpeed = edgeSpeed;
     k_resid_blocks<<<kResidBlocks, kResidBlockThreads, 0, c->stream>>>(c->sc, resid_units(c));
     k_step_end<<<1, kResidBlocks, 0, c->stream>>>(c->sc, c->prm.local_time_stepping);
     cudaMemcpyAsync(c->tapeSc, c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, c->stream);

@@ -235,8 +235,12 @@ int gcfd_rhs_vjp(gcfd_ctx* ctx, double time, int32_t nshards, const int32_t* Kma
  * slot per step of a segment).  A mixed-precision context checkpoints its
  * compensated state as hi + lo in FP64, which restores it exactly; with
  * checkpoint_every >= nsteps it keeps every step's tape while recording when a
- * slot per step fits in device memory (9 FP32 state copies per step), and
- * gcfd_step_vjp then recomputes nothing. */
+ * slot per step fits in device memory (10 FP32 state copies per step; 10 FP64
+ * ones on an FP64 context), and gcfd_step_vjp then recomputes nothing.  The
+ * window's device blocks are kept when the next window is recorded and reused
+ * where it asks for blocks of the same size (the same shape of window asks for
+ * the same blocks); what it does not reuse stays held until an allocation
+ * fails (then it is freed and the allocation tried again) or gcfd_destroy. */
 int gcfd_record_steps(gcfd_ctx* ctx, int32_t nsteps, int32_t checkpoint_every, double* time, double* dt_last);
 
 /* Adjoint of the recorded window (RungeKutta5SSP.Step x nsteps, euler.go:408-418):

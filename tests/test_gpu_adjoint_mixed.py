@@ -272,3 +272,27 @@ def test_mixed_window_taped_while_recording():
         a2 = g.step_vjp(Qbf)[0]
     assert np.array_equal(a1, a2)
     assert np.linalg.norm(a1 - res[nsteps][0]) == 0.0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_window_blocks_carried_to_the_next_window(precision):
+    """A window's device blocks go to the next window (blocks of the same size
+    reused, the rest held): a sequence of taped and checkpointed windows of
+    different lengths on one context gives each window the adjoint a fresh
+    context gives it, bit for bit."""
+    mesh = meshes.vortex_box(6, jitter=0.1)
+    N, t0 = 3, 0.1
+    ip = params(N, init="ivortex", cfl=0.5)
+    ora = oracle_for(mesh, N, init="ivortex", cfl=0.5)
+    Q0 = perturbed(ora.Q, 11, 0.01)
+    Qbf = np.random.default_rng(11).standard_normal(Q0.shape)
+    seq = [(8, 8), (4, 4), (8, 4), (8, 8), (6, 2), (4, 4)]
+    fresh = {w: window_adjoint(mesh, ip, precision, Q0, t0, w[0], w[1], Qbf)[0] for w in set(seq)}
+    with Euler(ip, mesh, 1, precision=precision, vortex_center=(5.0, 0.0)) as g:
+        for n, every in seq:
+            g.set_global_state(Q0)
+            g.time = t0
+            g.record(n, every)
+            assert g.window_taped() == (every >= n)
+            a = g.step_vjp(Qbf)[0]
+            assert np.array_equal(a, fresh[(n, every)]), (n, every)
