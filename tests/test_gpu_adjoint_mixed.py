@@ -279,7 +279,9 @@ def test_window_blocks_carried_to_the_next_window(precision):
     """A window's device blocks go to the next window (blocks of the same size
     reused, the rest held): a sequence of taped and checkpointed windows of
     different lengths on one context gives each window the adjoint a fresh
-    context gives it, bit for bit."""
+    context gives it — bit for bit on the mixed path; to 1e-13 relative on the
+    FP64 path, whose global-dt adjoint sums its warps' FP64 partials by atomics
+    (the order of those additions sets the last bits)."""
     mesh = meshes.vortex_box(6, jitter=0.1)
     N, t0 = 3, 0.1
     ip = params(N, init="ivortex", cfl=0.5)
@@ -295,4 +297,8 @@ def test_window_blocks_carried_to_the_next_window(precision):
             g.record(n, every)
             assert g.window_taped() == (every >= n)
             a = g.step_vjp(Qbf)[0]
-            assert np.array_equal(a, fresh[(n, every)]), (n, every)
+            ref = fresh[(n, every)]
+            if precision == "fp32":
+                assert np.array_equal(a, ref), (n, every)
+            else:
+                assert np.max(np.abs(a - ref)) <= 1e-13 * np.max(np.abs(ref)), (n, every)
