@@ -302,3 +302,38 @@ def test_window_blocks_carried_to_the_next_window(precision):
                 assert np.array_equal(a, ref), (n, every)
             else:
                 assert np.max(np.abs(a - ref)) <= 1e-13 * np.max(np.abs(ref)), (n, every)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_window_blocks_held_once_and_freed_with_the_context(precision):
+    """Repeated windows of one shape take no further device memory, and
+    gcfd_destroy frees the window's blocks with the pool."""
+    import torch
+    mesh = meshes.vortex_box(48, jitter=0.1)
+    ip = params(3, init="ivortex", cfl=0.5)
+    Qbf = None
+
+    def free():
+        torch.cuda.synchronize()
+        return torch.cuda.mem_get_info()[0]
+
+    def lifetime(windows):
+        nonlocal Qbf
+        with Euler(ip, mesh, 1, precision=precision, vortex_center=(0.0, 0.0)) as g:
+            if Qbf is None:
+                Qbf = np.random.default_rng(3).standard_normal(g.get_global_state().shape)
+            seen = []
+            for n, every in windows:
+                g.record(n, every)
+                g.step_vjp(Qbf)
+                seen.append(free())
+        return seen
+
+    lifetime([(6, 6), (6, 2)])  # first launches (lazy module loading), then the baseline
+    base = free()
+    seen = lifetime([(6, 6), (6, 6), (6, 6), (6, 2), (6, 6)])
+    slot = 10 * 4 * 10 * mesh.EToV.shape[0] * (4 if precision == "fp32" else 8)
+    assert base - seen[0] >= 6 * slot                    # the taped window is held
+    assert seen[1] == seen[0] and seen[2] == seen[0]     # the same shape again: nothing new
+    assert seen[4] >= seen[3] - 2 ** 21                  # back to the taped shape: from the pool
+    assert free() >= base - 2 ** 22                      # destroyed: all of it back
