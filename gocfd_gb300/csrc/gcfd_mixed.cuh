@@ -924,13 +924,13 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const int eslot[3
 // so all four warps of a CTA run the same instructions on different operands
 // (the exact algebra of delta_flux_c, regrouped).
 template <int N>
-__device__ __forceinline__ void interior_columns(int n, const BasePrim& b, const float (*sq0)[MixedDims<N>::NP][32],
-                                                 const float (*sds)[MixedDims<N>::NP][32],
-                                                 const float (*spr)[MixedDims<N>::NP][32], int lane, int s,
+__device__ __forceinline__ void interior_columns(int n, const BasePrim& b, const float (*sd)[MixedDims<N>::NP][32],
+                                                 const float (*spr)[MixedDims<N>::NP][32], int lane,
                                                  float Jd, float J0, float J1, float J2, float J3, float2 acc[]) {
   constexpr int NP = MixedDims<N>::NP;
   const int ra = (n == 3) ? 3 : 1, rb = (n == 3) ? 3 : 2;  // rows of sx and sy
   const int wxr = (n == 2) ? 1 : 0, wyr = (n == 1) ? 0 : 1;  // du or dv
+  const bool twoRows = n != 3, hasW = n != 0, twoW = n == 3;  // which reads the variable needs
   const float mw = (n == 0) ? 0.0f : 1.0f;                   // variable 0 has no velocity term
   const float ms = (n == 3) ? 1.0f : 0.0f;                   // energy: s = d3 + dp
   const float mcx = (n == 1) ? 1.0f : 0.0f, mcy = (n == 2) ? 1.0f : 0.0f;
@@ -938,14 +938,20 @@ __device__ __forceinline__ void interior_columns(int n, const BasePrim& b, const
   const float Py = (n == 3) ? b.H : ((n == 0) ? 0.0f : b.n);
   const float Bx = (n == 0) ? 1.0f : ((n == 2) ? b.v : b.u);
   const float By = (n == 0) ? 1.0f : ((n == 1) ? b.u : b.v);
-  const float oa = (s >= 1) ? sds[ra][0][lane] : 0.0f;
-  const float ob = (s >= 1) ? sds[rb][0][lane] : 0.0f;
 #pragma unroll
   for (int i = 0; i < NP; ++i) {
     const float dp = spr[2][i][lane];
-    const float sx = fmaf(ms, dp, sq0[ra][i][lane] + ((s >= 1) ? sds[ra][i][lane] - oa : 0.0f));
-    const float sy = fmaf(ms, dp, sq0[rb][i][lane] + ((s >= 1) ? sds[rb][i][lane] - ob : 0.0f));
-    const float wx = mw * spr[wxr][i][lane], wy = mw * spr[wyr][i][lane];
+    const float xa = sd[ra][i][lane];
+    float xb = xa, wxv = 0.0f, wyv = 0.0f;
+    if (twoRows) xb = sd[rb][i][lane];
+    if (hasW) {
+      wxv = spr[wxr][i][lane];
+      wyv = wxv;
+      if (twoW) wyv = spr[wyr][i][lane];
+    }
+    const float sx = fmaf(ms, dp, xa);
+    const float sy = fmaf(ms, dp, xb);
+    const float wx = mw * wxv, wy = mw * wyv;
     const float fx = fmaf(Px, wx, fmaf(sx, Bx + wx, mcx * dp));
     const float fy = fmaf(Py, wy, fmaf(sy, By + wy, mcy * dp));
     const float Fr = Jd * (J0 * fx + J1 * fy);
@@ -981,8 +987,12 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
   constexpr int NEP = MixedDims<N>::NEP, CH = StageDims<N>::CH, RW = StageDims<N>::RW;
   constexpr int NH = NPP / 2;
   // Rows are indexed by lane, so a 32-float stride is free of bank conflicts.
-  __shared__ float sq0[4][NP][32];
+  // sds: the stage increments D_s; sd: the conserved deltas against the stage
+  // state (dQ0 + D_s - D_s[0]) and spr: the velocity and pressure deltas, both
+  // per point for all four variables, so that each variable's interior flux
+  // reads only the rows it uses (3 or 4 words per point).
   __shared__ float sds[4][NP][32];
+  __shared__ float sd[4][NP][32];
   __shared__ float spr[3][NP][32];
   __shared__ __align__(16) float srec[32 * RW];
   __shared__ double sdt;
@@ -1016,9 +1026,23 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
   asm volatile("cp.async.commit_group;\n" ::);
   stage_tail_prefetch<N>(a, blockIdx.x, n, lane, sK, s);
   float Jd = 0.f, J0 = 0.f, J1 = 0.f, J2 = 0.f, J3 = 0.f, ooJ = 0.f;
+  // dQ0 of the points whose deltas this warp forms (n, n+4, ...), all four
+  // variables, loaded before the barrier and used after it.
+  constexpr int NT = (NP + 3) / 4;
+  float q0p[NT][4];
+#pragma unroll
+  for (int t = 0; t < NT; ++t)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) q0p[t][c] = 0.0f;
   if (active) {
 #pragma unroll
-    for (int i = 0; i < NP; ++i) sq0[n][i][lane] = a.dQ0[off + i * sK];
+    for (int t = 0; t < NT; ++t) {
+      const int i = n + 4 * t;
+      if (i < NP) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) q0p[t][c] = a.dQ0[(static_cast<size_t>(c) * NP + i) * sK + k];
+      }
+    }
     if (s >= 1) {
 #pragma unroll
       for (int i = 0; i < NP; ++i) sds[n][i][lane] = a.D[s][off + i * sK];
@@ -1032,10 +1056,7 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
   } else {
     // lanes past K: zero deltas for the shared work
 #pragma unroll
-    for (int i = 0; i < NP; ++i) {
-      sq0[n][i][lane] = 0.0f;
-      sds[n][i][lane] = 0.0f;
-    }
+    for (int i = 0; i < NP; ++i) sds[n][i][lane] = 0.0f;
   }
   // Local time step of this stage: DT persists across stages, so every thread
   // of the element reads it before the barrier and one writes it after.
@@ -1060,14 +1081,17 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
     bq[3] = b23.z;
   }
   const BasePrim b = base_prim(bq, gm1);
-  // Velocity and pressure deltas of points n, n+4, ... for the whole element.
+  // Conserved, velocity and pressure deltas of points n, n+4, ... for the whole element.
 #pragma unroll
-  for (int t = 0; t < (NP + 3) / 4; ++t) {
+  for (int t = 0; t < NT; ++t) {
     const int i = n + 4 * t;
     if (i < NP) {
       float d[4];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) d[c] = sq0[c][i][lane] + ((s >= 1) ? sds[c][i][lane] - sds[c][0][lane] : 0.0f);
+      for (int c = 0; c < 4; ++c) {
+        d[c] = q0p[t][c] + ((s >= 1) ? sds[c][i][lane] - sds[c][0][lane] : 0.0f);
+        sd[c][i][lane] = d[c];
+      }
       const DeltaPrim q = delta_prim(b, d, gm1);
       spr[0][i][lane] = q.du;
       spr[1][i][lane] = q.dv;
@@ -1078,7 +1102,7 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
   float2 acc[NH];
 #pragma unroll
   for (int h = 0; h < NH; ++h) acc[h] = make_float2(0.0f, 0.0f);
-  interior_columns<N>(n, b, sq0, sds, spr, lane, s, Jd, J0, J1, J2, J3, acc);
+  interior_columns<N>(n, b, sd, spr, lane, Jd, J0, J1, J2, J3, acc);
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();  // every thread's record chunks
   float rmax = -3.4028235e38f, rabs = 0.0f;
@@ -1109,8 +1133,10 @@ __global__ void __launch_bounds__(128, 7) k_mixed_stage(MixedArgs a) {
 #pragma unroll
     for (int r = 0; r < NP; ++r) {
       rhs[r] = -((r & 1) ? acc[r >> 1].y : acc[r >> 1].x) * ooJ;
-      dq0[r] = sq0[n][r][lane];
+      // dQ0 back from the stage delta (exact at stage 0; at later stages to
+      // the rounding of dQ0 + (D_s - D_s[0]))
       ds[r] = (s >= 1) ? sds[n][r][lane] : 0.0f;
+      dq0[r] = (s >= 1) ? sd[n][r][lane] - (ds[r] - sds[n][0][lane]) : sd[n][r][lane];
     }
     stage_tail<N>(a, eslot, n, k, off, sK, s, rhs, dq0, ds, dtk, rmax, rabs, rs2);
   }
