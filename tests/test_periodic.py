@@ -106,17 +106,21 @@ def test_periodic_step_parity(precision, tol, ttol):
 
 
 @pytest.mark.gpu
-def test_periodic_step_vjp_against_oracle_fd():
+@pytest.mark.parametrize("precision,every,rtol", [("fp64", 3, 1e-6), ("fp32", 3, 1e-5), ("fp32", 6, 1e-5)])
+def test_periodic_step_vjp_against_oracle_fd(precision, every, rtol):
     """The adjoint runs through the paired periodic edges like any shared edge:
-    a 6-step window (checkpoint every 3) against the oracle's central differences."""
+    a 6-step window (checkpoint every 3, or taped while recording) against the
+    oracle's central differences, on the FP64 path and the mixed path's FP32
+    adjoint."""
     mesh = meshes.periodic_box(6, jitter=0.1, seed=8)
-    gpu, ora = _pair(mesh, 2)
+    gpu, ora = _pair(mesh, 2, precision=precision)
     rng = np.random.default_rng(21)
     Q0 = np.ascontiguousarray(ora.Q * (1.0 + 0.01 * rng.uniform(-1, 1, ora.Q.shape)))
     nsteps = 6
     gpu.set_global_state(Q0)
     gpu.time = 0.0
-    gpu.record(nsteps, 3)
+    gpu.record(nsteps, every)
+    assert gpu.window_taped() == (every >= nsteps)
     Qbf = rng.standard_normal(Q0.shape)
     Qb0, _, _ = gpu.step_vjp(Qbf)
     d = rng.standard_normal(Q0.shape) * np.abs(Q0)
@@ -129,7 +133,7 @@ def test_periodic_step_vjp_against_oracle_fd():
         return float(np.sum(Qbf * ora.Q))
     fd = (J(1.0) - J(-1.0)) / (2 * h)
     ad = float(np.sum(Qb0 * d))
-    assert abs(ad - fd) <= 1e-6 * max(abs(ad), abs(fd)), (ad, fd)
+    assert abs(ad - fd) <= rtol * max(abs(ad), abs(fd)), (ad, fd)
     gpu.close()
 
 
