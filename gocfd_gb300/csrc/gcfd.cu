@@ -273,6 +273,7 @@ int build_mixed(gcfd_ctx* c) {
   for (int i = 1; i <= 4; ++i)
     if ((rc = dalloc(c, &c->Dk[i], nS))) return rc;
   if ((rc = dalloc(c, &c->R3, nS))) return rc;
+  if ((rc = dalloc(c, &c->P23, nS))) return rc;
   const int NEP = (NE + 1) & ~1;  // edge-major stride, see MixedDims::NEP
   if ((rc = dalloc(c, &c->mfaces, static_cast<size_t>(c->nEdges) * 2 * 4 * NEP))) return rc;
   if ((rc = dalloc(c, &c->mfhat, static_cast<size_t>(c->nEdges) * 4 * NEP))) return rc;

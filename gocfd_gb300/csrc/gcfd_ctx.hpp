@@ -63,6 +63,7 @@ struct gcfd_ctx {
   float* dQ0 = nullptr;
   float* Dk[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   float* R3 = nullptr;
+  float* P23 = nullptr;  // A2 D2 + A3 D3, formed at stage 2 for the final stage
   float *mfaces = nullptr, *mfhat = nullptr, *mcorr = nullptr;
   float2* mbase = nullptr;
   double* mexBC = nullptr;

@@ -243,6 +243,7 @@ struct MixedLaunch {
     a.dQ0 = c->dQ0;
     for (int i = 0; i < 5; ++i) a.D[i] = c->Dk[i];
     a.R3 = c->R3;
+    a.P23 = c->P23;
     a.faces = c->mfaces;
     a.fhat = c->mfhat;
     a.corr = c->mcorr;

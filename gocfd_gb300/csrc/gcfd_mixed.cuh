@@ -270,6 +270,7 @@ struct MixedArgs {
   float* dQ0;                 // Q0 - Q0(point 0)
   float* D[5];                // D[1..4] stage increments (D[0] unused)
   float* R3;                  // stage-3 RHS
+  float* P23;                 // A2 D2 + A3 D3 of rkAdvance's last stage, formed at stage 2 for stage 4
   float* faces;               // [g][2][4][NE]
   float* fhat;                // [g][4][NE]
   float* corr;                // [g][4]
@@ -721,7 +722,7 @@ __device__ __forceinline__ void prefetch_l2(const void* p) {
 
 // L2 prefetch of what stage_tail will read for block blk, issued by one warp
 // per variable n: the compensated state at point 0 (stages 0-3), or the whole
-// compensated state, the stage-2/3 increments and the stage-3 RHS (stage 4).
+// compensated state, the stage-2/3 combination P23 and the stage-3 RHS (stage 4).
 // With K % 4 == 0 every row of the block is 128 contiguous, 16-byte aligned
 // bytes and lane j bulk-prefetches rows j, j+32, ...; otherwise each thread
 // prefetches its own element's lines.
@@ -742,8 +743,7 @@ __device__ __forceinline__ void stage_tail_prefetch(const MixedArgs& a, int blk,
       prefetch_l2(a.Qhi + base + lane + r * sK);
       prefetch_l2(a.Qlo + base + lane + r * sK);
       if (s == 4) {
-        prefetch_l2(a.D[2] + base + lane + r * sK);
-        prefetch_l2(a.D[3] + base + lane + r * sK);
+        prefetch_l2(a.P23 + base + lane + r * sK);
         prefetch_l2(a.R3 + base + lane + r * sK);
       }
     }
@@ -753,9 +753,9 @@ __device__ __forceinline__ void stage_tail_prefetch(const MixedArgs& a, int blk,
     if (lane < 2) bulk_prefetch_l2((lane ? a.Qlo : a.Qhi) + base, 128);
     return;
   }
-  for (int it = lane; it < 5 * NP; it += 32) {
+  for (int it = lane; it < 4 * NP; it += 32) {
     const int arr = it / NP, r = it - arr * NP;
-    const float* p = arr == 0 ? a.Qhi : arr == 1 ? a.Qlo : arr == 2 ? a.D[2] : arr == 3 ? a.D[3] : a.R3;
+    const float* p = arr == 0 ? a.Qhi : arr == 1 ? a.Qlo : arr == 2 ? a.P23 : a.R3;
     bulk_prefetch_l2(p + base + r * sK, 128);
   }
 }
@@ -848,8 +848,13 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const int eslot[3
 #pragma unroll
       for (int r = 0; r < NP; ++r) dn[r] = kSspB1 * ds[r] + kSspC1 * (dt * rhs[r]);
     } else if (s == 2) {
+      // D3 is known here and D2 is ds: their share of the final combination is
+      // formed now, so that stage 4 reads one array for both
 #pragma unroll
-      for (int r = 0; r < NP; ++r) dn[r] = kSspB2 * ds[r] + kSspC2 * (dt * rhs[r]);
+      for (int r = 0; r < NP; ++r) {
+        dn[r] = kSspB2 * ds[r] + kSspC2 * (dt * rhs[r]);
+        a.P23[off + r * sK] = fmaf(kSspA3, dn[r], kSspA2 * ds[r]);
+      }
     } else if (s == 3) {
 #pragma unroll
       for (int r = 0; r < NP; ++r) {
@@ -878,8 +883,8 @@ __device__ __forceinline__ void stage_tail(const MixedArgs& a, const int eslot[3
       float qh[NP], ql[NP];
 #pragma unroll
       for (int r = 0; r < NP; ++r) {
-        const float inc = kSspA2 * a.D[2][off + r * sK] + kSspA3 * a.D[3][off + r * sK] + kSspA4 * ds[r] +
-                          kSspR3 * (dt * a.R3[off + r * sK]) + kSspC4 * (dt * rhs[r]);
+        const float inc =
+            fmaf(kSspC4, dt * rhs[r], fmaf(kSspR3, dt * a.R3[off + r * sK], fmaf(kSspA4, ds[r], a.P23[off + r * sK])));
         qh[r] = a.Qhi[off + r * sK];
         ql[r] = a.Qlo[off + r * sK];
         if (a.tapeQ0) a.tapeQ0[off + r * sK] = qh[r];
