@@ -21,7 +21,8 @@
 //
 // Layouts (HBM):
 //   Qhi/Qlo[n][i][k] FP32 pair (state), dQ0[n][i][k] = Q0 - Q0(point 0) FP32,
-//   D1..D4, R3 FP32 stage increments / stage-3 RHS
+//   D1..D4, R3 FP32 stage increments / stage-3 RHS,
+//   P23 = A2 D2 + A3 D3 FP32 (formed at stage 2, read at stage 4)
 //   faces[g][side][n][p]  FP32 dQ at edge points, side 0 = left element's CCW
 //                         order, side 1 = right element's CCW order; p padded
 //                         to NEP = NpEdge rounded up to even
