@@ -382,6 +382,8 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_pipe(const __grid_consta
   }
   if (TC) {
     __syncthreads();
+    // freed even after a wait that gave up (see k_mixed_stage_tc): kept
+    // columns would hold later CTAs in an unbounded tcgen05.alloc
     if (n == 0) {
       tc::fence_after();
       tc::dealloc(tbase, NCOLS);

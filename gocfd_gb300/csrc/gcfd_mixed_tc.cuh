@@ -289,6 +289,10 @@ __global__ void __launch_bounds__(128, 4) k_mixed_stage_tc(MixedArgs a) {
   }
   tc::fence_before();
   __syncthreads();
+  // The columns are freed even when both bounded waits gave up: a CTA that kept
+  // them would leave later CTAs on this SM in tcgen05.alloc, which waits without
+  // bound, while an MMA still pending at the free can only disturb a step that
+  // already reports the timeout.
   if (n == 0) {
     tc::fence_after();
     tc::dealloc(tbase, NCOLS);
