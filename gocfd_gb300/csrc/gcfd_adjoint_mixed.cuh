@@ -54,9 +54,17 @@ constexpr float kAdjA2 = 8677707.0f * kAdjQ, kAdjA3 = 1611615.0f * kAdjQ, kAdjA4
 // faces (when not null) receives the stage state's FP32 faces, FluxEdgeInterp
 // applied to Q0 + Ds per variable: the linearisation point of the edge
 // adjoints that follow.
+//
+// qbF is the adjoint of the step's final state, which feeds stages 2, 3 and 4
+// directly (rkAdvance's A2 Q2 + A3 Q3 + ... + W3 dt R3).  Stage 4 completes it
+// in place (its own input, plus the face transpose of the next step's stage 0
+// when that is pending), and stages 3 and 2 read it for their shares, so no
+// A2 / A3 / W3 dt4 products are stored between the stages; dtK4 is stage 4's
+// local dt (local time stepping).
 template <int N>
-__global__ void __launch_bounds__(128) k_adj_div32(AdjArgs<float> a, const float* __restrict__ geo,
-                                                   const float* __restrict__ QFbNext, float* __restrict__ faces) {
+__global__ void __launch_bounds__(128, 7) k_adj_div32(AdjArgs<float> a, const float* __restrict__ geo,
+                                                   const float* __restrict__ QFbNext, float* __restrict__ faces,
+                                                   float* qbF, const double* __restrict__ dtK4) {
   constexpr int NP = Dims<N>::NP, NE3 = Dims<N>::NE3;
   constexpr int NEH = AdjDims<N>::NEH, NPH = AdjDims<N>::NPH;
   __shared__ float sFx[4][NP][32], sFy[4][NP][32], sC[4][NP][32];
@@ -104,15 +112,13 @@ __global__ void __launch_bounds__(128) k_adj_div32(AdjArgs<float> a, const float
       }
     } else if (s == 4) {
       const float dt4 = static_cast<float>(a.localDT ? a.dtK[k] : a.dtS[4]);
-      const float A2 = kAdjA2, A3 = kAdjA3, A4 = kAdjA4, W3 = kSSP[4][3], C4 = kSSP[4][4];
+      const float A4 = kAdjA4, W3 = kSSP[4][3], C4 = kSSP[4][4];
 #pragma unroll
       for (int r = 0; r < NP; ++r) {
         const size_t ind = off + r * sK;
         Rb[r] = C4 * dt4 * qb[r];
-        a.Rb3[ind] = W3 * dt4 * qb[r];
+        if (QFbNext) qbF[ind] = qb[r];  // completed (otherwise it is qbF already)
         dtb += qb[r] * (W3 * a.rhs3[ind] + C4 * a.rhs[ind]);
-        a.Qb2[ind] = A2 * qb[r];
-        a.Qb3[ind] = A3 * qb[r];
         sC[n][r][lane] = A4 * qb[r];
       }
     } else {
@@ -120,10 +126,11 @@ __global__ void __launch_bounds__(128) k_adj_div32(AdjArgs<float> a, const float
       stage_coeffs(s, ald, bed, gad);
       const float al = kAdjAl[s], be = kAdjBe[s], ga = static_cast<float>(gad);
       const float dt = static_cast<float>(a.localDT ? a.dtK[k] : a.dtS[s]);
+      const float W3dt4 = (s == 3) ? kSSP[4][3] * static_cast<float>(a.localDT ? dtK4[k] : a.dtS[4]) : 0.0f;
 #pragma unroll
       for (int r = 0; r < NP; ++r) {
         const size_t ind = off + r * sK;
-        Rb[r] = ga * dt * qb[r] + (s == 3 ? a.Rb3[ind] : 0.0f);
+        Rb[r] = ga * dt * qb[r] + (s == 3 ? W3dt4 * qbF[ind] : 0.0f);
         dtb += ga * qb[r] * a.rhs[ind];
         if (!alias0) {
           if (s == 3) a.Qb0[ind] = al * qb[r];
@@ -186,6 +193,9 @@ __global__ void __launch_bounds__(128) k_adj_div32(AdjArgs<float> a, const float
   // point phase: warp w takes points w, w + 4, ...; the interior flux Jacobian^T
   // needs all four variables of a point
   const bool first = (s == 1 || s == 4);  // first writers of Qbs
+  // stages 2 and 3 start from their share of the final state's adjoint
+  const float Aw = (s == 2) ? kAdjA2 : kAdjA3;
+  const bool fromF = (s == 2 || s == 3);
   for (int i = n; i < NP; i += 4) {
     float q[4], Fxb[4], Fyb[4], qbp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
@@ -200,7 +210,7 @@ __global__ void __launch_bounds__(128) k_adj_div32(AdjArgs<float> a, const float
     for (int m = 0; m < 4; ++m) {
       const size_t ind = (static_cast<size_t>(m) * NP + i) * sK + k;
       const float v = sC[m][i][lane] + qbp[m];
-      a.Qbs[ind] = first ? v : a.Qbs[ind] + v;
+      a.Qbs[ind] = first ? v : (fromF ? Aw * qbF[ind] : a.Qbs[ind]) + v;
     }
   }
 }

@@ -393,7 +393,8 @@ struct AdjLaunch {
     const float* Qbn = (s == 4) ? c->Qbf32 : c->Qb32[s + 1];
     const bool pending = (s < 4) || c->adjFacesPending;
     k_adj_div32<N><<<(c->K + 31) / 32, 128, 0, c->stream>>>(adj_args32(c, s, Q0, Qbn, c->Qb32[s]), c->mgeo,
-                                                           pending ? c->QFb32 : nullptr, c->QF32);
+                                                           pending ? c->QFb32 : nullptr, c->QF32, c->Qbf32,
+                                                           c->tapeDT[4]);
     c->adjFacesPending = false;
     const EdgeArgs<double> e = edge_args(c, &c->tapeSc0->time);
     const AdjEdgeArgs<float> x = adj_edge_args32(c);
