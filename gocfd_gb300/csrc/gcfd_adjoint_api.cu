@@ -91,8 +91,7 @@ int adj_init(gcfd_ctx* c) {
       if ((rc = dalloc(c, &c->tapeDT[s], static_cast<size_t>(c->K)))) return rc;
       if ((rc = dalloc(c, &c->Qb32[s], S))) return rc;
     }
-    for (float** p : {&c->Qbf32, &c->Rb3_32})
-      if ((rc = dalloc(c, p, S))) return rc;
+    if ((rc = dalloc(c, &c->Qbf32, S))) return rc;
     for (float** p : {&c->QF32, &c->QFb32, &c->FEb32})
       if ((rc = dalloc(c, p, F))) return rc;
     if ((rc = dalloc(c, &c->tapeSc0, 1))) return rc;

@@ -112,7 +112,7 @@ struct gcfd_ctx {
   // Q0 + D_s with the forward's own increments Dk)
   float* tapeRHS32[5] = {};
   float* Qb32[5] = {};
-  float *Qbf32 = nullptr, *Rb3_32 = nullptr, *QF32 = nullptr, *QFb32 = nullptr, *FEb32 = nullptr;
+  float *Qbf32 = nullptr, *QF32 = nullptr, *QFb32 = nullptr, *FEb32 = nullptr;
   bool adjFacesPending = false;  // QFb32 holds stage-0 face adjoints not yet in Qbf32
   float* tapeQ0hi = nullptr;     // where the next taped step writes its starting Qhi
   double *dXs = nullptr, *dYs = nullptr, *edgeW = nullptr;

@@ -356,9 +356,9 @@ struct AdjLaunch {
     a.rhs3 = c->tapeRHS32[3];
     a.Qb0 = c->Qb32[0];
     a.Qbs = Qbs;
-    a.Qb2 = c->Qb32[2];
-    a.Qb3 = c->Qb32[3];
-    a.Rb3 = c->Rb3_32;
+    a.Qb2 = nullptr;  // k_adj_div32 takes the final state's shares from Qbf32
+    a.Qb3 = nullptr;
+    a.Rb3 = nullptr;
     a.dtS = c->tapeSc->dt;
     a.dtK = s >= 0 ? c->tapeDT[s] : nullptr;
     a.dtbarG = c->adjS;
