@@ -461,7 +461,13 @@ def run_ours(a, world, rank, local):
         if precision != "fp64":
             # the whole window taped while recording (checkpoint_every >= nsteps,
             # when a tape slot per step fits): the reverse sweep recomputes nothing;
-            # the cost is the reverse plus the taping's extra over the plain forward
+            # the cost is the reverse plus the taping's extra over the plain forward.
+            # On a fresh context: the checkpointed windows' blocks, held for reuse,
+            # would otherwise be freed and re-allocated around the taped slots
+            # (~160 GB here), which leaves the later slots' mappings fragmented.
+            sa.close()
+            sa = Euler(ip, mesh, 1, precision=precision, device=local, vortex_center=(0.0, 0.0))
+
             def taped(n, reps=1):
                 r = v = float("inf")
                 for _ in range(reps):
