@@ -173,6 +173,20 @@ func (c *Context) Step(nsteps int) (time, dt float64, resid [4]float64, err erro
 	return float64(t), float64(d), resid, err
 }
 
+// SetTime sets the solver time (RungeKutta5SSP.Time, euler.go:332), e.g. on a
+// restart; the IVortex boundaries and the FinalTime clip read it.
+func (c *Context) SetTime(t float64) error {
+	return status(c.ctx, C.gcfd_set_time(c.ctx, C.double(t)))
+}
+
+// Time returns the solver time and the number of steps taken.
+func (c *Context) Time() (t float64, steps int, err error) {
+	var tt C.double
+	var n C.int32_t
+	err = status(c.ctx, C.gcfd_get_time(c.ctx, &tt, &n))
+	return float64(tt), int(n), err
+}
+
 // SetStagePipeline selects the mixed path's persistent TMA-pipelined stage
 // kernel (true) or the one-block kernel (false, the default);
 // GCFD_OPT_STAGE_PIPELINE of gcfd.h.
