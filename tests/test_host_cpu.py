@@ -30,6 +30,21 @@ def test_library_exports_every_header_symbol():
     assert sorted(_lib.EXPORTS) == syms
 
 
+def test_go_binding_calls_every_entry_a_go_caller_needs():
+    """The cgo binding (gocfd_gb300/go/gcfd/gcfd.go) calls every header entry
+    but the ones left to other callers (device pointers and streams, the C++
+    mesh reader, the allocation-free residual norms, measurement and host
+    helpers), and calls nothing the header does not declare."""
+    go = open(os.path.join(ROOT, "gocfd_gb300", "go", "gcfd", "gcfd.go")).read()
+    called = set(re.findall(r"C\.(gcfd_[a-z0-9_]+)\(", go))
+    others = {"gcfd_set_state_device", "gcfd_get_state_device", "gcfd_get_stream", "gcfd_enqueue_steps",
+              "gcfd_read_mesh", "gcfd_free_mesh", "gcfd_residual_norms_static", "gcfd_profile_step",
+              "gcfd_device_fma_peaks", "gcfd_host_operator", "gcfd_host_graph_element"}
+    syms = set(header_symbols())
+    assert called <= syms, sorted(called - syms)
+    assert syms - others <= called, sorted(syms - others - called)
+
+
 @pytest.mark.parametrize("N", range(5))
 def test_product_operators_match_oracle(N):
     el = dfr_ops.build_element(N)
