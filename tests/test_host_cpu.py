@@ -30,6 +30,49 @@ def test_library_exports_every_header_symbol():
     assert sorted(_lib.EXPORTS) == syms
 
 
+def test_header_builds_as_c_and_a_c_caller_links(tmp_path):
+    """include/gcfd.h is plain C (C99, pedantic, no warnings), and a C program
+    links against libgcfd.so and gets the documented status codes for invalid
+    arguments (checked on the host before any CUDA call)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lib = _lib.load()
+    libdir = os.path.dirname(lib._name)
+    src = tmp_path / "caller.c"
+    src.write_text(r'''
+#include "gcfd.h"
+#include <stdio.h>
+#include <string.h>
+int main(void) {
+  gcfd_ctx* ctx = NULL;
+  gcfd_params p;
+  memset(&p, 0, sizeof p);
+  if (gcfd_create(NULL, &p, &ctx) != GCFD_ERR_ARG || ctx != NULL) return 1;
+  if (strlen(gcfd_last_error(NULL)) == 0) return 2;
+  double vx[3] = {0.0, 1.0, 0.0}, vy[3] = {0.0, 0.0, 1.0};
+  int32_t etov[3] = {0, 1, 2};
+  gcfd_mesh m;
+  memset(&m, 0, sizeof m);
+  m.nverts = 3; m.K = 0; m.vx = vx; m.vy = vy; m.etov = etov;
+  if (gcfd_create(&m, &p, &ctx) != GCFD_ERR_ARG) return 3;       /* K = 0 */
+  if (gcfd_step(NULL, 1, NULL, NULL, NULL, NULL, NULL) != GCFD_ERR_ARG) return 4;
+  gcfd_destroy(NULL);
+  printf("ok: %s\n", gcfd_last_error(NULL));
+  return 0;
+}
+''')
+    exe = tmp_path / "caller"
+    cmd = [cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+           str(src), "-o", str(exe), "-L", libdir, "-l:libgcfd.so", f"-Wl,-rpath,{libdir}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.startswith("ok:"), (r.returncode, r.stdout, r.stderr)
+
+
 def test_go_binding_calls_every_entry_a_go_caller_needs():
     """The cgo binding (gocfd_gb300/go/gcfd/gcfd.go) calls every header entry
     but the ones left to other callers (device pointers and streams, the C++
