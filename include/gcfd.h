@@ -246,9 +246,13 @@ int gcfd_record_steps(gcfd_ctx* ctx, int32_t nsteps, int32_t checkpoint_every, d
 /* Adjoint of the recorded window (RungeKutta5SSP.Step x nsteps, euler.go:408-418):
  * from the adjoint of the final state (and of the final time) to the adjoint
  * of the window's initial state, the far-field Qinf (4) and the initial time.
- * Each segment of checkpoint_every steps is recomputed from its checkpoint and
- * each step once more with its stage tape.  The solver state and time are the
- * window's end again on return. */
+ * Each segment of checkpoint_every steps is recomputed once from its
+ * checkpoint with every step's stage tape kept (a slot per step, when they fit;
+ * otherwise each step is recomputed once more with its tape), then reversed; a
+ * window taped while it was recorded is only reversed.  On a mixed-precision
+ * context the recompute is the mixed forward and the reverse sweep runs in
+ * FP32 (PerssonC0 and the pipelined stage kernel: GCFD_ERR_UNSUPPORTED there).
+ * The solver state and time are the window's end again on return. */
 int gcfd_step_vjp(gcfd_ctx* ctx, int32_t nshards, const int32_t* Kmax, const double* const* Qfinal_bar,
                   double tfinal_bar, double* const* Q0_bar, double* qinf_bar4, double* t0_bar);
 
