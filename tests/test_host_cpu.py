@@ -243,3 +243,37 @@ def test_bc_tag_parsing():
     assert meshes.bc_flag("inflow") == 1 and meshes.bc_flag("Outflow") == 8
     with pytest.raises(ValueError):
         meshes.bc_flag("bogus")
+
+
+# The reference's own input files (test_cases/Euler2D/*/input*.yaml, copied
+# into tests/fixtures/inputs/): every one parses, to the values its live lines
+# set (commented alternatives ignored, Go zero values / CLI defaults elsewhere).
+REFERENCE_INPUTS = {
+    "SU2-naca12_input-base.yaml": dict(CFL=5.0, FluxType="Roe", InitType="Freestream", PolynomialOrder=4,
+                                       FinalTime=20.0, Minf=0.8, Alpha=1.25, LocalTimeStepping=True,
+                                       MaxIterations=50000, Limiter="PerssonC0", Kappa=4.5,
+                                       PlotFields=["mach", "pressure coefficient"]),
+    "Wedge_input.yaml": dict(CFL=1.0, FluxType="Roe", InitType="Freestream", PolynomialOrder=7, FinalTime=20.0,
+                             Minf=2.0, Alpha=0.0, LocalTimeStepping=True, MaxIterations=15000, Limiter="PerssonC0",
+                             Kappa=6.0, PlotFields=["mach"]),
+    "isentropic-vortex_input-bench.yaml": dict(CFL=1.0, FluxType="Lax", InitType="IVortex", PolynomialOrder=2,
+                                               FinalTime=0.5, LocalTimeStepping=False, MaxIterations=0),
+    "isentropic-vortex_input.yaml": dict(CFL=4.0, FluxType="Roe", InitType="IVortex", PolynomialOrder=2,
+                                         FinalTime=200.0, MaxIterations=10000),
+    "naca_12_input-bench.yaml": dict(CFL=1.0, FluxType="Roe", InitType="Freestream", PolynomialOrder=2,
+                                     FinalTime=20.0, Minf=0.3, LocalTimeStepping=True, MaxIterations=100),
+    "naca_12_input-wall.yaml": dict(CFL=2.0, FluxType="Roe", InitType="Freestream", PolynomialOrder=0,
+                                    FinalTime=20.0, Minf=0.8, Alpha=1.25, LocalTimeStepping=True, MaxIterations=6000,
+                                    Limiter="PerssonC0", Kappa=4.5, PlotFields=["mach", "pressure coefficient"]),
+    "shock-tube_input-wall.yaml": dict(CFL=5.0, FluxType="Roe", InitType="shocktube", PolynomialOrder=7,
+                                       FinalTime=0.2, LocalTimeStepping=False, MaxIterations=80000,
+                                       Limiter="persson c0", Kappa=5.0, PlotFields=["mach"]),
+}
+
+
+@pytest.mark.parametrize("name", sorted(REFERENCE_INPUTS))
+def test_reference_input_files_parse(name):
+    ip = InputParameters2D.from_file(os.path.join(ROOT, "tests", "fixtures", "inputs", name))
+    for k, v in REFERENCE_INPUTS[name].items():
+        assert getattr(ip, k) == v, (k, getattr(ip, k), v)
+    assert ip.Gamma == 1.4
