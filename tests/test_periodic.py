@@ -39,6 +39,23 @@ def test_oracle_pairs_every_edge_of_a_periodic_box():
         assert abs(g.nx[el_, kl] + g.nx[er, kr]) < 1e-12 and abs(g.ny[el_, kl] + g.ny[er, kr]) < 1e-12
 
 
+def test_oracle_pairs_the_reference_periodic_vortex_mesh():
+    """The reference's own periodic vortex mesh (test_cases/Euler2D/isentropic-vortex/
+    geometry/vnew-coarse.su2: far field and a PeriodicReversed pair): its 28
+    periodic edges become 14 shared edges between equal, opposite faces."""
+    from conftest import fixture
+    mesh = meshes.read_mesh(fixture("vnew-coarse.su2"))
+    assert {f & 0xFF for _, _, f in mesh.bc_edges} == {4, 11}
+    el = dfr_ops.build_element(2)
+    g = dfr_ops.build_geometry(el, mesh.VX, mesh.VY, mesh.EToV, mesh.bc_edges)
+    nfar = sum(1 for _, _, f in mesh.bc_edges if f & 0xFF == 4)
+    assert int(np.sum(g.kR < 0)) == nfar == 28
+    assert len(g.kL) == (3 * mesh.K - nfar - 28) // 2 + 14 + nfar
+    for en in np.nonzero(g.kR >= 0)[0]:
+        kl, el_, kr, er = g.kL[en], g.eL[en], g.kR[en], g.eR[en]
+        assert abs(g.nx[el_, kl] + g.nx[er, kr]) < 1e-12 and abs(g.ny[el_, kl] + g.ny[er, kr]) < 1e-12
+
+
 def test_oracle_rejects_odd_periodic_lists():
     mesh = meshes.periodic_box(3)
     bc = [e for e in mesh.bc_edges if (e[2] >> 8) == 0][:-1] + [e for e in mesh.bc_edges if (e[2] >> 8) == 1]
@@ -72,6 +89,21 @@ def _pair(mesh, N, precision="fp64", init="ivortex", center=(0.0, 0.0), minf=0.5
 def test_periodic_rhs_parity(N):
     mesh = meshes.periodic_box(10, jitter=0.1, seed=4)
     gpu, ora = _pair(mesh, N)
+    amp = max(1.0, np.abs(_lib.host_operator(N, 1)).max() / 50.0)
+    for t in (0.0, 0.3):
+        r, ref = gpu.rhs_global(ora.Q, t), ora.rhs(ora.Q, t)
+        assert np.abs(r - ref).max() <= 1e-9 * amp * np.abs(ref).max() + 1e-13
+    gpu.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("N", [2, 3])
+def test_reference_periodic_vortex_mesh_rhs_parity(N):
+    """RHS parity on the reference's own PeriodicReversed vortex mesh
+    (vnew-coarse.su2, vortex at its default centre (5, 0))."""
+    from conftest import fixture
+    mesh = meshes.read_mesh(fixture("vnew-coarse.su2"))
+    gpu, ora = _pair(mesh, N, center=(5.0, 0.0))
     amp = max(1.0, np.abs(_lib.host_operator(N, 1)).max() / 50.0)
     for t in (0.0, 0.3):
         r, ref = gpu.rhs_global(ora.Q, t), ora.rhs(ora.Q, t)
