@@ -117,6 +117,30 @@ def test_step_parity_fp64_bc_mesh_sharded():
     gpu.close()
 
 
+@pytest.mark.parametrize("N", [2, 4])
+def test_rhs_parity_reference_wedge_mesh(N):
+    """The reference's own Mach-2 wedge mesh (test_cases/Euler2D/Wedge/wedge.su2:
+    walls and a supersonic far field), its input's Minf = 2, on a perturbed
+    freestream state."""
+    mesh = meshes.read_mesh(fixture("wedge.su2"))
+    gpu, ora = make_pair(mesh, N, flux="roe", minf=2.0)
+    Q = perturbed(ora.Q, seed=10 + N)
+    assert_rhs_close(gpu.rhs_global(Q), ora.rhs(Q), N=N)
+    gpu.close()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32", 1e-7)])
+def test_step_parity_reference_wedge_mesh_lts(precision, tol):
+    """20 local-time-stepping steps from the freestream on the reference's wedge
+    mesh (its input: Roe, LTS, Minf 2), FP64 and mixed against the oracle."""
+    mesh = meshes.read_mesh(fixture("wedge.su2"))
+    gpu, ora = make_pair(mesh, 2, flux="roe", minf=2.0, local_dt=True, cfl=0.5, precision=precision)
+    gpu.step(20)
+    ora.step(20)
+    assert rel_l2(gpu.get_global_state(), ora.Q) <= tol
+    gpu.close()
+
+
 def test_local_time_stepping_parity():
     """Supersonic far-field (copy) branch, slip walls, local time stepping."""
     mesh = meshes.wedge_channel(24, 12)
