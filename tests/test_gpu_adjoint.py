@@ -275,6 +275,24 @@ def test_wall_force_functional(kind, comp):
     gpu.close()
 
 
+@pytest.mark.parametrize("kind,comp", [("wall_force_x", 0), ("wall_force_y", 1)])
+def test_wall_force_on_the_reference_airfoil(kind, comp):
+    """The wall force on the reference's own NACA 0012 mesh
+    (test_cases/Euler2D/naca_12/mesh/naca12_2d-medium-lal.su2) at its input's
+    Minf = 0.8, alpha = 1.25 (input-wall.yaml), on a perturbed freestream state:
+    J against the oracle's faces, and the RHS there."""
+    mesh = meshes.read_mesh(fixture("naca12_2d-medium-lal.su2"))
+    gpu, ora = make_pair(mesh, 2, minf=0.8, alpha=1.25)
+    Q = perturbed(ora.Q, 8, 0.05)
+    gpu.set_global_state(Q)
+    J, Qb, _ = gpu.functional(kind)
+    ref = wall_force_numpy(ora, mesh, Q, comp)
+    assert abs(J - ref) <= 1e-12 * max(1.0, abs(ref))
+    r, rr = gpu.rhs_global(Q), ora.rhs(Q)
+    assert np.abs(r - rr).max() <= 1e-9 * np.abs(rr).max() + 1e-13
+    gpu.close()
+
+
 def test_vortex_error_functional():
     mesh = meshes.vortex_box(4, jitter=0.1)
     gpu, ora = make_pair(mesh, 3, init="ivortex", vortex_center=(0.0, 0.0))
