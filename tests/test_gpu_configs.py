@@ -44,3 +44,33 @@ def test_wedge_force_sensitivities_reduced():
     out = configs.wedge_sensitivity(steps=20, every=5, scale=1 / 32, fd_h=1e-5)
     assert out["rel_diff_Minf"] <= 1e-6, out
     assert out["rel_diff_alpha"] <= 1e-6, out
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32", 1e-7)])
+def test_reference_vortex_benchmark_input(precision, tol):
+    """The reference's isentropic-vortex benchmark input as it ships
+    (test_cases/Euler2D/isentropic-vortex/input-bench.yaml: Lax flux, IVortex,
+    N = 2, CFL 1, FinalTime 0.5) on its mesh (vortex-new.su2, the vortex at the
+    reference's default centre (5, 0)): 40 steps through the C ABI against the
+    oracle with the same parameters, and both against the exact vortex.  (Its
+    MaxIterations is absent, i.e. 0, so the reference's Solve stops after one
+    step; the steps here are taken directly.)"""
+    from conftest import fixture
+    from gocfd_gb300 import meshes
+    from gocfd_gb300.euler2d import Euler, InputParameters2D
+    ip = InputParameters2D.from_file(fixture("inputs/isentropic-vortex_input-bench.yaml"))
+    assert (ip.FluxType, ip.InitType, ip.PolynomialOrder, ip.MaxIterations) == ("Lax", "IVortex", 2, 0)
+    mesh = meshes.read_mesh(fixture("vortex-new.su2"))
+    ora = oracle.OracleSolver(ip.PolynomialOrder, mesh.VX, mesh.VY, mesh.EToV, mesh.bc_edges, flux="lax",
+                              init="ivortex", cfl=ip.CFL, final_time=ip.FinalTime, minf=ip.Minf, gamma=ip.Gamma,
+                              vortex_center=(5.0, 0.0))
+    with Euler(ip, mesh, 1, precision=precision, vortex_center=(5.0, 0.0)) as g:
+        info = g.step(40)
+        Q = g.get_global_state()
+        t = info["time"]
+    ora.step(40)
+    assert abs(t - ora.time) <= (1e-12 if precision == "fp64" else 1e-7) * max(1.0, ora.time)
+    assert np.linalg.norm(Q - ora.Q) <= tol * np.linalg.norm(ora.Q)
+    ex = oracle.ivortex_state(ora.vortex, ora.time, ora.geo.SolX, ora.geo.SolY)
+    e_gpu, e_ora = np.linalg.norm(Q - ex), np.linalg.norm(ora.Q - ex)
+    assert abs(e_gpu - e_ora) <= 1e-3 * e_ora
