@@ -74,3 +74,25 @@ def test_reference_vortex_benchmark_input(precision, tol):
     ex = oracle.ivortex_state(ora.vortex, ora.time, ora.geo.SolX, ora.geo.SolY)
     e_gpu, e_ora = np.linalg.norm(Q - ex), np.linalg.norm(ora.Q - ex)
     assert abs(e_gpu - e_ora) <= 1e-3 * e_ora
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32", 1e-7)])
+def test_reference_airfoil_wall_input(precision, tol):
+    """The reference's NACA 0012 input (test_cases/Euler2D/naca_12/input-wall.yaml:
+    Roe, N = 0, Minf 0.8, alpha 1.25, local time stepping; its PerssonC0 limiter is
+    off at N = 0, as NewEuler builds it only for N > 0) on its medium mesh: 30
+    steps against the oracle."""
+    from conftest import fixture
+    from gocfd_gb300 import meshes
+    from gocfd_gb300.euler2d import Euler, InputParameters2D
+    ip = InputParameters2D.from_file(fixture("inputs/naca_12_input-wall.yaml"))
+    assert (ip.PolynomialOrder, ip.LocalTimeStepping, ip.Minf, ip.Alpha) == (0, True, 0.8, 1.25)
+    mesh = meshes.read_mesh(fixture("naca12_2d-medium-lal.su2"))
+    ora = oracle.OracleSolver(0, mesh.VX, mesh.VY, mesh.EToV, mesh.bc_edges, flux="roe", init="freestream",
+                              cfl=ip.CFL, final_time=ip.FinalTime, minf=ip.Minf, gamma=ip.Gamma, alpha=ip.Alpha,
+                              local_dt=True)
+    with Euler(ip, mesh, 1, precision=precision) as g:
+        g.step(30)
+        Q = g.get_global_state()
+    ora.step(30)
+    assert np.linalg.norm(Q - ora.Q) <= tol * np.linalg.norm(ora.Q)
